@@ -1,0 +1,71 @@
+// Host-side context of one simulation on one GPU (opaque cf_ctx of the C ABI).
+#pragma once
+#include <string>
+#include <vector>
+
+#include "../../include/cajitafluids_gb300.h"
+#include "cf_internal.cuh"
+
+struct cf_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cf::Phys ph{};
+    int precision = 0;
+    double density = 1.0;
+
+    // fields, two versions each (src/ProblemManager.hpp:143-165); index cur is Current
+    cf::Grid<double> q64[2]{}, u[2]{}, v[2]{};
+    cf::Grid<float> q32[2]{};
+    int cur = 0;
+
+    // solver vectors (owned cells)
+    int vpitch = 0;
+    cf::Vec64 x{}, r{}, pa{}, pb{}, qv{}, b{};
+    cf::Vec32 e32{}, r32{}, pa32{}, pb32{};
+    double* partials = nullptr;  // 4 * n_units
+    int G = 0, B = 0, n_units = 0;
+    cf::SolverState* S = nullptr;   // device
+    cf::SolverState* hS = nullptr;  // pinned host mirror
+    double* d_out = nullptr;        // small device output slots
+    double* h_out = nullptr;        // pinned host mirror
+    double* staging = nullptr;      // FP64 staging for conversions / strided copies
+    size_t staging_elems = 0;
+
+    // CUDA graphs of batches of solver iterations, rebuilt when the stencil changes
+    cudaGraphExec_t g64 = nullptr, g32 = nullptr;
+    int g64_batch = 0, g32_batch = 0;
+    cf::Stencil g64_st{}, g32_st{};
+
+    long long launches = 0;
+    std::string err;
+    std::vector<void*> allocs;
+};
+
+namespace cf {
+// helpers implemented in cf_api.cu
+int fail(cf_ctx* c, int code, const char* fmt, ...);
+int cuda_check(cf_ctx* c, cudaError_t e, const char* what);
+void build_stencil(const cf_ctx* c, double dt, int precon_none, Stencil* st);
+
+// launchers (cf_fields.cu)
+cudaError_t launch_fill_ghosts(cf_ctx* c);
+cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs);
+cudaError_t launch_add_inputs(cf_ctx* c, double dt);
+cudaError_t launch_interp_points(cf_ctx* c, int field, int order, int n, const double* d_xy, double* d_out);
+cudaError_t launch_trace_points(cf_ctx* c, int n, const double* d_xy, double dt, double* d_out);
+cudaError_t launch_max_velocity(cf_ctx* c, double* d_out);
+cudaError_t launch_convert_q(cf_ctx* c, int to_device, int version);
+
+// projection (cf_project.cu)
+struct SolveOpts {
+    double tol, abs_tol, inner_tol;
+    int max_iter, max_outer;
+    int precon_none;
+};
+struct SolveResult {
+    int iterations, outer, status;
+    double bb, rr, div_l2, div_linf;
+};
+int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res);
+int div_norms(cf_ctx* c, double* l2, double* linf);
+}  // namespace cf

@@ -1,0 +1,511 @@
+// Field kernels: on-device ghost fill, fused RK3 semi-Lagrangian advection
+// (FP64 and FP32 arithmetic), inflow / body force / wall inputs, and the
+// point-sampling test exports.
+//
+// FP64 arithmetic follows the reference step by step so the FP64 path is
+// reproducible: src/TimeIntegrator.hpp:36-116 (rk3, advect),
+// src/Interpolation.hpp:30-54 (spline sample), src/Solver.hpp:181-263
+// (_addInputs), src/InflowSource.hpp:33-77, src/BodyForce.hpp:44-60,
+// src/BoundaryConditions.hpp:102-129.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "cf_ctx.cuh"
+
+namespace cf {
+
+static __constant__ double ENT_OFF_D[3][2] = {{0.5, 0.5}, {0.0, 0.5}, {0.5, 0.0}};
+
+// --------------------------------------------------------------------------
+// Ghost fill: the one-GPU form of Cajita's advection halo gather
+// (src/ProblemManager.hpp:173-176, 394-398).  Wall ghosts keep their
+// construction zeros; periodic ghosts copy the wrapped owned entity.
+template <typename T>
+__global__ void k_fill_ghosts(Grid<T> g, int nox, int noy, int per_x, int per_y) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.ex || j >= g.ey) return;
+    int gi = i - CF_HALO, gj = j - CF_HALO;
+    bool in_x = gi >= 0 && gi < nox, in_y = gj >= 0 && gj < noy;
+    if (in_x && in_y) return;
+    if (!in_x) {
+        if (!per_x) return;
+        gi = ((gi % nox) + nox) % nox;
+    }
+    if (!in_y) {
+        if (!per_y) return;
+        gj = ((gj % noy) + noy) % noy;
+    }
+    g.at(i, j) = g.at(gi + CF_HALO, gj + CF_HALO);
+}
+
+// --------------------------------------------------------------------------
+// FP64 spline sample (Cajita B-spline order 1 / 3, evaluated separably).
+template <int ORDER>
+__device__ __forceinline__ void weights64(double xi, int ext, int& k0, double* w) {
+    if (ORDER == 1) {
+        xi = fmin(fmax(xi, 0.0), (double)(ext - 1));
+        int k = (int)xi;
+        if (k > ext - 2) k = ext - 2;
+        double t = xi - (double)k;
+        w[0] = 1.0 - t;
+        w[1] = t;
+        k0 = k;
+    } else {
+        xi = fmin(fmax(xi, 1.0), (double)(ext - 2));
+        int k = (int)xi;
+        if (k > ext - 3) k = ext - 3;
+        double t = xi - (double)k;
+        double s = 1.0 - t;
+        double t2 = t * t;
+        double t3 = t2 * t;
+        double s3 = (s * s) * s;
+        w[0] = s3 * (1.0 / 6.0);
+        w[1] = fma(0.5, t3, -t2) + (2.0 / 3.0);
+        w[2] = fma(0.5, (t + t2) - t3, 1.0 / 6.0);
+        w[3] = t3 * (1.0 / 6.0);
+        k0 = k - 1;
+    }
+}
+
+template <int ORDER>
+__device__ double sample64(const Grid<double>& g, double lx, double ly, double rdx, double x, double y) {
+    constexpr int n = ORDER == 1 ? 2 : 4;
+    double xi = (x - lx) * rdx;
+    double yi = (y - ly) * rdx;
+    int kx, ky;
+    double wx[n], wy[n];
+    weights64<ORDER>(xi, g.ex, kx, wx);
+    weights64<ORDER>(yi, g.ey, ky, wy);
+    double val = 0.0;
+#pragma unroll
+    for (int b = 0; b < n; ++b) {
+        const double* row = g.o + (size_t)(ky + b) * g.pitch + kx;
+        double rs = wx[0] * __ldg(row);
+#pragma unroll
+        for (int a = 1; a < n; ++a) rs = fma(wx[a], __ldg(row + a), rs);
+        val = (b == 0) ? wy[0] * rs : fma(wy[b], rs, val);
+    }
+    return val;
+}
+
+__device__ __forceinline__ double entity_coord(const Phys& p, int ent, int axis, int idx) {
+    double t = (double)idx + ENT_OFF_D[ent][axis];
+    return p.gl[axis] + t * p.dx;
+}
+
+// rk3 backtrace (src/TimeIntegrator.hpp:36-77), linear velocity samples.
+__device__ void rk3_64(const Phys& p, const Grid<double>& u, const Grid<double>& v, double dt,
+                       double x0, double y0, double& tx, double& ty) {
+    const double ulx = p.low[E_FACEI][0], uly = p.low[E_FACEI][1];
+    const double vlx = p.low[E_FACEJ][0], vly = p.low[E_FACEJ][1];
+    double v0x = sample64<1>(u, ulx, uly, p.rdx, x0, y0);
+    double v0y = sample64<1>(v, vlx, vly, p.rdx, x0, y0);
+    double h1 = 0.5 * dt;
+    double x1 = fma(-h1, v0x, x0), y1 = fma(-h1, v0y, y0);
+    double v1x = sample64<1>(u, ulx, uly, p.rdx, x1, y1);
+    double v1y = sample64<1>(v, vlx, vly, p.rdx, x1, y1);
+    double h2 = 0.75 * dt;
+    bool ralston = (p.quirks & 2u) != 0;
+    double sx = ralston ? v1x : v0x, sy = ralston ? v1y : v0y;
+    double x2 = fma(-h2, sx, x0), y2 = fma(-h2, sy, y0);
+    double v2x = sample64<1>(u, ulx, uly, p.rdx, x2, y2);
+    double v2y = sample64<1>(v, vlx, vly, p.rdx, x2, y2);
+    double ax = (2.0 / 9.0) * v0x;
+    ax = fma(3.0 / 9.0, v1x, ax);
+    ax = fma(4.0 / 9.0, v2x, ax);
+    double ay = (2.0 / 9.0) * v0y;
+    ay = fma(3.0 / 9.0, v1y, ay);
+    ay = fma(4.0 / 9.0, v2y, ay);
+    tx = fma(-dt, ax, x0);
+    ty = fma(-dt, ay, y0);
+}
+
+// --------------------------------------------------------------------------
+// Inputs (src/Solver.hpp:181-263) applied to one entity value.
+__device__ __forceinline__ bool in_box(const Phys& p, double x, double y) {
+    return x >= p.bbox[0] && x < p.bbox[2] && y >= p.bbox[1] && y < p.bbox[3];
+}
+
+__device__ __forceinline__ double inputs_cell(const Phys& p, double q, double x, double y, double dt) {
+    if (in_box(p, x, y)) {
+        if (p.src_mode == 0) {
+            if (q < p.src_q) q = p.src_q;
+        } else {
+            q = fma(p.src_q, dt, q);
+        }
+    }
+    return q;
+}
+
+// axis 0: I-face (u), axis 1: J-face (v); rho is used only with a density-scaled force.
+__device__ __forceinline__ double inputs_face(const Phys& p, int axis, double w, double x, double y,
+                                              double dt, int gidx, double rho) {
+    if (in_box(p, x, y) && fabs(w) < fabs(p.src_vel[axis])) w = p.src_vel[axis];
+    if (p.force_density)
+        w = fma(p.force[axis] * rho, dt, w);
+    else
+        w = fma(p.force[axis], dt, w);
+    int per = axis == 0 ? p.per_x : p.per_y;
+    int n = axis == 0 ? p.nx : p.ny;
+    if (!per) {
+        if (gidx <= 0 && p.bc[axis] == 0) w = 0.0;
+        if (gidx > n - 1 && p.bc[axis + 2] == 0) w = 0.0;
+    }
+    return w;
+}
+
+// --------------------------------------------------------------------------
+// FP64 advection: one thread per owned entity; blockIdx.z selects the
+// entity (cell q, I-face u, J-face v).  Reads Current, writes Next.
+struct Adv64 {
+    Phys p;
+    Grid<double> q, u, v, qn, un, vn;
+    double dt;
+    int fuse;
+};
+
+template <int ORDER>
+__global__ void __launch_bounds__(256) k_advect64(Adv64 a) {
+    const Phys& p = a.p;
+    int ent = blockIdx.z;
+    int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    int ox = p.nx + ((ent == E_FACEI && !p.per_x) ? 1 : 0);
+    int oy = p.ny + ((ent == E_FACEJ && !p.per_y) ? 1 : 0);
+    if (gi >= ox || gj >= oy) return;
+    const Grid<double>& f = ent == E_CELL ? a.q : (ent == E_FACEI ? a.u : a.v);
+    const Grid<double>& fn = ent == E_CELL ? a.qn : (ent == E_FACEI ? a.un : a.vn);
+    double x0 = entity_coord(p, ent, 0, gi + CF_HALO);
+    double y0 = entity_coord(p, ent, 1, gj + CF_HALO);
+    double tx, ty;
+    rk3_64(p, a.u, a.v, a.dt, x0, y0, tx, ty);
+    double val = sample64<ORDER>(f, p.low[ent][0], p.low[ent][1], p.rdx, tx, ty);
+    if (a.fuse) {
+        if (ent == E_CELL)
+            val = inputs_cell(p, val, x0, y0, a.dt);
+        else if (ent == E_FACEI)
+            val = inputs_face(p, 0, val, x0, y0, a.dt, gi, 0.0);
+        else
+            val = inputs_face(p, 1, val, x0, y0, a.dt, gj, 0.0);
+    }
+    fn.at(gi + CF_HALO, gj + CF_HALO) = val;
+}
+
+// --------------------------------------------------------------------------
+// FP32 advection (mixed precision).  Positions are kept as an integer base
+// (the entity's local index) plus a small FP32 displacement in cell units,
+// so FP32 keeps full relative precision at any grid size.  u and v are
+// stored in FP64 (the projection works on them in FP64); q is FP32.
+struct Adv32 {
+    Phys p;
+    Grid<float> q, qn;
+    Grid<double> u, v, un, vn;
+    float c;      // dt / dx
+    double dt;
+    int fuse;
+};
+
+template <typename T>
+__device__ __forceinline__ float lin32(const Grid<T>& g, int bi, int bj, float fx, float fy) {
+    float flx = floorf(fx), fly = floorf(fy);
+    int ix = bi + (int)flx, iy = bj + (int)fly;
+    float tx = fx - flx, ty = fy - fly;
+    if (ix < 0) { ix = 0; tx = 0.f; }
+    if (ix > g.ex - 2) { ix = g.ex - 2; tx = 1.f; }
+    if (iy < 0) { iy = 0; ty = 0.f; }
+    if (iy > g.ey - 2) { iy = g.ey - 2; ty = 1.f; }
+    const T* r0 = g.o + (size_t)iy * g.pitch + ix;
+    const T* r1 = r0 + g.pitch;
+    float a0 = (float)__ldg(r0), a1 = (float)__ldg(r0 + 1);
+    float b0 = (float)__ldg(r1), b1 = (float)__ldg(r1 + 1);
+    float s0 = fmaf(tx, a1 - a0, a0);
+    float s1 = fmaf(tx, b1 - b0, b0);
+    return fmaf(ty, s1 - s0, s0);
+}
+
+__device__ __forceinline__ void cubic_w32(float t, float* w) {
+    float s = 1.f - t, t2 = t * t, t3 = t2 * t;
+    w[0] = s * s * s * (1.f / 6.f);
+    w[1] = fmaf(0.5f, t3, -t2) + (2.f / 3.f);
+    w[2] = fmaf(0.5f, (t + t2) - t3, 1.f / 6.f);
+    w[3] = t3 * (1.f / 6.f);
+}
+
+template <typename T>
+__device__ __forceinline__ float cub32(const Grid<T>& g, int bi, int bj, float fx, float fy) {
+    float flx = floorf(fx), fly = floorf(fy);
+    int ix = bi + (int)flx, iy = bj + (int)fly;
+    float tx = fx - flx, ty = fy - fly;
+    if (ix < 1) { ix = 1; tx = 0.f; }
+    if (ix > g.ex - 3) { ix = g.ex - 3; tx = 1.f; }
+    if (iy < 1) { iy = 1; ty = 0.f; }
+    if (iy > g.ey - 3) { iy = g.ey - 3; ty = 1.f; }
+    float wx[4], wy[4];
+    cubic_w32(tx, wx);
+    cubic_w32(ty, wy);
+    float val = 0.f;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const T* row = g.o + (size_t)(iy - 1 + b) * g.pitch + (ix - 1);
+        float rs = wx[0] * (float)__ldg(row);
+#pragma unroll
+        for (int k = 1; k < 4; ++k) rs = fmaf(wx[k], (float)__ldg(row + k), rs);
+        val = b == 0 ? wy[0] * rs : fmaf(wy[b], rs, val);
+    }
+    return val;
+}
+
+template <int ORDER>
+__global__ void __launch_bounds__(256) k_advect32(Adv32 a) {
+    const Phys& p = a.p;
+    int ent = blockIdx.z;
+    int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    int ox = p.nx + ((ent == E_FACEI && !p.per_x) ? 1 : 0);
+    int oy = p.ny + ((ent == E_FACEJ && !p.per_y) ? 1 : 0);
+    if (gi >= ox || gj >= oy) return;
+    int li = gi + CF_HALO, lj = gj + CF_HALO;
+    // entity offset minus the velocity grids' offsets (u: (0, .5), v: (.5, 0))
+    float ox_e = ent == E_FACEI ? 0.f : 0.5f;
+    float oy_e = ent == E_FACEJ ? 0.f : 0.5f;
+    float uox = ox_e, uoy = oy_e - 0.5f, vox = ox_e - 0.5f, voy = oy_e;
+    float v0x = lin32(a.u, li, lj, uox, uoy);
+    float v0y = lin32(a.v, li, lj, vox, voy);
+    float h1 = -0.5f * a.c, h2 = -0.75f * a.c;
+    float d1x = h1 * v0x, d1y = h1 * v0y;
+    float v1x = lin32(a.u, li, lj, uox + d1x, uoy + d1y);
+    float v1y = lin32(a.v, li, lj, vox + d1x, voy + d1y);
+    bool ralston = (p.quirks & 2u) != 0;
+    float d2x = h2 * (ralston ? v1x : v0x), d2y = h2 * (ralston ? v1y : v0y);
+    float v2x = lin32(a.u, li, lj, uox + d2x, uoy + d2y);
+    float v2y = lin32(a.v, li, lj, vox + d2x, voy + d2y);
+    float ax = fmaf(4.f / 9.f, v2x, fmaf(3.f / 9.f, v1x, (2.f / 9.f) * v0x));
+    float ay = fmaf(4.f / 9.f, v2y, fmaf(3.f / 9.f, v1y, (2.f / 9.f) * v0y));
+    float dx = -a.c * ax, dy = -a.c * ay;
+    float val;
+    if (ent == E_CELL)
+        val = ORDER == 1 ? lin32(a.q, li, lj, dx, dy) : cub32(a.q, li, lj, dx, dy);
+    else if (ent == E_FACEI)
+        val = ORDER == 1 ? lin32(a.u, li, lj, dx, dy) : cub32(a.u, li, lj, dx, dy);
+    else
+        val = ORDER == 1 ? lin32(a.v, li, lj, dx, dy) : cub32(a.v, li, lj, dx, dy);
+    double w = (double)val;
+    if (a.fuse) {
+        double x0 = entity_coord(p, ent, 0, li), y0 = entity_coord(p, ent, 1, lj);
+        if (ent == E_CELL)
+            w = inputs_cell(p, w, x0, y0, a.dt);
+        else if (ent == E_FACEI)
+            w = inputs_face(p, 0, w, x0, y0, a.dt, gi, 0.0);
+        else
+            w = inputs_face(p, 1, w, x0, y0, a.dt, gj, 0.0);
+    }
+    if (ent == E_CELL)
+        a.qn.at(li, lj) = (float)w;
+    else if (ent == E_FACEI)
+        a.un.at(li, lj) = w;
+    else
+        a.vn.at(li, lj) = w;
+}
+
+// --------------------------------------------------------------------------
+// Standalone inputs (Solver::setup and density-scaled body forces): pass 0
+// updates cells, pass 1 updates faces reading the updated cells.
+template <typename TQ>
+struct Inp {
+    Phys p;
+    Grid<TQ> q;
+    Grid<double> u, v;
+    double dt;
+};
+
+template <typename TQ>
+__device__ __forceinline__ double cell_q(const Inp<TQ>& a, int gi, int gj) {
+    int ci = wrap_index(gi, a.p.nx, a.p.per_x), cj = wrap_index(gj, a.p.ny, a.p.per_y);
+    if (ci < 0 || cj < 0) return 0.0;
+    return (double)a.q.at(ci + CF_HALO, cj + CF_HALO);
+}
+
+template <typename TQ>
+__global__ void k_inputs_cells(Inp<TQ> a) {
+    int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    if (gi >= a.p.nx || gj >= a.p.ny) return;
+    double x = entity_coord(a.p, E_CELL, 0, gi + CF_HALO), y = entity_coord(a.p, E_CELL, 1, gj + CF_HALO);
+    TQ& q = a.q.at(gi + CF_HALO, gj + CF_HALO);
+    q = (TQ)inputs_cell(a.p, (double)q, x, y, a.dt);
+}
+
+template <typename TQ>
+__global__ void k_inputs_faces(Inp<TQ> a) {
+    const Phys& p = a.p;
+    int axis = blockIdx.z;
+    int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    int ox = p.nx + ((axis == 0 && !p.per_x) ? 1 : 0);
+    int oy = p.ny + ((axis == 1 && !p.per_y) ? 1 : 0);
+    if (gi >= ox || gj >= oy) return;
+    int ent = axis == 0 ? E_FACEI : E_FACEJ;
+    double x = entity_coord(p, ent, 0, gi + CF_HALO), y = entity_coord(p, ent, 1, gj + CF_HALO);
+    double rho = 0.0;
+    if (p.force_density)
+        rho = axis == 0 ? (cell_q(a, gi - 1, gj) + cell_q(a, gi, gj)) * 0.5
+                        : (cell_q(a, gi, gj - 1) + cell_q(a, gi, gj)) * 0.5;
+    double& w = axis == 0 ? a.u.at(gi + CF_HALO, gj + CF_HALO) : a.v.at(gi + CF_HALO, gj + CF_HALO);
+    w = inputs_face(p, axis, w, x, y, a.dt, axis == 0 ? gi : gj, rho);
+}
+
+// --------------------------------------------------------------------------
+// Test exports and small utilities.
+struct Pts {
+    Phys p;
+    Grid<double> f, u, v;
+    int ent, order, n;
+    const double* xy;
+    double* out;
+    double dt;
+};
+
+__global__ void k_interp_points(Pts a) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    double x = a.xy[2 * k], y = a.xy[2 * k + 1];
+    a.out[k] = a.order == 1 ? sample64<1>(a.f, a.p.low[a.ent][0], a.p.low[a.ent][1], a.p.rdx, x, y)
+                            : sample64<3>(a.f, a.p.low[a.ent][0], a.p.low[a.ent][1], a.p.rdx, x, y);
+}
+
+__global__ void k_trace_points(Pts a) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    double tx, ty;
+    rk3_64(a.p, a.u, a.v, a.dt, a.xy[2 * k], a.xy[2 * k + 1], tx, ty);
+    a.out[2 * k] = tx;
+    a.out[2 * k + 1] = ty;
+}
+
+// max |w| over the owned faces of one axis; non-negative doubles order like
+// their bit patterns, so an integer atomicMax is exact and order-free.
+__global__ void k_max_abs(Grid<double> g, int ox, int oy, unsigned long long* out) {
+    int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    double m = 0.0;
+    if (gi < ox && gj < oy) m = fabs(g.at(gi + CF_HALO, gj + CF_HALO));
+    if (m != m) m = INFINITY;
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// FP64 staging <-> FP32 quantity (owned region, staging row pitch = ox)
+__global__ void k_q_convert(Grid<float> q, double* st, int nx, int ny, int to_device) {
+    int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    if (gi >= nx || gj >= ny) return;
+    size_t k = (size_t)gj * nx + gi;
+    if (to_device)
+        q.at(gi + CF_HALO, gj + CF_HALO) = (float)st[k];
+    else
+        st[k] = (double)q.at(gi + CF_HALO, gj + CF_HALO);
+}
+
+// --------------------------------------------------------------------------
+// launchers
+static inline dim3 grid2(int ex, int ey, dim3 blk, int z = 1) {
+    return dim3((ex + blk.x - 1) / blk.x, (ey + blk.y - 1) / blk.y, z);
+}
+
+cudaError_t launch_fill_ghosts(cf_ctx* c) {
+    const Phys& p = c->ph;
+    if (!p.per_x && !p.per_y) return cudaSuccess;  // wall ghosts are never written
+    dim3 blk(32, 8);
+    int s = c->cur;
+    int nqx = p.nx, nqy = p.ny;
+    int nux = p.per_x ? p.nx : p.nx + 1, nvy = p.per_y ? p.ny : p.ny + 1;
+    if (c->precision == CF_PREC_FP64) {
+        k_fill_ghosts<double><<<grid2(c->q64[s].ex, c->q64[s].ey, blk), blk, 0, c->stream>>>(c->q64[s], nqx, nqy, p.per_x, p.per_y);
+    } else {
+        k_fill_ghosts<float><<<grid2(c->q32[s].ex, c->q32[s].ey, blk), blk, 0, c->stream>>>(c->q32[s], nqx, nqy, p.per_x, p.per_y);
+    }
+    k_fill_ghosts<double><<<grid2(c->u[s].ex, c->u[s].ey, blk), blk, 0, c->stream>>>(c->u[s], nux, p.ny, p.per_x, p.per_y);
+    k_fill_ghosts<double><<<grid2(c->v[s].ex, c->v[s].ey, blk), blk, 0, c->stream>>>(c->v[s], p.nx, nvy, p.per_x, p.per_y);
+    c->launches += 3;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs) {
+    const Phys& p = c->ph;
+    int s = c->cur, n = 1 - s;
+    dim3 blk(32, 8);
+    dim3 grd = grid2(p.nx + 1, p.ny + 1, blk, 3);
+    if (c->precision == CF_PREC_FP64) {
+        Adv64 a{p, c->q64[s], c->u[s], c->v[s], c->q64[n], c->u[n], c->v[n], dt, fuse_inputs};
+        if (order == 1)
+            k_advect64<1><<<grd, blk, 0, c->stream>>>(a);
+        else
+            k_advect64<3><<<grd, blk, 0, c->stream>>>(a);
+    } else {
+        Adv32 a{p, c->q32[s], c->q32[n], c->u[s], c->v[s], c->u[n], c->v[n], (float)(dt / p.dx), dt, fuse_inputs};
+        if (order == 1)
+            k_advect32<1><<<grd, blk, 0, c->stream>>>(a);
+        else
+            k_advect32<3><<<grd, blk, 0, c->stream>>>(a);
+    }
+    c->launches += 1;
+    c->cur = n;  // ProblemManager::advance for q, u, v
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add_inputs(cf_ctx* c, double dt) {
+    const Phys& p = c->ph;
+    int s = c->cur;
+    dim3 blk(32, 8);
+    if (c->precision == CF_PREC_FP64) {
+        Inp<double> a{p, c->q64[s], c->u[s], c->v[s], dt};
+        k_inputs_cells<double><<<grid2(p.nx, p.ny, blk), blk, 0, c->stream>>>(a);
+        k_inputs_faces<double><<<grid2(p.nx + 1, p.ny + 1, blk, 2), blk, 0, c->stream>>>(a);
+    } else {
+        Inp<float> a{p, c->q32[s], c->u[s], c->v[s], dt};
+        k_inputs_cells<float><<<grid2(p.nx, p.ny, blk), blk, 0, c->stream>>>(a);
+        k_inputs_faces<float><<<grid2(p.nx + 1, p.ny + 1, blk, 2), blk, 0, c->stream>>>(a);
+    }
+    c->launches += 2;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_interp_points(cf_ctx* c, int field, int order, int n, const double* d_xy, double* d_out) {
+    int s = c->cur;
+    Grid<double> f = field == CF_FIELD_QUANTITY ? c->q64[s] : (field == CF_FIELD_U ? c->u[s] : c->v[s]);
+    Pts a{c->ph, f, c->u[s], c->v[s], field, order, n, d_xy, d_out, 0.0};
+    k_interp_points<<<(n + 127) / 128, 128, 0, c->stream>>>(a);
+    c->launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_points(cf_ctx* c, int n, const double* d_xy, double dt, double* d_out) {
+    int s = c->cur;
+    Pts a{c->ph, c->u[s], c->u[s], c->v[s], 0, 1, n, d_xy, d_out, dt};
+    k_trace_points<<<(n + 127) / 128, 128, 0, c->stream>>>(a);
+    c->launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_max_velocity(cf_ctx* c, double* d_out) {
+    const Phys& p = c->ph;
+    int s = c->cur;
+    cudaMemsetAsync(d_out, 0, sizeof(double), c->stream);
+    dim3 blk(32, 8);
+    int nux = p.per_x ? p.nx : p.nx + 1, nvy = p.per_y ? p.ny : p.ny + 1;
+    k_max_abs<<<grid2(nux, p.ny, blk), blk, 0, c->stream>>>(c->u[s], nux, p.ny, (unsigned long long*)d_out);
+    k_max_abs<<<grid2(p.nx, nvy, blk), blk, 0, c->stream>>>(c->v[s], p.nx, nvy, (unsigned long long*)d_out);
+    c->launches += 2;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_convert_q(cf_ctx* c, int to_device, int version) {
+    dim3 blk(32, 8);
+    k_q_convert<<<grid2(c->ph.nx, c->ph.ny, blk), blk, 0, c->stream>>>(c->q32[version], c->staging, c->ph.nx,
+                                                                       c->ph.ny, to_device);
+    c->launches += 1;
+    return cudaGetLastError();
+}
+
+}  // namespace cf

@@ -1,0 +1,172 @@
+// Internal declarations shared by the CUDA translation units of libcfgpu.
+//
+// Storage (one GPU holds the whole grid):
+//   * q, u, v: ghosted arrays, ghost depth 3 (src/Solver.hpp:78), x fastest.
+//     Local index (i, j) of the ghosted Cajita space maps to
+//     origin[j * pitch + i]; the owned corner (3, 3) sits on a 256-byte
+//     boundary.  Extents: cells (nx+6, ny+6), I-faces (nx+7, ny+6),
+//     J-faces (nx+6, ny+7) (tests/tstMesh.cpp:61-68).
+//   * solver vectors: owned cells only, row pitch a multiple of 32 words.
+//
+// FP64 kernels are compiled with --fmad=false; every fused multiply-add is
+// an explicit fma() so that results are reproducible bit for bit.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define CF_HALO 3
+#define CF_UNIT_COLS 64   // columns per reduction unit (32 lanes x 2)
+#define CF_BAND_ROWS 16   // rows per reduction unit
+#define CF_RED_THREADS 256
+#define CF_RED_WARPS (CF_RED_THREADS / 32)
+
+namespace cf {
+
+enum Entity { E_CELL = 0, E_FACEI = 1, E_FACEJ = 2 };
+enum SolveStatus { ST_CONVERGED = 0, ST_MAXIT = 1, ST_BREAKDOWN = 2, ST_NAN = 3, ST_RUNNING = 100 };
+
+template <typename T>
+struct Grid {
+    T* o;       // local (0, 0)
+    int pitch;  // elements per row
+    int ex, ey; // ghosted extents
+    __host__ __device__ T& at(int i, int j) const { return o[(size_t)j * pitch + i]; }
+};
+
+// Physical setup shared by the kernels (passed by value).
+struct Phys {
+    int nx, ny;
+    int per_x, per_y;
+    double dx, rdx;
+    double gl[2];       // low corner of the ghosted local mesh
+    double low[3][2];   // coordinate of local index 0 per entity (spline origin)
+    int bc[4];          // left, bottom, right, top
+    double bbox[4];     // inflow box x0, y0, x1, y1
+    double src_q;
+    double src_vel[2];
+    int src_mode;
+    double force[2];
+    int force_density;
+    unsigned quirks;
+};
+
+// Matrix tables indexed by wall-adjacency bits (1 left, 2 right, 4 bottom, 8 top).
+struct Stencil {
+    double diag[16];
+    double minv[16];
+    double ms;          // -scale (off-diagonal legs)
+    float diag32[16];
+    float minv32[16];
+    float ms32;
+};
+
+// Device-resident solver scalars.
+struct SolverState {
+    double bb, rr, rho, alpha, beta;
+    double tol2, abs2, area;
+    // mixed precision: inner solve
+    double rr_in0, rr_in, rho_in, alpha_in, beta_in, tau2;
+    double rr_out, inner_tol2, target2;
+    int use_abs;
+    int iter, max_iter, status;
+    int inner_iter, inner_status;
+    int outer_iter, max_outer;
+    unsigned int ticket[8];
+};
+
+struct Vec64 {
+    double* a;
+    int pitch;
+};
+struct Vec32 {
+    float* a;
+    int pitch;
+};
+
+// --------------------------------------------------------------------------
+// Fixed-order reductions.  One warp reduces one unit of 64 x 16 cells: lane l
+// owns columns 64g + 2l, 64g + 2l + 1 and accumulates row by row; the lane
+// sums are folded by a xor butterfly; the last block to finish folds all
+// unit partials: 256 strided accumulators, a butterfly per warp, and the 8
+// warp sums added in order.
+__device__ __forceinline__ double warp_fold(double s) {
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, m);
+    return s;
+}
+
+__device__ __forceinline__ double warp_max(double s) {
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) s = fmax(s, __shfl_xor_sync(0xffffffffu, s, m));
+    return s;
+}
+
+// Returns true in the block that arrives last.  Every thread fences its own
+// global writes before the block takes its ticket.
+__device__ __forceinline__ bool last_block_arrive(unsigned int* ticket) {
+    __shared__ bool am_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int t = atomicAdd(ticket, 1u);
+        am_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (am_last) __threadfence();
+    return am_last;
+}
+
+// Canonical final sum over n partials; blockDim.x must be 256.  All threads
+// return the same value.
+__device__ __forceinline__ double final_tree(const double* partial, int n) {
+    __shared__ double ws[CF_RED_WARPS];
+    double s = 0.0;
+    for (int u = threadIdx.x; u < n; u += CF_RED_THREADS) s = s + __ldcg(partial + u);
+    s = warp_fold(s);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    double tot = ws[0];
+#pragma unroll
+    for (int k = 1; k < CF_RED_WARPS; ++k) tot = tot + ws[k];
+    __syncthreads();
+    return tot;
+}
+
+__device__ __forceinline__ double final_max(const double* partial, int n) {
+    __shared__ double ws[CF_RED_WARPS];
+    double s = 0.0;
+    for (int u = threadIdx.x; u < n; u += CF_RED_THREADS) s = fmax(s, __ldcg(partial + u));
+    s = warp_max(s);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    double tot = ws[0];
+#pragma unroll
+    for (int k = 1; k < CF_RED_WARPS; ++k) tot = fmax(tot, ws[k]);
+    __syncthreads();
+    return tot;
+}
+
+// Wall-adjacency bits of cell (gi, gj); periodic axes have no walls.
+__device__ __forceinline__ int edge_bits(int gi, int gj, int nx, int ny, int per_x, int per_y) {
+    int b = 0;
+    if (!per_x) b |= (gi == 0 ? 1 : 0) | (gi == nx - 1 ? 2 : 0);
+    if (!per_y) b |= (gj == 0 ? 4 : 0) | (gj == ny - 1 ? 8 : 0);
+    return b;
+}
+
+// Wrap an index along a periodic axis; returns -1 outside a wall axis.
+__device__ __forceinline__ int wrap_index(int g, int n, int per) {
+    if (g >= 0 && g < n) return g;
+    if (!per) return -1;
+    g %= n;
+    return g < 0 ? g + n : g;
+}
+
+}  // namespace cf
+
+// Launch helpers implemented in the .cu files (called by cf_api.cu).
+namespace cf {
+struct Ctx;
+}

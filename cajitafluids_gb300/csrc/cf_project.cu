@@ -1,0 +1,971 @@
+// Pressure projection: VelocityCorrector::correctVelocity
+// (src/VelocityCorrector.hpp:182-282) on one GPU.
+//
+//   divergence + CG init  (_buildRHS, :182-212, cold start :272)
+//   Jacobi-PCG            (Cajita ReferenceConjugateGradient, restated;
+//                          matrix :116-144 + BoundaryConditions.hpp:57-97,
+//                          Jacobi :158-180)
+//   gradient subtraction  (_applyPressure, :214-264, quirk Q1 at :260)
+//
+// The matrix is never stored: the diagonal and 1/diagonal are looked up
+// from a 16-entry table indexed by the cell's wall-adjacency bits, and the
+// legs are -scale.  Scalars (alpha, beta, norms, status) stay on the device;
+// the last block of each reduction kernel finishes the sum in a fixed order
+// and advances the solver state, so the host only polls the status between
+// CUDA-graph batches of iterations.
+//
+// FP64 CG per iteration (two kernels, 80 bytes per cell moved):
+//   K1  p <- M^-1 r + beta p ; q <- A p ; partial p.q       (R r, p_old; W p_new, q)
+//   K2  x += alpha p ; r -= alpha q ; partial r.z, r.r      (R x, p, r, q; W x, r)
+// p ping-pongs between two buffers because K1 recomputes the new direction
+// on its halo from the old one.
+//
+// Mixed precision: inner Jacobi-PCG on FP32 vectors (e, r, p) with FP64
+// scalars, 32 bytes per cell per iteration (A p is recomputed in K2 instead
+// of stored); the FP64 outer loop forms r = b - A x in FP64 and restarts the
+// inner solve on it until the FP64 residual meets the tolerance.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "cf_ctx.cuh"
+
+namespace cf {
+
+#define FULLMASK 0xffffffffu
+
+struct Cg64 {
+    int nx, ny, per_x, per_y, G, U, pitch;
+    Stencil st;
+    double *x, *r, *pa, *pb, *qv;
+    double *part0, *part1;
+    SolverState* S;
+};
+
+__device__ __forceinline__ int ebits(const Cg64& a, int c, int j) {
+    return edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y);
+}
+
+__device__ __forceinline__ bool converged(const SolverState* S, double rr) {
+    return rr <= S->tol2 * S->bb || (S->use_abs && rr * S->area <= S->abs2);
+}
+
+// new search direction at one cell (0 outside a wall)
+__device__ __forceinline__ double pn1(const Cg64& a, const double* pold, int c, int j, bool first, double beta) {
+    int cc = wrap_index(c, a.nx, a.per_x), jj = wrap_index(j, a.ny, a.per_y);
+    if (cc < 0 || jj < 0) return 0.0;
+    size_t k = (size_t)jj * a.pitch + cc;
+    double z = a.st.minv[ebits(a, cc, jj)] * __ldg(a.r + k);
+    return first ? z : fma(beta, __ldg(pold + k), z);
+}
+
+// new search direction at columns c0, c0+1 of row j
+__device__ __forceinline__ double2 pn2(const Cg64& a, const double* pold, int c0, int j, bool first, double beta) {
+    int jj = wrap_index(j, a.ny, a.per_y);
+    if (jj < 0) return make_double2(0.0, 0.0);
+    if (c0 + 1 < a.nx) {
+        size_t k = (size_t)jj * a.pitch + c0;
+        double2 rv = __ldg(reinterpret_cast<const double2*>(a.r + k));
+        double z0 = a.st.minv[ebits(a, c0, jj)] * rv.x;
+        double z1 = a.st.minv[ebits(a, c0 + 1, jj)] * rv.y;
+        if (first) return make_double2(z0, z1);
+        double2 po = __ldg(reinterpret_cast<const double2*>(pold + k));
+        return make_double2(fma(beta, po.x, z0), fma(beta, po.y, z1));
+    }
+    return make_double2(pn1(a, pold, c0, jj, first, beta), pn1(a, pold, c0 + 1, jj, first, beta));
+}
+
+// K1: direction update + stencil apply + partial p.q
+__global__ void __launch_bounds__(CF_RED_THREADS) k_cg_dir_matvec64(Cg64 a) {
+    SolverState* S = a.S;
+    if (*(volatile int*)&S->status != ST_RUNNING) return;
+    const int it = S->iter;
+    const bool first = it == 0;
+    const double beta = S->beta;
+    const double* pold = (it & 1) ? a.pb : a.pa;
+    double* pnew = (it & 1) ? a.pa : a.pb;
+    const double ms = a.st.ms;
+    const int lane = threadIdx.x & 31;
+    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
+    double acc = 0.0;
+    if (unit < a.U) {
+        const int g = unit % a.G, band = unit / a.G;
+        const int c0 = g * CF_UNIT_COLS + 2 * lane;
+        const int j0 = band * CF_BAND_ROWS;
+        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
+        double2 pm = pn2(a, pold, c0, j0 - 1, first, beta);
+        double2 pc = pn2(a, pold, c0, j0, first, beta);
+        for (int j = j0; j < j1; ++j) {
+            double2 pp = pn2(a, pold, c0, j + 1, first, beta);
+            double left = __shfl_up_sync(FULLMASK, pc.y, 1);
+            double right = __shfl_down_sync(FULLMASK, pc.x, 1);
+            if (lane == 0) left = pn1(a, pold, c0 - 1, j, first, beta);
+            if (lane == 31) right = pn1(a, pold, c0 + 2, j, first, beta);
+            if (c0 < a.nx) {
+                size_t k = (size_t)j * a.pitch + c0;
+                double q0 = a.st.diag[ebits(a, c0, j)] * pc.x;
+                q0 = fma(ms, left, q0);
+                q0 = fma(ms, pc.y, q0);
+                q0 = fma(ms, pm.x, q0);
+                q0 = fma(ms, pp.x, q0);
+                acc = fma(pc.x, q0, acc);
+                if (c0 + 1 < a.nx) {
+                    double q1 = a.st.diag[ebits(a, c0 + 1, j)] * pc.y;
+                    q1 = fma(ms, pc.x, q1);
+                    q1 = fma(ms, right, q1);
+                    q1 = fma(ms, pm.y, q1);
+                    q1 = fma(ms, pp.y, q1);
+                    acc = fma(pc.y, q1, acc);
+                    *reinterpret_cast<double2*>(pnew + k) = pc;
+                    *reinterpret_cast<double2*>(a.qv + k) = make_double2(q0, q1);
+                } else {
+                    pnew[k] = pc.x;
+                    a.qv[k] = q0;
+                }
+            }
+            pm = pc;
+            pc = pp;
+        }
+    }
+    acc = warp_fold(acc);
+    if (unit < a.U && lane == 0) a.part0[unit] = acc;
+    if (last_block_arrive(&S->ticket[0])) {
+        double pq = final_tree(a.part0, a.U);
+        if (threadIdx.x == 0) {
+            S->ticket[0] = 0;
+            if (!(pq > 0.0))
+                S->status = isnan(pq) ? ST_NAN : ST_BREAKDOWN;
+            else
+                S->alpha = S->rho / pq;
+        }
+    }
+}
+
+// K2: solution / residual update + partial r.z and r.r
+__global__ void __launch_bounds__(CF_RED_THREADS) k_cg_update64(Cg64 a) {
+    SolverState* S = a.S;
+    if (*(volatile int*)&S->status != ST_RUNNING) return;
+    const int it = S->iter;
+    const double* pv = (it & 1) ? a.pa : a.pb;
+    const double alpha = S->alpha, malpha = -alpha;
+    const int lane = threadIdx.x & 31;
+    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
+    double arz = 0.0, arr = 0.0;
+    if (unit < a.U) {
+        const int g = unit % a.G, band = unit / a.G;
+        const int c0 = g * CF_UNIT_COLS + 2 * lane;
+        const int j0 = band * CF_BAND_ROWS;
+        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
+        if (c0 + 1 < a.nx) {
+            for (int j = j0; j < j1; ++j) {
+                size_t k = (size_t)j * a.pitch + c0;
+                double2 xv = *reinterpret_cast<const double2*>(a.x + k);
+                double2 p2 = __ldg(reinterpret_cast<const double2*>(pv + k));
+                double2 rv = *reinterpret_cast<const double2*>(a.r + k);
+                double2 qv = __ldg(reinterpret_cast<const double2*>(a.qv + k));
+                xv.x = fma(alpha, p2.x, xv.x);
+                xv.y = fma(alpha, p2.y, xv.y);
+                rv.x = fma(malpha, qv.x, rv.x);
+                rv.y = fma(malpha, qv.y, rv.y);
+                double z0 = a.st.minv[ebits(a, c0, j)] * rv.x;
+                double z1 = a.st.minv[ebits(a, c0 + 1, j)] * rv.y;
+                arz = fma(rv.x, z0, arz);
+                arr = fma(rv.x, rv.x, arr);
+                arz = fma(rv.y, z1, arz);
+                arr = fma(rv.y, rv.y, arr);
+                *reinterpret_cast<double2*>(a.x + k) = xv;
+                *reinterpret_cast<double2*>(a.r + k) = rv;
+            }
+        } else if (c0 < a.nx) {
+            for (int j = j0; j < j1; ++j) {
+                size_t k = (size_t)j * a.pitch + c0;
+                double xv = fma(alpha, pv[k], a.x[k]);
+                double rv = fma(malpha, a.qv[k], a.r[k]);
+                double z0 = a.st.minv[ebits(a, c0, j)] * rv;
+                arz = fma(rv, z0, arz);
+                arr = fma(rv, rv, arr);
+                a.x[k] = xv;
+                a.r[k] = rv;
+            }
+        }
+    }
+    arz = warp_fold(arz);
+    arr = warp_fold(arr);
+    if (unit < a.U && lane == 0) {
+        a.part0[unit] = arz;
+        a.part1[unit] = arr;
+    }
+    if (last_block_arrive(&S->ticket[1])) {
+        double rz = final_tree(a.part0, a.U);
+        double rr = final_tree(a.part1, a.U);
+        if (threadIdx.x == 0) {
+            S->ticket[1] = 0;
+            S->beta = rz / S->rho;
+            S->rho = rz;
+            S->rr = rr;
+            S->iter = it + 1;
+            if (isnan(rr))
+                S->status = ST_NAN;
+            else if (converged(S, rr))
+                S->status = ST_CONVERGED;
+            else if (it + 1 >= S->max_iter)
+                S->status = ST_MAXIT;
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// Divergence: b = -(1/dx) (u(i+1) - u(i) + v(j+1) - v(j))  (:204-210)
+struct DivArgs {
+    int nx, ny, per_x, per_y, G, U, pitch, pitch32;
+    Grid<double> u, v;
+    double mscale;  // -(1/dx)
+    Stencil st;
+    double *x, *r, *b;
+    float *r32, *e32;
+    double *part0, *part1, *part2;
+    double* out;
+    SolverState* S;
+};
+
+__device__ __forceinline__ double div_b(const DivArgs& a, int gi, int gj) {
+    int ie = gi + 1, jn = gj + 1;
+    if (a.per_x && ie == a.nx) ie = 0;
+    if (a.per_y && jn == a.ny) jn = 0;
+    double u0 = a.u.at(gi + CF_HALO, gj + CF_HALO), u1 = a.u.at(ie + CF_HALO, gj + CF_HALO);
+    double v0 = a.v.at(gi + CF_HALO, gj + CF_HALO), v1 = a.v.at(gi + CF_HALO, jn + CF_HALO);
+    double t = u1 - u0;
+    t = t + v1;
+    t = t - v0;
+    return a.mscale * t;
+}
+
+// FP64 init: b, r = b, x = 0, partial r.z and r.r
+__global__ void __launch_bounds__(CF_RED_THREADS) k_div_init64(DivArgs a) {
+    SolverState* S = a.S;
+    const int lane = threadIdx.x & 31;
+    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
+    double arz = 0.0, arr = 0.0;
+    if (unit < a.U) {
+        const int g = unit % a.G, band = unit / a.G;
+        const int c0 = g * CF_UNIT_COLS + 2 * lane;
+        const int j0 = band * CF_BAND_ROWS;
+        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
+        for (int j = j0; j < j1; ++j)
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                int c = c0 + s;
+                if (c >= a.nx) continue;
+                double b = div_b(a, c, j);
+                size_t k = (size_t)j * a.pitch + c;
+                a.r[k] = b;
+                a.x[k] = 0.0;
+                double z = a.st.minv[edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y)] * b;
+                arz = fma(b, z, arz);
+                arr = fma(b, b, arr);
+            }
+    }
+    arz = warp_fold(arz);
+    arr = warp_fold(arr);
+    if (unit < a.U && lane == 0) {
+        a.part0[unit] = arz;
+        a.part1[unit] = arr;
+    }
+    if (last_block_arrive(&S->ticket[2])) {
+        double rz = final_tree(a.part0, a.U);
+        double rr = final_tree(a.part1, a.U);
+        if (threadIdx.x == 0) {
+            S->ticket[2] = 0;
+            S->bb = rr;
+            S->rr = rr;
+            S->rho = rz;
+            S->beta = 0.0;
+            S->iter = 0;
+            if (rr == 0.0 || converged(S, rr))
+                S->status = ST_CONVERGED;
+            else if (S->max_iter <= 0)
+                S->status = ST_MAXIT;
+            else if (isnan(rr))
+                S->status = ST_NAN;
+            else
+                S->status = ST_RUNNING;
+        }
+    }
+}
+
+// Mixed init: b (FP64, kept for the outer residual), x = 0, inner r = (float)b,
+// e = 0; partial b.b (FP64), inner r.z and r.r (FP32 per lane, FP64 beyond).
+__global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
+    SolverState* S = a.S;
+    const int lane = threadIdx.x & 31;
+    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
+    double abb = 0.0;
+    float arz = 0.f, arr = 0.f;
+    if (unit < a.U) {
+        const int g = unit % a.G, band = unit / a.G;
+        const int c0 = g * CF_UNIT_COLS + 2 * lane;
+        const int j0 = band * CF_BAND_ROWS;
+        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
+        for (int j = j0; j < j1; ++j)
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                int c = c0 + s;
+                if (c >= a.nx) continue;
+                double b = div_b(a, c, j);
+                size_t k = (size_t)j * a.pitch + c;
+                size_t k32 = (size_t)j * a.pitch32 + c;
+                a.b[k] = b;
+                a.x[k] = 0.0;
+                float r = (float)b;
+                a.r32[k32] = r;
+                a.e32[k32] = 0.f;
+                float z = a.st.minv32[edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y)] * r;
+                abb = fma(b, b, abb);
+                arz = fmaf(r, z, arz);
+                arr = fmaf(r, r, arr);
+            }
+    }
+    abb = warp_fold(abb);
+    double drz = warp_fold((double)arz), drr = warp_fold((double)arr);
+    if (unit < a.U && lane == 0) {
+        a.part0[unit] = abb;
+        a.part1[unit] = drz;
+        a.part2[unit] = drr;
+    }
+    if (last_block_arrive(&S->ticket[2])) {
+        double bb = final_tree(a.part0, a.U);
+        double rz = final_tree(a.part1, a.U);
+        double rr = final_tree(a.part2, a.U);
+        if (threadIdx.x == 0) {
+            S->ticket[2] = 0;
+            S->bb = bb;
+            S->rr = bb;
+            S->rr_out = bb;
+            S->rho_in = rz;
+            S->rr_in0 = rr;
+            S->rr_in = rr;
+            S->beta_in = 0.0;
+            S->iter = 0;
+            S->inner_iter = 0;
+            S->outer_iter = 0;
+            S->target2 = S->tol2 * bb;
+            if (S->use_abs) S->target2 = fmax(S->target2, S->abs2 / S->area);
+            S->tau2 = fmax(S->inner_tol2, 0.25 * S->target2 / bb);
+            if (bb == 0.0 || converged(S, bb))
+                S->status = ST_CONVERGED;
+            else if (isnan(bb))
+                S->status = ST_NAN;
+            else if (S->max_iter <= 0)
+                S->status = ST_MAXIT;
+            else
+                S->status = ST_RUNNING;
+            S->inner_status = ST_RUNNING;
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// Mixed inner solve (FP32 vectors).
+struct Cg32 {
+    int nx, ny, per_x, per_y, G, U, pitch;
+    Stencil st;
+    float *e, *r, *pa, *pb;
+    double *part0, *part1;
+    SolverState* S;
+};
+
+__device__ __forceinline__ int ebits32(const Cg32& a, int c, int j) {
+    return edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y);
+}
+
+__device__ __forceinline__ float pn1f(const Cg32& a, const float* pold, int c, int j, bool first, float beta) {
+    int cc = wrap_index(c, a.nx, a.per_x), jj = wrap_index(j, a.ny, a.per_y);
+    if (cc < 0 || jj < 0) return 0.f;
+    size_t k = (size_t)jj * a.pitch + cc;
+    float z = a.st.minv32[ebits32(a, cc, jj)] * __ldg(a.r + k);
+    return first ? z : fmaf(beta, __ldg(pold + k), z);
+}
+
+__device__ __forceinline__ float2 pn2f(const Cg32& a, const float* pold, int c0, int j, bool first, float beta) {
+    int jj = wrap_index(j, a.ny, a.per_y);
+    if (jj < 0) return make_float2(0.f, 0.f);
+    if (c0 + 1 < a.nx) {
+        size_t k = (size_t)jj * a.pitch + c0;
+        float2 rv = __ldg(reinterpret_cast<const float2*>(a.r + k));
+        float z0 = a.st.minv32[ebits32(a, c0, jj)] * rv.x;
+        float z1 = a.st.minv32[ebits32(a, c0 + 1, jj)] * rv.y;
+        if (first) return make_float2(z0, z1);
+        float2 po = __ldg(reinterpret_cast<const float2*>(pold + k));
+        return make_float2(fmaf(beta, po.x, z0), fmaf(beta, po.y, z1));
+    }
+    return make_float2(pn1f(a, pold, c0, jj, first, beta), pn1f(a, pold, c0 + 1, jj, first, beta));
+}
+
+// plain read of the (final) direction at one cell / two cells
+__device__ __forceinline__ float p1f(const Cg32& a, const float* p, int c, int j) {
+    int cc = wrap_index(c, a.nx, a.per_x), jj = wrap_index(j, a.ny, a.per_y);
+    if (cc < 0 || jj < 0) return 0.f;
+    return __ldg(p + (size_t)jj * a.pitch + cc);
+}
+
+__device__ __forceinline__ float2 p2f(const Cg32& a, const float* p, int c0, int j) {
+    int jj = wrap_index(j, a.ny, a.per_y);
+    if (jj < 0) return make_float2(0.f, 0.f);
+    if (c0 + 1 < a.nx) return __ldg(reinterpret_cast<const float2*>(p + (size_t)jj * a.pitch + c0));
+    return make_float2(p1f(a, p, c0, jj), p1f(a, p, c0 + 1, jj));
+}
+
+__device__ __forceinline__ float stencil32(const Cg32& a, int c, int j, float pc, float w, float e, float s,
+                                           float n) {
+    float q = a.st.diag32[ebits32(a, c, j)] * pc;
+    q = fmaf(a.st.ms32, w, q);
+    q = fmaf(a.st.ms32, e, q);
+    q = fmaf(a.st.ms32, s, q);
+    q = fmaf(a.st.ms32, n, q);
+    return q;
+}
+
+__device__ __forceinline__ bool inner_running(const SolverState* S) {
+    return *(volatile const int*)&S->status == ST_RUNNING &&
+           *(volatile const int*)&S->inner_status == ST_RUNNING;
+}
+
+__global__ void __launch_bounds__(CF_RED_THREADS) k_in_dir_matvec32(Cg32 a) {
+    SolverState* S = a.S;
+    if (!inner_running(S)) return;
+    const int it = S->inner_iter;
+    const bool first = it == 0;
+    const float beta = (float)S->beta_in;
+    const float* pold = (it & 1) ? a.pb : a.pa;
+    float* pnew = (it & 1) ? a.pa : a.pb;
+    const int lane = threadIdx.x & 31;
+    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
+    float acc = 0.f;
+    if (unit < a.U) {
+        const int g = unit % a.G, band = unit / a.G;
+        const int c0 = g * CF_UNIT_COLS + 2 * lane;
+        const int j0 = band * CF_BAND_ROWS;
+        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
+        float2 pm = pn2f(a, pold, c0, j0 - 1, first, beta);
+        float2 pc = pn2f(a, pold, c0, j0, first, beta);
+        for (int j = j0; j < j1; ++j) {
+            float2 pp = pn2f(a, pold, c0, j + 1, first, beta);
+            float left = __shfl_up_sync(FULLMASK, pc.y, 1);
+            float right = __shfl_down_sync(FULLMASK, pc.x, 1);
+            if (lane == 0) left = pn1f(a, pold, c0 - 1, j, first, beta);
+            if (lane == 31) right = pn1f(a, pold, c0 + 2, j, first, beta);
+            if (c0 < a.nx) {
+                size_t k = (size_t)j * a.pitch + c0;
+                float q0 = stencil32(a, c0, j, pc.x, left, pc.y, pm.x, pp.x);
+                acc = fmaf(pc.x, q0, acc);
+                if (c0 + 1 < a.nx) {
+                    float q1 = stencil32(a, c0 + 1, j, pc.y, pc.x, right, pm.y, pp.y);
+                    acc = fmaf(pc.y, q1, acc);
+                    *reinterpret_cast<float2*>(pnew + k) = pc;
+                } else {
+                    pnew[k] = pc.x;
+                }
+            }
+            pm = pc;
+            pc = pp;
+        }
+    }
+    double dacc = warp_fold((double)acc);
+    if (unit < a.U && lane == 0) a.part0[unit] = dacc;
+    if (last_block_arrive(&S->ticket[5])) {
+        double pq = final_tree(a.part0, a.U);
+        if (threadIdx.x == 0) {
+            S->ticket[5] = 0;
+            if (isnan(pq))
+                S->status = ST_NAN;
+            else if (!(pq > 0.0))
+                S->inner_status = ST_BREAKDOWN;  // FP32 noise floor: hand back to the outer loop
+            else
+                S->alpha_in = S->rho_in / pq;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(CF_RED_THREADS) k_in_update32(Cg32 a) {
+    SolverState* S = a.S;
+    if (!inner_running(S)) return;
+    const int it = S->inner_iter;
+    const float* pv = (it & 1) ? a.pa : a.pb;
+    const float alpha = (float)S->alpha_in, malpha = -alpha;
+    const int lane = threadIdx.x & 31;
+    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
+    float arz = 0.f, arr = 0.f;
+    if (unit < a.U) {
+        const int g = unit % a.G, band = unit / a.G;
+        const int c0 = g * CF_UNIT_COLS + 2 * lane;
+        const int j0 = band * CF_BAND_ROWS;
+        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
+        float2 pm = p2f(a, pv, c0, j0 - 1);
+        float2 pc = p2f(a, pv, c0, j0);
+        for (int j = j0; j < j1; ++j) {
+            float2 pp = p2f(a, pv, c0, j + 1);
+            float left = __shfl_up_sync(FULLMASK, pc.y, 1);
+            float right = __shfl_down_sync(FULLMASK, pc.x, 1);
+            if (lane == 0) left = p1f(a, pv, c0 - 1, j);
+            if (lane == 31) right = p1f(a, pv, c0 + 2, j);
+            if (c0 < a.nx) {
+                size_t k = (size_t)j * a.pitch + c0;
+                float q0 = stencil32(a, c0, j, pc.x, left, pc.y, pm.x, pp.x);
+                if (c0 + 1 < a.nx) {
+                    float q1 = stencil32(a, c0 + 1, j, pc.y, pc.x, right, pm.y, pp.y);
+                    float2 ev = *reinterpret_cast<const float2*>(a.e + k);
+                    float2 rv = *reinterpret_cast<const float2*>(a.r + k);
+                    ev.x = fmaf(alpha, pc.x, ev.x);
+                    ev.y = fmaf(alpha, pc.y, ev.y);
+                    rv.x = fmaf(malpha, q0, rv.x);
+                    rv.y = fmaf(malpha, q1, rv.y);
+                    float z0 = a.st.minv32[ebits32(a, c0, j)] * rv.x;
+                    float z1 = a.st.minv32[ebits32(a, c0 + 1, j)] * rv.y;
+                    arz = fmaf(rv.x, z0, arz);
+                    arr = fmaf(rv.x, rv.x, arr);
+                    arz = fmaf(rv.y, z1, arz);
+                    arr = fmaf(rv.y, rv.y, arr);
+                    *reinterpret_cast<float2*>(a.e + k) = ev;
+                    *reinterpret_cast<float2*>(a.r + k) = rv;
+                } else {
+                    float ev = fmaf(alpha, pc.x, a.e[k]);
+                    float rv = fmaf(malpha, q0, a.r[k]);
+                    float z0 = a.st.minv32[ebits32(a, c0, j)] * rv;
+                    arz = fmaf(rv, z0, arz);
+                    arr = fmaf(rv, rv, arr);
+                    a.e[k] = ev;
+                    a.r[k] = rv;
+                }
+            }
+            pm = pc;
+            pc = pp;
+        }
+    }
+    double drz = warp_fold((double)arz), drr = warp_fold((double)arr);
+    if (unit < a.U && lane == 0) {
+        a.part0[unit] = drz;
+        a.part1[unit] = drr;
+    }
+    if (last_block_arrive(&S->ticket[6])) {
+        double rz = final_tree(a.part0, a.U);
+        double rr = final_tree(a.part1, a.U);
+        if (threadIdx.x == 0) {
+            S->ticket[6] = 0;
+            S->beta_in = rz / S->rho_in;
+            S->rho_in = rz;
+            S->rr_in = rr;
+            S->inner_iter = it + 1;
+            S->iter = S->iter + 1;
+            if (isnan(rr))
+                S->status = ST_NAN;
+            else if (rr <= S->tau2 * S->rr_in0)
+                S->inner_status = ST_CONVERGED;
+            else if (S->iter >= S->max_iter)
+                S->inner_status = ST_MAXIT;
+        }
+    }
+}
+
+// Outer refinement, part 1: x += e (FP64 += FP32)
+__global__ void k_outer_add(double* x, const float* e, int nx, int ny, int pitch, int pitch32) {
+    int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    if (gi >= nx || gj >= ny) return;
+    size_t k = (size_t)gj * pitch + gi;
+    x[k] = x[k] + (double)e[(size_t)gj * pitch32 + gi];
+}
+
+// Outer refinement, part 2: r = b - A x in FP64; inner r = (float)r, e = 0.
+struct Outer {
+    int nx, ny, per_x, per_y, G, U, pitch, pitch32;
+    Stencil st;
+    const double *x, *b;
+    float *r32, *e32;
+    double *part0, *part1, *part2;
+    SolverState* S;
+};
+
+__device__ __forceinline__ double xval(const Outer& a, int c, int j) {
+    int cc = wrap_index(c, a.nx, a.per_x), jj = wrap_index(j, a.ny, a.per_y);
+    if (cc < 0 || jj < 0) return 0.0;
+    return a.x[(size_t)jj * a.pitch + cc];
+}
+
+__global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
+    SolverState* S = a.S;
+    const int lane = threadIdx.x & 31;
+    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
+    double arr64 = 0.0;
+    float arz = 0.f, arr = 0.f;
+    const double ms = a.st.ms;
+    if (unit < a.U) {
+        const int g = unit % a.G, band = unit / a.G;
+        const int c0 = g * CF_UNIT_COLS + 2 * lane;
+        const int j0 = band * CF_BAND_ROWS;
+        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
+        for (int j = j0; j < j1; ++j)
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                int c = c0 + s;
+                if (c >= a.nx) continue;
+                int eb = edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y);
+                double ax = a.st.diag[eb] * xval(a, c, j);
+                ax = fma(ms, xval(a, c - 1, j), ax);
+                ax = fma(ms, xval(a, c + 1, j), ax);
+                ax = fma(ms, xval(a, c, j - 1), ax);
+                ax = fma(ms, xval(a, c, j + 1), ax);
+                double r = a.b[(size_t)j * a.pitch + c] - ax;
+                arr64 = fma(r, r, arr64);
+                float r32 = (float)r;
+                size_t k32 = (size_t)j * a.pitch32 + c;
+                a.r32[k32] = r32;
+                a.e32[k32] = 0.f;
+                float z = a.st.minv32[eb] * r32;
+                arz = fmaf(r32, z, arz);
+                arr = fmaf(r32, r32, arr);
+            }
+    }
+    arr64 = warp_fold(arr64);
+    double drz = warp_fold((double)arz), drr = warp_fold((double)arr);
+    if (unit < a.U && lane == 0) {
+        a.part0[unit] = arr64;
+        a.part1[unit] = drz;
+        a.part2[unit] = drr;
+    }
+    if (last_block_arrive(&S->ticket[4])) {
+        double rr64 = final_tree(a.part0, a.U);
+        double rz = final_tree(a.part1, a.U);
+        double rr = final_tree(a.part2, a.U);
+        if (threadIdx.x == 0) {
+            S->ticket[4] = 0;
+            S->outer_iter += 1;
+            S->rr = rr64;
+            S->rr_out = rr64;
+            if (isnan(rr64))
+                S->status = ST_NAN;
+            else if (converged(S, rr64))
+                S->status = ST_CONVERGED;
+            else if (S->iter >= S->max_iter || S->outer_iter >= S->max_outer)
+                S->status = ST_MAXIT;
+            else {
+                S->rho_in = rz;
+                S->rr_in0 = rr;
+                S->rr_in = rr;
+                S->beta_in = 0.0;
+                S->inner_iter = 0;
+                S->inner_status = ST_RUNNING;
+                S->tau2 = fmax(S->inner_tol2, 0.25 * S->target2 / rr64);
+            }
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// _applyPressure (:214-264).  z = 0: I-faces, z = 1: J-faces.  Quirk Q1 (the
+// J-face wall condition lands on u, :260) zeroes u in row 0 (done in the
+// I-face pass, which owns u) and u's ghost row ny (done in the J-face pass).
+struct Press {
+    Phys p;
+    Grid<double> u, v;
+    const double* x;
+    int pitch;
+    double ms;  // -(dt / (density dx))
+};
+
+__device__ __forceinline__ double pval(const Press& a, int gi, int gj) {
+    int ci = wrap_index(gi, a.p.nx, a.p.per_x), cj = wrap_index(gj, a.p.ny, a.p.per_y);
+    if (ci < 0 || cj < 0) return 0.0;
+    return a.x[(size_t)cj * a.pitch + ci];
+}
+
+__global__ void k_apply_pressure(Press a) {
+    const Phys& p = a.p;
+    int axis = blockIdx.z;
+    int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    int ox = p.nx + ((axis == 0 && !p.per_x) ? 1 : 0);
+    int oy = p.ny + ((axis == 1 && !p.per_y) ? 1 : 0);
+    if (gi >= ox || gj >= oy) return;
+    const bool fix_q1 = (p.quirks & 1u) != 0;
+    if (axis == 0) {
+        double& u = a.u.at(gi + CF_HALO, gj + CF_HALO);
+        double d = pval(a, gi, gj) - pval(a, gi - 1, gj);
+        double w = fma(a.ms, d, u);
+        if (!p.per_x) {
+            if (gi <= 0 && p.bc[0] == 0) w = 0.0;
+            if (gi > p.nx - 1 && p.bc[2] == 0) w = 0.0;
+        }
+        if (!fix_q1 && !p.per_y && gj == 0 && gi < p.nx && p.bc[1] == 0) w = 0.0;
+        u = w;
+    } else {
+        double& v = a.v.at(gi + CF_HALO, gj + CF_HALO);
+        double d = pval(a, gi, gj) - pval(a, gi, gj - 1);
+        double w = fma(a.ms, d, v);
+        if (!p.per_y) {
+            if (fix_q1) {
+                if (gj <= 0 && p.bc[1] == 0) w = 0.0;
+                if (gj > p.ny - 1 && p.bc[3] == 0) w = 0.0;
+            } else if (gj > p.ny - 1 && p.bc[3] == 0) {
+                a.u.at(gi + CF_HALO, gj + CF_HALO) = 0.0;  // u ghost row ny
+            }
+        }
+        v = w;
+    }
+}
+
+// ||div u||: canonical sum of b^2 and max |b|
+__global__ void __launch_bounds__(CF_RED_THREADS) k_div_norms(DivArgs a) {
+    SolverState* S = a.S;
+    const int lane = threadIdx.x & 31;
+    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
+    double ass = 0.0, amx = 0.0;
+    if (unit < a.U) {
+        const int g = unit % a.G, band = unit / a.G;
+        const int c0 = g * CF_UNIT_COLS + 2 * lane;
+        const int j0 = band * CF_BAND_ROWS;
+        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
+        for (int j = j0; j < j1; ++j)
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                int c = c0 + s;
+                if (c >= a.nx) continue;
+                double b = div_b(a, c, j);
+                ass = fma(b, b, ass);
+                amx = fmax(amx, fabs(b));
+            }
+    }
+    ass = warp_fold(ass);
+    amx = warp_max(amx);
+    if (unit < a.U && lane == 0) {
+        a.part0[unit] = ass;
+        a.part1[unit] = amx;
+    }
+    if (last_block_arrive(&S->ticket[3])) {
+        double ss = final_tree(a.part0, a.U);
+        double mx = final_max(a.part1, a.U);
+        if (threadIdx.x == 0) {
+            S->ticket[3] = 0;
+            a.out[0] = ss;
+            a.out[1] = mx;
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// host side
+static DivArgs div_args(cf_ctx* c, const Stencil& st) {
+    DivArgs a{};
+    a.nx = c->ph.nx;
+    a.ny = c->ph.ny;
+    a.per_x = c->ph.per_x;
+    a.per_y = c->ph.per_y;
+    a.G = c->G;
+    a.U = c->n_units;
+    a.pitch = c->vpitch;
+    a.pitch32 = c->vpitch;
+    a.u = c->u[c->cur];
+    a.v = c->v[c->cur];
+    a.mscale = -(1.0 / c->ph.dx);
+    a.st = st;
+    a.x = c->x.a;
+    a.r = c->r.a;
+    a.b = c->b.a;
+    a.r32 = c->r32.a;
+    a.e32 = c->e32.a;
+    a.part0 = c->partials;
+    a.part1 = c->partials + c->n_units;
+    a.part2 = c->partials + 2 * c->n_units;
+    a.out = c->d_out;
+    a.S = c->S;
+    return a;
+}
+
+static Cg64 cg64_args(cf_ctx* c, const Stencil& st) {
+    Cg64 a{};
+    a.nx = c->ph.nx;
+    a.ny = c->ph.ny;
+    a.per_x = c->ph.per_x;
+    a.per_y = c->ph.per_y;
+    a.G = c->G;
+    a.U = c->n_units;
+    a.pitch = c->vpitch;
+    a.st = st;
+    a.x = c->x.a;
+    a.r = c->r.a;
+    a.pa = c->pa.a;
+    a.pb = c->pb.a;
+    a.qv = c->qv.a;
+    a.part0 = c->partials;
+    a.part1 = c->partials + c->n_units;
+    a.S = c->S;
+    return a;
+}
+
+static Cg32 cg32_args(cf_ctx* c, const Stencil& st) {
+    Cg32 a{};
+    a.nx = c->ph.nx;
+    a.ny = c->ph.ny;
+    a.per_x = c->ph.per_x;
+    a.per_y = c->ph.per_y;
+    a.G = c->G;
+    a.U = c->n_units;
+    a.pitch = c->vpitch;
+    a.st = st;
+    a.e = c->e32.a;
+    a.r = c->r32.a;
+    a.pa = c->pa32.a;
+    a.pb = c->pb32.a;
+    a.part0 = c->partials;
+    a.part1 = c->partials + c->n_units;
+    a.S = c->S;
+    return a;
+}
+
+static int red_blocks(const cf_ctx* c) { return (c->n_units + CF_RED_WARPS - 1) / CF_RED_WARPS; }
+
+static const int kBatch = 32;  // CG iterations per graph launch
+
+// Build (or reuse) the graph of kBatch iterations for the current stencil.
+static int ensure_graph(cf_ctx* c, const Stencil& st, bool mixed) {
+    cudaGraphExec_t& ge = mixed ? c->g32 : c->g64;
+    Stencil& key = mixed ? c->g32_st : c->g64_st;
+    if (ge && std::memcmp(&key, &st, sizeof(Stencil)) == 0) return CF_OK;
+    if (ge) {
+        cudaGraphExecDestroy(ge);
+        ge = nullptr;
+    }
+    cudaGraph_t g;
+    int rc = cuda_check(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "capture begin");
+    if (rc) return rc;
+    int nb = red_blocks(c);
+    if (mixed) {
+        Cg32 a = cg32_args(c, st);
+        for (int i = 0; i < kBatch; ++i) {
+            k_in_dir_matvec32<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
+            k_in_update32<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
+        }
+    } else {
+        Cg64 a = cg64_args(c, st);
+        for (int i = 0; i < kBatch; ++i) {
+            k_cg_dir_matvec64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
+            k_cg_update64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
+        }
+    }
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if ((rc = cuda_check(c, e, "capture end"))) return rc;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if ((rc = cuda_check(c, e, "graph instantiate"))) return rc;
+    key = st;
+    return CF_OK;
+}
+
+static int read_state(cf_ctx* c) {
+    cudaMemcpyAsync(c->hS, c->S, sizeof(SolverState), cudaMemcpyDeviceToHost, c->stream);
+    return cuda_check(c, cudaStreamSynchronize(c->stream), "solver state read");
+}
+
+int div_norms(cf_ctx* c, double* l2, double* linf) {
+    Stencil st{};
+    DivArgs a = div_args(c, st);
+    k_div_norms<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(a);
+    c->launches += 1;
+    cudaMemcpyAsync(c->h_out, c->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    int rc = cuda_check(c, cudaStreamSynchronize(c->stream), "div norms");
+    if (rc) return rc;
+    *l2 = sqrt(c->h_out[0]) * c->ph.dx;
+    *linf = c->h_out[1];
+    return CF_OK;
+}
+
+int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res) {
+    Stencil st;
+    build_stencil(c, dt, o.precon_none, &st);
+    const bool mixed = c->precision == CF_PREC_MIXED;
+    int rc = ensure_graph(c, st, mixed);
+    if (rc) return rc;
+
+    // solver parameters
+    SolverState* h = c->hS;
+    memset(h, 0, sizeof(SolverState));
+    h->tol2 = o.tol * o.tol;
+    h->abs2 = o.abs_tol * o.abs_tol;
+    h->use_abs = o.abs_tol > 0.0 ? 1 : 0;
+    h->area = c->ph.dx * c->ph.dx;
+    h->max_iter = o.max_iter;
+    h->max_outer = o.max_outer;
+    h->inner_tol2 = o.inner_tol * o.inner_tol;
+    h->status = ST_RUNNING;
+    cudaMemcpyAsync(c->S, h, sizeof(SolverState), cudaMemcpyHostToDevice, c->stream);
+    int nb = red_blocks(c);
+    DivArgs da = div_args(c, st);
+    if (!mixed) {
+        k_div_init64<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
+        c->launches += 1;
+        int max_launch = o.max_iter / kBatch + 3;
+        for (int l = 0;; ++l) {
+            if ((rc = read_state(c))) return rc;
+            if (c->hS->status != ST_RUNNING) break;
+            if (l >= max_launch) return fail(c, CF_ERR_NUMERIC, "solver did not stop after %d batches", l);
+            if ((rc = cuda_check(c, cudaGraphLaunch(c->g64, c->stream), "graph launch"))) return rc;
+            c->launches += 2 * kBatch;
+        }
+    } else {
+        k_div_init_mixed<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
+        c->launches += 1;
+        if ((rc = read_state(c))) return rc;
+        Outer oa{};
+        oa.nx = c->ph.nx;
+        oa.ny = c->ph.ny;
+        oa.per_x = c->ph.per_x;
+        oa.per_y = c->ph.per_y;
+        oa.G = c->G;
+        oa.U = c->n_units;
+        oa.pitch = c->vpitch;
+        oa.pitch32 = c->vpitch;
+        oa.st = st;
+        oa.x = c->x.a;
+        oa.b = c->b.a;
+        oa.r32 = c->r32.a;
+        oa.e32 = c->e32.a;
+        oa.part0 = c->partials;
+        oa.part1 = c->partials + c->n_units;
+        oa.part2 = c->partials + 2 * c->n_units;
+        oa.S = c->S;
+        dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
+        int max_launch = o.max_iter / kBatch + 3 * (o.max_outer + 1);
+        int launches = 0;
+        while (c->hS->status == ST_RUNNING) {
+            while (c->hS->status == ST_RUNNING && c->hS->inner_status == ST_RUNNING) {
+                if (++launches > max_launch) return fail(c, CF_ERR_NUMERIC, "mixed solver did not stop");
+                if ((rc = cuda_check(c, cudaGraphLaunch(c->g32, c->stream), "graph launch"))) return rc;
+                c->launches += 2 * kBatch;
+                if ((rc = read_state(c))) return rc;
+            }
+            if (c->hS->status != ST_RUNNING) break;
+            k_outer_add<<<grd, blk, 0, c->stream>>>(c->x.a, c->e32.a, c->ph.nx, c->ph.ny, c->vpitch, c->vpitch);
+            k_outer_resid<<<nb, CF_RED_THREADS, 0, c->stream>>>(oa);
+            c->launches += 2;
+            if ((rc = read_state(c))) return rc;
+            if (++launches > max_launch) return fail(c, CF_ERR_NUMERIC, "mixed solver did not stop");
+        }
+    }
+    const SolverState* hs = c->hS;
+    res->iterations = hs->iter;
+    res->outer = hs->outer_iter;
+    res->status = hs->status == ST_RUNNING ? ST_MAXIT : hs->status;
+    res->bb = hs->bb;
+    res->rr = hs->rr;
+
+    // gradient subtraction
+    Press pa{c->ph, c->u[c->cur], c->v[c->cur], c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx))};
+    dim3 blk(32, 8), grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
+    k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
+    c->launches += 1;
+    if ((rc = cuda_check(c, cudaGetLastError(), "apply pressure"))) return rc;
+    return div_norms(c, &res->div_l2, &res->div_linf);
+}
+
+}  // namespace cf

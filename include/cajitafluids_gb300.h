@@ -1,0 +1,190 @@
+/*
+ * cajitafluids_gb300: C ABI of the GB300-native per-timestep hot path of
+ * cajitafluids (RK3 semi-Lagrangian advection, inputs/boundary conditions,
+ * pressure projection with a matrix-free Jacobi-PCG Poisson solve).
+ *
+ * Conventions
+ *   - Every function returns int: CF_OK (0) or a negative CF_ERR_* code.
+ *     cf_last_error(ctx) describes the last failure on that context.
+ *   - No C++ exception crosses this boundary.
+ *   - One CUDA stream per context.  Calls on one context are not
+ *     thread-safe; distinct contexts are independent.
+ *   - All device memory is owned by the context.  Host pointers passed in
+ *     are read or written only during the call; every call that touches
+ *     host memory returns after the copy has completed.
+ *   - Field values are addressed by GLOBAL entity index (gi, gj) of the
+ *     owned region, with element (gi, gj) at base[gi * stride_i +
+ *     gj * stride_j] (strides in elements), so both Kokkos LayoutLeft and
+ *     LayoutRight host mirrors can be passed without a copy.
+ *
+ * Reference interfaces replaced (paths inside CUP-ECS/cajitafluids):
+ *   SolverBase / Solver<2>            src/Solver.hpp:41-48, 55-279
+ *   TimeIntegrator::step / advect     src/TimeIntegrator.hpp:81-177
+ *   Interpolation::interpolate*       src/Interpolation.hpp:30-54
+ *   VelocityCorrectorBase             src/VelocityCorrector.hpp:37-42,
+ *     + createVelocityCorrector        src/VelocityCorrector.hpp:297-339
+ *   Solver::_addInputs + POD functors src/Solver.hpp:181-263,
+ *     BoundaryCondition<2>            src/BoundaryConditions.hpp:50-135
+ *     InflowSource<2>                 src/InflowSource.hpp:30-98
+ *     BodyForce<2>                    src/BodyForce.hpp:30-69
+ *   ProblemManager get/advance/gather src/ProblemManager.hpp:281-403
+ *   Mesh geometry                     src/Mesh.hpp:41-103, 119-134
+ */
+#ifndef CAJITAFLUIDS_GB300_H
+#define CAJITAFLUIDS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CF_ABI_VERSION 1
+
+/* return codes */
+#define CF_OK 0
+#define CF_ERR_INVALID (-1)       /* bad argument (null handle, bad size, ...) */
+#define CF_ERR_CUDA (-2)          /* a CUDA runtime call failed */
+#define CF_ERR_UNSUPPORTED (-3)   /* valid request that this build does not implement */
+#define CF_ERR_NOT_CONVERGED (-4) /* solver stopped at max_iter; state is consistent */
+#define CF_ERR_NUMERIC (-5)       /* NaN/Inf or CG breakdown; state is consistent */
+#define CF_ERR_NOMEM (-6)         /* device allocation failed */
+#define CF_ERR_MESH (-7)          /* extent not evenly divisible (src/Mesh.hpp:478-486) */
+
+/* fields */
+#define CF_FIELD_QUANTITY 0 /* cell-centred advected scalar          */
+#define CF_FIELD_U 1        /* x-velocity on I-faces                 */
+#define CF_FIELD_V 2        /* y-velocity on J-faces                 */
+#define CF_FIELD_PRESSURE 3 /* last projection's pressure (cells)    */
+
+/* boundary types (src/BoundaryConditions.hpp:30-37) */
+#define CF_BC_SOLID 0
+#define CF_BC_FREE 1
+
+/* precision of a context */
+#define CF_PREC_FP64 0  /* all arithmetic and storage in FP64 */
+#define CF_PREC_MIXED 1 /* FP32 advection + inner PCG, FP64 outer refinement */
+
+/* quirk switches (default 0 = reproduce the reference) */
+#define CF_FIX_Q1 1u /* apply the J-face wall condition to v after projection
+                        (reference applies it to u: VelocityCorrector.hpp:260) */
+#define CF_FIX_Q3 2u /* RK3 x2 stage uses v1 (Ralston) instead of v0
+                        (reference: TimeIntegrator.hpp:57-58) */
+
+/* solver status codes (cf_solve_stats.status) */
+#define CF_SOLVE_CONVERGED 0
+#define CF_SOLVE_MAX_ITER 1
+#define CF_SOLVE_BREAKDOWN 2
+#define CF_SOLVE_NAN 3
+
+typedef struct cf_ctx cf_ctx;
+
+/* Mesh + storage description (src/Mesh.hpp:41-103; the reference hard-codes
+ * periodic = false, :85-87; periodic axes are an extension). */
+typedef struct {
+    int nx, ny;          /* global cells per axis */
+    double lo[2], hi[2]; /* global bounding box (x0, y0), (x1, y1) */
+    int periodic[2];
+    int precision;       /* CF_PREC_FP64 or CF_PREC_MIXED */
+    int device;          /* CUDA device ordinal */
+} cf_grid_desc;
+
+/* Pressure-solver options (src/VelocityCorrector.hpp:96-106, 297-339).
+ * solver: "Reference" or "PCG" (both run the GPU Jacobi-PCG); other HYPRE
+ * solver names return CF_ERR_UNSUPPORTED.
+ * precon: "Jacobi", "Diagonal" (same), "None" or "none" (unpreconditioned
+ * is not implemented: CF_ERR_UNSUPPORTED), "PFMG"/"SMG" -> CF_ERR_UNSUPPORTED.
+ * Convergence: ||r||_2 <= tol * ||b||_2, or, when abs_tol > 0,
+ * ||div u||_L2 = ||r||_2 * dx <= abs_tol.  The reference hard-codes
+ * tol 1e-6 and max_iter 2000 (:103-104). */
+typedef struct {
+    const char* solver;
+    const char* precon;
+    double tol;
+    double abs_tol;
+    int max_iter;        /* FP64 CG iterations, or total inner iterations (mixed) */
+    double inner_tol;    /* mixed: relative reduction per inner solve (0 = 1e-4) */
+    int max_outer;       /* mixed: outer refinement limit (0 = 30) */
+} cf_solver_opts;
+
+typedef struct {
+    int iterations;       /* CG iterations (mixed: total inner iterations) */
+    int outer_iterations; /* mixed: FP64 refinement steps; FP64: 0 */
+    int status;           /* CF_SOLVE_* */
+    double b_norm;        /* ||b||_2 of the projection right-hand side */
+    double r_norm;        /* ||r||_2 at exit (FP64 residual) */
+    double div_l2;        /* L2 norm of the stored field's divergence (unit-area cells) */
+    double div_linf;      /* max |div u| of the stored field */
+} cf_solve_stats;
+
+/* ---- context (replaces Solver ctor + ProblemManager storage) ---- */
+/* src/Solver.hpp:69-123, src/ProblemManager.hpp:127-180, src/Mesh.hpp:41-103 */
+int cf_ctx_create(const cf_grid_desc* desc, cf_ctx** out);
+int cf_ctx_destroy(cf_ctx* ctx);
+const char* cf_last_error(const cf_ctx* ctx);
+int cf_abi_version(void);
+/* owned extent of a field: cells nx*ny, I-faces (nx+1-px)*ny, J-faces nx*(ny+1-py) */
+int cf_owned_extent(const cf_ctx* ctx, int field, int* ex, int* ey);
+/* mesh accessors: Mesh::cellSize (src/Mesh.hpp:119-122) */
+int cf_cell_size(const cf_ctx* ctx, double* dx);
+
+/* ---- inputs: POD functors of src/BoundaryConditions.hpp, InflowSource.hpp, BodyForce.hpp ---- */
+/* type[4] in the reference order [left, bottom, right, top] (BoundaryConditions.hpp:68-92) */
+int cf_set_bc(cf_ctx* ctx, const int type[4]);
+/* InflowSource(location, size, velocity, quantity) (InflowSource.hpp:78-88);
+ * mode 0 = clamp q to max(q, Q) (reference), 1 = rate q += Q dt (extension) */
+int cf_set_source(cf_ctx* ctx, const double location[2], const double size[2],
+                  const double velocity[2], double quantity, int mode);
+/* BodyForce(fx, fy) (BodyForce.hpp:62-66); density_scaled (extension) scales the
+ * face force by the mean quantity of the two adjacent cells */
+int cf_set_body_force(cf_ctx* ctx, const double force[2], int density_scaled);
+/* density used by the VelocityCorrector (src/VelocityCorrector.hpp:72-76) */
+int cf_set_density(cf_ctx* ctx, double density);
+int cf_set_quirks(cf_ctx* ctx, unsigned flags);
+
+/* ---- state (ProblemManager::get / initialize / advance) ---- */
+int cf_upload(cf_ctx* ctx, int field, const double* host, ptrdiff_t stride_i, ptrdiff_t stride_j);
+int cf_download(cf_ctx* ctx, int field, double* host, ptrdiff_t stride_i, ptrdiff_t stride_j);
+/* full ghosted array (local index, x fastest) for halo tests */
+int cf_download_ghosted(cf_ctx* ctx, int field, double* host, int* ex, int* ey);
+/* ProblemManager::gather(Current) (src/ProblemManager.hpp:394-398): on one GPU,
+ * an on-device ghost fill (wrap copy along periodic axes; wall ghosts stay 0) */
+int cf_fill_ghosts(cf_ctx* ctx);
+
+/* ---- hot path ---- */
+/* TimeIntegrator::step<2> (src/TimeIntegrator.hpp:120-177): gather, advect q, u, v
+ * from Current into Next, swap.  value_order = 1 (linear) or 3 (cubic, reference). */
+int cf_advect(cf_ctx* ctx, double dt, int value_order);
+/* Solver::_addInputs (src/Solver.hpp:181-263) */
+int cf_add_inputs(cf_ctx* ctx, double dt);
+/* VelocityCorrectorBase::correctVelocity (src/VelocityCorrector.hpp:266-282) */
+int cf_project(cf_ctx* ctx, double dt, const cf_solver_opts* opts, cf_solve_stats* stats);
+/* Solver::setup (src/Solver.hpp:125-133): add inputs, correct velocity */
+int cf_setup(cf_ctx* ctx, double dt, const cf_solver_opts* opts, cf_solve_stats* stats);
+/* Solver::step (src/Solver.hpp:135-147): advect, add inputs, correct velocity.
+ * The input stage is fused into the advection kernel unless the body force
+ * is density scaled. */
+int cf_step(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* opts,
+            cf_solve_stats* stats);
+/* divergence norms of the current velocity field */
+int cf_div_norms(cf_ctx* ctx, double* l2, double* linf);
+/* max |u|, |v| over owned faces (for CFL time steps) */
+int cf_max_velocity(cf_ctx* ctx, double* umax);
+
+/* ---- test exports (Interpolation / rk3 at arbitrary points) ---- */
+/* Interpolation::interpolateField (src/Interpolation.hpp:30-41) of a state field
+ * at n physical points xy[2n] */
+int cf_interp_points(cf_ctx* ctx, int field, int order, int n, const double* xy, double* out);
+/* TimeIntegrator::rk3 (src/TimeIntegrator.hpp:36-77) of n points */
+int cf_trace_points(cf_ctx* ctx, int n, const double* xy, double dt, double* out);
+
+/* ---- instrumentation ---- */
+/* number of kernels this context has launched (graph nodes included) */
+long long cf_launch_count(const cf_ctx* ctx);
+/* CUDA stream of the context (cudaStream_t), for event timing by the caller */
+void* cf_stream(const cf_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
