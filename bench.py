@@ -1,0 +1,412 @@
+#!/usr/bin/env python3
+"""Benchmark of the cajitafluids per-timestep hot path on GB300.
+
+Workload (one step = Solver::step: advect q/u/v, inputs, pressure projection):
+  4096^2 periodic, seeded spectral velocity (rms |u| = 1, k <= 64) and
+  scalar, cubic interpolation, dt = 0.5 dx / max|u|, projection to
+  ||div u||_L2 <= 1e-8 (FP64 residual), mixed precision (FP32 advection and
+  inner PCG, FP64 outer refinement).  The same steps in plain FP64 are timed
+  for the mixed-vs-FP64 ratio, and the scalar error of the mixed run against
+  the FP64 run is reported.
+
+Output: one JSON line (rank 0).  value = steps/s of the mixed form over all
+ranks (each rank runs an independent replica; the path is single-GPU).
+--impl reference times the reference algorithm's CPU implementation (the
+oracle port, all host threads) on the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "steps/s at 4096² mixed-prec vs FP64 at ‖div u‖≤1e-8; adjoint/forward ratio"
+# Algorithmic bytes per cell per CG iteration (minimal compulsory traffic):
+# FP64 CG 88 B (r, p read twice-free form: SpMV 2 + update 6 + direction 3
+# words), mixed inner FP32 CG 44 B.
+ALG_BYTES_FP64_ITER = 88.0
+ALG_BYTES_MIXED_ITER = 44.0
+# bytes the kernels of this build must move per cell per iteration
+KERNEL_BYTES_FP64_ITER = 80.0
+KERNEL_BYTES_MIXED_ITER = 32.0
+# CG iterations per step of this workload in FP64 (the FP64 GPU path and the
+# CPU oracle are bit-identical, so they take the same count); the reference
+# arm extrapolates its sampled CG cost to this count.  Measured by this
+# bench's FP64 leg on GB300 (see fp64.cg_iters_per_step in its output).
+FP64_ITERS_PER_STEP_4096 = None
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_context(w, precision, device):
+    from cajitafluids_gb300 import Context
+    c = Context(w.nx, w.ny, periodic=w.periodic, precision=precision, device=device)
+    c.set_bc(w.bc)
+    if w.source is not None:
+        c.set_source(*w.source, mode=w.source_mode)
+    c.set_body_force(w.body, w.body_density_scaled)
+    c.set_density(w.density)
+    c.upload("q", w.q0)
+    c.upload("u", w.u0)
+    c.upload("v", w.v0)
+    return c
+
+
+def solver_opts(w):
+    from cajitafluids_gb300 import SolverOptions
+    return SolverOptions(tol=w.tol, abs_tol=w.abs_tol, max_iter=w.max_iter)
+
+
+def run_steps(c, w, n, stats=None):
+    o = solver_opts(w)
+    for _ in range(n):
+        s = c.step(w.dt, w.order, o, raise_on_maxit=True)
+        if stats is not None:
+            stats.append(s)
+
+
+def barrier_sync(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------------------
+def cpu_reference_sample(w, k_iters, m1=5, m2=15, steps=1):
+    """Oracle (CPU port of the reference algorithm, all OpenMP threads) timed
+    on a bounded sample of the workload: one advection + inputs, and the
+    projection capped at m1 and m2 CG iterations; the CG cost per iteration
+    and the fixed projection cost are extrapolated to k_iters iterations."""
+    from oracle import Oracle, threads
+    o = Oracle(w.nx, w.ny, periodic=w.periodic, bc=w.bc, source=w.source, source_mode=w.source_mode,
+               body=w.body, body_density_scaled=w.body_density_scaled, density=w.density)
+    o.set("q", w.q0)
+    o.set("u", w.u0)
+    o.set("v", w.v0)
+    per_step = []
+    detail = {}
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        o.advect(w.dt, w.order)
+        o.add_inputs(w.dt)
+        t1 = time.perf_counter()
+        snap = {f: o.get(f) for f in ("u", "v")}
+        o.project(w.dt, tol=w.tol, abs_tol=w.abs_tol, max_iter=m1)
+        t2 = time.perf_counter()
+        o.set("u", snap["u"])
+        o.set("v", snap["v"])
+        o.project(w.dt, tol=w.tol, abs_tol=w.abs_tol, max_iter=m2)
+        t3 = time.perf_counter()
+        t_iter = max((t3 - t2) - (t2 - t1), 0.0) / (m2 - m1)
+        t_fixed = max((t2 - t1) - m1 * t_iter, 0.0)
+        t_step = (t1 - t0) + t_fixed + k_iters * t_iter
+        per_step.append(t_step)
+        detail = {"advect_inputs_s": t1 - t0, "cg_iter_s": t_iter, "projection_fixed_s": t_fixed,
+                  "sampled_wall_s": t3 - t0}
+    return per_step, threads(), detail
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+# --------------------------------------------------------------------------
+def bench_gb300(args, rank, world, dist, device):
+    from cajitafluids_gb300.workloads import config2
+    t_gen = time.perf_counter()
+    w = config2(args.size, steps=args.steps)
+    w.max_iter = 400000
+    t_gen = time.perf_counter() - t_gen
+    ncell = w.nx * w.ny
+
+    # ---- mixed precision (headline) ----
+    cm = make_context(w, "mixed", device)
+    warm_stats = []
+    run_steps(cm, w, args.warmup, warm_stats)
+    q_mixed_w = cm.download("q")
+    cm.profile_enable(True)
+    l0 = cm.launches
+    stats = []
+    clocks = ClockSampler(device)
+    barrier_sync(dist)
+    cm.timer_start()
+    t_wall = time.perf_counter()
+    clocks.start()
+    run_steps(cm, w, args.steps, stats)
+    ms = cm.timer_stop()
+    clk = clocks.stop()
+    t_wall = time.perf_counter() - t_wall
+    launches = cm.launches - l0
+    prof = cm.profile_read()
+    cm.profile_enable(False)
+    ms_max = max_over_ranks(dist, ms)
+    value = world * args.steps / (ms_max / 1e3)
+
+    # ---- e2e through the C ABI with host buffers ----
+    from cajitafluids_gb300.api import PinnedArray
+    hq = PinnedArray(cm.owned_shape("q"))
+    hu = PinnedArray(cm.owned_shape("u"))
+    hv = PinnedArray(cm.owned_shape("v"))
+    for h, f in ((hq, "q"), (hu, "u"), (hv, "v")):
+        cm.download(f, h.array)
+    o = solver_opts(w)
+    e2e_steps = max(1, args.e2e_steps)
+    cm.step(w.dt, w.order, o)  # warm the pinned path
+    for h, f in ((hq, "q"), (hu, "u"), (hv, "v")):
+        cm.download(f, h.array)
+    barrier_sync(dist)
+    cm.timer_start()
+    t_e2e = time.perf_counter()
+    for _ in range(e2e_steps):
+        for h, f in ((hq, "q"), (hu, "u"), (hv, "v")):
+            cm.upload(f, h.array)
+        cm.step(w.dt, w.order, o, raise_on_maxit=True)
+        for h, f in ((hq, "q"), (hu, "u"), (hv, "v")):
+            cm.download(f, h.array)
+    e2e_ms = cm.timer_stop()
+    t_e2e = time.perf_counter() - t_e2e
+    e2e_ms = max_over_ranks(dist, max(e2e_ms, t_e2e * 1e3))
+    e2e_value = world * e2e_steps / (e2e_ms / 1e3)
+    io_bytes = 8 * (hq.array.size + hu.array.size + hv.array.size)
+    for h in (hq, hu, hv):
+        h.free()
+    cm.close()
+
+    # ---- plain FP64 on the same steps ----
+    cf = make_context(w, "fp64", device)
+    fstats = []
+    run_steps(cf, w, args.warmup, fstats)
+    q64_w = cf.download("q")
+    cf.profile_enable(True)
+    barrier_sync(dist)
+    cf.timer_start()
+    run_steps(cf, w, args.fp64_steps, fstats)
+    ms64 = cf.timer_stop()
+    prof64 = cf.profile_read()
+    cf.close()
+    ms64 = max_over_ranks(dist, ms64)
+    value64 = world * args.fp64_steps / (ms64 / 1e3)
+    k64 = statistics.mean(s["iterations"] for s in fstats[args.warmup:]) if args.fp64_steps else None
+
+    err = q_mixed_w - q64_w
+    scalar_err = {"after_steps": args.warmup, "linf": float(np.abs(err).max()),
+                  "l2": float(np.sqrt(np.mean(err * err)))}
+
+    # ---- roofline of the dominant kernels: one inner CG iteration ----
+    peak, peak_kind = measured_peaks()
+    it_ms = prof["solve_ms"] / prof["solve_iters"] if prof["solve_iters"] else float("nan")
+    achieved = ALG_BYTES_MIXED_ITER * ncell / (it_ms / 1e3) / 1e9
+    kern = KERNEL_BYTES_MIXED_ITER * ncell / (it_ms / 1e3) / 1e9
+    it64_ms = prof64["solve_ms"] / prof64["solve_iters"] if prof64["solve_iters"] else float("nan")
+    achieved64 = ALG_BYTES_FP64_ITER * ncell / (it64_ms / 1e3) / 1e9
+
+    inner = statistics.mean(s["iterations"] for s in stats)
+    outer = statistics.mean(s["outer_iterations"] for s in stats)
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64",
+        "data": "synthetic: seeded spectral velocity (k<=64, per-mode power k^-11/3, rms|u|=1) and scalar",
+        "config": {"workload": f"{w.nx}x{w.ny} periodic spectral, mixed precision (FP32 advection + inner PCG, "
+                               f"FP64 outer refinement), cubic, ||div u||_L2 <= {w.abs_tol:g}",
+                   "nx": w.nx, "ny": w.ny, "periodic": True, "precision": "mixed", "value_order": w.order,
+                   "dt": w.dt, "abs_tol_div_l2": w.abs_tol, "parallelism": f"replicas x{world}",
+                   "l2_policy": "inputs larger than L2 (state + solver vectors ~0.9 GB)"},
+        "cell_updates_per_s": value * ncell,
+        "mixed": {"cg_inner_iters_per_step": inner, "outer_refinements_per_step": outer,
+                  "div_l2_max": max(s["div_l2"] for s in stats), "div_linf_max": max(s["div_linf"] for s in stats),
+                  "advect_ms_per_step": prof["advect_ms"] / max(prof["advect_calls"], 1),
+                  "cg_iter_ms": it_ms, "project_ms_per_step": prof["project_ms"] / max(prof["projects"], 1)},
+        "fp64": {"steps_per_s": value64, "cg_iters_per_step": k64, "cg_iter_ms": it64_ms,
+                 "roofline_hbm_frac": achieved64 / peak,
+                 "div_l2_max": max(s["div_l2"] for s in fstats) if fstats else None},
+        "mixed_vs_fp64": value / value64 if value64 else None,
+        "scalar_error_vs_fp64": scalar_err,
+        "adjoint_forward_ratio": None,
+        "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
+                "path": "cf_upload(q,u,v from pinned host) + cf_step + cf_download(q,u,v)"},
+        "roofline": {"bound": "hbm", "kernel": "inner CG iteration (k_in_dir_matvec32 + k_in_update32)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": f"hbm_gbs {peak_kind}", "traffic": None,
+                     "algorithmic_bytes_per_cell": ALG_BYTES_MIXED_ITER,
+                     "kernel_bytes_per_cell": KERNEL_BYTES_MIXED_ITER, "kernel_bytes_gbs": kern},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "timing": {"device_ms": ms, "wall_s": t_wall, "workload_gen_s": t_gen},
+    }
+
+    # ---- CPU baseline (rank 0, N = 1) ----
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        k_ref = k64 if k64 else inner
+        per_step, cores, detail = cpu_reference_sample(w, k_ref)
+        line["cpu_baseline"] = {"value": 1.0 / statistics.mean(per_step), "unit": "steps/s", "cores": cores,
+                                "kind": "port", "cpu": cpu_model(),
+                                "sample": f"oracle FP64 on the same {w.nx}^2 state: 1 advection+inputs and the "
+                                          f"projection capped at 5 and 15 CG iterations, extrapolated to "
+                                          f"{k_ref:.0f} iterations/step", **detail}
+    return line
+
+
+def bench_reference(args, rank, world, dist):
+    """The reference algorithm's CPU implementation (oracle port) on the same
+    workload and metric; rank 0 only."""
+    if rank != 0:
+        return None
+    from cajitafluids_gb300.workloads import config2
+    w = config2(args.size, steps=args.steps)
+    k_ref = FP64_ITERS_PER_STEP_4096 if (FP64_ITERS_PER_STEP_4096 and args.size == 4096) else args.ref_iters
+    per = []
+    detail = {}
+    total = max(1, args.steps) + max(0, min(args.warmup, 1))
+    for s in range(total):
+        p, cores, detail = cpu_reference_sample(w, k_ref)
+        if s >= total - max(1, args.steps):
+            per.extend(p)
+    value = 1.0 / statistics.mean(per)
+    return {
+        "metric": METRIC, "impl": "reference", "value": value, "unit": "steps/s", "n_gpus": world,
+        "steps": len(per), "warmup": total - len(per), "ms_per_step": 1e3 * statistics.mean(per),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded spectral velocity (k<=64, per-mode power k^-11/3, rms|u|=1) and scalar",
+        "config": {"workload": f"{w.nx}x{w.ny} periodic spectral, FP64 reference algorithm (CPU), cubic, "
+                               f"||div u||_L2 <= {w.abs_tol:g}", "nx": w.nx, "ny": w.ny},
+        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port", "cpu": cpu_model(),
+                         "sample": f"per step: 1 advection+inputs and the projection capped at 5 and 15 CG "
+                                   f"iterations, extrapolated to {k_ref} iterations/step", **detail},
+        "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_unbuildable": "Kokkos/Cabana-Cajita/HYPRE/MPI are not available; the oracle is the CPU port",
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--size", type=int, default=4096)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--ref-iters", type=int, default=12000)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+
+    world = env_int("WORLD_SIZE", 1)
+    rank = env_int("RANK", 0)
+    local = env_int("LOCAL_RANK", 0)
+    dist = None
+    if world > 1:
+        import torch.distributed as td
+        backend = "gloo"
+        td.init_process_group(backend=backend)
+        dist = td
+    if args.impl == "reference":
+        line = bench_reference(args, rank, world, dist)
+    else:
+        from __graft_entry__ import build
+        build()
+        line = bench_gb300(args, rank, world, dist, local)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -81,6 +81,19 @@ class SolveStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Profile(ctypes.Structure):
+    _fields_ = [
+        ("solve_ms", ctypes.c_double), ("solve_iters", ctypes.c_longlong), ("solve_batches", ctypes.c_longlong),
+        ("advect_ms", ctypes.c_double), ("advect_calls", ctypes.c_longlong),
+        ("project_ms", ctypes.c_double), ("projects", ctypes.c_longlong),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+CF_CG_BATCH = 32
+
 # exported symbol -> (restype, argtypes); the list is the ABI surface
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -114,6 +127,12 @@ SIGNATURES = {
     "cf_trace_points": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_double, _dp]),
     "cf_launch_count": (ctypes.c_longlong, [_vp]),
     "cf_stream": (_vp, [_vp]),
+    "cf_timer_start": (ctypes.c_int, [_vp]),
+    "cf_timer_stop": (ctypes.c_int, [_vp, _dp]),
+    "cf_profile_enable": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "cf_profile_read": (ctypes.c_int, [_vp, ctypes.POINTER(Profile)]),
+    "cf_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_vp)]),
+    "cf_host_free": (ctypes.c_int, [_vp]),
 }
 
 _LIB = None

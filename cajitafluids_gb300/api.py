@@ -214,3 +214,46 @@ class Context:
     @property
     def stream(self) -> int:
         return int(self.lib.cf_stream(self.h) or 0)
+
+    def timer_start(self):
+        self._check(self.lib.cf_timer_start(self.h))
+
+    def timer_stop(self) -> float:
+        ms = ctypes.c_double()
+        self._check(self.lib.cf_timer_stop(self.h, ctypes.byref(ms)))
+        return ms.value
+
+    def profile_enable(self, on: bool = True):
+        self._check(self.lib.cf_profile_enable(self.h, int(bool(on))))
+
+    def profile_read(self) -> dict:
+        p = L.Profile()
+        self._check(self.lib.cf_profile_read(self.h, ctypes.byref(p)))
+        return p.as_dict()
+
+
+class PinnedArray:
+    """Page-locked host buffer viewed as a float64 numpy array."""
+
+    def __init__(self, shape):
+        self.lib = L.load()
+        n = int(np.prod(shape))
+        ptr = ctypes.c_void_p()
+        rc = self.lib.cf_host_alloc(n * 8, ctypes.byref(ptr))
+        if rc != L.CF_OK:
+            raise CfError(rc, "cf_host_alloc failed")
+        self.ptr = ptr
+        buf = (ctypes.c_double * n).from_address(ptr.value)
+        self.array = np.frombuffer(buf, dtype=np.float64).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            self.lib.cf_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

@@ -175,6 +175,16 @@ int do_project(cf_ctx* c, double dt, const cf_solver_opts* opts, cf_solve_stats*
     return rc;
 }
 
+int record_advect(cf_ctx* c) {
+    int rc = cuda_check(c, cudaEventSynchronize(c->ev[3]), "advect timing");
+    float ms = 0.f;
+    if (!rc && cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]) == cudaSuccess) {
+        c->pd.advect_ms += ms;
+        c->pd.advect_calls += 1;
+    }
+    return rc;
+}
+
 #define CF_GUARD_BEGIN try {
 #define CF_GUARD_END                                                   \
     }                                                                  \
@@ -270,6 +280,7 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
     if (!rc) rc = alloc_dev(c, c->staging, c->staging_elems);
     if (!rc) rc = cuda_check(c, cudaMallocHost(&c->hS, sizeof(SolverState)), "cudaMallocHost");
     if (!rc) rc = cuda_check(c, cudaMallocHost(&c->h_out, 4 * sizeof(double)), "cudaMallocHost");
+    for (int k = 0; k < 8 && !rc; ++k) rc = cuda_check(c, cudaEventCreate(&c->ev[k]), "event create");
     if (!rc) rc = sync(c, "context init");
     if (rc) {
         cf_ctx_destroy(c);
@@ -283,6 +294,8 @@ int cf_ctx_destroy(cf_ctx* ctx) {
     if (!ctx) return CF_ERR_INVALID;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (cudaEvent_t e : ctx->ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->g64) cudaGraphExecDestroy(ctx->g64);
     if (ctx->g32) cudaGraphExecDestroy(ctx->g32);
     for (void* p : ctx->allocs) cudaFree(p);
@@ -480,7 +493,12 @@ int cf_advect(cf_ctx* ctx, double dt, int value_order) {
     if (!isfinite(dt)) return fail(ctx, CF_ERR_INVALID, "dt must be finite");
     cudaSetDevice(ctx->device);
     int rc = cuda_check(ctx, launch_fill_ghosts(ctx), "fill ghosts");
+    if (ctx->prof) cudaEventRecord(ctx->ev[2], ctx->stream);
     if (!rc) rc = cuda_check(ctx, launch_advect(ctx, dt, value_order, 0), "advect");
+    if (ctx->prof) {
+        cudaEventRecord(ctx->ev[3], ctx->stream);
+        rc = rc ? rc : record_advect(ctx);
+    }
     return rc;
 }
 
@@ -520,7 +538,12 @@ int cf_step(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* opts,
     if (rc) return rc;
     const bool fuse = !ctx->ph.force_density;
     rc = cuda_check(ctx, launch_fill_ghosts(ctx), "fill ghosts");
+    if (ctx->prof) cudaEventRecord(ctx->ev[2], ctx->stream);
     if (!rc) rc = cuda_check(ctx, launch_advect(ctx, dt, value_order, fuse ? 1 : 0), "advect");
+    if (ctx->prof) {
+        cudaEventRecord(ctx->ev[3], ctx->stream);
+        rc = rc ? rc : record_advect(ctx);
+    }
     if (!rc && !fuse) rc = cuda_check(ctx, launch_add_inputs(ctx, dt), "add inputs");
     if (rc) return rc;
     return do_project(ctx, dt, opts, stats);
@@ -583,5 +606,45 @@ int cf_trace_points(cf_ctx* ctx, int n, const double* xy, double dt, double* out
 long long cf_launch_count(const cf_ctx* ctx) { return ctx ? ctx->launches : -1; }
 
 void* cf_stream(const cf_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int cf_timer_start(cf_ctx* ctx) {
+    if (!ctx) return CF_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    return cuda_check(ctx, cudaEventRecord(ctx->ev[6], ctx->stream), "timer start");
+}
+
+int cf_timer_stop(cf_ctx* ctx, double* ms) {
+    if (!ctx || !ms) return CF_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    int rc = cuda_check(ctx, cudaEventRecord(ctx->ev[7], ctx->stream), "timer stop");
+    if (!rc) rc = cuda_check(ctx, cudaEventSynchronize(ctx->ev[7]), "timer stop");
+    float f = 0.f;
+    if (!rc) rc = cuda_check(ctx, cudaEventElapsedTime(&f, ctx->ev[6], ctx->ev[7]), "timer elapsed");
+    *ms = f;
+    return rc;
+}
+
+int cf_profile_enable(cf_ctx* ctx, int on) {
+    if (!ctx) return CF_ERR_INVALID;
+    if (on) ctx->pd = cf_profile{};
+    ctx->prof = on ? 1 : 0;
+    return CF_OK;
+}
+
+int cf_profile_read(const cf_ctx* ctx, cf_profile* out) {
+    if (!ctx || !out) return CF_ERR_INVALID;
+    *out = ctx->pd;
+    return CF_OK;
+}
+
+int cf_host_alloc(size_t bytes, void** ptr) {
+    if (!ptr || bytes == 0) return CF_ERR_INVALID;
+    return cudaMallocHost(ptr, bytes) == cudaSuccess ? CF_OK : CF_ERR_NOMEM;
+}
+
+int cf_host_free(void* ptr) {
+    if (!ptr) return CF_ERR_INVALID;
+    return cudaFreeHost(ptr) == cudaSuccess ? CF_OK : CF_ERR_CUDA;
+}
 
 }  // extern "C"

@@ -37,6 +37,10 @@ struct cf_ctx {
     cf::Stencil g64_st{}, g32_st{};
 
     long long launches = 0;
+    // profiling (cf_profile_enable)
+    int prof = 0;
+    cf_profile pd{};
+    cudaEvent_t ev[8] = {};
     std::string err;
     std::vector<void*> allocs;
 };

@@ -825,7 +825,7 @@ static Cg32 cg32_args(cf_ctx* c, const Stencil& st) {
 
 static int red_blocks(const cf_ctx* c) { return (c->n_units + CF_RED_WARPS - 1) / CF_RED_WARPS; }
 
-static const int kBatch = 32;  // CG iterations per graph launch
+static const int kBatch = CF_CG_BATCH;  // CG iterations per graph launch
 
 // Build (or reuse) the graph of kBatch iterations for the current stencil.
 static int ensure_graph(cf_ctx* c, const Stencil& st, bool mixed) {
@@ -860,6 +860,17 @@ static int ensure_graph(cf_ctx* c, const Stencil& st, bool mixed) {
     if ((rc = cuda_check(c, e, "graph instantiate"))) return rc;
     key = st;
     return CF_OK;
+}
+
+// accumulate the device time of a CG batch in which every iteration ran
+static void batch_profile(cf_ctx* c, int iters) {
+    if (!c->prof || iters != kBatch) return;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]) == cudaSuccess) {
+        c->pd.solve_ms += ms;
+        c->pd.solve_iters += iters;
+        c->pd.solve_batches += 1;
+    }
 }
 
 static int read_state(cf_ctx* c) {
@@ -901,15 +912,21 @@ int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res) {
     cudaMemcpyAsync(c->S, h, sizeof(SolverState), cudaMemcpyHostToDevice, c->stream);
     int nb = red_blocks(c);
     DivArgs da = div_args(c, st);
+    if (c->prof) cudaEventRecord(c->ev[4], c->stream);
     if (!mixed) {
         k_div_init64<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
         c->launches += 1;
         int max_launch = o.max_iter / kBatch + 3;
+        int prev_iter = 0;
         for (int l = 0;; ++l) {
             if ((rc = read_state(c))) return rc;
+            if (l > 0) batch_profile(c, c->hS->iter - prev_iter);
+            prev_iter = c->hS->iter;
             if (c->hS->status != ST_RUNNING) break;
             if (l >= max_launch) return fail(c, CF_ERR_NUMERIC, "solver did not stop after %d batches", l);
+            if (c->prof) cudaEventRecord(c->ev[0], c->stream);
             if ((rc = cuda_check(c, cudaGraphLaunch(c->g64, c->stream), "graph launch"))) return rc;
+            if (c->prof) cudaEventRecord(c->ev[1], c->stream);
             c->launches += 2 * kBatch;
         }
     } else {
@@ -940,9 +957,13 @@ int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res) {
         while (c->hS->status == ST_RUNNING) {
             while (c->hS->status == ST_RUNNING && c->hS->inner_status == ST_RUNNING) {
                 if (++launches > max_launch) return fail(c, CF_ERR_NUMERIC, "mixed solver did not stop");
+                int prev_iter = c->hS->iter;
+                if (c->prof) cudaEventRecord(c->ev[0], c->stream);
                 if ((rc = cuda_check(c, cudaGraphLaunch(c->g32, c->stream), "graph launch"))) return rc;
+                if (c->prof) cudaEventRecord(c->ev[1], c->stream);
                 c->launches += 2 * kBatch;
                 if ((rc = read_state(c))) return rc;
+                batch_profile(c, c->hS->iter - prev_iter);
             }
             if (c->hS->status != ST_RUNNING) break;
             k_outer_add<<<grd, blk, 0, c->stream>>>(c->x.a, c->e32.a, c->ph.nx, c->ph.ny, c->vpitch, c->vpitch);
@@ -965,7 +986,16 @@ int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res) {
     k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
     c->launches += 1;
     if ((rc = cuda_check(c, cudaGetLastError(), "apply pressure"))) return rc;
-    return div_norms(c, &res->div_l2, &res->div_linf);
+    if (c->prof) cudaEventRecord(c->ev[5], c->stream);
+    rc = div_norms(c, &res->div_l2, &res->div_linf);
+    if (!rc && c->prof) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]) == cudaSuccess) {
+            c->pd.project_ms += ms;
+            c->pd.projects += 1;
+        }
+    }
+    return rc;
 }
 
 }  // namespace cf

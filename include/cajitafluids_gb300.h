@@ -183,6 +183,32 @@ int cf_trace_points(cf_ctx* ctx, int n, const double* xy, double dt, double* out
 long long cf_launch_count(const cf_ctx* ctx);
 /* CUDA stream of the context (cudaStream_t), for event timing by the caller */
 void* cf_stream(const cf_ctx* ctx);
+/* CUDA-event timer on the context stream: start, then stop returns the
+ * device time between the two events in milliseconds (waits for the stop) */
+int cf_timer_start(cf_ctx* ctx);
+int cf_timer_stop(cf_ctx* ctx, double* ms);
+
+/* Device-time profile kept by the context while enabled.  The CG solver
+ * runs in CUDA-graph batches of CF_CG_BATCH iterations; only batches in
+ * which every iteration ran are counted, so solve_ms / solve_iters is the
+ * device time of one CG iteration (both kernels). */
+#define CF_CG_BATCH 32
+typedef struct {
+    double solve_ms;
+    long long solve_iters;
+    long long solve_batches;
+    double advect_ms;
+    long long advect_calls;
+    double project_ms;
+    long long projects;
+} cf_profile;
+/* on != 0 resets the counters and starts recording; 0 stops recording */
+int cf_profile_enable(cf_ctx* ctx, int on);
+int cf_profile_read(const cf_ctx* ctx, cf_profile* out);
+
+/* page-locked host memory for fast cf_upload / cf_download */
+int cf_host_alloc(size_t bytes, void** ptr);
+int cf_host_free(void* ptr);
 
 #ifdef __cplusplus
 }
