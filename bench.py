@@ -204,133 +204,126 @@ def bench_gb300(args, rank, world, dist, device):
     t_gen = time.perf_counter() - t_gen
     ncell = w.nx * w.ny
 
-    # ---- mixed precision (headline) ----
-    cm = make_context(w, "mixed", device)
-    warm_stats = []
-    run_steps(cm, w, args.warmup, warm_stats)
-    q_mixed_w = cm.download("q")
-    cm.profile_enable(True)
-    l0 = cm.launches
-    stats = []
-    clocks = ClockSampler(device)
-    barrier_sync(dist)
-    cm.timer_start()
-    t_wall = time.perf_counter()
-    clocks.start()
-    run_steps(cm, w, args.steps, stats)
-    ms = cm.timer_stop()
-    clk = clocks.stop()
-    t_wall = time.perf_counter() - t_wall
-    launches = cm.launches - l0
-    prof = cm.profile_read()
-    cm.profile_enable(False)
-    ms_max = max_over_ranks(dist, ms)
-    value = world * args.steps / (ms_max / 1e3)
-
-    # ---- e2e through the C ABI with host buffers ----
-    from cajitafluids_gb300.api import PinnedArray
-    hq = PinnedArray(cm.owned_shape("q"))
-    hu = PinnedArray(cm.owned_shape("u"))
-    hv = PinnedArray(cm.owned_shape("v"))
-    for h, f in ((hq, "q"), (hu, "u"), (hv, "v")):
-        cm.download(f, h.array)
-    o = solver_opts(w)
-    e2e_steps = max(1, args.e2e_steps)
-    cm.step(w.dt, w.order, o)  # warm the pinned path
-    for h, f in ((hq, "q"), (hu, "u"), (hv, "v")):
-        cm.download(f, h.array)
-    barrier_sync(dist)
-    cm.timer_start()
-    t_e2e = time.perf_counter()
-    for _ in range(e2e_steps):
-        for h, f in ((hq, "q"), (hu, "u"), (hv, "v")):
-            cm.upload(f, h.array)
-        cm.step(w.dt, w.order, o, raise_on_maxit=True)
-        for h, f in ((hq, "q"), (hu, "u"), (hv, "v")):
-            cm.download(f, h.array)
-    e2e_ms = cm.timer_stop()
-    t_e2e = time.perf_counter() - t_e2e
-    e2e_ms = max_over_ranks(dist, max(e2e_ms, t_e2e * 1e3))
-    e2e_value = world * e2e_steps / (e2e_ms / 1e3)
-    io_bytes = 8 * (hq.array.size + hu.array.size + hv.array.size)
-    for h in (hq, hu, hv):
-        h.free()
-    cm.close()
-
-    # ---- plain FP64 on the same steps ----
-    cf = make_context(w, "fp64", device)
-    fstats = []
-    run_steps(cf, w, args.warmup, fstats)
-    q64_w = cf.download("q")
-    cf.profile_enable(True)
-    barrier_sync(dist)
-    cf.timer_start()
-    run_steps(cf, w, args.fp64_steps, fstats)
-    ms64 = cf.timer_stop()
-    prof64 = cf.profile_read()
-    cf.close()
-    ms64 = max_over_ranks(dist, ms64)
-    value64 = world * args.fp64_steps / (ms64 / 1e3)
-    k64 = statistics.mean(s["iterations"] for s in fstats[args.warmup:]) if args.fp64_steps else None
-
-    err = q_mixed_w - q64_w
-    scalar_err = {"after_steps": args.warmup, "linf": float(np.abs(err).max()),
-                  "l2": float(np.sqrt(np.mean(err * err)))}
-
-    # ---- roofline of the dominant kernels: one inner CG iteration ----
+    legs = set(args.legs.split(","))
     peak, peak_kind = measured_peaks()
-    it_ms = prof["solve_ms"] / prof["solve_iters"] if prof["solve_iters"] else float("nan")
-    achieved = ALG_BYTES_MIXED_ITER * ncell / (it_ms / 1e3) / 1e9
-    kern = KERNEL_BYTES_MIXED_ITER * ncell / (it_ms / 1e3) / 1e9
-    it64_ms = prof64["solve_ms"] / prof64["solve_iters"] if prof64["solve_iters"] else float("nan")
-    achieved64 = ALG_BYTES_FP64_ITER * ncell / (it64_ms / 1e3) / 1e9
-
-    inner = statistics.mean(s["iterations"] for s in stats)
-    outer = statistics.mean(s["outer_iterations"] for s in stats)
     line = {
-        "metric": METRIC,
-        "value": value,
-        "unit": "steps/s",
-        "n_gpus": world,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": ms_max / args.steps,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f32+f64",
+        "metric": METRIC, "value": None, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic: seeded spectral velocity (k<=64, per-mode power k^-11/3, rms|u|=1) and scalar",
         "config": {"workload": f"{w.nx}x{w.ny} periodic spectral, mixed precision (FP32 advection + inner PCG, "
                                f"FP64 outer refinement), cubic, ||div u||_L2 <= {w.abs_tol:g}",
                    "nx": w.nx, "ny": w.ny, "periodic": True, "precision": "mixed", "value_order": w.order,
                    "dt": w.dt, "abs_tol_div_l2": w.abs_tol, "parallelism": f"replicas x{world}",
                    "l2_policy": "inputs larger than L2 (state + solver vectors ~0.9 GB)"},
-        "cell_updates_per_s": value * ncell,
-        "mixed": {"cg_inner_iters_per_step": inner, "outer_refinements_per_step": outer,
-                  "div_l2_max": max(s["div_l2"] for s in stats), "div_linf_max": max(s["div_linf"] for s in stats),
-                  "advect_ms_per_step": prof["advect_ms"] / max(prof["advect_calls"], 1),
-                  "cg_iter_ms": it_ms, "project_ms_per_step": prof["project_ms"] / max(prof["projects"], 1)},
-        "fp64": {"steps_per_s": value64, "cg_iters_per_step": k64, "cg_iter_ms": it64_ms,
-                 "roofline_hbm_frac": achieved64 / peak,
-                 "div_l2_max": max(s["div_l2"] for s in fstats) if fstats else None},
-        "mixed_vs_fp64": value / value64 if value64 else None,
-        "scalar_error_vs_fp64": scalar_err,
         "adjoint_forward_ratio": None,
-        "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
-                "path": "cf_upload(q,u,v from pinned host) + cf_step + cf_download(q,u,v)"},
-        "roofline": {"bound": "hbm", "kernel": "inner CG iteration (k_in_dir_matvec32 + k_in_update32)",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": f"hbm_gbs {peak_kind}", "traffic": None,
-                     "algorithmic_bytes_per_cell": ALG_BYTES_MIXED_ITER,
-                     "kernel_bytes_per_cell": KERNEL_BYTES_MIXED_ITER, "kernel_bytes_gbs": kern},
-        "gpu_launches": launches,
-        "clocks": clk,
-        "timing": {"device_ms": ms, "wall_s": t_wall, "workload_gen_s": t_gen},
     }
+    q_mixed_w = None
+    value = None
+    stats = []
+    if "mixed" in legs:
+        # ---- mixed precision (headline) ----
+        cm = make_context(w, "mixed", device)
+        run_steps(cm, w, args.warmup)
+        q_mixed_w = cm.download("q")
+        cm.profile_enable(True)
+        l0 = cm.launches
+        clocks = ClockSampler(device)
+        barrier_sync(dist)
+        cm.timer_start()
+        t_wall = time.perf_counter()
+        clocks.start()
+        run_steps(cm, w, args.steps, stats)
+        ms = cm.timer_stop()
+        clk = clocks.stop()
+        t_wall = time.perf_counter() - t_wall
+        launches = cm.launches - l0
+        prof = cm.profile_read()
+        cm.profile_enable(False)
+        ms_max = max_over_ranks(dist, ms)
+        value = world * args.steps / (ms_max / 1e3)
+        it_ms = prof["solve_ms"] / prof["solve_iters"] if prof["solve_iters"] else float("nan")
+        achieved = ALG_BYTES_MIXED_ITER * ncell / (it_ms / 1e3) / 1e9
+        kern = KERNEL_BYTES_MIXED_ITER * ncell / (it_ms / 1e3) / 1e9
+        line.update({
+            "value": value, "ms_per_step": ms_max / args.steps, "cell_updates_per_s": value * ncell,
+            "mixed": {"cg_inner_iters_per_step": statistics.mean(s["iterations"] for s in stats),
+                      "outer_refinements_per_step": statistics.mean(s["outer_iterations"] for s in stats),
+                      "div_l2_max": max(s["div_l2"] for s in stats),
+                      "div_linf_max": max(s["div_linf"] for s in stats),
+                      "advect_ms_per_step": prof["advect_ms"] / max(prof["advect_calls"], 1),
+                      "cg_iter_ms": it_ms, "project_ms_per_step": prof["project_ms"] / max(prof["projects"], 1)},
+            "roofline": {"bound": "hbm", "kernel": "inner CG iteration (k_in_dir_matvec32 + k_in_update32)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": f"hbm_gbs {peak_kind}", "traffic": None,
+                         "algorithmic_bytes_per_cell": ALG_BYTES_MIXED_ITER,
+                         "kernel_bytes_per_cell": KERNEL_BYTES_MIXED_ITER, "kernel_bytes_gbs": kern},
+            "gpu_launches": launches, "clocks": clk,
+            "timing": {"device_ms": ms, "wall_s": t_wall, "workload_gen_s": t_gen},
+        })
+
+        if "e2e" in legs:
+            # ---- e2e through the C ABI with host buffers ----
+            from cajitafluids_gb300.api import PinnedArray
+            hq = PinnedArray(cm.owned_shape("q"))
+            hu = PinnedArray(cm.owned_shape("u"))
+            hv = PinnedArray(cm.owned_shape("v"))
+            for h, f in ((hq, "q"), (hu, "u"), (hv, "v")):
+                cm.download(f, h.array)
+            o = solver_opts(w)
+            e2e_steps = max(1, args.e2e_steps)
+            barrier_sync(dist)
+            cm.timer_start()
+            t_e2e = time.perf_counter()
+            for _ in range(e2e_steps):
+                for h, f in ((hq, "q"), (hu, "u"), (hv, "v")):
+                    cm.upload(f, h.array)
+                cm.step(w.dt, w.order, o, raise_on_maxit=True)
+                for h, f in ((hq, "q"), (hu, "u"), (hv, "v")):
+                    cm.download(f, h.array)
+            e2e_ms = cm.timer_stop()
+            t_e2e = time.perf_counter() - t_e2e
+            e2e_ms = max_over_ranks(dist, max(e2e_ms, t_e2e * 1e3))
+            io_bytes = 8 * (hq.array.size + hu.array.size + hv.array.size)
+            line["e2e"] = {"value": world * e2e_steps / (e2e_ms / 1e3), "unit": "steps/s",
+                           "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
+                           "path": "cf_upload(q,u,v from pinned host) + cf_step + cf_download(q,u,v)"}
+            for h in (hq, hu, hv):
+                h.free()
+        cm.close()
+
+    fstats = []
+    k64 = None
+    if "fp64" in legs:
+        # ---- plain FP64 on the same steps ----
+        cf = make_context(w, "fp64", device)
+        run_steps(cf, w, args.warmup, fstats)
+        q64_w = cf.download("q")
+        cf.profile_enable(True)
+        barrier_sync(dist)
+        cf.timer_start()
+        run_steps(cf, w, args.fp64_steps, fstats)
+        ms64 = cf.timer_stop()
+        prof64 = cf.profile_read()
+        cf.close()
+        ms64 = max_over_ranks(dist, ms64)
+        value64 = world * args.fp64_steps / (ms64 / 1e3) if args.fp64_steps else None
+        k64 = statistics.mean(s["iterations"] for s in fstats[args.warmup:]) if args.fp64_steps else None
+        it64_ms = prof64["solve_ms"] / prof64["solve_iters"] if prof64["solve_iters"] else float("nan")
+        achieved64 = ALG_BYTES_FP64_ITER * ncell / (it64_ms / 1e3) / 1e9
+        line["fp64"] = {"steps_per_s": value64, "cg_iters_per_step": k64, "cg_iter_ms": it64_ms,
+                        "roofline_hbm_frac": achieved64 / peak,
+                        "div_l2_max": max(s["div_l2"] for s in fstats) if fstats else None}
+        if value and value64:
+            line["mixed_vs_fp64"] = value / value64
+        if q_mixed_w is not None:
+            err = q_mixed_w - q64_w
+            line["scalar_error_vs_fp64"] = {"after_steps": args.warmup, "linf": float(np.abs(err).max()),
+                                            "l2": float(np.sqrt(np.mean(err * err)))}
 
     # ---- CPU baseline (rank 0, N = 1) ----
-    if rank == 0 and world == 1 and not args.skip_cpu:
-        k_ref = k64 if k64 else inner
+    if rank == 0 and world == 1 and "cpu" in legs and not args.skip_cpu:
+        k_ref = k64 if k64 else (line.get("mixed", {}).get("cg_inner_iters_per_step") or args.ref_iters)
         per_step, cores, detail = cpu_reference_sample(w, k_ref)
         line["cpu_baseline"] = {"value": 1.0 / statistics.mean(per_step), "unit": "steps/s", "cores": cores,
                                 "kind": "port", "cpu": cpu_model(),
@@ -381,6 +374,8 @@ def main():
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--legs", default="mixed,e2e,fp64,cpu",
+                    help="comma list of legs to run: mixed (headline), e2e, fp64, cpu")
     ap.add_argument("--ref-iters", type=int, default=12000)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
