@@ -20,6 +20,8 @@ CF_ERR_NOT_CONVERGED = -4
 CF_ERR_NUMERIC = -5
 CF_ERR_NOMEM = -6
 CF_ERR_MESH = -7
+CF_ERR_TOO_LARGE = -8
+CF_NOALLOC_MAX_UNITS = 65536
 
 ERROR_NAMES = {
     CF_ERR_INVALID: "CF_ERR_INVALID",
@@ -29,6 +31,7 @@ ERROR_NAMES = {
     CF_ERR_NUMERIC: "CF_ERR_NUMERIC",
     CF_ERR_NOMEM: "CF_ERR_NOMEM",
     CF_ERR_MESH: "CF_ERR_MESH",
+    CF_ERR_TOO_LARGE: "CF_ERR_TOO_LARGE",
 }
 
 CF_FIELD_QUANTITY = 0
@@ -133,6 +136,8 @@ SIGNATURES = {
     "cf_profile_read": (ctypes.c_int, [_vp, ctypes.POINTER(Profile)]),
     "cf_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_vp)]),
     "cf_host_free": (ctypes.c_int, [_vp]),
+    "cf_div_norms_noalloc": (ctypes.c_int, [_vp, _pd, _vp, _pd, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_double, _vp, _vp]),
 }
 
 _LIB = None

@@ -210,6 +210,34 @@ int cf_profile_read(const cf_ctx* ctx, cf_profile* out);
 int cf_host_alloc(size_t bytes, void** ptr);
 int cf_host_free(void* ptr);
 
+/* ---- allocation-free divergence norms (no counterpart in the reference) ----
+ * For callers that own their velocity arrays on the device and cannot
+ * allocate device memory where they need the norm: codes whose device
+ * memory belongs to their own pool allocator or fixed memory budget, and
+ * hooks inside latency-critical loops where cudaMalloc/cudaFree would
+ * synchronise the device.  cf_div_norms needs a context, and creating one
+ * allocates the whole state.  This entry point allocates nothing (no
+ * cudaMalloc, cudaFree or allocating library call); its reduction scratch
+ * is a fixed 1 MiB device array inside this library, held by every GPU that
+ * loads the library until the process exits.
+ *
+ * u: device pointer to u(0, 0) of the owned I-faces, u(gi, gj) at
+ *    u[gj * u_pitch + gi], (nx + 1 - periodic_x) x ny values; v likewise
+ *    for the J-faces, nx x (ny + 1 - periodic_y).  out: device pointer to two
+ *    doubles, written with the same values cf_div_norms returns (L2 norm with
+ *    unit-area cells, max |div u|).  stream: a cudaStream_t (NULL = default
+ *    stream).  The call only enqueues work; read out after the stream.
+ * Limits: at most CF_NOALLOC_MAX_UNITS units of 64 x 16 cells (8192 x 8192
+ * cells); larger grids return CF_ERR_TOO_LARGE without touching the GPU.
+ * The first call on each device looks up the scratch address on that
+ * device (make that first call before any stream capture).  All calls share
+ * the one scratch array: calls that overlap on the GPU (different streams,
+ * or threads without ordering) race and give wrong results. */
+#define CF_ERR_TOO_LARGE (-8)
+#define CF_NOALLOC_MAX_UNITS 65536
+int cf_div_norms_noalloc(const double* u, ptrdiff_t u_pitch, const double* v, ptrdiff_t v_pitch, int nx, int ny,
+                         int periodic_x, int periodic_y, double dx, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
