@@ -130,8 +130,8 @@ int parse_opts(cf_ctx* c, const cf_solver_opts* o, SolveOpts* so) {
     so->tol = o ? o->tol : 1.0e-6;
     so->abs_tol = o ? o->abs_tol : 0.0;
     so->max_iter = o ? o->max_iter : 2000;
-    so->inner_tol = (o && o->inner_tol > 0.0) ? o->inner_tol : 1.0e-4;
-    so->max_outer = (o && o->max_outer > 0) ? o->max_outer : 30;
+    so->inner_tol = (o && o->inner_tol > 0.0) ? o->inner_tol : 0.1;
+    so->max_outer = (o && o->max_outer > 0) ? o->max_outer : 200;
     if (!(so->tol >= 0.0) || !(so->abs_tol >= 0.0) || so->max_iter < 0 || !(so->inner_tol < 1.0))
         return fail(c, CF_ERR_INVALID, "invalid solver options");
     return CF_OK;

@@ -66,8 +66,8 @@ struct SolverState {
     double tol2, abs2, area;
     // mixed precision: inner solve
     double rr_in0, rr_in, rho_in, alpha_in, beta_in, tau2;
-    double rr_out, inner_tol2, target2;
-    int use_abs;
+    double rr_out, inner_tol2, target2, rho_prev;
+    int use_abs, restart;
     int iter, max_iter, status;
     int inner_iter, inner_status;
     int outer_iter, max_outer;

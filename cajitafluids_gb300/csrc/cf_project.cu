@@ -20,10 +20,13 @@
 // p ping-pongs between two buffers because K1 recomputes the new direction
 // on its halo from the old one.
 //
-// Mixed precision: inner Jacobi-PCG on FP32 vectors (e, r, p) with FP64
-// scalars, 32 bytes per cell per iteration (A p is recomputed in K2 instead
-// of stored); the FP64 outer loop forms r = b - A x in FP64 and restarts the
-// inner solve on it until the FP64 residual meets the tolerance.
+// Mixed precision: Jacobi-PCG on FP32 vectors (e, r, p) with FP64 scalars,
+// 32 bytes per cell per iteration (A p is recomputed in K2 instead of
+// stored), with reliable updates (residual replacement, van der Vorst & Ye
+// 2000): whenever the recursive FP32 residual has fallen by a factor delta
+// since the last update, x += e in FP64, r = b - A x is formed in FP64 and
+// replaces the FP32 residual, and the iteration continues with the same
+// search direction.  Convergence is judged only on the FP64 residual.
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -352,7 +355,8 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
             S->outer_iter = 0;
             S->target2 = S->tol2 * bb;
             if (S->use_abs) S->target2 = fmax(S->target2, S->abs2 / S->area);
-            S->tau2 = fmax(S->inner_tol2, 0.25 * S->target2 / bb);
+            S->tau2 = S->inner_tol2;
+            S->restart = 1;
             if (bb == 0.0 || converged(S, bb))
                 S->status = ST_CONVERGED;
             else if (isnan(bb))
@@ -436,7 +440,7 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_in_dir_matvec32(Cg32 a) {
     SolverState* S = a.S;
     if (!inner_running(S)) return;
     const int it = S->inner_iter;
-    const bool first = it == 0;
+    const bool first = it == 0 || S->restart;
     const float beta = (float)S->beta_in;
     const float* pold = (it & 1) ? a.pb : a.pa;
     float* pnew = (it & 1) ? a.pa : a.pb;
@@ -478,10 +482,11 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_in_dir_matvec32(Cg32 a) {
         double pq = final_tree(a.part0, a.U);
         if (threadIdx.x == 0) {
             S->ticket[5] = 0;
+            S->restart = 0;
             if (isnan(pq))
                 S->status = ST_NAN;
             else if (!(pq > 0.0))
-                S->inner_status = ST_BREAKDOWN;  // FP32 noise floor: hand back to the outer loop
+                S->inner_status = ST_BREAKDOWN;  // FP32 noise floor: refine and restart
             else
                 S->alpha_in = S->rho_in / pq;
         }
@@ -553,14 +558,18 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_in_update32(Cg32 a) {
         double rr = final_tree(a.part1, a.U);
         if (threadIdx.x == 0) {
             S->ticket[6] = 0;
+            S->rho_prev = S->rho_in;
             S->beta_in = rz / S->rho_in;
             S->rho_in = rz;
             S->rr_in = rr;
+            if (rr > S->rr_in0) S->rr_in0 = rr;
             S->inner_iter = it + 1;
             S->iter = S->iter + 1;
+            // reliable update when the recursive residual fell by delta since
+            // the last one, or already looks converged
             if (isnan(rr))
                 S->status = ST_NAN;
-            else if (rr <= S->tau2 * S->rr_in0)
+            else if (rr <= S->tau2 * S->rr_in0 || rr <= S->target2)
                 S->inner_status = ST_CONVERGED;
             else if (S->iter >= S->max_iter)
                 S->inner_status = ST_MAXIT;
@@ -650,13 +659,18 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
             else if (S->iter >= S->max_iter || S->outer_iter >= S->max_outer)
                 S->status = ST_MAXIT;
             else {
+                // residual replacement: keep the search direction, rescale beta
+                // to the replaced residual (restart only after an FP32 breakdown)
+                if (S->inner_status == ST_BREAKDOWN) {
+                    S->restart = 1;
+                    S->beta_in = 0.0;
+                } else {
+                    S->beta_in = rz / S->rho_prev;
+                }
                 S->rho_in = rz;
                 S->rr_in0 = rr;
                 S->rr_in = rr;
-                S->beta_in = 0.0;
-                S->inner_iter = 0;
                 S->inner_status = ST_RUNNING;
-                S->tau2 = fmax(S->inner_tol2, 0.25 * S->target2 / rr64);
             }
         }
     }

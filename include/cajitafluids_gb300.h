@@ -102,9 +102,10 @@ typedef struct {
     const char* precon;
     double tol;
     double abs_tol;
-    int max_iter;        /* FP64 CG iterations, or total inner iterations (mixed) */
-    double inner_tol;    /* mixed: relative reduction per inner solve (0 = 1e-4) */
-    int max_outer;       /* mixed: outer refinement limit (0 = 30) */
+    int max_iter;        /* FP64 CG iterations, or total FP32 iterations (mixed) */
+    double inner_tol;    /* mixed: FP32 residual reduction that triggers an FP64
+                            reliable update (0 = 0.1) */
+    int max_outer;       /* mixed: limit on FP64 reliable updates (0 = 200) */
 } cf_solver_opts;
 
 typedef struct {
