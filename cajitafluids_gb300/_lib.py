@@ -21,6 +21,7 @@ CF_ERR_NUMERIC = -5
 CF_ERR_NOMEM = -6
 CF_ERR_MESH = -7
 CF_ERR_TOO_LARGE = -8
+CF_ERR_TIMEOUT = -9
 CF_NOALLOC_MAX_UNITS = 65536
 
 ERROR_NAMES = {
@@ -32,6 +33,7 @@ ERROR_NAMES = {
     CF_ERR_NOMEM: "CF_ERR_NOMEM",
     CF_ERR_MESH: "CF_ERR_MESH",
     CF_ERR_TOO_LARGE: "CF_ERR_TOO_LARGE",
+    CF_ERR_TIMEOUT: "CF_ERR_TIMEOUT",
 }
 
 CF_FIELD_QUANTITY = 0
@@ -52,6 +54,7 @@ CF_SOLVE_CONVERGED = 0
 CF_SOLVE_MAX_ITER = 1
 CF_SOLVE_BREAKDOWN = 2
 CF_SOLVE_NAN = 3
+CF_SOLVE_TIMEOUT = 4
 
 
 class GridDesc(ctypes.Structure):

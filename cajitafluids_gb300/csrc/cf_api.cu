@@ -141,6 +141,7 @@ int status_code(int st) {
     switch (st) {
         case ST_CONVERGED: return CF_OK;
         case ST_MAXIT: return CF_ERR_NOT_CONVERGED;
+        case ST_TIMEOUT: return CF_ERR_TIMEOUT;
         default: return CF_ERR_NUMERIC;
     }
 }
@@ -170,7 +171,8 @@ int do_project(cf_ctx* c, double dt, const cf_solver_opts* opts, cf_solve_stats*
         fail(c, rc, "pressure solve stopped at max_iter (%d iterations, |r|/|b| = %g)", r.iterations,
              r.bb > 0 ? sqrt(r.rr / r.bb) : 0.0);
     else if (rc)
-        fail(c, rc, "pressure solve failed (%s) after %d iterations", r.status == ST_NAN ? "NaN" : "breakdown",
+        fail(c, rc, "pressure solve failed (%s) after %d iterations",
+             r.status == ST_NAN ? "NaN" : (r.status == ST_TIMEOUT ? "device wait timed out" : "breakdown"),
              r.iterations);
     return rc;
 }
@@ -265,10 +267,16 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
         if (!rc) rc = alloc_dev(c, c->qv.a, vn);
     } else {
         if (!rc) rc = alloc_dev(c, c->b.a, vn);
-        if (!rc) rc = alloc_dev(c, c->e32.a, vn);
-        if (!rc) rc = alloc_dev(c, c->r32.a, vn);
-        if (!rc) rc = alloc_dev(c, c->pa32.a, vn);
-        if (!rc) rc = alloc_dev(c, c->pb32.a, vn);
+        // FP32 vectors with a one-cell ghost ring, owned column 0 on 16 bytes
+        c->p32 = (int)round_up((size_t)nx + 8, 32);
+        size_t n32 = (size_t)c->p32 * (ny + 2);
+        float** bases[4] = {&c->e32b, &c->r32b, &c->pa32b, &c->pb32b};
+        cf::Vec32* vecs[4] = {&c->e32, &c->r32, &c->pa32, &c->pb32};
+        for (int k = 0; k < 4 && !rc; ++k) {
+            rc = alloc_dev(c, *bases[k], n32);
+            vecs[k]->a = *bases[k] + c->p32 + 4;
+            vecs[k]->pitch = c->p32;
+        }
     }
     c->G = (nx + CF_UNIT_COLS - 1) / CF_UNIT_COLS;
     c->B = (ny + CF_BAND_ROWS - 1) / CF_BAND_ROWS;
@@ -280,6 +288,7 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
     if (!rc) rc = alloc_dev(c, c->staging, c->staging_elems);
     if (!rc) rc = cuda_check(c, cudaMallocHost(&c->hS, sizeof(SolverState)), "cudaMallocHost");
     if (!rc) rc = cuda_check(c, cudaMallocHost(&c->h_out, 4 * sizeof(double)), "cudaMallocHost");
+    if (!rc && c->precision == CF_PREC_MIXED) rc = cg32_setup(c);
     for (int k = 0; k < 8 && !rc; ++k) rc = cuda_check(c, cudaEventCreate(&c->ev[k]), "event create");
     if (!rc) rc = sync(c, "context init");
     if (rc) {

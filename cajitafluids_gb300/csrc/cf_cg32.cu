@@ -1,0 +1,479 @@
+// FP32 inner Jacobi-PCG iteration of the mixed-precision projection, fed by
+// TMA.
+//
+// The FP32 solver vectors (e, r, p twice) carry a one-cell ghost ring:
+// element (i, j), i in [-1, nx], j in [-1, ny], lives at
+// base[(j + 1) * pitch + i + 4], so owned column 0 sits on a 16-byte boundary.
+// Wall ghosts stay zero; along a periodic axis the thread that writes an
+// edge cell also writes its ghost copy, so every halo a kernel reads was
+// written by an earlier launch.
+//
+// Each kernel is persistent (two CTAs per SM).  A CTA walks tiles of 128 x 16
+// owned cells; for each tile a single thread issues 2-D TMA copies
+// (cp.async.bulk.tensor) of 136 x 18 boxes -- the tile, one halo row above and
+// below and a 4-column (16-byte) pad on each side -- into one of three
+// shared-memory stages, completing on an mbarrier.  While a tile is computed
+// from shared memory the next two are in flight.  Stores go straight from
+// registers (float4 where a full vector is owned).
+//
+//   K1  p <- M^-1 r + beta p (halo too, in shared memory) ; q <- A p ; p.q
+//   K2  q <- A p (recomputed) ; e += alpha p ; r -= alpha q ; r.z , r.r
+//
+// Dot products: FP32 per thread within a tile, FP64 across tiles, warps and
+// CTAs; the last CTA finishes the sum and advances the solver state.
+// mbarrier waits are bounded: on timeout the CTA records ST_TIMEOUT, waits
+// (bounded) for its own copies still in flight, and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "cf_ctx.cuh"
+
+namespace cf {
+
+#define FULLMASK32 0xffffffffu
+
+constexpr int kTW = 128;                 // owned columns per tile
+constexpr int kTH = 16;                  // owned rows per tile
+constexpr int kBX = kTW + 8;             // box columns
+constexpr int kBY = kTH + 2;             // box rows
+constexpr int kBoxBytes = kBX * kBY * 4; // 9792
+constexpr int kSlot = 9856;              // 128-byte aligned slot
+constexpr int kStages = 3;
+constexpr int kThreads = 256;
+constexpr unsigned kWaitLimit = 1u << 22;
+
+struct Cg32T {
+    int nx, ny, per_x, per_y, tiles_x, tiles, pitch;
+    Stencil st;
+    float *e, *r, *pa, *pb;  // element (0, 0)
+    double *part0, *part1;
+    SolverState* S;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait; true when the phase completed
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned limit) {
+    for (unsigned k = 0; k < limit; ++k)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ int ebits32t(const Cg32T& a, int i, int j) {
+    int ci = wrap_index(i, a.nx, a.per_x), cj = wrap_index(j, a.ny, a.per_y);
+    if (ci < 0) ci = 0;
+    if (cj < 0) cj = 0;
+    return edge_bits(ci, cj, a.nx, a.ny, a.per_x, a.per_y);
+}
+
+// store one owned value and, along a periodic axis, its ghost copy
+__device__ __forceinline__ void put_ghosted(const Cg32T& a, float* o, int i, int j, float val) {
+    const ptrdiff_t row = (ptrdiff_t)j * a.pitch;
+    o[row + i] = val;
+    if (a.per_x) {
+        if (i == 0) o[row + a.nx] = val;
+        if (i == a.nx - 1) o[row - 1] = val;
+    }
+    if (a.per_y) {
+        if (j == 0) o[(ptrdiff_t)a.ny * a.pitch + i] = val;
+        if (j == a.ny - 1) o[-(ptrdiff_t)a.pitch + i] = val;
+    }
+}
+
+// store four consecutive owned values starting at column i
+__device__ __forceinline__ void put4(const Cg32T& a, float* o, int i, int j, float4 v, bool ghosts) {
+    if (i + 3 < a.nx) {
+        *reinterpret_cast<float4*>(o + (ptrdiff_t)j * a.pitch + i) = v;
+        if (ghosts && ((a.per_x && (i == 0 || i + 3 == a.nx - 1)) || (a.per_y && (j == 0 || j == a.ny - 1)))) {
+            put_ghosted(a, o, i, j, v.x);
+            put_ghosted(a, o, i + 1, j, v.y);
+            put_ghosted(a, o, i + 2, j, v.z);
+            put_ghosted(a, o, i + 3, j, v.w);
+        }
+        return;
+    }
+    float vv[4] = {v.x, v.y, v.z, v.w};
+    for (int k = 0; k < 4; ++k)
+        if (i + k < a.nx) {
+            if (ghosts)
+                put_ghosted(a, o, i + k, j, vv[k]);
+            else
+                o[(ptrdiff_t)j * a.pitch + i + k] = vv[k];
+        }
+}
+
+__device__ __forceinline__ float stencil1(const Cg32T& a, int i, int j, float c, float w, float e, float s, float n) {
+    float q = a.st.diag32[ebits32t(a, i, j)] * c;
+    q = fmaf(a.st.ms32, w, q);
+    q = fmaf(a.st.ms32, e, q);
+    q = fmaf(a.st.ms32, s, q);
+    q = fmaf(a.st.ms32, n, q);
+    return q;
+}
+
+// A p for the four cells (i0..i0+3, j) of a lane from the shared tile P
+// (row stride kBX, owned (c, r) at [r + 1][c + 4]).
+__device__ __forceinline__ float4 apply4(const Cg32T& a, const float* P, int lane, int row, int i0, int j,
+                                         float4& pc) {
+    const float* rc = P + (row + 1) * kBX + 4 + 4 * lane;
+    pc = *reinterpret_cast<const float4*>(rc);
+    float4 pu = *reinterpret_cast<const float4*>(rc - kBX);
+    float4 pd = *reinterpret_cast<const float4*>(rc + kBX);
+    float left = __shfl_up_sync(FULLMASK32, pc.w, 1);
+    float right = __shfl_down_sync(FULLMASK32, pc.x, 1);
+    if (lane == 0) left = rc[-1];
+    if (lane == 31) right = rc[4];
+    float4 q;
+    q.x = stencil1(a, i0, j, pc.x, left, pc.y, pu.x, pd.x);
+    q.y = stencil1(a, i0 + 1, j, pc.y, pc.x, pc.z, pu.y, pd.y);
+    q.z = stencil1(a, i0 + 2, j, pc.z, pc.y, pc.w, pu.z, pd.z);
+    q.w = stencil1(a, i0 + 3, j, pc.w, pc.z, right, pu.w, pd.w);
+    return q;
+}
+
+__device__ __forceinline__ bool running(const SolverState* S) {
+    return *(volatile const int*)&S->status == ST_RUNNING && *(volatile const int*)&S->inner_status == ST_RUNNING;
+}
+
+__device__ __forceinline__ double block_sum(double v, double* red) {
+    v = warp_fold(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = red[0];
+    for (int k = 1; k < kThreads / 32; ++k) t = t + red[k];
+    __syncthreads();
+    return t;
+}
+
+// Timeout path: record the status and wait (bounded) for this CTA's copies.
+__device__ void abandon(SolverState* S, const uint64_t* bars, int kfirst, int ktiles) {
+    if (threadIdx.x == 0) {
+        atomicExch(&S->status, (int)ST_TIMEOUT);
+        for (int k = kfirst; k < ktiles && k < kfirst + kStages; ++k)
+            mbar_wait(smem_u32(&bars[k % kStages]), (uint32_t)((k / kStages) & 1), kWaitLimit >> 4);
+    }
+    __syncthreads();
+}
+
+// K1: new direction (with halo) in shared memory, stencil, p.q
+__global__ void __launch_bounds__(kThreads, 2)
+    k_tma_dir_matvec32(const __grid_constant__ CUtensorMap map_r, const __grid_constant__ CUtensorMap map_pa,
+                       const __grid_constant__ CUtensorMap map_pb, Cg32T a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[kStages];
+    __shared__ double red[kThreads / 32];
+    SolverState* S = a.S;
+    if (!running(S)) return;
+    const int it = S->inner_iter;
+    const bool first = it == 0 || S->restart;
+    const float beta = (float)S->beta_in;
+    const CUtensorMap* map_old = (it & 1) ? &map_pb : &map_pa;
+    float* pnew = (it & 1) ? a.pa : a.pb;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ntile = (a.tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    unsigned char* sb = smem + ((128u - (smem_u32(smem) & 127u)) & 127u);  // TMA wants 128-byte slots
+    auto stage_ptr = [&](int s, int arr) { return reinterpret_cast<float*>(sb + (s * 2 + arr) * kSlot); };
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int k) {
+        int t = (int)blockIdx.x + k * (int)gridDim.x;
+        int s = k % kStages;
+        int x = (t % a.tiles_x) * kTW, y = (t / a.tiles_x) * kTH;
+        uint32_t bar = smem_u32(&bars[s]);
+        mbar_expect_tx(bar, 2 * kBoxBytes);
+        tma_load_2d(smem_u32(stage_ptr(s, 0)), &map_r, x, y, bar);
+        tma_load_2d(smem_u32(stage_ptr(s, 1)), map_old, x, y, bar);
+    };
+    if (tid == 0)
+        for (int k = 0; k < kStages && k < ntile; ++k) issue(k);
+    double acc = 0.0;
+    for (int k = 0; k < ntile; ++k) {
+        const int s = k % kStages;
+        const int t = (int)blockIdx.x + k * (int)gridDim.x;
+        const int i0 = (t % a.tiles_x) * kTW, j0 = (t / a.tiles_x) * kTH;
+        bool ok = mbar_wait(smem_u32(&bars[s]), (uint32_t)((k / kStages) & 1), kWaitLimit);
+        if (__syncthreads_or(!ok)) {
+            abandon(S, bars, k, ntile);
+            return;
+        }
+        float* R = stage_ptr(s, 0);
+        float* P = stage_ptr(s, 1);
+        // phase 1: P <- M^-1 R + beta P over the whole box (halo included)
+        for (int v = tid; v < kBY * (kBX / 4); v += kThreads) {
+            int row = v / (kBX / 4), c4 = v % (kBX / 4);
+            int j = j0 - 1 + row, i = i0 - 4 + 4 * c4;
+            float4 rv = reinterpret_cast<float4*>(R)[v];
+            float4 pv = reinterpret_cast<float4*>(P)[v];
+            float4 o;
+            o.x = a.st.minv32[ebits32t(a, i, j)] * rv.x;
+            o.y = a.st.minv32[ebits32t(a, i + 1, j)] * rv.y;
+            o.z = a.st.minv32[ebits32t(a, i + 2, j)] * rv.z;
+            o.w = a.st.minv32[ebits32t(a, i + 3, j)] * rv.w;
+            if (!first) {
+                o.x = fmaf(beta, pv.x, o.x);
+                o.y = fmaf(beta, pv.y, o.y);
+                o.z = fmaf(beta, pv.z, o.z);
+                o.w = fmaf(beta, pv.w, o.w);
+            }
+            reinterpret_cast<float4*>(P)[v] = o;
+        }
+        __syncthreads();
+        // phase 2: q = A p on the owned cells, p.q, store p
+        float part = 0.f;
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) {
+            const int row = 2 * warp + rr, j = j0 + row, i = i0 + 4 * lane;
+            float4 pc;
+            float4 q = apply4(a, P, lane, row, i, j, pc);
+            if (j < a.ny && i < a.nx) {
+                part = fmaf(pc.x, q.x, part);
+                if (i + 1 < a.nx) part = fmaf(pc.y, q.y, part);
+                if (i + 2 < a.nx) part = fmaf(pc.z, q.z, part);
+                if (i + 3 < a.nx) part = fmaf(pc.w, q.w, part);
+                put4(a, pnew, i, j, pc, true);
+            }
+        }
+        acc = acc + (double)part;
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0 && k + kStages < ntile) issue(k + kStages);
+    }
+    double tot = block_sum(acc, red);
+    if (tid == 0) a.part0[blockIdx.x] = tot;
+    if (last_block_arrive(&S->ticket[5])) {
+        double pq = final_tree(a.part0, gridDim.x);
+        if (tid == 0) {
+            S->ticket[5] = 0;
+            S->restart = 0;
+            if (isnan(pq))
+                S->status = ST_NAN;
+            else if (!(pq > 0.0))
+                S->inner_status = ST_BREAKDOWN;  // FP32 noise floor: refine and restart
+            else
+                S->alpha_in = S->rho_in / pq;
+        }
+    }
+}
+
+// K2: recompute A p, update e and r, r.z and r.r
+__global__ void __launch_bounds__(kThreads, 2)
+    k_tma_update32(const __grid_constant__ CUtensorMap map_e, const __grid_constant__ CUtensorMap map_r,
+                   const __grid_constant__ CUtensorMap map_pa, const __grid_constant__ CUtensorMap map_pb, Cg32T a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[kStages];
+    __shared__ double red[kThreads / 32];
+    SolverState* S = a.S;
+    if (!running(S)) return;
+    const int it = S->inner_iter;
+    const CUtensorMap* map_p = (it & 1) ? &map_pa : &map_pb;
+    const float alpha = (float)S->alpha_in, malpha = -alpha;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ntile = (a.tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    unsigned char* sb = smem + ((128u - (smem_u32(smem) & 127u)) & 127u);  // TMA wants 128-byte slots
+    auto stage_ptr = [&](int s, int arr) { return reinterpret_cast<float*>(sb + (s * 3 + arr) * kSlot); };
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int k) {
+        int t = (int)blockIdx.x + k * (int)gridDim.x;
+        int s = k % kStages;
+        int x = (t % a.tiles_x) * kTW, y = (t / a.tiles_x) * kTH;
+        uint32_t bar = smem_u32(&bars[s]);
+        mbar_expect_tx(bar, 3 * kBoxBytes);
+        tma_load_2d(smem_u32(stage_ptr(s, 0)), map_p, x, y, bar);
+        tma_load_2d(smem_u32(stage_ptr(s, 1)), &map_e, x, y, bar);
+        tma_load_2d(smem_u32(stage_ptr(s, 2)), &map_r, x, y, bar);
+    };
+    if (tid == 0)
+        for (int k = 0; k < kStages && k < ntile; ++k) issue(k);
+    double arz = 0.0, arr = 0.0;
+    for (int k = 0; k < ntile; ++k) {
+        const int s = k % kStages;
+        const int t = (int)blockIdx.x + k * (int)gridDim.x;
+        const int i0 = (t % a.tiles_x) * kTW, j0 = (t / a.tiles_x) * kTH;
+        bool ok = mbar_wait(smem_u32(&bars[s]), (uint32_t)((k / kStages) & 1), kWaitLimit);
+        if (__syncthreads_or(!ok)) {
+            abandon(S, bars, k, ntile);
+            return;
+        }
+        const float* P = stage_ptr(s, 0);
+        const float* E = stage_ptr(s, 1);
+        const float* R = stage_ptr(s, 2);
+        float prz = 0.f, prr = 0.f;
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) {
+            const int row = 2 * warp + rr, j = j0 + row, i = i0 + 4 * lane;
+            float4 pc;
+            float4 q = apply4(a, P, lane, row, i, j, pc);
+            const int off = (row + 1) * kBX + 4 + 4 * lane;
+            float4 ev = *reinterpret_cast<const float4*>(E + off);
+            float4 rv = *reinterpret_cast<const float4*>(R + off);
+            ev.x = fmaf(alpha, pc.x, ev.x);
+            ev.y = fmaf(alpha, pc.y, ev.y);
+            ev.z = fmaf(alpha, pc.z, ev.z);
+            ev.w = fmaf(alpha, pc.w, ev.w);
+            rv.x = fmaf(malpha, q.x, rv.x);
+            rv.y = fmaf(malpha, q.y, rv.y);
+            rv.z = fmaf(malpha, q.z, rv.z);
+            rv.w = fmaf(malpha, q.w, rv.w);
+            if (j < a.ny && i < a.nx) {
+                float rvs[4] = {rv.x, rv.y, rv.z, rv.w};
+                for (int c = 0; c < 4; ++c)
+                    if (i + c < a.nx) {
+                        float z = a.st.minv32[ebits32t(a, i + c, j)] * rvs[c];
+                        prz = fmaf(rvs[c], z, prz);
+                        prr = fmaf(rvs[c], rvs[c], prr);
+                    }
+                put4(a, a.e, i, j, ev, false);
+                put4(a, a.r, i, j, rv, true);
+            }
+        }
+        arz = arz + (double)prz;
+        arr = arr + (double)prr;
+        __syncthreads();
+        if (tid == 0 && k + kStages < ntile) issue(k + kStages);
+    }
+    double trz = block_sum(arz, red);
+    double trr = block_sum(arr, red);
+    if (tid == 0) {
+        a.part0[blockIdx.x] = trz;
+        a.part1[blockIdx.x] = trr;
+    }
+    if (last_block_arrive(&S->ticket[6])) {
+        double rz = final_tree(a.part0, gridDim.x);
+        double rr = final_tree(a.part1, gridDim.x);
+        if (tid == 0) {
+            S->ticket[6] = 0;
+            S->rho_prev = S->rho_in;
+            S->beta_in = rz / S->rho_in;
+            S->rho_in = rz;
+            S->rr_in = rr;
+            if (rr > S->rr_in0) S->rr_in0 = rr;
+            S->inner_iter = it + 1;
+            S->iter = S->iter + 1;
+            // reliable update when the recursive residual fell by delta since
+            // the last one, or already looks converged
+            if (isnan(rr))
+                S->status = ST_NAN;
+            else if (rr <= S->tau2 * S->rr_in0 || rr <= S->target2)
+                S->inner_status = ST_CONVERGED;
+            else if (S->iter >= S->max_iter)
+                S->inner_status = ST_MAXIT;
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// host side
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 2-D map over a ghosted FP32 vector's storage (pitch x (ny + 2) floats)
+static int make_map(cf_ctx* c, CUtensorMap* m, float* base) {
+    auto fn = encode_fn();
+    if (!fn) return fail(c, CF_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    cuuint64_t dims[2] = {(cuuint64_t)c->p32, (cuuint64_t)(c->ph.ny + 2)};
+    cuuint64_t strides[1] = {(cuuint64_t)c->p32 * sizeof(float)};
+    cuuint32_t box[2] = {(cuuint32_t)kBX, (cuuint32_t)kBY};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(c, CF_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return CF_OK;
+}
+
+int cg32_setup(cf_ctx* c) {
+    int rc = make_map(c, &c->map_e, c->e32b);
+    if (!rc) rc = make_map(c, &c->map_r, c->r32b);
+    if (!rc) rc = make_map(c, &c->map_pa, c->pa32b);
+    if (!rc) rc = make_map(c, &c->map_pb, c->pb32b);
+    if (rc) return rc;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    c->tiles_x = (c->ph.nx + kTW - 1) / kTW;
+    c->tiles = c->tiles_x * ((c->ph.ny + kTH - 1) / kTH);
+    c->cta32 = c->tiles < 2 * sms ? c->tiles : 2 * sms;
+    rc = cuda_check(c, cudaFuncSetAttribute(k_tma_dir_matvec32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            kStages * 2 * kSlot + 128),
+                    "smem attribute");
+    if (!rc)
+        rc = cuda_check(c, cudaFuncSetAttribute(k_tma_update32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                kStages * 3 * kSlot + 128),
+                        "smem attribute");
+    return rc;
+}
+
+void cg32_launch_iteration(cf_ctx* c, const Stencil& st) {
+    Cg32T a{};
+    a.nx = c->ph.nx;
+    a.ny = c->ph.ny;
+    a.per_x = c->ph.per_x;
+    a.per_y = c->ph.per_y;
+    a.tiles_x = c->tiles_x;
+    a.tiles = c->tiles;
+    a.pitch = c->p32;
+    a.st = st;
+    a.e = c->e32.a;
+    a.r = c->r32.a;
+    a.pa = c->pa32.a;
+    a.pb = c->pb32.a;
+    a.part0 = c->partials;
+    a.part1 = c->partials + c->n_units;
+    a.S = c->S;
+    k_tma_dir_matvec32<<<c->cta32, kThreads, kStages * 2 * kSlot + 128, c->stream>>>(c->map_r, c->map_pa, c->map_pb, a);
+    k_tma_update32<<<c->cta32, kThreads, kStages * 3 * kSlot + 128, c->stream>>>(c->map_e, c->map_r, c->map_pa,
+                                                                            c->map_pb, a);
+}
+
+}  // namespace cf

@@ -3,6 +3,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
+
 #include "../../include/cajitafluids_gb300.h"
 #include "cf_internal.cuh"
 
@@ -21,7 +23,13 @@ struct cf_ctx {
     // solver vectors (owned cells)
     int vpitch = 0;
     cf::Vec64 x{}, r{}, pa{}, pb{}, qv{}, b{};
+    // FP32 vectors with a one-cell ghost ring: element (i, j) at a[j * p32 + i],
+    // storage base = a - p32 - 4 (see cf_cg32.cu)
     cf::Vec32 e32{}, r32{}, pa32{}, pb32{};
+    float *e32b = nullptr, *r32b = nullptr, *pa32b = nullptr, *pb32b = nullptr;
+    int p32 = 0;
+    CUtensorMap map_e{}, map_r{}, map_pa{}, map_pb{};
+    int tiles_x = 0, tiles = 0, cta32 = 0;
     double* partials = nullptr;  // 4 * n_units
     int G = 0, B = 0, n_units = 0;
     cf::SolverState* S = nullptr;   // device
@@ -71,5 +79,8 @@ struct SolveResult {
     double bb, rr, div_l2, div_linf;
 };
 int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res);
+// FP32 TMA inner CG (cf_cg32.cu)
+int cg32_setup(cf_ctx* c);
+void cg32_launch_iteration(cf_ctx* c, const Stencil& st);
 int div_norms(cf_ctx* c, double* l2, double* linf);
 }  // namespace cf

@@ -23,7 +23,7 @@
 namespace cf {
 
 enum Entity { E_CELL = 0, E_FACEI = 1, E_FACEJ = 2 };
-enum SolveStatus { ST_CONVERGED = 0, ST_MAXIT = 1, ST_BREAKDOWN = 2, ST_NAN = 3, ST_RUNNING = 100 };
+enum SolveStatus { ST_CONVERGED = 0, ST_MAXIT = 1, ST_BREAKDOWN = 2, ST_NAN = 3, ST_TIMEOUT = 4, ST_RUNNING = 100 };
 
 template <typename T>
 struct Grid {

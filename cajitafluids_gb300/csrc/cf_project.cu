@@ -245,6 +245,22 @@ __device__ __forceinline__ double div_b(const DivArgs& a, int gi, int gj) {
     return a.mscale * t;
 }
 
+// FP32 solver vectors carry a ghost ring (cf_cg32.cu); r's periodic ghost
+// copies are written by whoever writes r.
+__device__ __forceinline__ void put_r32(float* o, int pitch, int nx, int ny, int per_x, int per_y, int i, int j,
+                                        float val) {
+    const ptrdiff_t row = (ptrdiff_t)j * pitch;
+    o[row + i] = val;
+    if (per_x) {
+        if (i == 0) o[row + nx] = val;
+        if (i == nx - 1) o[row - 1] = val;
+    }
+    if (per_y) {
+        if (j == 0) o[(ptrdiff_t)ny * pitch + i] = val;
+        if (j == ny - 1) o[-(ptrdiff_t)pitch + i] = val;
+    }
+}
+
 // FP64 init: b, r = b, x = 0, partial r.z and r.r
 __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init64(DivArgs a) {
     SolverState* S = a.S;
@@ -318,12 +334,11 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
                 if (c >= a.nx) continue;
                 double b = div_b(a, c, j);
                 size_t k = (size_t)j * a.pitch + c;
-                size_t k32 = (size_t)j * a.pitch32 + c;
                 a.b[k] = b;
                 a.x[k] = 0.0;
                 float r = (float)b;
-                a.r32[k32] = r;
-                a.e32[k32] = 0.f;
+                put_r32(a.r32, a.pitch32, a.nx, a.ny, a.per_x, a.per_y, c, j, r);
+                a.e32[(ptrdiff_t)j * a.pitch32 + c] = 0.f;
                 float z = a.st.minv32[edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y)] * r;
                 abb = fma(b, b, abb);
                 arz = fmaf(r, z, arz);
@@ -370,220 +385,13 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
     }
 }
 
-// --------------------------------------------------------------------------
-// Mixed inner solve (FP32 vectors).
-struct Cg32 {
-    int nx, ny, per_x, per_y, G, U, pitch;
-    Stencil st;
-    float *e, *r, *pa, *pb;
-    double *part0, *part1;
-    SolverState* S;
-};
-
-__device__ __forceinline__ int ebits32(const Cg32& a, int c, int j) {
-    return edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y);
-}
-
-__device__ __forceinline__ float pn1f(const Cg32& a, const float* pold, int c, int j, bool first, float beta) {
-    int cc = wrap_index(c, a.nx, a.per_x), jj = wrap_index(j, a.ny, a.per_y);
-    if (cc < 0 || jj < 0) return 0.f;
-    size_t k = (size_t)jj * a.pitch + cc;
-    float z = a.st.minv32[ebits32(a, cc, jj)] * __ldg(a.r + k);
-    return first ? z : fmaf(beta, __ldg(pold + k), z);
-}
-
-__device__ __forceinline__ float2 pn2f(const Cg32& a, const float* pold, int c0, int j, bool first, float beta) {
-    int jj = wrap_index(j, a.ny, a.per_y);
-    if (jj < 0) return make_float2(0.f, 0.f);
-    if (c0 + 1 < a.nx) {
-        size_t k = (size_t)jj * a.pitch + c0;
-        float2 rv = __ldg(reinterpret_cast<const float2*>(a.r + k));
-        float z0 = a.st.minv32[ebits32(a, c0, jj)] * rv.x;
-        float z1 = a.st.minv32[ebits32(a, c0 + 1, jj)] * rv.y;
-        if (first) return make_float2(z0, z1);
-        float2 po = __ldg(reinterpret_cast<const float2*>(pold + k));
-        return make_float2(fmaf(beta, po.x, z0), fmaf(beta, po.y, z1));
-    }
-    return make_float2(pn1f(a, pold, c0, jj, first, beta), pn1f(a, pold, c0 + 1, jj, first, beta));
-}
-
-// plain read of the (final) direction at one cell / two cells
-__device__ __forceinline__ float p1f(const Cg32& a, const float* p, int c, int j) {
-    int cc = wrap_index(c, a.nx, a.per_x), jj = wrap_index(j, a.ny, a.per_y);
-    if (cc < 0 || jj < 0) return 0.f;
-    return __ldg(p + (size_t)jj * a.pitch + cc);
-}
-
-__device__ __forceinline__ float2 p2f(const Cg32& a, const float* p, int c0, int j) {
-    int jj = wrap_index(j, a.ny, a.per_y);
-    if (jj < 0) return make_float2(0.f, 0.f);
-    if (c0 + 1 < a.nx) return __ldg(reinterpret_cast<const float2*>(p + (size_t)jj * a.pitch + c0));
-    return make_float2(p1f(a, p, c0, jj), p1f(a, p, c0 + 1, jj));
-}
-
-__device__ __forceinline__ float stencil32(const Cg32& a, int c, int j, float pc, float w, float e, float s,
-                                           float n) {
-    float q = a.st.diag32[ebits32(a, c, j)] * pc;
-    q = fmaf(a.st.ms32, w, q);
-    q = fmaf(a.st.ms32, e, q);
-    q = fmaf(a.st.ms32, s, q);
-    q = fmaf(a.st.ms32, n, q);
-    return q;
-}
-
-__device__ __forceinline__ bool inner_running(const SolverState* S) {
-    return *(volatile const int*)&S->status == ST_RUNNING &&
-           *(volatile const int*)&S->inner_status == ST_RUNNING;
-}
-
-__global__ void __launch_bounds__(CF_RED_THREADS) k_in_dir_matvec32(Cg32 a) {
-    SolverState* S = a.S;
-    if (!inner_running(S)) return;
-    const int it = S->inner_iter;
-    const bool first = it == 0 || S->restart;
-    const float beta = (float)S->beta_in;
-    const float* pold = (it & 1) ? a.pb : a.pa;
-    float* pnew = (it & 1) ? a.pa : a.pb;
-    const int lane = threadIdx.x & 31;
-    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
-    float acc = 0.f;
-    if (unit < a.U) {
-        const int g = unit % a.G, band = unit / a.G;
-        const int c0 = g * CF_UNIT_COLS + 2 * lane;
-        const int j0 = band * CF_BAND_ROWS;
-        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
-        float2 pm = pn2f(a, pold, c0, j0 - 1, first, beta);
-        float2 pc = pn2f(a, pold, c0, j0, first, beta);
-        for (int j = j0; j < j1; ++j) {
-            float2 pp = pn2f(a, pold, c0, j + 1, first, beta);
-            float left = __shfl_up_sync(FULLMASK, pc.y, 1);
-            float right = __shfl_down_sync(FULLMASK, pc.x, 1);
-            if (lane == 0) left = pn1f(a, pold, c0 - 1, j, first, beta);
-            if (lane == 31) right = pn1f(a, pold, c0 + 2, j, first, beta);
-            if (c0 < a.nx) {
-                size_t k = (size_t)j * a.pitch + c0;
-                float q0 = stencil32(a, c0, j, pc.x, left, pc.y, pm.x, pp.x);
-                acc = fmaf(pc.x, q0, acc);
-                if (c0 + 1 < a.nx) {
-                    float q1 = stencil32(a, c0 + 1, j, pc.y, pc.x, right, pm.y, pp.y);
-                    acc = fmaf(pc.y, q1, acc);
-                    *reinterpret_cast<float2*>(pnew + k) = pc;
-                } else {
-                    pnew[k] = pc.x;
-                }
-            }
-            pm = pc;
-            pc = pp;
-        }
-    }
-    double dacc = warp_fold((double)acc);
-    if (unit < a.U && lane == 0) a.part0[unit] = dacc;
-    if (last_block_arrive(&S->ticket[5])) {
-        double pq = final_tree(a.part0, a.U);
-        if (threadIdx.x == 0) {
-            S->ticket[5] = 0;
-            S->restart = 0;
-            if (isnan(pq))
-                S->status = ST_NAN;
-            else if (!(pq > 0.0))
-                S->inner_status = ST_BREAKDOWN;  // FP32 noise floor: refine and restart
-            else
-                S->alpha_in = S->rho_in / pq;
-        }
-    }
-}
-
-__global__ void __launch_bounds__(CF_RED_THREADS) k_in_update32(Cg32 a) {
-    SolverState* S = a.S;
-    if (!inner_running(S)) return;
-    const int it = S->inner_iter;
-    const float* pv = (it & 1) ? a.pa : a.pb;
-    const float alpha = (float)S->alpha_in, malpha = -alpha;
-    const int lane = threadIdx.x & 31;
-    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
-    float arz = 0.f, arr = 0.f;
-    if (unit < a.U) {
-        const int g = unit % a.G, band = unit / a.G;
-        const int c0 = g * CF_UNIT_COLS + 2 * lane;
-        const int j0 = band * CF_BAND_ROWS;
-        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
-        float2 pm = p2f(a, pv, c0, j0 - 1);
-        float2 pc = p2f(a, pv, c0, j0);
-        for (int j = j0; j < j1; ++j) {
-            float2 pp = p2f(a, pv, c0, j + 1);
-            float left = __shfl_up_sync(FULLMASK, pc.y, 1);
-            float right = __shfl_down_sync(FULLMASK, pc.x, 1);
-            if (lane == 0) left = p1f(a, pv, c0 - 1, j);
-            if (lane == 31) right = p1f(a, pv, c0 + 2, j);
-            if (c0 < a.nx) {
-                size_t k = (size_t)j * a.pitch + c0;
-                float q0 = stencil32(a, c0, j, pc.x, left, pc.y, pm.x, pp.x);
-                if (c0 + 1 < a.nx) {
-                    float q1 = stencil32(a, c0 + 1, j, pc.y, pc.x, right, pm.y, pp.y);
-                    float2 ev = *reinterpret_cast<const float2*>(a.e + k);
-                    float2 rv = *reinterpret_cast<const float2*>(a.r + k);
-                    ev.x = fmaf(alpha, pc.x, ev.x);
-                    ev.y = fmaf(alpha, pc.y, ev.y);
-                    rv.x = fmaf(malpha, q0, rv.x);
-                    rv.y = fmaf(malpha, q1, rv.y);
-                    float z0 = a.st.minv32[ebits32(a, c0, j)] * rv.x;
-                    float z1 = a.st.minv32[ebits32(a, c0 + 1, j)] * rv.y;
-                    arz = fmaf(rv.x, z0, arz);
-                    arr = fmaf(rv.x, rv.x, arr);
-                    arz = fmaf(rv.y, z1, arz);
-                    arr = fmaf(rv.y, rv.y, arr);
-                    *reinterpret_cast<float2*>(a.e + k) = ev;
-                    *reinterpret_cast<float2*>(a.r + k) = rv;
-                } else {
-                    float ev = fmaf(alpha, pc.x, a.e[k]);
-                    float rv = fmaf(malpha, q0, a.r[k]);
-                    float z0 = a.st.minv32[ebits32(a, c0, j)] * rv;
-                    arz = fmaf(rv, z0, arz);
-                    arr = fmaf(rv, rv, arr);
-                    a.e[k] = ev;
-                    a.r[k] = rv;
-                }
-            }
-            pm = pc;
-            pc = pp;
-        }
-    }
-    double drz = warp_fold((double)arz), drr = warp_fold((double)arr);
-    if (unit < a.U && lane == 0) {
-        a.part0[unit] = drz;
-        a.part1[unit] = drr;
-    }
-    if (last_block_arrive(&S->ticket[6])) {
-        double rz = final_tree(a.part0, a.U);
-        double rr = final_tree(a.part1, a.U);
-        if (threadIdx.x == 0) {
-            S->ticket[6] = 0;
-            S->rho_prev = S->rho_in;
-            S->beta_in = rz / S->rho_in;
-            S->rho_in = rz;
-            S->rr_in = rr;
-            if (rr > S->rr_in0) S->rr_in0 = rr;
-            S->inner_iter = it + 1;
-            S->iter = S->iter + 1;
-            // reliable update when the recursive residual fell by delta since
-            // the last one, or already looks converged
-            if (isnan(rr))
-                S->status = ST_NAN;
-            else if (rr <= S->tau2 * S->rr_in0 || rr <= S->target2)
-                S->inner_status = ST_CONVERGED;
-            else if (S->iter >= S->max_iter)
-                S->inner_status = ST_MAXIT;
-        }
-    }
-}
-
 // Outer refinement, part 1: x += e (FP64 += FP32)
 __global__ void k_outer_add(double* x, const float* e, int nx, int ny, int pitch, int pitch32) {
     int gi = blockIdx.x * blockDim.x + threadIdx.x;
     int gj = blockIdx.y * blockDim.y + threadIdx.y;
     if (gi >= nx || gj >= ny) return;
     size_t k = (size_t)gj * pitch + gi;
-    x[k] = x[k] + (double)e[(size_t)gj * pitch32 + gi];
+    x[k] = x[k] + (double)e[(ptrdiff_t)gj * pitch32 + gi];
 }
 
 // Outer refinement, part 2: r = b - A x in FP64; inner r = (float)r, e = 0.
@@ -628,9 +436,8 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
                 double r = a.b[(size_t)j * a.pitch + c] - ax;
                 arr64 = fma(r, r, arr64);
                 float r32 = (float)r;
-                size_t k32 = (size_t)j * a.pitch32 + c;
-                a.r32[k32] = r32;
-                a.e32[k32] = 0.f;
+                put_r32(a.r32, a.pitch32, a.nx, a.ny, a.per_x, a.per_y, c, j, r32);
+                a.e32[(ptrdiff_t)j * a.pitch32 + c] = 0.f;
                 float z = a.st.minv32[eb] * r32;
                 arz = fmaf(r32, z, arz);
                 arr = fmaf(r32, r32, arr);
@@ -778,7 +585,7 @@ static DivArgs div_args(cf_ctx* c, const Stencil& st) {
     a.G = c->G;
     a.U = c->n_units;
     a.pitch = c->vpitch;
-    a.pitch32 = c->vpitch;
+    a.pitch32 = c->p32;
     a.u = c->u[c->cur];
     a.v = c->v[c->cur];
     a.mscale = -(1.0 / c->ph.dx);
@@ -817,26 +624,6 @@ static Cg64 cg64_args(cf_ctx* c, const Stencil& st) {
     return a;
 }
 
-static Cg32 cg32_args(cf_ctx* c, const Stencil& st) {
-    Cg32 a{};
-    a.nx = c->ph.nx;
-    a.ny = c->ph.ny;
-    a.per_x = c->ph.per_x;
-    a.per_y = c->ph.per_y;
-    a.G = c->G;
-    a.U = c->n_units;
-    a.pitch = c->vpitch;
-    a.st = st;
-    a.e = c->e32.a;
-    a.r = c->r32.a;
-    a.pa = c->pa32.a;
-    a.pb = c->pb32.a;
-    a.part0 = c->partials;
-    a.part1 = c->partials + c->n_units;
-    a.S = c->S;
-    return a;
-}
-
 static int red_blocks(const cf_ctx* c) { return (c->n_units + CF_RED_WARPS - 1) / CF_RED_WARPS; }
 
 static const int kBatch = CF_CG_BATCH;  // CG iterations per graph launch
@@ -855,11 +642,7 @@ static int ensure_graph(cf_ctx* c, const Stencil& st, bool mixed) {
     if (rc) return rc;
     int nb = red_blocks(c);
     if (mixed) {
-        Cg32 a = cg32_args(c, st);
-        for (int i = 0; i < kBatch; ++i) {
-            k_in_dir_matvec32<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
-            k_in_update32<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
-        }
+        for (int i = 0; i < kBatch; ++i) cg32_launch_iteration(c, st);
     } else {
         Cg64 a = cg64_args(c, st);
         for (int i = 0; i < kBatch; ++i) {
@@ -955,7 +738,7 @@ int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res) {
         oa.G = c->G;
         oa.U = c->n_units;
         oa.pitch = c->vpitch;
-        oa.pitch32 = c->vpitch;
+        oa.pitch32 = c->p32;
         oa.st = st;
         oa.x = c->x.a;
         oa.b = c->b.a;
@@ -980,7 +763,7 @@ int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res) {
                 batch_profile(c, c->hS->iter - prev_iter);
             }
             if (c->hS->status != ST_RUNNING) break;
-            k_outer_add<<<grd, blk, 0, c->stream>>>(c->x.a, c->e32.a, c->ph.nx, c->ph.ny, c->vpitch, c->vpitch);
+            k_outer_add<<<grd, blk, 0, c->stream>>>(c->x.a, c->e32.a, c->ph.nx, c->ph.ny, c->vpitch, c->p32);
             k_outer_resid<<<nb, CF_RED_THREADS, 0, c->stream>>>(oa);
             c->launches += 2;
             if ((rc = read_state(c))) return rc;

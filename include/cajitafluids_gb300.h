@@ -50,6 +50,7 @@ extern "C" {
 #define CF_ERR_NUMERIC (-5)       /* NaN/Inf or CG breakdown; state is consistent */
 #define CF_ERR_NOMEM (-6)         /* device allocation failed */
 #define CF_ERR_MESH (-7)          /* extent not evenly divisible (src/Mesh.hpp:478-486) */
+#define CF_ERR_TIMEOUT (-9)       /* a bounded device-side wait ran out; state is consistent */
 
 /* fields */
 #define CF_FIELD_QUANTITY 0 /* cell-centred advected scalar          */
@@ -76,6 +77,7 @@ extern "C" {
 #define CF_SOLVE_MAX_ITER 1
 #define CF_SOLVE_BREAKDOWN 2
 #define CF_SOLVE_NAN 3
+#define CF_SOLVE_TIMEOUT 4
 
 typedef struct cf_ctx cf_ctx;
 
