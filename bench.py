@@ -43,7 +43,7 @@ KERNEL_BYTES_MIXED_ITER = 32.0
 # CPU oracle are bit-identical, so they take the same count); the reference
 # arm extrapolates its sampled CG cost to this count.  Measured by this
 # bench's FP64 leg on GB300 (see fp64.cg_iters_per_step in its output).
-FP64_ITERS_PER_STEP_4096 = None
+FP64_ITERS_PER_STEP_4096 = 7890
 
 
 def env_int(name, default):

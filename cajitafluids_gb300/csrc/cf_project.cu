@@ -104,8 +104,14 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_cg_dir_matvec64(Cg64 a) {
             double2 pp = pn2(a, pold, c0, j + 1, first, beta);
             double left = __shfl_up_sync(FULLMASK, pc.y, 1);
             double right = __shfl_down_sync(FULLMASK, pc.x, 1);
-            if (lane == 0) left = pn1(a, pold, c0 - 1, j, first, beta);
-            if (lane == 31) right = pn1(a, pold, c0 + 2, j, first, beta);
+            // the two cells just outside the warp's 64 columns, in one branch
+            if (lane == 0 || lane == 31) {
+                double ext = pn1(a, pold, lane == 0 ? c0 - 1 : c0 + 2, j, first, beta);
+                if (lane == 0)
+                    left = ext;
+                else
+                    right = ext;
+            }
             if (c0 < a.nx) {
                 size_t k = (size_t)j * a.pitch + c0;
                 double q0 = a.st.diag[ebits(a, c0, j)] * pc.x;

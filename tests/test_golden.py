@@ -1,0 +1,117 @@
+"""Committed golden fixtures (tests/golden/*.npz, made by make_golden.py).
+
+CPU: the oracle reproduces them bit for bit (it is deterministic and
+contraction-free, so x86 and Arm give the same bits).
+GPU: the FP64 CUDA path reproduces them bit for bit through the C ABI.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import Oracle
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+INFLOW = ((0.45, 0.10), (0.10, 0.05), (0.0, 3.0), 1.0)
+
+
+def _load(name):
+    return dict(np.load(os.path.join(GOLDEN, name)))
+
+
+def _run_config0(sim, g, gpu):
+    n = int(g["n"])
+    dt = float(g["dt"])
+    its = []
+    if gpu:
+        from cajitafluids_gb300 import SolverOptions
+        o = SolverOptions(tol=float(g["tol"]), max_iter=20000)
+        its.append(sim.setup(dt, o)["iterations"])
+        for _ in range(int(g["steps"])):
+            its.append(sim.step(dt, int(g["order"]), o)["iterations"])
+    else:
+        its.append(sim.setup(dt, tol=float(g["tol"]), max_iter=20000)["iterations"])
+        for _ in range(int(g["steps"])):
+            its.append(sim.step(dt, int(g["order"]), tol=float(g["tol"]), max_iter=20000)["iterations"])
+    return np.array(its)
+
+
+def test_oracle_reproduces_config0_fixture(built):
+    g = _load("config0_32.npz")
+    n = int(g["n"])
+    o = Oracle(n, n, source=INFLOW, density=0.1)
+    its = _run_config0(o, g, gpu=False)
+    assert np.array_equal(its, g["iterations"])
+    for f in ("q", "u", "v", "p"):
+        assert np.array_equal(o.get(f), g[f]), f
+
+
+def test_oracle_reproduces_periodic_fixture(built):
+    g = _load("periodic_spectral_32.npz")
+    n = int(g["n"])
+    o = Oracle(n, n, periodic=(True, True), density=0.1)
+    for f in ("q", "u", "v"):
+        o.set(f, g[f + "0"])
+    its = [o.step(float(g["dt"]), 3, tol=0.0, abs_tol=float(g["abs_tol"]), max_iter=20000)["iterations"]
+           for _ in range(int(g["steps"]))]
+    assert np.array_equal(its, g["iterations"])
+    for f in ("q", "u", "v", "p"):
+        assert np.array_equal(o.get(f), g[f]), f
+
+
+def test_oracle_reproduces_interpolation_fixture(built):
+    g = _load("interp_kat_24.npz")
+    n = int(g["n"])
+    o = Oracle(n, n, periodic=(True, True))
+    for f in ("q", "u", "v"):
+        o.set(f, g[f])
+    o.fill_ghosts()
+    for f in ("q", "u", "v"):
+        for order in (1, 3):
+            assert np.array_equal(o.sample(f, order, g["xy"]), g[f"{f}_o{order}"])
+    assert np.array_equal(o.trace(g["xy"], 0.01), g["trace"])
+
+
+@pytest.mark.gpu
+def test_gpu_reproduces_config0_fixture(built):
+    from cajitafluids_gb300 import Context
+    g = _load("config0_32.npz")
+    n = int(g["n"])
+    c = Context(n, n)
+    c.set_source(*INFLOW)
+    c.set_density(0.1)
+    its = _run_config0(c, g, gpu=True)
+    assert np.array_equal(its, g["iterations"])
+    for f in ("q", "u", "v", "p"):
+        assert np.array_equal(c.download(f), g[f]), f
+
+
+@pytest.mark.gpu
+def test_gpu_reproduces_periodic_fixture(built):
+    from cajitafluids_gb300 import Context, SolverOptions
+    g = _load("periodic_spectral_32.npz")
+    n = int(g["n"])
+    c = Context(n, n, periodic=(True, True))
+    c.set_density(0.1)
+    for f in ("q", "u", "v"):
+        c.upload(f, g[f + "0"])
+    o = SolverOptions(tol=0.0, abs_tol=float(g["abs_tol"]), max_iter=20000)
+    its = [c.step(float(g["dt"]), 3, o)["iterations"] for _ in range(int(g["steps"]))]
+    assert np.array_equal(its, g["iterations"])
+    for f in ("q", "u", "v", "p"):
+        assert np.array_equal(c.download(f), g[f]), f
+
+
+@pytest.mark.gpu
+def test_gpu_reproduces_interpolation_fixture(built):
+    from cajitafluids_gb300 import Context
+    g = _load("interp_kat_24.npz")
+    n = int(g["n"])
+    c = Context(n, n, periodic=(True, True))
+    for f in ("q", "u", "v"):
+        c.upload(f, g[f])
+    c.fill_ghosts()
+    for f in ("q", "u", "v"):
+        for order in (1, 3):
+            assert np.array_equal(c.interp_points(f, order, g["xy"]), g[f"{f}_o{order}"])
+    assert np.array_equal(c.trace_points(g["xy"], 0.01), g["trace"])
