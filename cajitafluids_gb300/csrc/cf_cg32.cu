@@ -145,6 +145,7 @@ __device__ __forceinline__ float stencil1(const Cg32T& a, int i, int j, float c,
 
 // A p for the four cells (i0..i0+3, j) of a lane from the shared tile P
 // (row stride kBX, owned (c, r) at [r + 1][c + 4]).
+template <bool INTERIOR>
 __device__ __forceinline__ float4 apply4(const Cg32T& a, const float* P, int lane, int row, int i0, int j,
                                          float4& pc) {
     const float* rc = P + (row + 1) * kBX + 4 + 4 * lane;
@@ -156,11 +157,28 @@ __device__ __forceinline__ float4 apply4(const Cg32T& a, const float* P, int lan
     if (lane == 0) left = rc[-1];
     if (lane == 31) right = rc[4];
     float4 q;
-    q.x = stencil1(a, i0, j, pc.x, left, pc.y, pu.x, pd.x);
-    q.y = stencil1(a, i0 + 1, j, pc.y, pc.x, pc.z, pu.y, pd.y);
-    q.z = stencil1(a, i0 + 2, j, pc.z, pc.y, pc.w, pu.z, pd.z);
-    q.w = stencil1(a, i0 + 3, j, pc.w, pc.z, right, pu.w, pd.w);
+    if (INTERIOR) {
+        const float d0 = a.st.diag32[0], ms = a.st.ms32;
+        q.x = fmaf(ms, pd.x, fmaf(ms, pu.x, fmaf(ms, pc.y, fmaf(ms, left, d0 * pc.x))));
+        q.y = fmaf(ms, pd.y, fmaf(ms, pu.y, fmaf(ms, pc.z, fmaf(ms, pc.x, d0 * pc.y))));
+        q.z = fmaf(ms, pd.z, fmaf(ms, pu.z, fmaf(ms, pc.w, fmaf(ms, pc.y, d0 * pc.z))));
+        q.w = fmaf(ms, pd.w, fmaf(ms, pu.w, fmaf(ms, right, fmaf(ms, pc.z, d0 * pc.w))));
+    } else {
+        q.x = stencil1(a, i0, j, pc.x, left, pc.y, pu.x, pd.x);
+        q.y = stencil1(a, i0 + 1, j, pc.y, pc.x, pc.z, pu.y, pd.y);
+        q.z = stencil1(a, i0 + 2, j, pc.z, pc.y, pc.w, pu.z, pd.z);
+        q.w = stencil1(a, i0 + 3, j, pc.w, pc.z, right, pu.w, pd.w);
+    }
     return q;
+}
+
+// true when no cell of the tile or of its halo is next to a wall: every
+// diagonal and preconditioner entry is then the interior value
+__device__ __forceinline__ bool interior_tile(const Cg32T& a, int i0, int j0) {
+    bool wx = !a.per_x && (i0 <= 1 || i0 + kTW >= a.nx - 1);
+    bool wy = !a.per_y && (j0 <= 1 || j0 + kTH >= a.ny - 1);
+    bool full = i0 + kTW <= a.nx && j0 + kTH <= a.ny;
+    return full && !(wx || wy);
 }
 
 __device__ __forceinline__ bool running(const SolverState* S) {
@@ -234,17 +252,26 @@ __global__ void __launch_bounds__(kThreads, 2)
         }
         float* R = stage_ptr(s, 0);
         float* P = stage_ptr(s, 1);
+        const bool inner = interior_tile(a, i0, j0);
         // phase 1: P <- M^-1 R + beta P over the whole box (halo included)
         for (int v = tid; v < kBY * (kBX / 4); v += kThreads) {
-            int row = v / (kBX / 4), c4 = v % (kBX / 4);
-            int j = j0 - 1 + row, i = i0 - 4 + 4 * c4;
             float4 rv = reinterpret_cast<float4*>(R)[v];
             float4 pv = reinterpret_cast<float4*>(P)[v];
             float4 o;
-            o.x = a.st.minv32[ebits32t(a, i, j)] * rv.x;
-            o.y = a.st.minv32[ebits32t(a, i + 1, j)] * rv.y;
-            o.z = a.st.minv32[ebits32t(a, i + 2, j)] * rv.z;
-            o.w = a.st.minv32[ebits32t(a, i + 3, j)] * rv.w;
+            if (inner) {
+                const float m0 = a.st.minv32[0];
+                o.x = m0 * rv.x;
+                o.y = m0 * rv.y;
+                o.z = m0 * rv.z;
+                o.w = m0 * rv.w;
+            } else {
+                int row = v / (kBX / 4), c4 = v % (kBX / 4);
+                int j = j0 - 1 + row, i = i0 - 4 + 4 * c4;
+                o.x = a.st.minv32[ebits32t(a, i, j)] * rv.x;
+                o.y = a.st.minv32[ebits32t(a, i + 1, j)] * rv.y;
+                o.z = a.st.minv32[ebits32t(a, i + 2, j)] * rv.z;
+                o.w = a.st.minv32[ebits32t(a, i + 3, j)] * rv.w;
+            }
             if (!first) {
                 o.x = fmaf(beta, pv.x, o.x);
                 o.y = fmaf(beta, pv.y, o.y);
@@ -260,7 +287,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         for (int rr = 0; rr < 2; ++rr) {
             const int row = 2 * warp + rr, j = j0 + row, i = i0 + 4 * lane;
             float4 pc;
-            float4 q = apply4(a, P, lane, row, i, j, pc);
+            float4 q = inner ? apply4<true>(a, P, lane, row, i, j, pc) : apply4<false>(a, P, lane, row, i, j, pc);
             if (j < a.ny && i < a.nx) {
                 part = fmaf(pc.x, q.x, part);
                 if (i + 1 < a.nx) part = fmaf(pc.y, q.y, part);
@@ -337,12 +364,13 @@ __global__ void __launch_bounds__(kThreads, 2)
         const float* P = stage_ptr(s, 0);
         const float* E = stage_ptr(s, 1);
         const float* R = stage_ptr(s, 2);
+        const bool inner = interior_tile(a, i0, j0);
         float prz = 0.f, prr = 0.f;
 #pragma unroll
         for (int rr = 0; rr < 2; ++rr) {
             const int row = 2 * warp + rr, j = j0 + row, i = i0 + 4 * lane;
             float4 pc;
-            float4 q = apply4(a, P, lane, row, i, j, pc);
+            float4 q = inner ? apply4<true>(a, P, lane, row, i, j, pc) : apply4<false>(a, P, lane, row, i, j, pc);
             const int off = (row + 1) * kBX + 4 + 4 * lane;
             float4 ev = *reinterpret_cast<const float4*>(E + off);
             float4 rv = *reinterpret_cast<const float4*>(R + off);
@@ -354,7 +382,14 @@ __global__ void __launch_bounds__(kThreads, 2)
             rv.y = fmaf(malpha, q.y, rv.y);
             rv.z = fmaf(malpha, q.z, rv.z);
             rv.w = fmaf(malpha, q.w, rv.w);
-            if (j < a.ny && i < a.nx) {
+            if (inner) {
+                const float m0 = a.st.minv32[0];
+                float s2 = fmaf(rv.w, rv.w, fmaf(rv.z, rv.z, fmaf(rv.y, rv.y, rv.x * rv.x)));
+                prr += s2;
+                prz = fmaf(m0, s2, prz);
+                put4(a, a.e, i, j, ev, false);
+                put4(a, a.r, i, j, rv, true);
+            } else if (j < a.ny && i < a.nx) {
                 float rvs[4] = {rv.x, rv.y, rv.z, rv.w};
                 for (int c = 0; c < 4; ++c)
                     if (i + c < a.nx) {
@@ -443,7 +478,6 @@ int cg32_setup(cf_ctx* c) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     c->tiles_x = (c->ph.nx + kTW - 1) / kTW;
     c->tiles = c->tiles_x * ((c->ph.ny + kTH - 1) / kTH);
-    c->cta32 = c->tiles < 2 * sms ? c->tiles : 2 * sms;
     rc = cuda_check(c, cudaFuncSetAttribute(k_tma_dir_matvec32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             kStages * 2 * kSlot + 128),
                     "smem attribute");
@@ -451,6 +485,21 @@ int cg32_setup(cf_ctx* c) {
         rc = cuda_check(c, cudaFuncSetAttribute(k_tma_update32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 kStages * 3 * kSlot + 128),
                         "smem attribute");
+    // persistent grids: as many CTAs as fit on the GPU at once
+    int occ1 = 0, occ2 = 0;
+    if (!rc)
+        rc = cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, k_tma_dir_matvec32, kThreads,
+                                                                         kStages * 2 * kSlot + 128),
+                        "occupancy");
+    if (!rc)
+        rc = cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_tma_update32, kThreads,
+                                                                         kStages * 3 * kSlot + 128),
+                        "occupancy");
+    if (rc) return rc;
+    occ1 = occ1 < 1 ? 1 : occ1;
+    occ2 = occ2 < 1 ? 1 : occ2;
+    c->cta32 = c->tiles < occ1 * sms ? c->tiles : occ1 * sms;
+    c->cta32b = c->tiles < occ2 * sms ? c->tiles : occ2 * sms;
     return rc;
 }
 
@@ -472,7 +521,7 @@ void cg32_launch_iteration(cf_ctx* c, const Stencil& st) {
     a.part1 = c->partials + c->n_units;
     a.S = c->S;
     k_tma_dir_matvec32<<<c->cta32, kThreads, kStages * 2 * kSlot + 128, c->stream>>>(c->map_r, c->map_pa, c->map_pb, a);
-    k_tma_update32<<<c->cta32, kThreads, kStages * 3 * kSlot + 128, c->stream>>>(c->map_e, c->map_r, c->map_pa,
+    k_tma_update32<<<c->cta32b, kThreads, kStages * 3 * kSlot + 128, c->stream>>>(c->map_e, c->map_r, c->map_pa,
                                                                             c->map_pb, a);
 }
 

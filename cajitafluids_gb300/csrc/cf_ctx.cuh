@@ -29,7 +29,7 @@ struct cf_ctx {
     float *e32b = nullptr, *r32b = nullptr, *pa32b = nullptr, *pb32b = nullptr;
     int p32 = 0;
     CUtensorMap map_e{}, map_r{}, map_pa{}, map_pb{};
-    int tiles_x = 0, tiles = 0, cta32 = 0;
+    int tiles_x = 0, tiles = 0, cta32 = 0, cta32b = 0;
     double* partials = nullptr;  // 4 * n_units
     int G = 0, B = 0, n_units = 0;
     cf::SolverState* S = nullptr;   // device
