@@ -75,5 +75,27 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+EXAMPLE_SRC = os.path.join(HERE, "cpp", "advection_gb300.cpp")
+EXAMPLE_HDR = os.path.join(HERE, "cpp", "CajitaFluidsGB300.hpp")
+EXAMPLE = os.path.join(HERE, "advection_gb300")
+
+
+def build_example(force: bool = False) -> str:
+    """The C++ driver over the reference-shaped interface (links libcfgpu.so)."""
+    lib = build_library()
+    if (not force and os.path.exists(EXAMPLE)
+            and all(os.path.getmtime(f) <= os.path.getmtime(EXAMPLE) for f in (EXAMPLE_SRC, EXAMPLE_HDR, lib))):
+        return EXAMPLE
+    cxx = os.environ.get("CXX", "g++")
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-Wextra", "-ffp-contract=off", f"-I{ROOT}", EXAMPLE_SRC,
+           f"-L{HERE}", "-lcfgpu", "-Wl,-rpath,$ORIGIN", "-o", EXAMPLE + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"example build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(EXAMPLE + ".tmp", EXAMPLE)
+    return EXAMPLE
+
+
 if __name__ == "__main__":
     print(build_library(force=True, verbose=True))
+    print(build_example(force=True))
