@@ -139,6 +139,9 @@ SIGNATURES = {
     "cf_profile_read": (ctypes.c_int, [_vp, ctypes.POINTER(Profile)]),
     "cf_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_vp)]),
     "cf_host_free": (ctypes.c_int, [_vp]),
+    "cf_forward_checkpointed": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                               ctypes.POINTER(SolverOpts), ctypes.POINTER(SolveStats)]),
+    "cf_backward": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "cf_div_norms_noalloc": (ctypes.c_int, [_vp, _pd, _vp, _pd, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int, ctypes.c_double, _vp, _vp]),
 }

@@ -184,6 +184,31 @@ class Context:
         return self._solve_call(self.lib.cf_step, ctypes.c_double(dt), ctypes.c_int(order), opts=opts,
                                 raise_on_maxit=raise_on_maxit)
 
+    # -- adjoint ----------------------------------------------------------------
+    def forward_checkpointed(self, nsteps: int, ckpt_every: int, dt: float, order: int = 3,
+                             opts: Optional[SolverOptions] = None) -> dict:
+        o = (opts or SolverOptions()).to_c()
+        st = L.SolveStats()
+        self._check(self.lib.cf_forward_checkpointed(self.h, int(nsteps), int(ckpt_every), float(dt), int(order),
+                                                     ctypes.byref(o), ctypes.byref(st)))
+        return st.as_dict()
+
+    def backward(self, dq_T: np.ndarray, du_T: Optional[np.ndarray] = None,
+                 dv_T: Optional[np.ndarray] = None) -> dict:
+        def arg(a, field):
+            if a is None:
+                return None, None
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            assert a.shape == self.owned_shape(field)
+            return a, _dptr(a)
+        keep = [arg(dq_T, "q"), arg(du_T, "u"), arg(dv_T, "v")]
+        out = {f: np.empty(self.owned_shape(f)) for f in ("q", "u", "v")}
+        rate = ctypes.c_double()
+        self._check(self.lib.cf_backward(self.h, keep[0][1], keep[1][1], keep[2][1], _dptr(out["q"]),
+                                         _dptr(out["u"]), _dptr(out["v"]), ctypes.byref(rate)))
+        out["rate"] = rate.value
+        return out
+
     def div_norms(self):
         a, b = ctypes.c_double(), ctypes.c_double()
         self._check(self.lib.cf_div_norms(self.h, ctypes.byref(a), ctypes.byref(b)))

@@ -305,6 +305,7 @@ int cf_ctx_destroy(cf_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (cudaEvent_t e : ctx->ev)
         if (e) cudaEventDestroy(e);
+    cf_adjoint_free(ctx);
     if (ctx->g64) cudaGraphExecDestroy(ctx->g64);
     if (ctx->g32) cudaGraphExecDestroy(ctx->g32);
     for (void* p : ctx->allocs) cudaFree(p);

@@ -44,6 +44,7 @@ struct cf_ctx {
     int g64_batch = 0, g32_batch = 0;
     cf::Stencil g64_st{}, g32_st{};
 
+    void* adjoint = nullptr;  // checkpoints and adjoint buffers (cf_adjoint.cu)
     long long launches = 0;
     // profiling (cf_profile_enable)
     int prof = 0;
@@ -79,8 +80,12 @@ struct SolveResult {
     double bb, rr, div_l2, div_linf;
 };
 int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res);
+int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Grid<double> gu, Grid<double> gv,
+                  int adjoint);
 // FP32 TMA inner CG (cf_cg32.cu)
 int cg32_setup(cf_ctx* c);
 void cg32_launch_iteration(cf_ctx* c, const Stencil& st);
 int div_norms(cf_ctx* c, double* l2, double* linf);
 }  // namespace cf
+
+void cf_adjoint_free(cf_ctx* c);

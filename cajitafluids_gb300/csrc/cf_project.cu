@@ -498,7 +498,8 @@ struct Press {
     Grid<double> u, v;
     const double* x;
     int pitch;
-    double ms;  // -(dt / (density dx))
+    double ms;    // -(dt / (density dx))
+    int adjoint;  // 1: transpose of the projection (masks applied by the caller, none here)
 };
 
 __device__ __forceinline__ double pval(const Press& a, int gi, int gj) {
@@ -520,17 +521,19 @@ __global__ void k_apply_pressure(Press a) {
         double& u = a.u.at(gi + CF_HALO, gj + CF_HALO);
         double d = pval(a, gi, gj) - pval(a, gi - 1, gj);
         double w = fma(a.ms, d, u);
-        if (!p.per_x) {
-            if (gi <= 0 && p.bc[0] == 0) w = 0.0;
-            if (gi > p.nx - 1 && p.bc[2] == 0) w = 0.0;
+        if (!a.adjoint) {
+            if (!p.per_x) {
+                if (gi <= 0 && p.bc[0] == 0) w = 0.0;
+                if (gi > p.nx - 1 && p.bc[2] == 0) w = 0.0;
+            }
+            if (!fix_q1 && !p.per_y && gj == 0 && gi < p.nx && p.bc[1] == 0) w = 0.0;
         }
-        if (!fix_q1 && !p.per_y && gj == 0 && gi < p.nx && p.bc[1] == 0) w = 0.0;
         u = w;
     } else {
         double& v = a.v.at(gi + CF_HALO, gj + CF_HALO);
         double d = pval(a, gi, gj) - pval(a, gi, gj - 1);
         double w = fma(a.ms, d, v);
-        if (!p.per_y) {
+        if (!p.per_y && !a.adjoint) {
             if (fix_q1) {
                 if (gj <= 0 && p.bc[1] == 0) w = 0.0;
                 if (gj > p.ny - 1 && p.bc[3] == 0) w = 0.0;
@@ -695,6 +698,14 @@ int div_norms(cf_ctx* c, double* l2, double* linf) {
 }
 
 int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res) {
+    return project_grids(c, dt, o, res, c->u[c->cur], c->v[c->cur], 0);
+}
+
+// The projection on the face arrays u, v.  adjoint = 1 applies the transpose
+// of the projection: the caller has applied the wall masks, and no mask is
+// applied after the gradient subtraction (see cf_adjoint.cu).
+int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Grid<double> gu, Grid<double> gv,
+                  int adjoint) {
     Stencil st;
     build_stencil(c, dt, o.precon_none, &st);
     const bool mixed = c->precision == CF_PREC_MIXED;
@@ -715,6 +726,8 @@ int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res) {
     cudaMemcpyAsync(c->S, h, sizeof(SolverState), cudaMemcpyHostToDevice, c->stream);
     int nb = red_blocks(c);
     DivArgs da = div_args(c, st);
+    da.u = gu;
+    da.v = gv;
     if (c->prof) cudaEventRecord(c->ev[4], c->stream);
     if (!mixed) {
         k_div_init64<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
@@ -784,12 +797,13 @@ int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res) {
     res->rr = hs->rr;
 
     // gradient subtraction
-    Press pa{c->ph, c->u[c->cur], c->v[c->cur], c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx))};
+    Press pa{c->ph, gu, gv, c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx)), adjoint};
     dim3 blk(32, 8), grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
     k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
     c->launches += 1;
     if ((rc = cuda_check(c, cudaGetLastError(), "apply pressure"))) return rc;
     if (c->prof) cudaEventRecord(c->ev[5], c->stream);
+    if (adjoint) return cuda_check(c, cudaStreamSynchronize(c->stream), "adjoint projection");
     rc = div_norms(c, &res->div_l2, &res->div_linf);
     if (!rc && c->prof) {
         float ms = 0.f;

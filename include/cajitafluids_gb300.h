@@ -174,6 +174,22 @@ int cf_div_norms(cf_ctx* ctx, double* l2, double* linf);
 /* max |u|, |v| over owned faces (for CFL time steps) */
 int cf_max_velocity(cf_ctx* ctx, double* umax);
 
+/* ---- adjoint (no counterpart in the reference: new functionality) ----
+ * Forward/backward contract of an autograd function over nsteps Solver::step
+ * calls (src/Solver.hpp:135-147) from the current state s_0.
+ * cf_forward_checkpointed runs the steps, storing the state every ckpt_every
+ * steps (sqrt(nsteps) keeps memory at O(sqrt(nsteps)) states); the context
+ * ends in s_T.  cf_backward takes dL/dq(T) and optionally dL/du(T), dL/dv(T)
+ * (NULL = 0), recomputes each segment from its checkpoint, runs the reverse
+ * steps, and writes dL/dq(0), dL/du(0), dL/dv(0) and dL/dQ for the quantity
+ * rate of a rate-form source (any output may be NULL); the context is left
+ * in s_T.  Host arrays are contiguous owned regions (x fastest).  FP64
+ * contexts only; see cf_adjoint.cu for the supported inputs. */
+int cf_forward_checkpointed(cf_ctx* ctx, int nsteps, int ckpt_every, double dt, int value_order,
+                            const cf_solver_opts* opts, cf_solve_stats* last);
+int cf_backward(cf_ctx* ctx, const double* dL_dq_T, const double* dL_du_T, const double* dL_dv_T, double* dL_dq0,
+                double* dL_du0, double* dL_dv0, double* dL_drate);
+
 /* ---- test exports (Interpolation / rk3 at arbitrary points) ---- */
 /* Interpolation::interpolateField (src/Interpolation.hpp:30-41) of a state field
  * at n physical points xy[2n] */
