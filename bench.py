@@ -321,6 +321,10 @@ def bench_gb300(args, rank, world, dist, device):
             line["scalar_error_vs_fp64"] = {"after_steps": args.warmup, "linf": float(np.abs(err).max()),
                                             "l2": float(np.sqrt(np.mean(err * err)))}
 
+    if "adjoint" in legs:
+        line["adjoint"] = bench_adjoint(args, device, dist)
+        line["adjoint_forward_ratio"] = line["adjoint"]["forward_plus_adjoint_over_forward"]
+
     # ---- CPU baseline (rank 0, N = 1) ----
     if rank == 0 and world == 1 and "cpu" in legs and not args.skip_cpu:
         k_ref = k64 if k64 else (line.get("mixed", {}).get("cg_inner_iters_per_step") or args.ref_iters)
@@ -331,6 +335,82 @@ def bench_gb300(args, rank, world, dist, device):
                                           f"projection capped at 5 and 15 CG iterations, extrapolated to "
                                           f"{k_ref:.0f} iterations/step", **detail}
     return line
+
+
+def bench_adjoint(args, device, dist):
+    """Forward + adjoint on the 512^2 walls problem with 8 Gaussian blobs:
+    loss = 1/2 |q(T) - target|^2, gradient with respect to q(0), u(0), v(0)
+    and the rate of a rate-form inflow, T steps, checkpoint every 14."""
+    from cajitafluids_gb300 import Context, SolverOptions
+    from cajitafluids_gb300 import _lib as L
+    from cajitafluids_gb300.workloads import config3
+    w = config3(args.adjoint_size, steps=args.adjoint_steps)
+    every = args.adjoint_every
+    opts = SolverOptions(tol=w.tol, max_iter=200000)
+    inflow = ((0.45, 0.10), (0.10, 0.05), (0.0, 0.0), 1.0)
+
+    def fresh(rate=1.0):
+        c = Context(w.nx, w.ny, device=device)
+        c.set_density(w.density)
+        c.set_quirks(L.CF_FIX_Q1)
+        c.set_source(inflow[0], inflow[1], inflow[2], rate, mode=1)
+        for f, a in (("q", w.q0), ("u", w.u0), ("v", w.v0)):
+            c.upload(f, a)
+        return c
+
+    c = fresh()
+    c.step(w.dt, w.order, opts)  # warm the graphs
+    c.close()
+    c = fresh()
+    barrier_sync(dist)
+    c.timer_start()
+    its = 0
+    for _ in range(w.steps):
+        its += c.step(w.dt, w.order, opts, raise_on_maxit=True)["iterations"]
+    t_fwd = c.timer_stop()
+    qT = c.download("q")
+    c.close()
+    c = fresh()
+    c.timer_start()
+    c.forward_checkpointed(w.steps, every, w.dt, w.order, opts)
+    t_fc = c.timer_stop()
+    target = w.extra["target"]
+    c.timer_start()
+    g = c.backward(c.download("q") - target)
+    t_bwd = c.timer_stop()
+    assert np.array_equal(c.download("q"), qT)   # checkpointed forward = plain forward
+    out = {"workload": f"{w.nx}^2 walls, spectral velocity + 8 Gaussian blobs, rate inflow, T={w.steps}, "
+                       f"checkpoint every {every}, FP64, CG tol {w.tol:g}",
+           "forward_ms": t_fwd, "forward_checkpointed_ms": t_fc, "backward_ms": t_bwd,
+           "forward_plus_adjoint_over_forward": (t_fc + t_bwd) / t_fwd,
+           "cg_iters_per_forward_step": its / w.steps,
+           "loss": 0.5 * float(np.sum((qT - target) ** 2))}
+    # central differences of the FP64 forward on seeded directions
+    rng = np.random.default_rng(16)
+    checks = []
+    for k in range(args.adjoint_fd):
+        dq = rng.standard_normal(w.q0.shape)
+        du = rng.standard_normal(w.u0.shape)
+        dv = rng.standard_normal(w.v0.shape)
+        du[:, 0] = du[:, -1] = 0.0
+        dv[0, :] = dv[-1, :] = 0.0
+        h = 1e-6
+        vals = []
+        for sgn in (1.0, -1.0):
+            c2 = fresh()
+            for f, a, d in (("q", w.q0, dq), ("u", w.u0, du), ("v", w.v0, dv)):
+                c2.upload(f, a + sgn * h * d)
+            for _ in range(w.steps):
+                c2.step(w.dt, w.order, opts)
+            vals.append(0.5 * float(np.sum((c2.download("q") - target) ** 2)))
+            c2.close()
+        fd = (vals[0] - vals[1]) / (2 * h)
+        ad = float(np.sum(g["q"] * dq) + np.sum(g["u"] * du) + np.sum(g["v"] * dv))
+        checks.append({"fd": fd, "adjoint": ad, "rel_err": abs(fd - ad) / max(abs(ad), 1e-300)})
+    out["fd_checks"] = checks
+    out["dL_drate"] = g["rate"]
+    c.close()
+    return out
 
 
 def bench_reference(args, rank, world, dist):
@@ -374,8 +454,12 @@ def main():
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--legs", default="mixed,e2e,fp64,cpu",
-                    help="comma list of legs to run: mixed (headline), e2e, fp64, cpu")
+    ap.add_argument("--legs", default="mixed,e2e,fp64,adjoint,cpu",
+                    help="comma list of legs to run: mixed (headline), e2e, fp64, adjoint, cpu")
+    ap.add_argument("--adjoint-size", type=int, default=512)
+    ap.add_argument("--adjoint-steps", type=int, default=56)
+    ap.add_argument("--adjoint-every", type=int, default=14)
+    ap.add_argument("--adjoint-fd", type=int, default=0, help="central-difference checks of the gradient")
     ap.add_argument("--ref-iters", type=int, default=12000)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
