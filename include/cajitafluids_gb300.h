@@ -94,8 +94,10 @@ typedef struct {
 /* Pressure-solver options (src/VelocityCorrector.hpp:96-106, 297-339).
  * solver: "Reference" or "PCG" (both run the GPU Jacobi-PCG); other HYPRE
  * solver names return CF_ERR_UNSUPPORTED.
- * precon: "Jacobi", "Diagonal" (same), "None" or "none" (unpreconditioned
- * is not implemented: CF_ERR_UNSUPPORTED), "PFMG"/"SMG" -> CF_ERR_UNSUPPORTED.
+ * precon (read for "PCG"; "Reference" always uses the diagonal preconditioner,
+ * src/VelocityCorrector.hpp:158-180): "Diagonal" or "Jacobi" -> diagonal
+ * (Jacobi) scaling, "None"/"none" -> unpreconditioned CG, "PFMG"/"SMG" and
+ * other HYPRE names -> CF_ERR_UNSUPPORTED.
  * Convergence: ||r||_2 <= tol * ||b||_2, or, when abs_tol > 0,
  * ||div u||_L2 = ||r||_2 * dx <= abs_tol.  The reference hard-codes
  * tol 1e-6 and max_iter 2000 (:103-104). */

@@ -606,12 +606,318 @@ static void apply_pressure(orc_state* st, double dt) {
         }
 }
 
+/* ------------------------------------------------------------------ */
+/* Geometric multigrid V-cycle preconditioner: the stand-in for the HYPRE
+ * PFMG/SMG preconditioners the reference selects by name
+ * (src/VelocityCorrector.hpp:324-338; PFMG is the CLI default,
+ * examples/advection.cpp:186-189).  Cell-centred levels halve both axes
+ * while both are even and at least 16; level l uses the fine stencil with
+ * scale / 4^l and the same wall rules.  Smoother: red-black Gauss-Seidel,
+ * MG_NU sweeps red-then-black before and black-then-red after the coarse
+ * correction; MG_NC such sweep pairs on the coarsest level.  Prolongation:
+ * cell-centred bilinear (3/4, 1/4 per axis; a SOLID wall reflects, a FREE
+ * wall reads zero, a periodic axis wraps); restriction: its transpose / 4.
+ * The cycle is a symmetric operator, as CG needs. */
+#define MG_MAX 16
+#define MG_NU 2
+#define MG_NC 16
+
+typedef struct {
+    int nx, ny;
+    double scale, ms;
+    double diag[16], invd[16];
+    double *x, *b, *r;
+} mg_level;
+
+static int mg_bits(const orc_params* p, int nx, int ny, int gi, int gj) {
+    int b = 0;
+    if (!p->periodic[0]) b |= (gi == 0 ? 1 : 0) | (gi == nx - 1 ? 2 : 0);
+    if (!p->periodic[1]) b |= (gj == 0 ? 4 : 0) | (gj == ny - 1 ? 8 : 0);
+    return b;
+}
+
+static double mg_at(const orc_params* p, const double* a, int nx, int ny, int gi, int gj) {
+    if (gi < 0 || gi >= nx) {
+        if (!p->periodic[0]) return 0.0;
+        gi = gi < 0 ? gi + nx : gi - nx;
+    }
+    if (gj < 0 || gj >= ny) {
+        if (!p->periodic[1]) return 0.0;
+        gj = gj < 0 ? gj + ny : gj - ny;
+    }
+    return a[(size_t)gj * nx + gi];
+}
+
+/* per-axis weight of coarse index I in the prolongation to fine index f */
+static double mg_pw(int f, int I, int nc, int per, int bclo, int bchi) {
+    int parent = f >> 1, nb = parent + ((f & 1) ? 1 : -1);
+    int nb_in = nb >= 0 && nb < nc;
+    if (!nb_in && per) {
+        nb = nb < 0 ? nb + nc : nb - nc;
+        nb_in = 1;
+    }
+    double wp = 0.75;
+    if (!nb_in && (nb < 0 ? bclo : bchi) == SOLID) wp = 1.0;
+    double w = 0.0;
+    if (parent == I) w = w + wp;
+    if (nb_in && nb == I) w = w + 0.25;
+    return w;
+}
+
+static void mg_smooth(const orc_params* p, mg_level* L, int color) {
+    int nx = L->nx, ny = L->ny;
+#pragma omp parallel for schedule(static)
+    for (int gj = 0; gj < ny; ++gj)
+        for (int gi = (gj + color) & 1; gi < nx; gi += 2) {
+            double s = mg_at(p, L->x, nx, ny, gi - 1, gj) + mg_at(p, L->x, nx, ny, gi + 1, gj);
+            s = s + mg_at(p, L->x, nx, ny, gi, gj - 1);
+            s = s + mg_at(p, L->x, nx, ny, gi, gj + 1);
+            size_t k = (size_t)gj * nx + gi;
+            double t = fma(L->scale, s, L->b[k]);
+            L->x[k] = t * L->invd[mg_bits(p, nx, ny, gi, gj)];
+        }
+}
+
+static void mg_residual(const orc_params* p, mg_level* L) {
+    int nx = L->nx, ny = L->ny;
+#pragma omp parallel for schedule(static)
+    for (int gj = 0; gj < ny; ++gj)
+        for (int gi = 0; gi < nx; ++gi) {
+            size_t k = (size_t)gj * nx + gi;
+            double ax = L->diag[mg_bits(p, nx, ny, gi, gj)] * L->x[k];
+            ax = fma(L->ms, mg_at(p, L->x, nx, ny, gi - 1, gj), ax);
+            ax = fma(L->ms, mg_at(p, L->x, nx, ny, gi + 1, gj), ax);
+            ax = fma(L->ms, mg_at(p, L->x, nx, ny, gi, gj - 1), ax);
+            ax = fma(L->ms, mg_at(p, L->x, nx, ny, gi, gj + 1), ax);
+            L->r[k] = L->b[k] - ax;
+        }
+}
+
+static void mg_restrict(const orc_params* p, const mg_level* F, mg_level* C) {
+    int nfx = F->nx, nfy = F->ny, ncx = C->nx, ncy = C->ny;
+#pragma omp parallel for schedule(static)
+    for (int J = 0; J < ncy; ++J)
+        for (int I = 0; I < ncx; ++I) {
+            double acc = 0.0;
+            for (int fy0 = 2 * J - 1; fy0 <= 2 * J + 2; ++fy0) {
+                int fy = fy0;
+                if (fy < 0 || fy >= nfy) {
+                    if (!p->periodic[1]) continue;
+                    fy = fy < 0 ? fy + nfy : fy - nfy;
+                }
+                double wy = mg_pw(fy, J, ncy, p->periodic[1], p->bc_type[1], p->bc_type[3]);
+                double rs = 0.0;
+                for (int fx0 = 2 * I - 1; fx0 <= 2 * I + 2; ++fx0) {
+                    int fx = fx0;
+                    if (fx < 0 || fx >= nfx) {
+                        if (!p->periodic[0]) continue;
+                        fx = fx < 0 ? fx + nfx : fx - nfx;
+                    }
+                    double wx = mg_pw(fx, I, ncx, p->periodic[0], p->bc_type[0], p->bc_type[2]);
+                    rs = fma(wx, F->r[(size_t)fy * nfx + fx], rs);
+                }
+                acc = fma(wy, rs, acc);
+            }
+            C->b[(size_t)J * ncx + I] = 0.25 * acc;
+        }
+}
+
+/* neighbour coarse index and weights along one axis for fine index f */
+static void mg_axis(int f, int nc, int per, int bclo, int bchi, int* I, int* N, double* wI, double* wN) {
+    int parent = f >> 1, nb = parent + ((f & 1) ? 1 : -1);
+    *I = parent;
+    *wI = 0.75;
+    *wN = 0.25;
+    if (nb < 0 || nb >= nc) {
+        if (per) {
+            nb = nb < 0 ? nb + nc : nb - nc;
+        } else {
+            if ((nb < 0 ? bclo : bchi) == SOLID) *wI = 1.0;
+            nb = -1;
+            *wN = 0.0;
+        }
+    }
+    *N = nb;
+}
+
+static void mg_prolong_add(const orc_params* p, const mg_level* C, mg_level* F) {
+    int nfx = F->nx, nfy = F->ny, ncx = C->nx, ncy = C->ny;
+#pragma omp parallel for schedule(static)
+    for (int fy = 0; fy < nfy; ++fy)
+        for (int fx = 0; fx < nfx; ++fx) {
+            int I, NI, J, NJ;
+            double wxI, wxN, wyJ, wyN;
+            mg_axis(fx, ncx, p->periodic[0], p->bc_type[0], p->bc_type[2], &I, &NI, &wxI, &wxN);
+            mg_axis(fy, ncy, p->periodic[1], p->bc_type[1], p->bc_type[3], &J, &NJ, &wyJ, &wyN);
+            double row0 = wxI * C->x[(size_t)J * ncx + I];
+            if (NI >= 0) row0 = fma(wxN, C->x[(size_t)J * ncx + NI], row0);
+            double v = wyJ * row0;
+            if (NJ >= 0) {
+                double row1 = wxI * C->x[(size_t)NJ * ncx + I];
+                if (NI >= 0) row1 = fma(wxN, C->x[(size_t)NJ * ncx + NI], row1);
+                v = fma(wyN, row1, v);
+            }
+            size_t k = (size_t)fy * nfx + fx;
+            F->x[k] = F->x[k] + v;
+        }
+}
+
+static void mg_vcycle(const orc_params* p, mg_level* lev, int nlev, int l) {
+    mg_level* L = &lev[l];
+    memset(L->x, 0, sizeof(double) * (size_t)L->nx * L->ny);
+    if (l == nlev - 1) {
+        for (int s = 0; s < MG_NC; ++s) {
+            mg_smooth(p, L, 0);
+            mg_smooth(p, L, 1);
+        }
+        for (int s = 0; s < MG_NC; ++s) {
+            mg_smooth(p, L, 1);
+            mg_smooth(p, L, 0);
+        }
+        return;
+    }
+    for (int s = 0; s < MG_NU; ++s) {
+        mg_smooth(p, L, 0);
+        mg_smooth(p, L, 1);
+    }
+    mg_residual(p, L);
+    mg_restrict(p, L, &lev[l + 1]);
+    mg_vcycle(p, lev, nlev, l + 1);
+    mg_prolong_add(p, &lev[l + 1], L);
+    for (int s = 0; s < MG_NU; ++s) {
+        mg_smooth(p, L, 1);
+        mg_smooth(p, L, 0);
+    }
+}
+
+static void mg_level_tables(const orc_params* p, mg_level* L) {
+    for (int b = 0; b < 16; ++b) {
+        double d = 4.0 * L->scale;
+        if ((b & 1) && p->bc_type[0] == SOLID) d = d - L->scale;
+        if ((b & 2) && p->bc_type[2] == SOLID) d = d - L->scale;
+        if ((b & 4) && p->bc_type[1] == SOLID) d = d - L->scale;
+        if ((b & 8) && p->bc_type[3] == SOLID) d = d - L->scale;
+        L->diag[b] = d;
+        L->invd[b] = 1.0 / d;
+    }
+    L->ms = -1.0 * L->scale;
+}
+
+/* levels for this grid; level 0 works in place on r (rhs) and z (result) */
+static int mg_build(orc_state* st, double scale, mg_level* lev) {
+    int nx = st->p.nx, ny = st->p.ny, n = 0;
+    for (;;) {
+        mg_level* L = &lev[n];
+        L->nx = nx;
+        L->ny = ny;
+        L->scale = n == 0 ? scale : lev[n - 1].scale * 0.25;
+        mg_level_tables(&st->p, L);
+        size_t cells = (size_t)nx * ny;
+        if (n == 0) {
+            L->b = st->r;
+            L->x = st->z;
+            L->r = st->qv;  /* scratch: free while the V-cycle runs */
+        } else {
+            L->b = (double*)calloc(cells, sizeof(double));
+            L->x = (double*)calloc(cells, sizeof(double));
+            L->r = (double*)calloc(cells, sizeof(double));
+        }
+        ++n;
+        if (n == MG_MAX || (nx & 1) || (ny & 1) || nx < 16 || ny < 16) break;
+        nx /= 2;
+        ny /= 2;
+    }
+    return n;
+}
+
+static void mg_free(mg_level* lev, int n) {
+    for (int l = 1; l < n; ++l) {
+        free(lev[l].b);
+        free(lev[l].x);
+        free(lev[l].r);
+    }
+}
+
+/* MG-preconditioned CG: the same recurrences as below with z = V-cycle(r);
+ * the V-cycle is skipped once the loop is about to stop. */
+static int project_mg(orc_state* st, double scale, double tol, double abs_tol, int max_iter, int* iters,
+                      double* bb_out, double* rr_out) {
+    int nx = st->p.nx, ny = st->p.ny;
+    size_t n = (size_t)nx * ny;
+    double area = st->dx * st->dx;
+    mg_level lev[MG_MAX];
+    int nlev = mg_build(st, scale, lev);
+    double rr = canon_dot_buf(nx, ny, st->r, st->r, st->partial);
+    double bb = rr, rho = 0.0, beta = 0.0;
+    double tol2 = tol * tol, abs2 = abs_tol * abs_tol;
+    int k = 0, status = 0;
+#define MG_CONVERGED(rr) ((rr) <= tol2 * bb || (abs_tol > 0.0 && (rr) * area <= abs2))
+    if (bb != 0.0 && !MG_CONVERGED(rr) && max_iter > 0) {
+        mg_vcycle(&st->p, lev, nlev, 0);
+        rho = canon_dot_buf(nx, ny, st->r, st->z, st->partial);
+    }
+    if (bb != 0.0) {
+        for (;;) {
+            if (MG_CONVERGED(rr)) { status = 0; break; }
+            if (k >= max_iter) { status = 1; break; }
+#pragma omp parallel for schedule(static)
+            for (size_t c = 0; c < n; ++c) st->pv[c] = (k == 0) ? st->z[c] : fma(beta, st->pv[c], st->z[c]);
+            matvec(st, scale, st->pv, st->qv);
+            double pq = canon_dot_buf(nx, ny, st->pv, st->qv, st->partial);
+            if (!(pq > 0.0)) { status = isnan(pq) ? 3 : 2; break; }
+            double alpha = rho / pq, malpha = -alpha;
+#pragma omp parallel for schedule(static)
+            for (size_t c = 0; c < n; ++c) {
+                st->x[c] = fma(alpha, st->pv[c], st->x[c]);
+                st->r[c] = fma(malpha, st->qv[c], st->r[c]);
+            }
+            rr = canon_dot_buf(nx, ny, st->r, st->r, st->partial);
+            k += 1;
+            if (isnan(rr)) { status = 3; break; }
+            if (MG_CONVERGED(rr) || k >= max_iter) continue;
+            mg_vcycle(&st->p, lev, nlev, 0);
+            double rho_new = canon_dot_buf(nx, ny, st->r, st->z, st->partial);
+            beta = rho_new / rho;
+            rho = rho_new;
+        }
+    }
+#undef MG_CONVERGED
+    mg_free(lev, nlev);
+    *iters = k;
+    *bb_out = bb;
+    *rr_out = rr;
+    return status;
+}
+
 /* Jacobi-preconditioned CG, cold start x0 = 0 (src/VelocityCorrector.hpp:
  * 158-180, 266-282; Cajita ReferenceConjugateGradient restated).  Stops
  * when ||r||^2 <= tol^2 ||b||^2, or ||r||^2 dx^2 <= abs_tol^2 when
  * abs_tol > 0, checked before each iteration. */
 int orc_project(orc_state* st, double dt, double tol, double abs_tol, int max_iter,
                 orc_solve_stats* stats) {
+    if (st->p.precon_mg) {
+        int nx = st->p.nx, ny = st->p.ny;
+        size_t n = (size_t)nx * ny;
+        double scale = dt / ((st->p.density * st->dx) * st->dx);
+        build_diag(st, dt);
+        divergence(st, st->rhs);
+        for (size_t k = 0; k < n; ++k) {
+            st->r[k] = st->rhs[k];
+            st->x[k] = 0.0;
+        }
+        int iters = 0;
+        double bb = 0.0, rr = 0.0;
+        int status = project_mg(st, scale, tol, abs_tol, max_iter, &iters, &bb, &rr);
+        apply_pressure(st, dt);
+        if (stats) {
+            stats->iterations = iters;
+            stats->status = status;
+            stats->bb = bb;
+            stats->rr = rr;
+            orc_div_norms(st, &stats->div_l2, &stats->div_linf);
+        }
+        return status;
+    }
     int nx = st->p.nx, ny = st->p.ny;
     size_t n = (size_t)nx * ny;
     double scale = dt / ((st->p.density * st->dx) * st->dx);

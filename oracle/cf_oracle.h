@@ -39,6 +39,7 @@ typedef struct {
     double density;
     unsigned quirks;         /* bit 0: fix Q1, bit 1: fix Q3 */
     int precon_none;         /* 1: unpreconditioned CG ("PCG" + "None") */
+    int precon_mg;           /* 1: geometric multigrid V-cycle preconditioner */
 } orc_params;
 
 typedef struct {
