@@ -18,7 +18,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcfgpu.so")
-SOURCES = ["cf_api.cu", "cf_fields.cu", "cf_project.cu", "cf_cg32.cu", "cf_adjoint.cu", "cf_noalloc.cu"]
+SOURCES = ["cf_api.cu", "cf_fields.cu", "cf_project.cu", "cf_cg32.cu", "cf_adjoint.cu", "cf_noalloc.cu", "cf_mg.cu"]
 HEADERS = ["cf_internal.cuh", "cf_ctx.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [

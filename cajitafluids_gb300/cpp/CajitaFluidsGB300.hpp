@@ -286,7 +286,7 @@ class VelocityCorrector : public VelocityCorrectorBase {
         if (_solver != "Reference" && _solver != "PCG")
             throw std::runtime_error("pressure solver '" + _solver + "' is not implemented");
         if (_solver == "PCG" && _precon != "Diagonal" && _precon != "Jacobi" && _precon != "None" &&
-            _precon != "none")
+            _precon != "none" && _precon != "PFMG" && _precon != "SMG" && _precon != "MG")
             throw std::runtime_error("preconditioner '" + _precon + "' is not implemented");
     }
     void correctVelocity() override {

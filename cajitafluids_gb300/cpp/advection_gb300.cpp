@@ -2,9 +2,8 @@
 // GB300 path: all-SOLID walls, zero initial state, one inflow block, body
 // force (0, -g), createSolver + solve (examples/advection.cpp:438-461).
 //
-// Defaults are the reference's (:168-189), except the preconditioner: the
-// reference defaults to HYPRE PFMG, which this build does not provide, so
-// the default here is the diagonal (Jacobi) preconditioner.
+// Defaults are the reference's (:168-189): PCG with the PFMG preconditioner
+// name, served here by the geometric multigrid V-cycle.
 //
 // Extra options: --steps N runs exactly N steps after setup instead of
 // t_final / dt; --linear samples the advected field linearly; --tol sets the
@@ -55,7 +54,7 @@ static void dump(const char* path, const CajitaFluids::ProblemManager<2>& pm) {
 }
 
 int main(int argc, char** argv) {
-    std::string device = "gb300", solver = "PCG", precon = "Diagonal", out;
+    std::string device = "gb300", solver = "PCG", precon = "PFMG", out;
     double t_final = 4.0, delta_t = 0.005, density = 0.1, gravity = 0.0, quantity = 3.0, tol = 1.0e-6;
     int n = 128, write_freq = 20, steps = -1, order = 3;
     std::array<double, 2> inLocation{{0.2, 0.45}}, inSize{{0.02, 0.1}}, inVelocity{{1.0, 0.0}};

@@ -121,11 +121,15 @@ int parse_opts(cf_ctx* c, const cf_solver_opts* o, SolveOpts* so) {
     if (strcmp(solver, "Reference") != 0 && strcmp(solver, "PCG") != 0)
         return fail(c, CF_ERR_UNSUPPORTED, "pressure solver '%s' is not implemented (use Reference or PCG)", solver);
     so->precon_none = 0;
+    so->precon_mg = 0;
     if (strcmp(solver, "PCG") == 0) {
         if (!strcmp(precon, "None") || !strcmp(precon, "none"))
             so->precon_none = 1;
+        else if (!strcmp(precon, "PFMG") || !strcmp(precon, "SMG") || !strcmp(precon, "MG"))
+            so->precon_mg = 1;
         else if (strcmp(precon, "Diagonal") != 0 && strcmp(precon, "Jacobi") != 0)
-            return fail(c, CF_ERR_UNSUPPORTED, "preconditioner '%s' is not implemented (use Diagonal, Jacobi or None)", precon);
+            return fail(c, CF_ERR_UNSUPPORTED,
+                        "preconditioner '%s' is not implemented (use Diagonal, Jacobi, PFMG, SMG, MG or None)", precon);
     }
     so->tol = o ? o->tol : 1.0e-6;
     so->abs_tol = o ? o->abs_tol : 0.0;
@@ -308,6 +312,9 @@ int cf_ctx_destroy(cf_ctx* ctx) {
     cf_adjoint_free(ctx);
     if (ctx->g64) cudaGraphExecDestroy(ctx->g64);
     if (ctx->g32) cudaGraphExecDestroy(ctx->g32);
+    if (ctx->gmg) cudaGraphExecDestroy(ctx->gmg);
+    if (ctx->gmg_pre) cudaGraphExecDestroy(ctx->gmg_pre);
+    cf::mg_free(ctx);
     for (void* p : ctx->allocs) cudaFree(p);
     if (ctx->hS) cudaFreeHost(ctx->hS);
     if (ctx->h_out) cudaFreeHost(ctx->h_out);

@@ -46,6 +46,7 @@ constexpr unsigned kWaitLimit = 1u << 22;
 
 struct Cg32T {
     int nx, ny, per_x, per_y, tiles_x, tiles, pitch;
+    int mg;  // MG-PCG: K1 reads z (minv = 1), K2 leaves beta and rho to k_mg_rz32
     Stencil st;
     float *e, *r, *pa, *pb;  // element (0, 0)
     double *part0, *part1;
@@ -418,8 +419,10 @@ __global__ void __launch_bounds__(kThreads, 2)
         if (tid == 0) {
             S->ticket[6] = 0;
             S->rho_prev = S->rho_in;
-            S->beta_in = rz / S->rho_in;
-            S->rho_in = rz;
+            if (!a.mg) {
+                S->beta_in = rz / S->rho_in;
+                S->rho_in = rz;
+            }
             S->rr_in = rr;
             if (rr > S->rr_in0) S->rr_in0 = rr;
             S->inner_iter = it + 1;
@@ -432,6 +435,63 @@ __global__ void __launch_bounds__(kThreads, 2)
                 S->inner_status = ST_CONVERGED;
             else if (S->iter >= S->max_iter)
                 S->inner_status = ST_MAXIT;
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
+// Mixed MG-PCG helpers.  z = V-cycle(r) is written to the owned cells of z32;
+// along periodic axes its ghost ring is refreshed here (wall ghosts stay 0).
+__global__ void k_z32_ghosts(float* z, int nx, int ny, int pitch, int per_x, int per_y) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (per_x && t < ny) {
+        float* row = z + (ptrdiff_t)t * pitch;
+        row[-1] = row[nx - 1];
+        row[nx] = row[0];
+    }
+    if (per_y && t < nx) {
+        z[-(ptrdiff_t)pitch + t] = z[(ptrdiff_t)(ny - 1) * pitch + t];
+        z[(ptrdiff_t)ny * pitch + t] = z[t];
+    }
+}
+
+// rho = r.z (FP32 per lane over a 64 x 16 unit, FP64 beyond).  mode 0 (after
+// an inner iteration): beta = rho_new / rho.  mode 1 (after the residual was
+// formed from the FP64 solution): beta = rho_new / rho_prev, which keeps the
+// search direction across a reliable update (ignored on a restart).
+__global__ void __launch_bounds__(CF_RED_THREADS)
+    k_mg_rz32(const float* r, const float* z, int nx, int ny, int pitch, int G, int U, double* part,
+              SolverState* S, int mode) {
+    if (!running(S)) return;
+    const int lane = threadIdx.x & 31;
+    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
+    float arz = 0.f;
+    if (unit < U) {
+        const int g = unit % G, band = unit / G;
+        const int c0 = g * CF_UNIT_COLS + 2 * lane;
+        const int j0 = band * CF_BAND_ROWS;
+        const int j1 = min(j0 + CF_BAND_ROWS, ny);
+        for (int j = j0; j < j1; ++j)
+            for (int s = 0; s < 2; ++s) {
+                const int c = c0 + s;
+                if (c >= nx) continue;
+                const ptrdiff_t k = (ptrdiff_t)j * pitch + c;
+                arz = fmaf(r[k], z[k], arz);
+            }
+    }
+    double drz = warp_fold((double)arz);
+    if (unit < U && lane == 0) part[unit] = drz;
+    if (last_block_arrive(&S->ticket[7])) {
+        double rz = final_tree(part, U);
+        if (threadIdx.x == 0) {
+            S->ticket[7] = 0;
+            double den = mode == 0 ? S->rho_in : S->rho_prev;
+            S->beta_in = den != 0.0 ? rz / den : 0.0;
+            S->rho_in = rz;
+            if (isnan(rz))
+                S->status = ST_NAN;
+            else if (!(rz > 0.0))
+                S->inner_status = ST_BREAKDOWN;  // FP32 noise floor: refine and restart
         }
     }
 }
@@ -503,7 +563,21 @@ int cg32_setup(cf_ctx* c) {
     return rc;
 }
 
-void cg32_launch_iteration(cf_ctx* c, const Stencil& st) {
+// z32 (ghosted, zero) and its tensor map, for the mixed MG-PCG
+int cg32_mg_setup(cf_ctx* c) {
+    if (c->z32b) return CF_OK;
+    size_t n32 = (size_t)c->p32 * (c->ph.ny + 2);
+    cudaError_t e = cudaMalloc(&c->z32b, n32 * sizeof(float));
+    if (e != cudaSuccess) return fail(c, CF_ERR_NOMEM, "z32: cudaMalloc failed");
+    c->allocs.push_back(c->z32b);
+    int rc = cuda_check(c, cudaMemsetAsync(c->z32b, 0, n32 * sizeof(float), c->stream), "z32 memset");
+    c->z32.a = c->z32b + c->p32 + 4;
+    c->z32.pitch = c->p32;
+    if (!rc) rc = make_map(c, &c->map_z, c->z32b);
+    return rc;
+}
+
+static Cg32T cg32_args(cf_ctx* c, const Stencil& st) {
     Cg32T a{};
     a.nx = c->ph.nx;
     a.ny = c->ph.ny;
@@ -520,9 +594,41 @@ void cg32_launch_iteration(cf_ctx* c, const Stencil& st) {
     a.part0 = c->partials;
     a.part1 = c->partials + c->n_units;
     a.S = c->S;
+    return a;
+}
+
+void cg32_launch_iteration(cf_ctx* c, const Stencil& st) {
+    Cg32T a = cg32_args(c, st);
     k_tma_dir_matvec32<<<c->cta32, kThreads, kStages * 2 * kSlot + 128, c->stream>>>(c->map_r, c->map_pa, c->map_pb, a);
     k_tma_update32<<<c->cta32b, kThreads, kStages * 3 * kSlot + 128, c->stream>>>(c->map_e, c->map_r, c->map_pa,
                                                                             c->map_pb, a);
+}
+
+// z = V-cycle(r32), its periodic ghosts, rho = r.z; returns kernels launched
+int cg32_mg_precondition(cf_ctx* c, double scale, int mode) {
+    int n = mg_vcycle(c, scale);
+    if (c->ph.per_x || c->ph.per_y) {
+        int m = c->ph.nx > c->ph.ny ? c->ph.nx : c->ph.ny;
+        k_z32_ghosts<<<(m + 255) / 256, 256, 0, c->stream>>>(c->z32.a, c->ph.nx, c->ph.ny, c->p32, c->ph.per_x,
+                                                             c->ph.per_y);
+        n += 1;
+    }
+    k_mg_rz32<<<(c->n_units + CF_RED_WARPS - 1) / CF_RED_WARPS, CF_RED_THREADS, 0, c->stream>>>(
+        c->r32.a, c->z32.a, c->ph.nx, c->ph.ny, c->p32, c->G, c->n_units, c->partials, c->S, mode);
+    return n + 1;
+}
+
+// one MG-PCG inner iteration: K1 on z (M^-1 = 1), K2, then the V-cycle and
+// r.z; returns kernels launched
+int cg32_launch_iteration_mg(cf_ctx* c, const Stencil& st, double scale) {
+    Stencil stz = st;
+    for (int b = 0; b < 16; ++b) stz.minv32[b] = 1.0f;
+    Cg32T a = cg32_args(c, stz);
+    a.mg = 1;
+    k_tma_dir_matvec32<<<c->cta32, kThreads, kStages * 2 * kSlot + 128, c->stream>>>(c->map_z, c->map_pa, c->map_pb, a);
+    k_tma_update32<<<c->cta32b, kThreads, kStages * 3 * kSlot + 128, c->stream>>>(c->map_e, c->map_r, c->map_pa,
+                                                                            c->map_pb, a);
+    return 2 + cg32_mg_precondition(c, scale, 0);
 }
 
 }  // namespace cf

@@ -45,6 +45,15 @@ struct cf_ctx {
     cf::Stencil g64_st{}, g32_st{};
 
     void* adjoint = nullptr;  // checkpoints and adjoint buffers (cf_adjoint.cu)
+    void* mg = nullptr;       // multigrid hierarchy (cf_mg.cu)
+    cudaGraphExec_t gmg = nullptr;      // batch of MG-PCG iterations
+    cudaGraphExec_t gmg_pre = nullptr;  // V-cycle + r.z after the residual is (re)formed
+    cf::Stencil gmg_st{};
+    int gmg_per_iter = 0, gmg_pre_launches = 0;
+    // FP32 z = M^-1 r of the mixed MG-PCG, ghost ring as the other FP32 vectors
+    cf::Vec32 z32{};
+    float* z32b = nullptr;
+    CUtensorMap map_z{};
     long long launches = 0;
     // profiling (cf_profile_enable)
     int prof = 0;
@@ -74,6 +83,7 @@ struct SolveOpts {
     double tol, abs_tol, inner_tol;
     int max_iter, max_outer;
     int precon_none;
+    int precon_mg;  // geometric multigrid V-cycle (cf_mg.cu)
 };
 struct SolveResult {
     int iterations, outer, status;
@@ -85,7 +95,16 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
 // FP32 TMA inner CG (cf_cg32.cu)
 int cg32_setup(cf_ctx* c);
 void cg32_launch_iteration(cf_ctx* c, const Stencil& st);
+int cg32_mg_setup(cf_ctx* c);
+int cg32_mg_precondition(cf_ctx* c, double scale, int mode);  // returns kernels launched
+int cg32_launch_iteration_mg(cf_ctx* c, const Stencil& st, double scale);
 int div_norms(cf_ctx* c, double* l2, double* linf);
+// multigrid preconditioner (cf_mg.cu)
+int mg_setup(cf_ctx* c);
+void mg_free(cf_ctx* c);
+int mg_vcycle(cf_ctx* c, double scale0);  // returns kernels launched
+int mg_levels(const cf_ctx* c);
+double* mg_z64(cf_ctx* c);
 }  // namespace cf
 
 void cf_adjoint_free(cf_ctx* c);

@@ -43,6 +43,8 @@ struct Cg64 {
     int nx, ny, per_x, per_y, G, U, pitch;
     Stencil st;
     double *x, *r, *pa, *pb, *qv;
+    const double* z;  // MG: z = V-cycle(r), read instead of M^-1 r
+    int mg;
     double *part0, *part1;
     SolverState* S;
 };
@@ -60,7 +62,7 @@ __device__ __forceinline__ double pn1(const Cg64& a, const double* pold, int c, 
     int cc = wrap_index(c, a.nx, a.per_x), jj = wrap_index(j, a.ny, a.per_y);
     if (cc < 0 || jj < 0) return 0.0;
     size_t k = (size_t)jj * a.pitch + cc;
-    double z = a.st.minv[ebits(a, cc, jj)] * __ldg(a.r + k);
+    double z = a.mg ? __ldg(a.z + k) : a.st.minv[ebits(a, cc, jj)] * __ldg(a.r + k);
     return first ? z : fma(beta, __ldg(pold + k), z);
 }
 
@@ -70,9 +72,16 @@ __device__ __forceinline__ double2 pn2(const Cg64& a, const double* pold, int c0
     if (jj < 0) return make_double2(0.0, 0.0);
     if (c0 + 1 < a.nx) {
         size_t k = (size_t)jj * a.pitch + c0;
-        double2 rv = __ldg(reinterpret_cast<const double2*>(a.r + k));
-        double z0 = a.st.minv[ebits(a, c0, jj)] * rv.x;
-        double z1 = a.st.minv[ebits(a, c0 + 1, jj)] * rv.y;
+        double z0, z1;
+        if (a.mg) {
+            double2 zv = __ldg(reinterpret_cast<const double2*>(a.z + k));
+            z0 = zv.x;
+            z1 = zv.y;
+        } else {
+            double2 rv = __ldg(reinterpret_cast<const double2*>(a.r + k));
+            z0 = a.st.minv[ebits(a, c0, jj)] * rv.x;
+            z1 = a.st.minv[ebits(a, c0 + 1, jj)] * rv.y;
+        }
         if (first) return make_double2(z0, z1);
         double2 po = __ldg(reinterpret_cast<const double2*>(pold + k));
         return make_double2(fma(beta, po.x, z0), fma(beta, po.y, z1));
@@ -211,8 +220,10 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_cg_update64(Cg64 a) {
         double rr = final_tree(a.part1, a.U);
         if (threadIdx.x == 0) {
             S->ticket[1] = 0;
-            S->beta = rz / S->rho;
-            S->rho = rz;
+            if (!a.mg) {
+                S->beta = rz / S->rho;
+                S->rho = rz;
+            }
             S->rr = rr;
             S->iter = it + 1;
             if (isnan(rr))
@@ -221,6 +232,46 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_cg_update64(Cg64 a) {
                 S->status = ST_CONVERGED;
             else if (it + 1 >= S->max_iter)
                 S->status = ST_MAXIT;
+        }
+    }
+}
+
+// MG-PCG: rho_new = r.z after the V-cycle, beta = rho_new / rho (init = 1:
+// rho only).  Runs only while the solve is live.
+__global__ void __launch_bounds__(CF_RED_THREADS) k_mg_rz64(Cg64 a, int init) {
+    SolverState* S = a.S;
+    if (*(volatile int*)&S->status != ST_RUNNING) return;
+    const int lane = threadIdx.x & 31;
+    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
+    double arz = 0.0;
+    if (unit < a.U) {
+        const int g = unit % a.G, band = unit / a.G;
+        const int c0 = g * CF_UNIT_COLS + 2 * lane;
+        const int j0 = band * CF_BAND_ROWS;
+        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
+        if (c0 + 1 < a.nx) {
+            for (int j = j0; j < j1; ++j) {
+                size_t k = (size_t)j * a.pitch + c0;
+                double2 rv = __ldg(reinterpret_cast<const double2*>(a.r + k));
+                double2 zv = __ldg(reinterpret_cast<const double2*>(a.z + k));
+                arz = fma(rv.x, zv.x, arz);
+                arz = fma(rv.y, zv.y, arz);
+            }
+        } else if (c0 < a.nx) {
+            for (int j = j0; j < j1; ++j) {
+                size_t k = (size_t)j * a.pitch + c0;
+                arz = fma(a.r[k], a.z[k], arz);
+            }
+        }
+    }
+    arz = warp_fold(arz);
+    if (unit < a.U && lane == 0) a.part0[unit] = arz;
+    if (last_block_arrive(&S->ticket[7])) {
+        double rz = final_tree(a.part0, a.U);
+        if (threadIdx.x == 0) {
+            S->ticket[7] = 0;
+            if (!init) S->beta = rz / S->rho;
+            S->rho = rz;
         }
     }
 }
@@ -636,6 +687,7 @@ static Cg64 cg64_args(cf_ctx* c, const Stencil& st) {
 static int red_blocks(const cf_ctx* c) { return (c->n_units + CF_RED_WARPS - 1) / CF_RED_WARPS; }
 
 static const int kBatch = CF_CG_BATCH;  // CG iterations per graph launch
+static const int kBatchMG = 4;          // MG-PCG iterations per graph launch
 
 // Build (or reuse) the graph of kBatch iterations for the current stencil.
 static int ensure_graph(cf_ctx* c, const Stencil& st, bool mixed) {
@@ -668,9 +720,67 @@ static int ensure_graph(cf_ctx* c, const Stencil& st, bool mixed) {
     return CF_OK;
 }
 
+// Capture the launches of fn into a graph.
+template <typename F>
+static int capture(cf_ctx* c, cudaGraphExec_t* ge, F&& fn) {
+    if (*ge) {
+        cudaGraphExecDestroy(*ge);
+        *ge = nullptr;
+    }
+    cudaGraph_t g;
+    int rc = cuda_check(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "capture begin");
+    if (rc) return rc;
+    fn();
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if ((rc = cuda_check(c, e, "capture end"))) return rc;
+    e = cudaGraphInstantiate(ge, g, 0);
+    cudaGraphDestroy(g);
+    return cuda_check(c, e, "graph instantiate");
+}
+
+// MG-PCG graphs for the current stencil: gmg = kBatchMG iterations of
+// K1 (z-mode), K2, V-cycle, r.z; gmg_pre = V-cycle and r.z after the
+// residual was formed (cold start, and after each reliable update).
+static int ensure_graph_mg(cf_ctx* c, const Stencil& st) {
+    if (c->gmg && c->gmg_pre && std::memcmp(&c->gmg_st, &st, sizeof(Stencil)) == 0) return CF_OK;
+    const bool mixed = c->precision == CF_PREC_MIXED;
+    const int nb = red_blocks(c);
+    const double scale = -st.ms;
+    Cg64 a = cg64_args(c, st);
+    a.mg = 1;
+    a.z = mixed ? nullptr : mg_z64(c);
+    int per = 0, pre = 0;
+    int rc = capture(c, &c->gmg, [&] {
+        for (int i = 0; i < kBatchMG; ++i) {
+            if (mixed) {
+                per = cg32_launch_iteration_mg(c, st, scale);
+            } else {
+                k_cg_dir_matvec64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
+                k_cg_update64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
+                per = 3 + mg_vcycle(c, scale);
+                k_mg_rz64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a, 0);
+            }
+        }
+    });
+    if (!rc)
+        rc = capture(c, &c->gmg_pre, [&] {
+            if (mixed) {
+                pre = cg32_mg_precondition(c, scale, 1);
+            } else {
+                pre = 1 + mg_vcycle(c, scale);
+                k_mg_rz64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a, 1);
+            }
+        });
+    if (rc) return rc;
+    c->gmg_st = st;
+    c->gmg_per_iter = per;
+    c->gmg_pre_launches = pre;
+    return CF_OK;
+}
+
 // accumulate the device time of a CG batch in which every iteration ran
-static void batch_profile(cf_ctx* c, int iters) {
-    if (!c->prof || iters != kBatch) return;
+static void batch_profile(cf_ctx* c, int iters, int batch = kBatch) {
+    if (!c->prof || iters != batch) return;
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]) == cudaSuccess) {
         c->pd.solve_ms += ms;
@@ -709,7 +819,9 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     Stencil st;
     build_stencil(c, dt, o.precon_none, &st);
     const bool mixed = c->precision == CF_PREC_MIXED;
-    int rc = ensure_graph(c, st, mixed);
+    const bool mg = o.precon_mg != 0;
+    int rc = mg ? mg_setup(c) : CF_OK;
+    if (!rc) rc = mg ? ensure_graph_mg(c, st) : ensure_graph(c, st, mixed);
     if (rc) return rc;
 
     // solver parameters
@@ -732,22 +844,38 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     if (!mixed) {
         k_div_init64<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
         c->launches += 1;
-        int max_launch = o.max_iter / kBatch + 3;
+        const int batch = mg ? kBatchMG : kBatch;
+        cudaGraphExec_t ge = mg ? c->gmg : c->g64;
+        const int per_batch = mg ? c->gmg_per_iter * kBatchMG : 2 * kBatch;
+        if (mg) {
+            if ((rc = cuda_check(c, cudaGraphLaunch(c->gmg_pre, c->stream), "graph launch"))) return rc;
+            c->launches += c->gmg_pre_launches;
+        }
+        int max_launch = o.max_iter / batch + 3;
         int prev_iter = 0;
         for (int l = 0;; ++l) {
             if ((rc = read_state(c))) return rc;
-            if (l > 0) batch_profile(c, c->hS->iter - prev_iter);
+            if (l > 0) batch_profile(c, c->hS->iter - prev_iter, batch);
             prev_iter = c->hS->iter;
             if (c->hS->status != ST_RUNNING) break;
             if (l >= max_launch) return fail(c, CF_ERR_NUMERIC, "solver did not stop after %d batches", l);
             if (c->prof) cudaEventRecord(c->ev[0], c->stream);
-            if ((rc = cuda_check(c, cudaGraphLaunch(c->g64, c->stream), "graph launch"))) return rc;
+            if ((rc = cuda_check(c, cudaGraphLaunch(ge, c->stream), "graph launch"))) return rc;
             if (c->prof) cudaEventRecord(c->ev[1], c->stream);
-            c->launches += 2 * kBatch;
+            c->launches += per_batch;
         }
     } else {
         k_div_init_mixed<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
         c->launches += 1;
+        const int batch = mg ? kBatchMG : kBatch;
+        cudaGraphExec_t ge = mg ? c->gmg : c->g32;
+        const int per_batch = mg ? c->gmg_per_iter * kBatchMG : 2 * kBatch;
+        auto precondition = [&]() -> int {
+            if (!mg) return CF_OK;
+            c->launches += c->gmg_pre_launches;
+            return cuda_check(c, cudaGraphLaunch(c->gmg_pre, c->stream), "graph launch");
+        };
+        if ((rc = precondition())) return rc;
         if ((rc = read_state(c))) return rc;
         Outer oa{};
         oa.nx = c->ph.nx;
@@ -768,23 +896,24 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
         oa.part2 = c->partials + 2 * c->n_units;
         oa.S = c->S;
         dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
-        int max_launch = o.max_iter / kBatch + 3 * (o.max_outer + 1);
+        int max_launch = o.max_iter / batch + 3 * (o.max_outer + 1);
         int launches = 0;
         while (c->hS->status == ST_RUNNING) {
             while (c->hS->status == ST_RUNNING && c->hS->inner_status == ST_RUNNING) {
                 if (++launches > max_launch) return fail(c, CF_ERR_NUMERIC, "mixed solver did not stop");
                 int prev_iter = c->hS->iter;
                 if (c->prof) cudaEventRecord(c->ev[0], c->stream);
-                if ((rc = cuda_check(c, cudaGraphLaunch(c->g32, c->stream), "graph launch"))) return rc;
+                if ((rc = cuda_check(c, cudaGraphLaunch(ge, c->stream), "graph launch"))) return rc;
                 if (c->prof) cudaEventRecord(c->ev[1], c->stream);
-                c->launches += 2 * kBatch;
+                c->launches += per_batch;
                 if ((rc = read_state(c))) return rc;
-                batch_profile(c, c->hS->iter - prev_iter);
+                batch_profile(c, c->hS->iter - prev_iter, batch);
             }
             if (c->hS->status != ST_RUNNING) break;
             k_outer_add<<<grd, blk, 0, c->stream>>>(c->x.a, c->e32.a, c->ph.nx, c->ph.ny, c->vpitch, c->p32);
             k_outer_resid<<<nb, CF_RED_THREADS, 0, c->stream>>>(oa);
             c->launches += 2;
+            if ((rc = precondition())) return rc;
             if ((rc = read_state(c))) return rc;
             if (++launches > max_launch) return fail(c, CF_ERR_NUMERIC, "mixed solver did not stop");
         }

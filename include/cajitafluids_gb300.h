@@ -92,12 +92,16 @@ typedef struct {
 } cf_grid_desc;
 
 /* Pressure-solver options (src/VelocityCorrector.hpp:96-106, 297-339).
- * solver: "Reference" or "PCG" (both run the GPU Jacobi-PCG); other HYPRE
- * solver names return CF_ERR_UNSUPPORTED.
+ * solver: "Reference" or "PCG" (both run the GPU preconditioned CG); other
+ * HYPRE solver names return CF_ERR_UNSUPPORTED.
  * precon (read for "PCG"; "Reference" always uses the diagonal preconditioner,
  * src/VelocityCorrector.hpp:158-180): "Diagonal" or "Jacobi" -> diagonal
- * (Jacobi) scaling, "None"/"none" -> unpreconditioned CG, "PFMG"/"SMG" and
- * other HYPRE names -> CF_ERR_UNSUPPORTED.
+ * (Jacobi) scaling, "None"/"none" -> unpreconditioned CG, "PFMG", "SMG" or
+ * "MG" -> one geometric multigrid V-cycle per iteration (cell-centred
+ * levels, red-black Gauss-Seidel, bilinear transfers; the reference CLI's
+ * default is PCG + PFMG, examples/advection.cpp:186-189; a periodic axis
+ * needs an even cell count, else CF_ERR_UNSUPPORTED), other HYPRE names ->
+ * CF_ERR_UNSUPPORTED.
  * Convergence: ||r||_2 <= tol * ||b||_2, or, when abs_tol > 0,
  * ||div u||_L2 = ||r||_2 * dx <= abs_tol.  The reference hard-codes
  * tol 1e-6 and max_iter 2000 (:103-104). */

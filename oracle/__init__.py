@@ -68,6 +68,7 @@ def lib():
             "orc_trace": (None, [vp, ctypes.c_int, dp, ctypes.c_double, dp]),
             "orc_matvec": (None, [vp, ctypes.c_double, dp, dp]),
             "orc_canonical_dot": (ctypes.c_double, [ctypes.c_int, ctypes.c_int, dp, dp]),
+            "orc_mg_apply": (ctypes.c_int, [vp, ctypes.c_double, dp, dp]),
             "orc_threads": (ctypes.c_int, []),
         }
         for k, (r, a) in sig.items():
@@ -200,6 +201,13 @@ class Oracle:
         out = np.empty_like(xy)
         self.lib.orc_trace(self.h, xy.shape[0], _dp(xy), float(dt), _dp(out))
         return out
+
+    def mg_apply(self, dt, r):
+        """One multigrid V-cycle applied to r; returns (z, levels)."""
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        z = np.empty_like(r)
+        nlev = self.lib.orc_mg_apply(self.h, float(dt), _dp(r), _dp(z))
+        return z, nlev
 
     def matvec(self, dt, p):
         p = np.ascontiguousarray(p, dtype=np.float64)

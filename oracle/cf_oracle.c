@@ -97,6 +97,10 @@ orc_state* orc_create(const orc_params* prm, char* err, int errlen) {
             return NULL;
         }
     }
+    if (prm->precon_mg && ((prm->periodic[0] && (prm->nx & 1)) || (prm->periodic[1] && (prm->ny & 1)))) {
+        snprintf(err, errlen, "multigrid needs an even cell count along periodic axes");
+        return NULL;
+    }
     orc_state* st = (orc_state*)calloc(1, sizeof(orc_state));
     st->p = *prm;
     st->dx = dx;
@@ -823,7 +827,11 @@ static int mg_build(orc_state* st, double scale, mg_level* lev) {
             L->r = (double*)calloc(cells, sizeof(double));
         }
         ++n;
+        /* halve while both axes are even and >= 16 and the halved extent
+         * stays even along periodic axes (no same-colour neighbours across
+         * the wrap, so each half sweep is independent of its order) */
         if (n == MG_MAX || (nx & 1) || (ny & 1) || nx < 16 || ny < 16) break;
+        if ((st->p.periodic[0] && ((nx / 2) & 1)) || (st->p.periodic[1] && ((ny / 2) & 1))) break;
         nx /= 2;
         ny /= 2;
     }
@@ -887,6 +895,20 @@ static int project_mg(orc_state* st, double scale, double tol, double abs_tol, i
     *bb_out = bb;
     *rr_out = rr;
     return status;
+}
+
+/* test export: z = one V-cycle applied to r at time step dt; returns the
+ * number of levels */
+int orc_mg_apply(orc_state* st, double dt, const double* r, double* z) {
+    size_t n = (size_t)st->p.nx * st->p.ny;
+    double scale = dt / ((st->p.density * st->dx) * st->dx);
+    mg_level lev[MG_MAX];
+    int nlev = mg_build(st, scale, lev);
+    memcpy(st->r, r, n * sizeof(double));
+    mg_vcycle(&st->p, lev, nlev, 0);
+    memcpy(z, st->z, n * sizeof(double));
+    mg_free(lev, nlev);
+    return nlev;
 }
 
 /* Jacobi-preconditioned CG, cold start x0 = 0 (src/VelocityCorrector.hpp:

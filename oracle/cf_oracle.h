@@ -80,6 +80,7 @@ void orc_trace(const orc_state* st, int n, const double* xy, double dt,
                double* out);
 void orc_matvec(const orc_state* st, double dt, const double* p, double* q);
 double orc_canonical_dot(int nx, int ny, const double* a, const double* b);
+int orc_mg_apply(orc_state* st, double dt, const double* r, double* z);
 int orc_threads(void);
 
 #ifdef __cplusplus

@@ -11,12 +11,13 @@ FIELDS = ("q", "u", "v")
 
 def make_pair(nx, ny, periodic=(False, False), bc=(0, 0, 0, 0), source=None, source_mode=0, body=(0.0, 0.0),
               body_density_scaled=False, density=0.1, quirks=0, precision="fp64", lo=(0.0, 0.0), hi=None,
-              precon_none=False):
+              precon_none=False, precon_mg=False):
     from oracle import Oracle
     if hi is None:
         hi = (lo[0] + 1.0, lo[1] + ny / nx)
     o = Oracle(nx, ny, lo=lo, hi=hi, periodic=periodic, bc=bc, source=source, source_mode=source_mode, body=body,
-               body_density_scaled=body_density_scaled, density=density, quirks=quirks, precon_none=precon_none)
+               body_density_scaled=body_density_scaled, density=density, quirks=quirks, precon_none=precon_none,
+               precon_mg=precon_mg)
     c = Context(nx, ny, lo=lo, hi=hi, periodic=periodic, precision=precision)
     c.set_bc(bc)
     if source is not None:

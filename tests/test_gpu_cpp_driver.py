@@ -26,17 +26,23 @@ def _read_dump(path):
     return out
 
 
-def test_cpp_driver_matches_oracle(built, tmp_path):
+@pytest.mark.parametrize("precon", [None, "Diagonal"])
+def test_cpp_driver_matches_oracle(built, tmp_path, precon):
+    """Default preconditioner (PFMG, the reference CLI's default, served by
+    the multigrid V-cycle) and the diagonal one."""
     from cajitafluids_gb300.build import build_example
     exe = build_example()
     n, steps = 40, 6
     out = os.path.join(tmp_path, "fields.bin")
-    r = subprocess.run([exe, "-n", str(n), "--steps", str(steps), "--linear", "--tol", "1e-9", "--inflow", "0.45",
-                        "0.10", "0.10", "0.05", "0.0", "3.0", "1.0", "-d", "0.005", "--out", out],
-                       capture_output=True, text=True, timeout=120)
+    cmd = [exe, "-n", str(n), "--steps", str(steps), "--linear", "--tol", "1e-9", "--inflow", "0.45",
+           "0.10", "0.10", "0.05", "0.0", "3.0", "1.0", "-d", "0.005", "--out", out]
+    if precon:
+        cmd += ["-p", precon]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     got = _read_dump(out)
-    o = Oracle(n, n, source=((0.45, 0.10), (0.10, 0.05), (0.0, 3.0), 1.0), density=0.1)
+    o = Oracle(n, n, source=((0.45, 0.10), (0.10, 0.05), (0.0, 3.0), 1.0), density=0.1,
+               precon_mg=precon is None)
     o.setup(0.005, tol=1e-9, max_iter=100000)
     for _ in range(steps):
         o.step(0.005, 1, tol=1e-9, max_iter=100000)
@@ -49,5 +55,5 @@ def test_cpp_driver_rejects_unsupported_backend_and_solver(built):
     exe = build_example()
     r = subprocess.run([exe, "-n", "8", "--steps", "1", "--device", "serial"], capture_output=True, text=True)
     assert r.returncode == 1 and "not part of this build" in r.stderr
-    r = subprocess.run([exe, "-n", "8", "--steps", "1", "-p", "PFMG"], capture_output=True, text=True)
+    r = subprocess.run([exe, "-n", "8", "--steps", "1", "-p", "Euclid"], capture_output=True, text=True)
     assert r.returncode == 1 and "not implemented" in r.stderr
