@@ -5,9 +5,11 @@ Workload (one step = Solver::step: advect q/u/v, inputs, pressure projection):
   4096^2 periodic, seeded spectral velocity (rms |u| = 1, k <= 64) and
   scalar, cubic interpolation, dt = 0.5 dx / max|u|, projection to
   ||div u||_L2 <= 1e-8 (FP64 residual), mixed precision (FP32 advection and
-  inner PCG, FP64 outer refinement).  The same steps in plain FP64 are timed
-  for the mixed-vs-FP64 ratio, and the scalar error of the mixed run against
-  the FP64 run is reported.
+  inner PCG, FP64 outer refinement), PCG preconditioned by "PFMG" (the
+  reference CLI's default pairing, served by the geometric multigrid
+  V-cycle; --precon Diagonal selects Jacobi-PCG).  The same steps in plain
+  FP64 are timed for the mixed-vs-FP64 ratio, and the scalar error of the
+  mixed run against the FP64 run is reported.
 
 Output: one JSON line (rank 0).  value = steps/s of the mixed form over all
 ranks (each rank runs an independent replica; the path is single-GPU).
@@ -39,11 +41,48 @@ ALG_BYTES_MIXED_ITER = 44.0
 # bytes the kernels of this build must move per cell per iteration
 KERNEL_BYTES_FP64_ITER = 80.0
 KERNEL_BYTES_MIXED_ITER = 32.0
-# CG iterations per step of this workload in FP64 (the FP64 GPU path and the
-# CPU oracle are bit-identical, so they take the same count); the reference
-# arm extrapolates its sampled CG cost to this count.  Measured by this
-# bench's FP64 leg on GB300 (see fp64.cg_iters_per_step in its output).
+# Jacobi-PCG iterations per step of this workload in FP64 (the FP64 GPU path
+# and the CPU oracle are bit-identical, so they take the same count); with
+# --precon Diagonal the reference arm extrapolates its sampled CG cost to this
+# count.  Measured by this bench's FP64 leg on GB300.
 FP64_ITERS_PER_STEP_4096 = 7890
+MG_NAMES = ("PFMG", "SMG", "MG")
+
+
+def mg_levels(nx, ny, periodic):
+    """Level extents of the multigrid hierarchy (the library's coarsening
+    rule: halve while both axes are even and >= 16 and the halved extent
+    stays even along periodic axes)."""
+    lv = [(nx, ny)]
+    while not (nx % 2 or ny % 2 or nx < 16 or ny < 16 or (periodic[0] and (nx // 2) % 2)
+               or (periodic[1] and (ny // 2) % 2)):
+        nx //= 2
+        ny //= 2
+        lv.append((nx, ny))
+    return lv
+
+
+def alg_bytes_per_iter(nx, ny, periodic, precon, word, outer_frac=0.0):
+    """Algorithmic (minimal compulsory) bytes of one PCG iteration.
+
+    Jacobi: 11 full-grid words per cell (SpMV + dot: R p, W Ap; update + dot:
+    R x, p, r, Ap, W x, r; direction: R z, p, W p; M^-1 from wall flags).
+    MG: the same 11 words with z read instead of recomputed, plus r.z (2 words)
+    and the V-cycle: per non-coarsest level 8 red/black half sweeps of 1.5
+    words each (other colour read, own b read, own x written), residual 3,
+    restriction 1.25, prolongation 2.25 words per cell of that level; the
+    one-CTA coarsest level 2 words.  Mixed: plus the FP64 reliable update
+    (R x, e, W x; R x, b, W r32, e32 = 44 B per cell) on the fraction of
+    iterations that run it."""
+    n = nx * ny
+    if precon not in MG_NAMES:
+        return 11 * word * n
+    b = 13 * word * n
+    lv = mg_levels(nx, ny, periodic)
+    for a, c in lv[:-1]:
+        b += 18.5 * word * a * c
+    b += 2 * word * lv[-1][0] * lv[-1][1]
+    return b + outer_frac * 44.0 * n
 
 
 def env_int(name, default):
@@ -124,7 +163,7 @@ def make_context(w, precision, device):
 
 def solver_opts(w):
     from cajitafluids_gb300 import SolverOptions
-    return SolverOptions(tol=w.tol, abs_tol=w.abs_tol, max_iter=w.max_iter)
+    return SolverOptions(tol=w.tol, abs_tol=w.abs_tol, max_iter=w.max_iter, precon=w.precon)
 
 
 def run_steps(c, w, n, stats=None):
@@ -152,17 +191,30 @@ def max_over_ranks(dist, x):
 # --------------------------------------------------------------------------
 def cpu_reference_sample(w, k_iters, m1=5, m2=15, steps=1):
     """Oracle (CPU port of the reference algorithm, all OpenMP threads) timed
-    on a bounded sample of the workload: one advection + inputs, and the
-    projection capped at m1 and m2 CG iterations; the CG cost per iteration
-    and the fixed projection cost are extrapolated to k_iters iterations."""
+    on a bounded sample of the workload.  MG-PCG: whole steps (one untimed
+    first).  Jacobi-PCG: one advection + inputs, and the projection capped at
+    m1 and m2 CG iterations; the CG cost per iteration and the fixed
+    projection cost are extrapolated to k_iters iterations."""
     from oracle import Oracle, threads
+    mg = w.precon in MG_NAMES
     o = Oracle(w.nx, w.ny, periodic=w.periodic, bc=w.bc, source=w.source, source_mode=w.source_mode,
-               body=w.body, body_density_scaled=w.body_density_scaled, density=w.density)
+               body=w.body, body_density_scaled=w.body_density_scaled, density=w.density, precon_mg=mg)
     o.set("q", w.q0)
     o.set("u", w.u0)
     o.set("v", w.v0)
     per_step = []
     detail = {}
+    if mg:
+        iters = []
+        for s in range(steps + 1):
+            t0 = time.perf_counter()
+            st = o.step(w.dt, w.order, tol=w.tol, abs_tol=w.abs_tol, max_iter=w.max_iter)
+            if s > 0:
+                per_step.append(time.perf_counter() - t0)
+                iters.append(st["iterations"])
+        detail = {"mg_iters_per_step": statistics.mean(iters), "sample_steps": steps,
+                  "sampled_wall_s": sum(per_step)}
+        return per_step, threads(), detail
     for _ in range(steps):
         t0 = time.perf_counter()
         o.advect(w.dt, w.order)
@@ -200,9 +252,12 @@ def bench_gb300(args, rank, world, dist, device):
     from cajitafluids_gb300.workloads import config2
     t_gen = time.perf_counter()
     w = config2(args.size, steps=args.steps)
-    w.max_iter = 400000
+    w.precon = args.precon
+    mg = w.precon in MG_NAMES
+    w.max_iter = 2000 if mg else 400000
     t_gen = time.perf_counter() - t_gen
     ncell = w.nx * w.ny
+    pc_text = "PCG + PFMG-named geometric multigrid V-cycle" if mg else f"PCG + {w.precon}"
 
     legs = set(args.legs.split(","))
     peak, peak_kind = measured_peaks()
@@ -212,10 +267,12 @@ def bench_gb300(args, rank, world, dist, device):
         "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic: seeded spectral velocity (k<=64, per-mode power k^-11/3, rms|u|=1) and scalar",
         "config": {"workload": f"{w.nx}x{w.ny} periodic spectral, mixed precision (FP32 advection + inner PCG, "
-                               f"FP64 outer refinement), cubic, ||div u||_L2 <= {w.abs_tol:g}",
+                               f"FP64 outer refinement), cubic, {pc_text}, ||div u||_L2 <= {w.abs_tol:g}",
                    "nx": w.nx, "ny": w.ny, "periodic": True, "precision": "mixed", "value_order": w.order,
-                   "dt": w.dt, "abs_tol_div_l2": w.abs_tol, "parallelism": f"replicas x{world}",
-                   "l2_policy": "inputs larger than L2 (state + solver vectors ~0.9 GB)"},
+                   "dt": w.dt, "abs_tol_div_l2": w.abs_tol, "solver": "PCG", "precon": w.precon,
+                   "mg_levels": len(mg_levels(w.nx, w.ny, w.periodic)) if mg else None,
+                   "parallelism": f"replicas x{world}",
+                   "l2_policy": "inputs larger than L2 (state + solver vectors ~1 GB)"},
         "adjoint_forward_ratio": None,
     }
     q_mixed_w = None
@@ -243,21 +300,30 @@ def bench_gb300(args, rank, world, dist, device):
         ms_max = max_over_ranks(dist, ms)
         value = world * args.steps / (ms_max / 1e3)
         it_ms = prof["solve_ms"] / prof["solve_iters"] if prof["solve_iters"] else float("nan")
-        achieved = ALG_BYTES_MIXED_ITER * ncell / (it_ms / 1e3) / 1e9
-        kern = KERNEL_BYTES_MIXED_ITER * ncell / (it_ms / 1e3) / 1e9
+        iters = statistics.mean(s["iterations"] for s in stats)
+        outers = statistics.mean(s["outer_iterations"] for s in stats)
+        it_bytes = alg_bytes_per_iter(w.nx, w.ny, w.periodic, w.precon, 4, min(outers / max(iters, 1), 1.0))
+        achieved = it_bytes / (it_ms / 1e3) / 1e9
+        if mg:
+            kname = ("MG-PCG inner iteration: k_tma_dir_matvec32 + k_tma_update32 + gated k_outer_add/"
+                     "k_outer_resid + V-cycle (k_mg_smooth/residual/restrict/prolong, k_mg_coarse) + k_mg_rz32")
+            kern_extra = {}
+        else:
+            kname = "inner CG iteration (k_tma_dir_matvec32 + k_tma_update32)"
+            kern_extra = {"kernel_bytes_per_cell": KERNEL_BYTES_MIXED_ITER,
+                          "kernel_bytes_gbs": KERNEL_BYTES_MIXED_ITER * ncell / (it_ms / 1e3) / 1e9}
         line.update({
             "value": value, "ms_per_step": ms_max / args.steps, "cell_updates_per_s": value * ncell,
-            "mixed": {"cg_inner_iters_per_step": statistics.mean(s["iterations"] for s in stats),
-                      "outer_refinements_per_step": statistics.mean(s["outer_iterations"] for s in stats),
+            "mixed": {"cg_inner_iters_per_step": iters, "outer_refinements_per_step": outers,
                       "div_l2_max": max(s["div_l2"] for s in stats),
                       "div_linf_max": max(s["div_linf"] for s in stats),
                       "advect_ms_per_step": prof["advect_ms"] / max(prof["advect_calls"], 1),
-                      "cg_iter_ms": it_ms, "project_ms_per_step": prof["project_ms"] / max(prof["projects"], 1)},
-            "roofline": {"bound": "hbm", "kernel": "inner CG iteration (k_in_dir_matvec32 + k_in_update32)",
+                      "cg_iter_ms": it_ms, "cg_iters_timed": prof["solve_iters"],
+                      "project_ms_per_step": prof["project_ms"] / max(prof["projects"], 1)},
+            "roofline": {"bound": "hbm", "kernel": kname,
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": f"hbm_gbs {peak_kind}", "traffic": None,
-                         "algorithmic_bytes_per_cell": ALG_BYTES_MIXED_ITER,
-                         "kernel_bytes_per_cell": KERNEL_BYTES_MIXED_ITER, "kernel_bytes_gbs": kern},
+                         "algorithmic_bytes_per_cell": it_bytes / ncell, **kern_extra},
             "gpu_launches": launches, "clocks": clk,
             "timing": {"device_ms": ms, "wall_s": t_wall, "workload_gen_s": t_gen},
         })
@@ -310,8 +376,10 @@ def bench_gb300(args, rank, world, dist, device):
         value64 = world * args.fp64_steps / (ms64 / 1e3) if args.fp64_steps else None
         k64 = statistics.mean(s["iterations"] for s in fstats[args.warmup:]) if args.fp64_steps else None
         it64_ms = prof64["solve_ms"] / prof64["solve_iters"] if prof64["solve_iters"] else float("nan")
-        achieved64 = ALG_BYTES_FP64_ITER * ncell / (it64_ms / 1e3) / 1e9
+        achieved64 = alg_bytes_per_iter(w.nx, w.ny, w.periodic, w.precon, 8) / (it64_ms / 1e3) / 1e9
         line["fp64"] = {"steps_per_s": value64, "cg_iters_per_step": k64, "cg_iter_ms": it64_ms,
+                        "advect_ms_per_step": prof64["advect_ms"] / max(prof64["advect_calls"], 1),
+                        "project_ms_per_step": prof64["project_ms"] / max(prof64["projects"], 1),
                         "roofline_hbm_frac": achieved64 / peak,
                         "div_l2_max": max(s["div_l2"] for s in fstats) if fstats else None}
         if value and value64:
@@ -328,12 +396,15 @@ def bench_gb300(args, rank, world, dist, device):
     # ---- CPU baseline (rank 0, N = 1) ----
     if rank == 0 and world == 1 and "cpu" in legs and not args.skip_cpu:
         k_ref = k64 if k64 else (line.get("mixed", {}).get("cg_inner_iters_per_step") or args.ref_iters)
-        per_step, cores, detail = cpu_reference_sample(w, k_ref)
+        per_step, cores, detail = cpu_reference_sample(w, k_ref, steps=2 if mg else 1)
+        if mg:
+            sample = (f"oracle FP64 MG-PCG on the same {w.nx}^2 state: 2 whole steps timed after 1 untimed "
+                      f"(advection + inputs + projection to the same tolerance)")
+        else:
+            sample = (f"oracle FP64 on the same {w.nx}^2 state: 1 advection+inputs and the projection capped "
+                      f"at 5 and 15 CG iterations, extrapolated to {k_ref:.0f} iterations/step")
         line["cpu_baseline"] = {"value": 1.0 / statistics.mean(per_step), "unit": "steps/s", "cores": cores,
-                                "kind": "port", "cpu": cpu_model(),
-                                "sample": f"oracle FP64 on the same {w.nx}^2 state: 1 advection+inputs and the "
-                                          f"projection capped at 5 and 15 CG iterations, extrapolated to "
-                                          f"{k_ref:.0f} iterations/step", **detail}
+                                "kind": "port", "cpu": cpu_model(), "sample": sample, **detail}
     return line
 
 
@@ -346,7 +417,8 @@ def bench_adjoint(args, device, dist):
     from cajitafluids_gb300.workloads import config3
     w = config3(args.adjoint_size, steps=args.adjoint_steps)
     every = args.adjoint_every
-    opts = SolverOptions(tol=w.tol, max_iter=200000)
+    mg = args.precon in MG_NAMES
+    opts = SolverOptions(tol=w.tol, max_iter=2000 if mg else 200000, precon=args.precon)
     inflow = ((0.45, 0.10), (0.10, 0.05), (0.0, 0.0), 1.0)
 
     def fresh(rate=1.0):
@@ -380,7 +452,7 @@ def bench_adjoint(args, device, dist):
     t_bwd = c.timer_stop()
     assert np.array_equal(c.download("q"), qT)   # checkpointed forward = plain forward
     out = {"workload": f"{w.nx}^2 walls, spectral velocity + 8 Gaussian blobs, rate inflow, T={w.steps}, "
-                       f"checkpoint every {every}, FP64, CG tol {w.tol:g}",
+                       f"checkpoint every {every}, FP64, PCG + {args.precon}, tol {w.tol:g}",
            "forward_ms": t_fwd, "forward_checkpointed_ms": t_fc, "backward_ms": t_bwd,
            "forward_plus_adjoint_over_forward": (t_fc + t_bwd) / t_fwd,
            "cg_iters_per_forward_step": its / w.steps,
@@ -420,25 +492,36 @@ def bench_reference(args, rank, world, dist):
         return None
     from cajitafluids_gb300.workloads import config2
     w = config2(args.size, steps=args.steps)
+    w.precon = args.precon
+    mg = w.precon in MG_NAMES
+    w.max_iter = 2000 if mg else 400000
     k_ref = FP64_ITERS_PER_STEP_4096 if (FP64_ITERS_PER_STEP_4096 and args.size == 4096) else args.ref_iters
     per = []
     detail = {}
-    total = max(1, args.steps) + max(0, min(args.warmup, 1))
-    for s in range(total):
-        p, cores, detail = cpu_reference_sample(w, k_ref)
-        if s >= total - max(1, args.steps):
-            per.extend(p)
+    if mg:
+        # whole steps; at 4096^2 one step is a few seconds on 16 cores
+        n_steps = max(1, min(args.steps, 3))
+        per, cores, detail = cpu_reference_sample(w, k_ref, steps=n_steps)
+        sample = f"{n_steps} whole MG-PCG steps after 1 untimed"
+    else:
+        total = max(1, args.steps) + max(0, min(args.warmup, 1))
+        for s in range(total):
+            p, cores, detail = cpu_reference_sample(w, k_ref)
+            if s >= total - max(1, args.steps):
+                per.extend(p)
+        sample = (f"per step: 1 advection+inputs and the projection capped at 5 and 15 CG iterations, "
+                  f"extrapolated to {k_ref} iterations/step")
     value = 1.0 / statistics.mean(per)
     return {
         "metric": METRIC, "impl": "reference", "value": value, "unit": "steps/s", "n_gpus": world,
-        "steps": len(per), "warmup": total - len(per), "ms_per_step": 1e3 * statistics.mean(per),
+        "steps": len(per), "warmup": 1, "ms_per_step": 1e3 * statistics.mean(per),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded spectral velocity (k<=64, per-mode power k^-11/3, rms|u|=1) and scalar",
         "config": {"workload": f"{w.nx}x{w.ny} periodic spectral, FP64 reference algorithm (CPU), cubic, "
-                               f"||div u||_L2 <= {w.abs_tol:g}", "nx": w.nx, "ny": w.ny},
+                               f"PCG + {w.precon}, ||div u||_L2 <= {w.abs_tol:g}", "nx": w.nx, "ny": w.ny,
+                   "precon": w.precon},
         "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port", "cpu": cpu_model(),
-                         "sample": f"per step: 1 advection+inputs and the projection capped at 5 and 15 CG "
-                                   f"iterations, extrapolated to {k_ref} iterations/step", **detail},
+                         "sample": sample, **detail},
         "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "reference_unbuildable": "Kokkos/Cabana-Cajita/HYPRE/MPI are not available; the oracle is the CPU port",
     }
@@ -457,10 +540,13 @@ def main():
     ap.add_argument("--legs", default="mixed,e2e,fp64,adjoint,cpu",
                     help="comma list of legs to run: mixed (headline), e2e, fp64, adjoint, cpu")
     ap.add_argument("--adjoint-size", type=int, default=512)
-    ap.add_argument("--adjoint-steps", type=int, default=56)
+    ap.add_argument("--adjoint-steps", type=int, default=200)
     ap.add_argument("--adjoint-every", type=int, default=14)
     ap.add_argument("--adjoint-fd", type=int, default=0, help="central-difference checks of the gradient")
     ap.add_argument("--ref-iters", type=int, default=12000)
+    ap.add_argument("--precon", default="PFMG",
+                    help="PCG preconditioner: PFMG/SMG/MG (geometric multigrid, the reference CLI default), "
+                         "Diagonal (Jacobi) or None")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

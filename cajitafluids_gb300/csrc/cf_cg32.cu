@@ -455,13 +455,13 @@ __global__ void k_z32_ghosts(float* z, int nx, int ny, int pitch, int per_x, int
     }
 }
 
-// rho = r.z (FP32 per lane over a 64 x 16 unit, FP64 beyond).  mode 0 (after
-// an inner iteration): beta = rho_new / rho.  mode 1 (after the residual was
-// formed from the FP64 solution): beta = rho_new / rho_prev, which keeps the
-// search direction across a reliable update (ignored on a restart).
+// rho = r.z (FP32 per lane over a 64 x 16 unit, FP64 beyond).  After an
+// inner iteration: beta = rho_new / rho.  After the residual was re-formed
+// from the FP64 solution (S->refreshed): beta = rho_new / rho_prev, which
+// keeps the search direction across a reliable update (ignored on a restart).
 __global__ void __launch_bounds__(CF_RED_THREADS)
     k_mg_rz32(const float* r, const float* z, int nx, int ny, int pitch, int G, int U, double* part,
-              SolverState* S, int mode) {
+              SolverState* S) {
     if (!running(S)) return;
     const int lane = threadIdx.x & 31;
     const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
@@ -485,7 +485,8 @@ __global__ void __launch_bounds__(CF_RED_THREADS)
         double rz = final_tree(part, U);
         if (threadIdx.x == 0) {
             S->ticket[7] = 0;
-            double den = mode == 0 ? S->rho_in : S->rho_prev;
+            double den = S->refreshed ? S->rho_prev : S->rho_in;
+            S->refreshed = 0;
             S->beta_in = den != 0.0 ? rz / den : 0.0;
             S->rho_in = rz;
             if (isnan(rz))
@@ -605,7 +606,7 @@ void cg32_launch_iteration(cf_ctx* c, const Stencil& st) {
 }
 
 // z = V-cycle(r32), its periodic ghosts, rho = r.z; returns kernels launched
-int cg32_mg_precondition(cf_ctx* c, double scale, int mode) {
+int cg32_mg_precondition(cf_ctx* c, double scale) {
     int n = mg_vcycle(c, scale);
     if (c->ph.per_x || c->ph.per_y) {
         int m = c->ph.nx > c->ph.ny ? c->ph.nx : c->ph.ny;
@@ -614,13 +615,12 @@ int cg32_mg_precondition(cf_ctx* c, double scale, int mode) {
         n += 1;
     }
     k_mg_rz32<<<(c->n_units + CF_RED_WARPS - 1) / CF_RED_WARPS, CF_RED_THREADS, 0, c->stream>>>(
-        c->r32.a, c->z32.a, c->ph.nx, c->ph.ny, c->p32, c->G, c->n_units, c->partials, c->S, mode);
+        c->r32.a, c->z32.a, c->ph.nx, c->ph.ny, c->p32, c->G, c->n_units, c->partials, c->S);
     return n + 1;
 }
 
-// one MG-PCG inner iteration: K1 on z (M^-1 = 1), K2, then the V-cycle and
-// r.z; returns kernels launched
-int cg32_launch_iteration_mg(cf_ctx* c, const Stencil& st, double scale) {
+// K1 on z (M^-1 = 1) and K2 of one MG-PCG inner iteration
+void cg32_launch_pair_mg(cf_ctx* c, const Stencil& st) {
     Stencil stz = st;
     for (int b = 0; b < 16; ++b) stz.minv32[b] = 1.0f;
     Cg32T a = cg32_args(c, stz);
@@ -628,7 +628,6 @@ int cg32_launch_iteration_mg(cf_ctx* c, const Stencil& st, double scale) {
     k_tma_dir_matvec32<<<c->cta32, kThreads, kStages * 2 * kSlot + 128, c->stream>>>(c->map_z, c->map_pa, c->map_pb, a);
     k_tma_update32<<<c->cta32b, kThreads, kStages * 3 * kSlot + 128, c->stream>>>(c->map_e, c->map_r, c->map_pa,
                                                                             c->map_pb, a);
-    return 2 + cg32_mg_precondition(c, scale, 0);
 }
 
 }  // namespace cf

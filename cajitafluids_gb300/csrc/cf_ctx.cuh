@@ -96,8 +96,8 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
 int cg32_setup(cf_ctx* c);
 void cg32_launch_iteration(cf_ctx* c, const Stencil& st);
 int cg32_mg_setup(cf_ctx* c);
-int cg32_mg_precondition(cf_ctx* c, double scale, int mode);  // returns kernels launched
-int cg32_launch_iteration_mg(cf_ctx* c, const Stencil& st, double scale);
+int cg32_mg_precondition(cf_ctx* c, double scale);  // returns kernels launched
+void cg32_launch_pair_mg(cf_ctx* c, const Stencil& st);
 int div_norms(cf_ctx* c, double* l2, double* linf);
 // multigrid preconditioner (cf_mg.cu)
 int mg_setup(cf_ctx* c);

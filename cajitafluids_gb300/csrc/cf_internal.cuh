@@ -68,6 +68,7 @@ struct SolverState {
     double rr_in0, rr_in, rho_in, alpha_in, beta_in, tau2;
     double rr_out, inner_tol2, target2, rho_prev;
     int use_abs, restart;
+    int refreshed;  // mixed MG: r was just re-formed from the FP64 solution
     int iter, max_iter, status;
     int inner_iter, inner_status;
     int outer_iter, max_outer;

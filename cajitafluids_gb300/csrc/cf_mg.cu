@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <cstdlib>
 #include <vector>
 
 #include "cf_ctx.cuh"
@@ -26,7 +27,6 @@ namespace cf {
 
 constexpr int MG_NU = 2;
 constexpr int MG_NC = 16;
-constexpr int MG_COARSE_MAX = 2048;  // cells handled by the one-CTA coarse solver
 
 template <typename T>
 struct MgLev {
@@ -244,51 +244,344 @@ __global__ void __launch_bounds__(MG_BX* MG_BY) k_mg_prolong(MgLev<T> C, MgLev<T
     }
 }
 
-// coarsest level in one CTA: x = 0, MG_NC (red, black) and MG_NC (black, red)
-// sweeps in shared memory
-template <typename T>
-__global__ void __launch_bounds__(256) k_mg_coarse(MgLev<T> L, MgBc p, SolverState* S, int inner) {
-    if (!block_live(S, inner)) return;
-    __shared__ T xs[MG_COARSE_MAX];
-    __shared__ T bs[MG_COARSE_MAX];
-    const int n = L.nx * L.ny;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        xs[k] = T(0);
-        bs[k] = L.b[(size_t)(k / L.nx) * L.pitch + (k % L.nx)];
+// ---------------------------------------------------------------------------
+// Fused level kernels (temporal blocking in shared memory).  A CTA owns a
+// tile of FT_W x TH fine cells and recomputes a shrinking halo, so that the
+// MG_NU = 2 sweep pairs of a level need one pass over memory:
+//   k_mg_pre : x = 4 half sweeps from x = 0 (red, black, red, black),
+//              r = b - A x (in shared memory), b_coarse = R r
+//                                              (R b; W x, b_coarse)
+//   k_mg_post: x += P x_coarse, then 4 half sweeps (black, red, black, red)
+//                                              (R x, b, x_coarse; W x)
+// Every cell value is computed from the same inputs with the same operations
+// as by the level-by-level kernels above, so the results are identical.
+// k_mg_pre leaves its x in the level's r array (free in this form) and
+// k_mg_post reads it from there and writes x: a CTA of k_mg_post reads its
+// halo from other tiles, which must not be written by the same launch.
+constexpr int FT_W = 64;
+constexpr int FT_THREADS = 256;
+
+// index along an axis after the periodic wrap; -1 beyond a wall
+__device__ __forceinline__ int mg_dom(int g, int n, int per) {
+    if (g >= 0 && g < n) return g;
+    if (!per) return -1;
+    return g < 0 ? g + n : g - n;
+}
+
+// one half sweep of colour c over the tile grown by h cells; arrays have halo H
+template <typename T, int TH, int H>
+__device__ __forceinline__ void ft_half(const MgLev<T>& L, const MgBc& p, T* xs, const T* bs, int i0, int j0, int c,
+                                        int h, bool first) {
+    constexpr int W = FT_W + 2 * H;
+    const int ncol = FT_W + 2 * h, nrow = TH + 2 * h, hw = ncol / 2;
+    const int gi0 = i0 - h;
+    for (int k = threadIdx.x; k < hw * nrow; k += FT_THREADS) {
+        const int rj = k / hw, pk = k % hw;
+        const int gj = j0 - h + rj;
+        const int gi = gi0 + ((c + gj + gi0) & 1) + 2 * pk;
+        const int wi = mg_dom(gi, L.nx, p.per_x), wj = mg_dom(gj, L.ny, p.per_y);
+        if (wi < 0 || wj < 0) continue;  // beyond a wall: stays 0
+        const int li = gi - (i0 - H), lj = gj - (j0 - H);
+        const int q = lj * W + li;
+        T s;
+        if (first) {
+            s = T(0);
+        } else {
+            s = xs[q - 1] + xs[q + 1];
+            s = s + xs[q - W];
+            s = s + xs[q + W];
+        }
+        T t = mg_fma(L.scale, s, bs[q]);
+        xs[q] = t * L.invd[mg_bits(p, L.nx, L.ny, wi, wj)];
     }
     __syncthreads();
-    auto at = [&](int gi, int gj) -> T {
-        if (gi < 0 || gi >= L.nx) {
-            if (!p.per_x) return T(0);
-            gi = gi < 0 ? gi + L.nx : gi - L.nx;
+}
+
+// load x from xsrc (0 when null) and b over the tile with halo H (wrapped; 0
+// beyond walls)
+template <typename T, int TH, int H>
+__device__ __forceinline__ void ft_load(const MgLev<T>& L, const MgBc& p, T* xs, T* bs, int i0, int j0,
+                                        const T* xsrc) {
+    constexpr int W = FT_W + 2 * H, HT = TH + 2 * H;
+    for (int q = threadIdx.x; q < W * HT; q += FT_THREADS) {
+        const int li = q % W, lj = q / W;
+        const int wi = mg_dom(i0 - H + li, L.nx, p.per_x), wj = mg_dom(j0 - H + lj, L.ny, p.per_y);
+        T xv = T(0), bv = T(0);
+        if (wi >= 0 && wj >= 0) {
+            const size_t k = (size_t)wj * L.pitch + wi;
+            bv = L.b[k];
+            if (xsrc) xv = xsrc[k];
         }
-        if (gj < 0 || gj >= L.ny) {
-            if (!p.per_y) return T(0);
-            gj = gj < 0 ? gj + L.ny : gj - L.ny;
+        xs[q] = xv;
+        bs[q] = bv;
+    }
+    __syncthreads();
+}
+
+template <typename T, int TH>
+__global__ void __launch_bounds__(FT_THREADS) k_mg_pre(MgLev<T> F, MgLev<T> C, MgBc p, SolverState* S, int inner) {
+    if (!block_live(S, inner)) return;
+    constexpr int H = 5, W = FT_W + 2 * H, HT = TH + 2 * H;
+    __shared__ T xs[W * HT];
+    __shared__ T bs[W * HT];  // b, then r in place on the residual ring
+    const int i0 = blockIdx.x * FT_W, j0 = blockIdx.y * TH;
+    ft_load<T, TH, H>(F, p, xs, bs, i0, j0, nullptr);
+    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 0, 5, true);
+    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 1, 4, false);
+    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 0, 3, false);
+    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 1, 2, false);
+    // residual on the tile grown by 1 (read by the restriction), in place of b
+    {
+        const int ncol = FT_W + 2, nrow = TH + 2;
+        for (int k = threadIdx.x; k < ncol * nrow; k += FT_THREADS) {
+            const int gi = i0 - 1 + k % ncol, gj = j0 - 1 + k / ncol;
+            const int wi = mg_dom(gi, F.nx, p.per_x), wj = mg_dom(gj, F.ny, p.per_y);
+            if (wi < 0 || wj < 0) continue;
+            const int q = (gj - (j0 - H)) * W + (gi - (i0 - H));
+            T ax = F.diag[mg_bits(p, F.nx, F.ny, wi, wj)] * xs[q];
+            ax = mg_fma(F.ms, xs[q - 1], ax);
+            ax = mg_fma(F.ms, xs[q + 1], ax);
+            ax = mg_fma(F.ms, xs[q - W], ax);
+            ax = mg_fma(F.ms, xs[q + W], ax);
+            bs[q] = bs[q] - ax;
         }
-        return xs[gj * L.nx + gi];
-    };
-    auto half = [&](int color) {
-        for (int k = threadIdx.x; k < n; k += blockDim.x) {
-            int gi = k % L.nx, gj = k / L.nx;
-            if (((gi + gj) & 1) != color) continue;
-            T s = at(gi - 1, gj) + at(gi + 1, gj);
-            s = s + at(gi, gj - 1);
-            s = s + at(gi, gj + 1);
-            T t = mg_fma(L.scale, s, bs[k]);
-            xs[k] = t * L.invd[mg_bits(p, L.nx, L.ny, gi, gj)];
+    }
+    __syncthreads();
+    // x on the tile, into the r array (read back by k_mg_post)
+    for (int k = threadIdx.x; k < FT_W * TH; k += FT_THREADS) {
+        const int gi = i0 + k % FT_W, gj = j0 + k / FT_W;
+        if (gi < F.nx && gj < F.ny) F.r[(size_t)gj * F.pitch + gi] = xs[(gj - (j0 - H)) * W + (gi - (i0 - H))];
+    }
+    // restriction of the coarse cells under the tile
+    for (int k = threadIdx.x; k < (FT_W / 2) * (TH / 2); k += FT_THREADS) {
+        const int I = i0 / 2 + k % (FT_W / 2), J = j0 / 2 + k / (FT_W / 2);
+        if (I >= C.nx || J >= C.ny) continue;
+        T acc = T(0);
+        for (int fy0 = 2 * J - 1; fy0 <= 2 * J + 2; ++fy0) {
+            const int fy = mg_dom(fy0, F.ny, p.per_y);
+            if (fy < 0) continue;
+            const T wy = (T)mg_pwq(fy, J, C.ny, p.per_y, p.bc[1], p.bc[3]) * T(0.25);
+            const int rowq = (fy0 - (j0 - H)) * W - (i0 - H);
+            T rs = T(0);
+            for (int fx0 = 2 * I - 1; fx0 <= 2 * I + 2; ++fx0) {
+                const int fx = mg_dom(fx0, F.nx, p.per_x);
+                if (fx < 0) continue;
+                const T wx = (T)mg_pwq(fx, I, C.nx, p.per_x, p.bc[0], p.bc[2]) * T(0.25);
+                rs = mg_fma(wx, bs[rowq + fx0], rs);
+            }
+            acc = mg_fma(wy, rs, acc);
+        }
+        C.b[(size_t)J * C.pitch + I] = T(0.25) * acc;
+    }
+}
+
+template <typename T, int TH>
+__global__ void __launch_bounds__(FT_THREADS) k_mg_post(MgLev<T> C, MgLev<T> F, MgBc p, SolverState* S, int inner) {
+    if (!block_live(S, inner)) return;
+    constexpr int H = 4, W = FT_W + 2 * H, HT = TH + 2 * H;
+    __shared__ T xs[W * HT];
+    __shared__ T bs[W * HT];
+    const int i0 = blockIdx.x * FT_W, j0 = blockIdx.y * TH;
+    ft_load<T, TH, H>(F, p, xs, bs, i0, j0, F.r);
+    // x += P x_coarse on every cell of the array inside the domain
+    for (int q = threadIdx.x; q < W * HT; q += FT_THREADS) {
+        const int fx = mg_dom(i0 - H + q % W, F.nx, p.per_x), fy = mg_dom(j0 - H + q / W, F.ny, p.per_y);
+        if (fx < 0 || fy < 0) continue;
+        int I, NI, J, NJ;
+        T wxI, wxN, wyJ, wyN;
+        mg_axis<T>(fx, C.nx, p.per_x, p.bc[0], p.bc[2], I, NI, wxI, wxN);
+        mg_axis<T>(fy, C.ny, p.per_y, p.bc[1], p.bc[3], J, NJ, wyJ, wyN);
+        T row0 = wxI * C.x[(size_t)J * C.pitch + I];
+        if (NI >= 0) row0 = mg_fma(wxN, C.x[(size_t)J * C.pitch + NI], row0);
+        T v = wyJ * row0;
+        if (NJ >= 0) {
+            T row1 = wxI * C.x[(size_t)NJ * C.pitch + I];
+            if (NI >= 0) row1 = mg_fma(wxN, C.x[(size_t)NJ * C.pitch + NI], row1);
+            v = mg_fma(wyN, row1, v);
+        }
+        xs[q] = xs[q] + v;
+    }
+    __syncthreads();
+    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 1, 3, false);
+    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 0, 2, false);
+    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 1, 1, false);
+    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 0, 0, false);
+    for (int k = threadIdx.x; k < FT_W * TH; k += FT_THREADS) {
+        const int gi = i0 + k % FT_W, gj = j0 + k / FT_W;
+        if (gi < F.nx && gj < F.ny) F.x[(size_t)gj * F.pitch + gi] = xs[(gj - (j0 - H)) * W + (gi - (i0 - H))];
+    }
+}
+
+// tile heights: FP64 tiles are lower to keep both arrays in 48 KB of shared memory
+template <typename T>
+struct FtRows {
+    static constexpr int value = 32;
+};
+template <>
+struct FtRows<double> {
+    static constexpr int value = 24;
+};
+
+// ---------------------------------------------------------------------------
+// Bottom of the V-cycle in one CTA: every level with at most MG_BOTTOM_MAX
+// cells, from the restricted right-hand side of the first of them down to the
+// coarsest and back, in shared memory.  The per-cell arithmetic is the same as
+// in the grid kernels above (same formulas and order), so the result is the
+// same as that of the level-by-level launches; each phase ends at a barrier.
+constexpr int MG_BOTTOM_MAX = 4096;
+constexpr int MG_BOTTOM_LEVELS = 6;
+constexpr int MG_BOTTOM_THREADS = 1024;
+
+template <typename T>
+struct MgBottom {
+    MgLev<T> lev[MG_BOTTOM_LEVELS];  // lev[0]: b read from and x written to global memory
+    int off[MG_BOTTOM_LEVELS];       // shared-memory offsets (elements) of x, b, r: off, off + n, off + 2n
+    int nlev;
+};
+
+template <typename T>
+__device__ __forceinline__ T gs_cell(const MgBc& p, const T* x, int nx, int ny, int gi, int gj, T bval, T scale,
+                                     const T* invd, bool first) {
+    T s;
+    if (first) {
+        s = T(0);
+    } else {
+        s = mg_at(p, x, nx, nx, ny, gi - 1, gj) + mg_at(p, x, nx, nx, ny, gi + 1, gj);
+        s = s + mg_at(p, x, nx, nx, ny, gi, gj - 1);
+        s = s + mg_at(p, x, nx, nx, ny, gi, gj + 1);
+    }
+    T t = mg_fma(scale, s, bval);
+    return t * invd[mg_bits(p, nx, ny, gi, gj)];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(MgBottom<T> P, MgBc p, SolverState* S, int inner) {
+    if (!block_live(S, inner)) return;
+    extern __shared__ __align__(16) unsigned char mg_smem[];
+    T* sm = reinterpret_cast<T*>(mg_smem);
+    const int tid = threadIdx.x, nt = blockDim.x;
+    auto X = [&](int l) { return sm + P.off[l]; };
+    auto B = [&](int l) { return sm + P.off[l] + P.lev[l].nx * P.lev[l].ny; };
+    auto R = [&](int l) { return sm + P.off[l] + 2 * P.lev[l].nx * P.lev[l].ny; };
+    {
+        const MgLev<T>& G = P.lev[0];
+        T* b = B(0);
+        for (int k = tid; k < G.nx * G.ny; k += nt) b[k] = G.b[(size_t)(k / G.nx) * G.pitch + (k % G.nx)];
+    }
+    __syncthreads();
+    auto half = [&](int l, int color, bool first) {
+        const MgLev<T>& L = P.lev[l];
+        T* x = X(l);
+        const T* b = B(l);
+        const int pairs = (L.nx + 1) / 2;
+        for (int k = tid; k < pairs * L.ny; k += nt) {
+            const int gj = k / pairs, pr = k % pairs;
+            const int par = (gj + color) & 1;
+            const int gi = 2 * pr + par, go = 2 * pr + 1 - par;
+            if (gi < L.nx) x[gj * L.nx + gi] = gs_cell(p, x, L.nx, L.ny, gi, gj, b[gj * L.nx + gi], L.scale, L.invd, first);
+            if (first && go < L.nx) x[gj * L.nx + go] = T(0);
         }
         __syncthreads();
     };
-    for (int s = 0; s < MG_NC; ++s) {
-        half(0);
-        half(1);
+    auto residual = [&](int l) {
+        const MgLev<T>& L = P.lev[l];
+        const T* x = X(l);
+        const T* b = B(l);
+        T* r = R(l);
+        for (int k = tid; k < L.nx * L.ny; k += nt) {
+            const int gi = k % L.nx, gj = k / L.nx;
+            T ax = L.diag[mg_bits(p, L.nx, L.ny, gi, gj)] * x[k];
+            ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi - 1, gj), ax);
+            ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi + 1, gj), ax);
+            ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi, gj - 1), ax);
+            ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi, gj + 1), ax);
+            r[k] = b[k] - ax;
+        }
+        __syncthreads();
+    };
+    auto restrict_to = [&](int l) {
+        const MgLev<T>& F = P.lev[l];
+        const MgLev<T>& C = P.lev[l + 1];
+        const T* fr = R(l);
+        T* cb = B(l + 1);
+        for (int k = tid; k < C.nx * C.ny; k += nt) {
+            const int I = k % C.nx, J = k / C.nx;
+            T acc = T(0);
+            for (int fy0 = 2 * J - 1; fy0 <= 2 * J + 2; ++fy0) {
+                int fy = fy0;
+                if (fy < 0 || fy >= F.ny) {
+                    if (!p.per_y) continue;
+                    fy = fy < 0 ? fy + F.ny : fy - F.ny;
+                }
+                const T wy = (T)mg_pwq(fy, J, C.ny, p.per_y, p.bc[1], p.bc[3]) * T(0.25);
+                T rs = T(0);
+                for (int fx0 = 2 * I - 1; fx0 <= 2 * I + 2; ++fx0) {
+                    int fx = fx0;
+                    if (fx < 0 || fx >= F.nx) {
+                        if (!p.per_x) continue;
+                        fx = fx < 0 ? fx + F.nx : fx - F.nx;
+                    }
+                    const T wx = (T)mg_pwq(fx, I, C.nx, p.per_x, p.bc[0], p.bc[2]) * T(0.25);
+                    rs = mg_fma(wx, fr[fy * F.nx + fx], rs);
+                }
+                acc = mg_fma(wy, rs, acc);
+            }
+            cb[k] = T(0.25) * acc;
+        }
+        __syncthreads();
+    };
+    auto prolong_from = [&](int l) {  // x_l += P x_{l+1}
+        const MgLev<T>& F = P.lev[l];
+        const MgLev<T>& C = P.lev[l + 1];
+        const T* cx = X(l + 1);
+        T* fx_ = X(l);
+        for (int k = tid; k < F.nx * F.ny; k += nt) {
+            const int fx = k % F.nx, fy = k / F.nx;
+            int I, NI, J, NJ;
+            T wxI, wxN, wyJ, wyN;
+            mg_axis<T>(fx, C.nx, p.per_x, p.bc[0], p.bc[2], I, NI, wxI, wxN);
+            mg_axis<T>(fy, C.ny, p.per_y, p.bc[1], p.bc[3], J, NJ, wyJ, wyN);
+            T row0 = wxI * cx[J * C.nx + I];
+            if (NI >= 0) row0 = mg_fma(wxN, cx[J * C.nx + NI], row0);
+            T v = wyJ * row0;
+            if (NJ >= 0) {
+                T row1 = wxI * cx[NJ * C.nx + I];
+                if (NI >= 0) row1 = mg_fma(wxN, cx[NJ * C.nx + NI], row1);
+                v = mg_fma(wyN, row1, v);
+            }
+            fx_[k] = fx_[k] + v;
+        }
+        __syncthreads();
+    };
+    const int nb = P.nlev;
+    for (int l = 0; l < nb - 1; ++l) {
+        for (int k = 0; k < MG_NU; ++k) {
+            half(l, 0, k == 0);
+            half(l, 1, false);
+        }
+        residual(l);
+        restrict_to(l);
     }
-    for (int s = 0; s < MG_NC; ++s) {
-        half(1);
-        half(0);
+    for (int k = 0; k < MG_NC; ++k) {
+        half(nb - 1, 0, k == 0);
+        half(nb - 1, 1, false);
     }
-    for (int k = threadIdx.x; k < n; k += blockDim.x) L.x[(size_t)(k / L.nx) * L.pitch + (k % L.nx)] = xs[k];
+    for (int k = 0; k < MG_NC; ++k) {
+        half(nb - 1, 1, false);
+        half(nb - 1, 0, false);
+    }
+    for (int l = nb - 2; l >= 0; --l) {
+        prolong_from(l);
+        for (int k = 0; k < MG_NU; ++k) {
+            half(l, 1, false);
+            half(l, 0, false);
+        }
+    }
+    {
+        const MgLev<T>& G = P.lev[0];
+        const T* x = X(0);
+        for (int k = tid; k < G.nx * G.ny; k += nt) G.x[(size_t)(k / G.nx) * G.pitch + (k % G.nx)] = x[k];
+    }
 }
 
 // --------------------------------------------------------------------------
@@ -309,8 +602,25 @@ static void level_tables(const cf_ctx* c, double scale, MgLev<T>& L) {
     L.ms = (T)(-1.0 * scale);
 }
 
+// first level handled by the one-CTA bottom solver (nlev when none is small
+// enough) and the bytes of shared memory it needs
+template <typename T>
+static int bottom_level(const MgLev<T>* lev, int nlev, size_t* smem) {
+    int lb = nlev;
+    for (int l = 0; l < nlev; ++l)
+        if ((long long)lev[l].nx * lev[l].ny <= MG_BOTTOM_MAX && nlev - l <= MG_BOTTOM_LEVELS) {
+            lb = l;
+            break;
+        }
+    size_t n = 0;
+    for (int l = lb; l < nlev; ++l) n += 3 * (size_t)lev[l].nx * lev[l].ny;
+    *smem = n * sizeof(T);
+    return lb;
+}
+
 struct MgHierarchy {
     int nlev = 0;
+    int fused = 1;
     MgLev<double> d[16];
     MgLev<float> f[16];
     double* z64 = nullptr;
@@ -345,6 +655,10 @@ int mg_setup(cf_ctx* c) {
     if (rc) return rc;
     MgHierarchy* H = new MgHierarchy();
     c->mg = H;
+    // FP32 levels are bound by memory traffic: fused; FP64 levels by the FP64
+    // pipe, where the fused tiles' halo recomputation costs more than it saves
+    H->fused = mixed ? 1 : 0;
+    if (const char* e = getenv("CF_MG_FUSED")) H->fused = atoi(e) != 0;
     int nx = c->ph.nx, ny = c->ph.ny;
     for (int l = 0; l < 16 && !rc; ++l) {
         if (l == 0) {
@@ -372,6 +686,18 @@ int mg_setup(cf_ctx* c) {
         nx /= 2;
         ny /= 2;
     }
+    if (!rc) {
+        size_t smem = 0;
+        if (mixed)
+            bottom_level(H->f, H->nlev, &smem);
+        else
+            bottom_level(H->d, H->nlev, &smem);
+        cudaError_t e = mixed ? cudaFuncSetAttribute(k_mg_bottom<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)smem)
+                              : cudaFuncSetAttribute(k_mg_bottom<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)smem);
+        rc = cuda_check(c, e, "multigrid bottom solver shared memory");
+    }
     return rc;
 }
 
@@ -385,8 +711,12 @@ void mg_free(cf_ctx* c) {
 
 double* mg_z64(cf_ctx* c) { return static_cast<MgHierarchy*>(c->mg)->z64; }
 
+// fused = 1: levels above the bottom solver run the fused pre/post kernels;
+// 0: one launch per half sweep, residual, restriction and prolongation (the
+// same arithmetic).  Default: fused for FP32, level by level for FP64;
+// CF_MG_FUSED=0/1 in the environment overrides it.
 template <typename T>
-static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner) {
+static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, int fused) {
     MgBc p{c->ph.per_x, c->ph.per_y, {c->ph.bc[0], c->ph.bc[1], c->ph.bc[2], c->ph.bc[3]}};
     double s = scale0;
     for (int l = 0; l < nlev; ++l) {
@@ -402,7 +732,17 @@ static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner) 
         k_mg_smooth<T><<<grid2((L.nx + 1) / 2, L.ny), blk, 0, c->stream>>>(L, p, color, first, c->S, inner);
         ++launches;
     };
-    for (int l = 0; l < nlev - 1; ++l) {
+    size_t smem = 0;
+    const int lb = bottom_level(lev, nlev, &smem);
+    const int top_end = lb < nlev ? lb : nlev - 1;  // levels smoothed by grid kernels on the way down
+    constexpr int TH = FtRows<T>::value;
+    auto tiles = [&](const MgLev<T>& L) { return dim3((L.nx + FT_W - 1) / FT_W, (L.ny + TH - 1) / TH); };
+    for (int l = 0; l < top_end; ++l) {
+        if (fused) {
+            k_mg_pre<T, TH><<<tiles(lev[l]), FT_THREADS, 0, c->stream>>>(lev[l], lev[l + 1], p, c->S, inner);
+            ++launches;
+            continue;
+        }
         for (int k = 0; k < MG_NU; ++k) {
             smooth(l, 0, k == 0);
             smooth(l, 1, 0);
@@ -412,11 +752,19 @@ static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner) 
                                                                                       inner);
         launches += 2;
     }
-    const MgLev<T>& Lc = lev[nlev - 1];
-    if (Lc.nx * Lc.ny <= MG_COARSE_MAX) {
-        k_mg_coarse<T><<<1, 256, 0, c->stream>>>(Lc, p, c->S, inner);
+    if (lb < nlev) {
+        MgBottom<T> P{};
+        P.nlev = nlev - lb;
+        int off = 0;
+        for (int l = 0; l < P.nlev; ++l) {
+            P.lev[l] = lev[lb + l];
+            P.off[l] = off;
+            off += 3 * lev[lb + l].nx * lev[lb + l].ny;
+        }
+        k_mg_bottom<T><<<1, MG_BOTTOM_THREADS, smem, c->stream>>>(P, p, c->S, inner);
         ++launches;
     } else {
+        // coarsest level too large for one CTA: sweeps by grid kernels
         for (int k = 0; k < MG_NC; ++k) {
             smooth(nlev - 1, 0, k == 0);
             smooth(nlev - 1, 1, 0);
@@ -426,7 +774,12 @@ static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner) 
             smooth(nlev - 1, 0, 0);
         }
     }
-    for (int l = nlev - 2; l >= 0; --l) {
+    for (int l = top_end - 1; l >= 0; --l) {
+        if (fused) {
+            k_mg_post<T, TH><<<tiles(lev[l]), FT_THREADS, 0, c->stream>>>(lev[l + 1], lev[l], p, c->S, inner);
+            ++launches;
+            continue;
+        }
         k_mg_prolong<T><<<grid2(lev[l].nx, lev[l].ny), blk, 0, c->stream>>>(lev[l + 1], lev[l], p, c->S, inner);
         ++launches;
         for (int k = 0; k < MG_NU; ++k) {
@@ -442,8 +795,8 @@ static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner) 
 // returns at once when the solve has stopped.
 int mg_vcycle(cf_ctx* c, double scale0) {
     MgHierarchy* H = static_cast<MgHierarchy*>(c->mg);
-    if (c->precision == CF_PREC_MIXED) return vcycle<float>(c, H->f, H->nlev, scale0, 1);
-    return vcycle<double>(c, H->d, H->nlev, scale0, 0);
+    if (c->precision == CF_PREC_MIXED) return vcycle<float>(c, H->f, H->nlev, scale0, 1, H->fused);
+    return vcycle<double>(c, H->d, H->nlev, scale0, 0, H->fused);
 }
 
 int mg_levels(const cf_ctx* c) { return c->mg ? static_cast<const MgHierarchy*>(c->mg)->nlev : 0; }

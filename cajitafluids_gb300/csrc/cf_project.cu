@@ -429,6 +429,7 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
             if (S->use_abs) S->target2 = fmax(S->target2, S->abs2 / S->area);
             S->tau2 = S->inner_tol2;
             S->restart = 1;
+            S->refreshed = 1;
             if (bb == 0.0 || converged(S, bb))
                 S->status = ST_CONVERGED;
             else if (isnan(bb))
@@ -442,8 +443,22 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
     }
 }
 
-// Outer refinement, part 1: x += e (FP64 += FP32)
-__global__ void k_outer_add(double* x, const float* e, int nx, int ny, int pitch, int pitch32) {
+// true while the outer refinement is due: the solve runs and the inner
+// iteration has stopped (read once per block)
+__device__ __forceinline__ bool outer_due(const SolverState* S) {
+    __shared__ int due;
+    if (threadIdx.x == 0 && threadIdx.y == 0)
+        due = *(volatile const int*)&S->status == ST_RUNNING &&
+              *(volatile const int*)&S->inner_status != ST_RUNNING;
+    __syncthreads();
+    return due != 0;
+}
+
+// Outer refinement, part 1: x += e (FP64 += FP32).  gated = 1 (inside the
+// MG-PCG graph): only while the refinement is due.
+__global__ void k_outer_add(double* x, const float* e, int nx, int ny, int pitch, int pitch32, const SolverState* S,
+                            int gated) {
+    if (gated && !outer_due(S)) return;
     int gi = blockIdx.x * blockDim.x + threadIdx.x;
     int gj = blockIdx.y * blockDim.y + threadIdx.y;
     if (gi >= nx || gj >= ny) return;
@@ -459,6 +474,7 @@ struct Outer {
     float *r32, *e32;
     double *part0, *part1, *part2;
     SolverState* S;
+    int gated;  // inside the MG-PCG graph: run only while the refinement is due
 };
 
 __device__ __forceinline__ double xval(const Outer& a, int c, int j) {
@@ -469,6 +485,7 @@ __device__ __forceinline__ double xval(const Outer& a, int c, int j) {
 
 __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
     SolverState* S = a.S;
+    if (a.gated && !outer_due(S)) return;
     const int lane = threadIdx.x & 31;
     const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
     double arr64 = 0.0;
@@ -534,6 +551,7 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
                 S->rho_in = rz;
                 S->rr_in0 = rr;
                 S->rr_in = rr;
+                S->refreshed = 1;
                 S->inner_status = ST_RUNNING;
             }
         }
@@ -686,6 +704,37 @@ static Cg64 cg64_args(cf_ctx* c, const Stencil& st) {
 
 static int red_blocks(const cf_ctx* c) { return (c->n_units + CF_RED_WARPS - 1) / CF_RED_WARPS; }
 
+static Outer outer_args(cf_ctx* c, const Stencil& st, int gated) {
+    Outer oa{};
+    oa.nx = c->ph.nx;
+    oa.ny = c->ph.ny;
+    oa.per_x = c->ph.per_x;
+    oa.per_y = c->ph.per_y;
+    oa.G = c->G;
+    oa.U = c->n_units;
+    oa.pitch = c->vpitch;
+    oa.pitch32 = c->p32;
+    oa.st = st;
+    oa.x = c->x.a;
+    oa.b = c->b.a;
+    oa.r32 = c->r32.a;
+    oa.e32 = c->e32.a;
+    oa.part0 = c->partials;
+    oa.part1 = c->partials + c->n_units;
+    oa.part2 = c->partials + 2 * c->n_units;
+    oa.S = c->S;
+    oa.gated = gated;
+    return oa;
+}
+
+// the two outer-refinement kernels; gated = 1 inside the MG-PCG graph
+static void launch_outer(cf_ctx* c, const Stencil& st, int gated) {
+    Outer oa = outer_args(c, st, gated);
+    dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
+    k_outer_add<<<grd, blk, 0, c->stream>>>(c->x.a, c->e32.a, c->ph.nx, c->ph.ny, c->vpitch, c->p32, c->S, gated);
+    k_outer_resid<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(oa);
+}
+
 static const int kBatch = CF_CG_BATCH;  // CG iterations per graph launch
 static const int kBatchMG = 4;          // MG-PCG iterations per graph launch
 
@@ -753,7 +802,9 @@ static int ensure_graph_mg(cf_ctx* c, const Stencil& st) {
     int rc = capture(c, &c->gmg, [&] {
         for (int i = 0; i < kBatchMG; ++i) {
             if (mixed) {
-                per = cg32_launch_iteration_mg(c, st, scale);
+                cg32_launch_pair_mg(c, st);
+                launch_outer(c, st, 1);
+                per = 4 + cg32_mg_precondition(c, scale);
             } else {
                 k_cg_dir_matvec64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
                 k_cg_update64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
@@ -765,7 +816,7 @@ static int ensure_graph_mg(cf_ctx* c, const Stencil& st) {
     if (!rc)
         rc = capture(c, &c->gmg_pre, [&] {
             if (mixed) {
-                pre = cg32_mg_precondition(c, scale, 1);
+                pre = cg32_mg_precondition(c, scale);
             } else {
                 pre = 1 + mg_vcycle(c, scale);
                 k_mg_rz64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a, 1);
@@ -867,55 +918,45 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     } else {
         k_div_init_mixed<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
         c->launches += 1;
-        const int batch = mg ? kBatchMG : kBatch;
-        cudaGraphExec_t ge = mg ? c->gmg : c->g32;
-        const int per_batch = mg ? c->gmg_per_iter * kBatchMG : 2 * kBatch;
-        auto precondition = [&]() -> int {
-            if (!mg) return CF_OK;
+        if (mg) {
+            // MG-PCG: the reliable updates run inside the graph (gated
+            // kernels), so the host only polls the status between batches
+            if ((rc = cuda_check(c, cudaGraphLaunch(c->gmg_pre, c->stream), "graph launch"))) return rc;
             c->launches += c->gmg_pre_launches;
-            return cuda_check(c, cudaGraphLaunch(c->gmg_pre, c->stream), "graph launch");
-        };
-        if ((rc = precondition())) return rc;
-        if ((rc = read_state(c))) return rc;
-        Outer oa{};
-        oa.nx = c->ph.nx;
-        oa.ny = c->ph.ny;
-        oa.per_x = c->ph.per_x;
-        oa.per_y = c->ph.per_y;
-        oa.G = c->G;
-        oa.U = c->n_units;
-        oa.pitch = c->vpitch;
-        oa.pitch32 = c->p32;
-        oa.st = st;
-        oa.x = c->x.a;
-        oa.b = c->b.a;
-        oa.r32 = c->r32.a;
-        oa.e32 = c->e32.a;
-        oa.part0 = c->partials;
-        oa.part1 = c->partials + c->n_units;
-        oa.part2 = c->partials + 2 * c->n_units;
-        oa.S = c->S;
-        dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
-        int max_launch = o.max_iter / batch + 3 * (o.max_outer + 1);
-        int launches = 0;
-        while (c->hS->status == ST_RUNNING) {
-            while (c->hS->status == ST_RUNNING && c->hS->inner_status == ST_RUNNING) {
-                if (++launches > max_launch) return fail(c, CF_ERR_NUMERIC, "mixed solver did not stop");
-                int prev_iter = c->hS->iter;
-                if (c->prof) cudaEventRecord(c->ev[0], c->stream);
-                if ((rc = cuda_check(c, cudaGraphLaunch(ge, c->stream), "graph launch"))) return rc;
-                if (c->prof) cudaEventRecord(c->ev[1], c->stream);
-                c->launches += per_batch;
+            int max_launch = (o.max_iter + o.max_outer) / kBatchMG + 3;
+            int prev_iter = 0;
+            for (int l = 0;; ++l) {
                 if ((rc = read_state(c))) return rc;
-                batch_profile(c, c->hS->iter - prev_iter, batch);
+                if (l > 0) batch_profile(c, c->hS->iter - prev_iter, kBatchMG);
+                prev_iter = c->hS->iter;
+                if (c->hS->status != ST_RUNNING) break;
+                if (l >= max_launch) return fail(c, CF_ERR_NUMERIC, "mixed MG solver did not stop");
+                if (c->prof) cudaEventRecord(c->ev[0], c->stream);
+                if ((rc = cuda_check(c, cudaGraphLaunch(c->gmg, c->stream), "graph launch"))) return rc;
+                if (c->prof) cudaEventRecord(c->ev[1], c->stream);
+                c->launches += c->gmg_per_iter * kBatchMG;
             }
-            if (c->hS->status != ST_RUNNING) break;
-            k_outer_add<<<grd, blk, 0, c->stream>>>(c->x.a, c->e32.a, c->ph.nx, c->ph.ny, c->vpitch, c->p32);
-            k_outer_resid<<<nb, CF_RED_THREADS, 0, c->stream>>>(oa);
-            c->launches += 2;
-            if ((rc = precondition())) return rc;
+        } else {
             if ((rc = read_state(c))) return rc;
-            if (++launches > max_launch) return fail(c, CF_ERR_NUMERIC, "mixed solver did not stop");
+            int max_launch = o.max_iter / kBatch + 3 * (o.max_outer + 1);
+            int launches = 0;
+            while (c->hS->status == ST_RUNNING) {
+                while (c->hS->status == ST_RUNNING && c->hS->inner_status == ST_RUNNING) {
+                    if (++launches > max_launch) return fail(c, CF_ERR_NUMERIC, "mixed solver did not stop");
+                    int prev_iter = c->hS->iter;
+                    if (c->prof) cudaEventRecord(c->ev[0], c->stream);
+                    if ((rc = cuda_check(c, cudaGraphLaunch(c->g32, c->stream), "graph launch"))) return rc;
+                    if (c->prof) cudaEventRecord(c->ev[1], c->stream);
+                    c->launches += 2 * kBatch;
+                    if ((rc = read_state(c))) return rc;
+                    batch_profile(c, c->hS->iter - prev_iter);
+                }
+                if (c->hS->status != ST_RUNNING) break;
+                launch_outer(c, st, 0);
+                c->launches += 2;
+                if ((rc = read_state(c))) return rc;
+                if (++launches > max_launch) return fail(c, CF_ERR_NUMERIC, "mixed solver did not stop");
+            }
         }
     }
     const SolverState* hs = c->hS;

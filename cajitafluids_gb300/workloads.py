@@ -43,6 +43,7 @@ class Workload:
     tol: float = 1e-8
     abs_tol: float = 0.0
     max_iter: int = 100000
+    precon: str = "Diagonal"                # PCG preconditioner name (PFMG/SMG/MG: multigrid)
     steps: int = 1
     q0: Optional[np.ndarray] = None
     u0: Optional[np.ndarray] = None

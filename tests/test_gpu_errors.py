@@ -41,7 +41,7 @@ def test_invalid_arguments(built):
     assert c.download("u").sum() == 72.0
 
 
-@pytest.mark.parametrize("solver,precon", [("GMRES", "Diagonal"), ("PCG", "PFMG"), ("PCG", "SMG"),
+@pytest.mark.parametrize("solver,precon", [("GMRES", "Diagonal"), ("PCG", "Euclid"), ("PCG", "ParaSails"),
                                             ("BiCGSTAB", "None")])
 def test_unsupported_solvers(built, solver, precon):
     c = Context(16, 16)

@@ -18,8 +18,9 @@ pytestmark = pytest.mark.gpu
 
 INFLOW = ((0.45, 0.10), (0.10, 0.05), (0.0, 3.0), 1.0)
 
-# (nx, ny, periodic, bc): power-of-two, ragged, single-level odd, a coarsest
-# level too large for the one-CTA coarse solver, periodic in one and both axes
+# (nx, ny, periodic, bc): power-of-two, ragged, single-level odd, periodic in
+# one and both axes, coarsest levels too large for the one-CTA bottom solver
+# (65^2 and 130^2 -> 65^2), and a deep hierarchy (512^2 -> 8^2)
 CASES = [
     (64, 64, (False, False), (0, 0, 0, 0)),
     (48, 40, (False, False), (0, 1, 1, 0)),
@@ -28,11 +29,18 @@ CASES = [
     (64, 32, (True, True), (0, 0, 0, 0)),
     (72, 36, (True, False), (0, 0, 0, 0)),
     (256, 128, (False, False), (0, 0, 0, 0)),
+    (65, 65, (False, False), (0, 0, 0, 0)),
+    (130, 130, (False, False), (0, 1, 0, 0)),
+    (512, 512, (True, True), (0, 0, 0, 0)),
 ]
 
 
+@pytest.mark.parametrize("fused", ["1", "0"])
 @pytest.mark.parametrize("nx,ny,periodic,bc", CASES)
-def test_project_mg_bitwise(built, nx, ny, periodic, bc):
+def test_project_mg_bitwise(built, monkeypatch, nx, ny, periodic, bc, fused):
+    """Both forms of the levels above the one-CTA bottom solver: the fused
+    pre/post kernels (default) and one launch per half sweep (CF_MG_FUSED=0)."""
+    monkeypatch.setenv("CF_MG_FUSED", fused)
     rng = np.random.default_rng(nx * 3 + ny)
     o, c = make_pair(nx, ny, periodic=periodic, bc=bc, precon_mg=True)
     load_state(o, c, random_state(o, rng))
