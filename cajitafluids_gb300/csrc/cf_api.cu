@@ -261,6 +261,10 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
         if (!rc) rc = alloc_grid(c, c->u[s], nx + 2 * CF_HALO + 1, ny + 2 * CF_HALO);
         if (!rc) rc = alloc_grid(c, c->v[s], nx + 2 * CF_HALO, ny + 2 * CF_HALO + 1);
     }
+    if (!rc && c->precision == CF_PREC_MIXED) {
+        rc = alloc_grid(c, c->u32, nx + 2 * CF_HALO + 1, ny + 2 * CF_HALO);
+        if (!rc) rc = alloc_grid(c, c->v32, nx + 2 * CF_HALO, ny + 2 * CF_HALO + 1);
+    }
     c->vpitch = (int)round_up(nx, 32);
     size_t vn = (size_t)c->vpitch * ny;
     if (!rc) rc = alloc_dev(c, c->x.a, vn);
@@ -357,6 +361,24 @@ int cf_set_source(cf_ctx* ctx, const double location[2], const double size[2], c
     p.src_vel[1] = velocity[1];
     p.src_q = quantity;
     p.src_mode = mode;
+    // index ranges of the box test x0 <= x < x1 on each entity's coordinates,
+    // x = gl + (idx + offset) dx exactly as the kernels evaluate it
+    static const double off[3][2] = {{0.5, 0.5}, {0.0, 0.5}, {0.5, 0.0}};
+    for (int e = 0; e < 3; ++e)
+        for (int a = 0; a < 2; ++a) {
+            const int n = (a == 0 ? p.nx : p.ny) + 2 * CF_HALO + 1;
+            int lo = 0, hi = 0;
+            for (int idx = 0; idx < n; ++idx) {
+                double t = (double)idx + off[e][a];
+                double x = p.gl[a] + t * p.dx;
+                if (x >= p.bbox[a] && x < p.bbox[a + 2]) {
+                    if (hi == 0) lo = idx;
+                    hi = idx + 1;
+                }
+            }
+            p.box[e][2 * a] = lo;
+            p.box[e][2 * a + 1] = hi;
+        }
     return CF_OK;
 }
 

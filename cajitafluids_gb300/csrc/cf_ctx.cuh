@@ -18,6 +18,7 @@ struct cf_ctx {
     // fields, two versions each (src/ProblemManager.hpp:143-165); index cur is Current
     cf::Grid<double> q64[2]{}, u[2]{}, v[2]{};
     cf::Grid<float> q32[2]{};
+    cf::Grid<float> u32{}, v32{};  // mixed: FP32 copies of the current u, v (ghosts included) for advection
     int cur = 0;
 
     // solver vectors (owned cells)

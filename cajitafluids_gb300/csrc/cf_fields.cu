@@ -196,15 +196,32 @@ __global__ void __launch_bounds__(256) k_advect64(Adv64 a) {
 // FP32 advection (mixed precision).  Positions are kept as an integer base
 // (the entity's local index) plus a small FP32 displacement in cell units,
 // so FP32 keeps full relative precision at any grid size.  u and v are
-// stored in FP64 (the projection works on them in FP64); q is FP32.
+// stored in FP64 (the projection works on them in FP64) and read here from
+// FP32 copies made once per step (k_to32), so no sample converts; q is FP32.
+// The inputs epilogue tests the inflow box on integer index ranges that the
+// host evaluated with the FP64 coordinate test, and works in FP64 only where
+// the FP64 result needs it (inside the box, a non-zero body force).
 struct Adv32 {
     Phys p;
     Grid<float> q, qn;
-    Grid<double> u, v, un, vn;
+    Grid<float> u, v;  // FP32 copies of the current velocities
+    Grid<double> un, vn;
     float c;      // dt / dx
     double dt;
     int fuse;
 };
+
+// FP32 copy of a ghosted FP64 array (ghosts included)
+__global__ void k_to32(Grid<double> src, Grid<float> dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= src.ex || j >= src.ey) return;
+    dst.at(i, j) = (float)src.at(i, j);
+}
+
+__device__ __forceinline__ bool in_box_idx(const Phys& p, int ent, int li, int lj) {
+    return li >= p.box[ent][0] && li < p.box[ent][1] && lj >= p.box[ent][2] && lj < p.box[ent][3];
+}
 
 template <typename T>
 __device__ __forceinline__ float lin32(const Grid<T>& g, int bi, int bj, float fx, float fy) {
@@ -290,19 +307,32 @@ __global__ void __launch_bounds__(256) k_advect32(Adv32 a) {
         val = ORDER == 1 ? lin32(a.u, li, lj, dx, dy) : cub32(a.u, li, lj, dx, dy);
     else
         val = ORDER == 1 ? lin32(a.v, li, lj, dx, dy) : cub32(a.v, li, lj, dx, dy);
+    if (ent == E_CELL) {
+        // cell inputs (src/Solver.hpp:181-263): the clamp max(q, Q) rounds to
+        // the same FP32 value when taken in FP32; the rate form in FP64
+        if (a.fuse && in_box_idx(p, E_CELL, li, lj)) {
+            if (p.src_mode == 0) {
+                const float qf = (float)p.src_q;
+                if (val < qf) val = qf;
+            } else {
+                val = (float)fma(p.src_q, a.dt, (double)val);
+            }
+        }
+        a.qn.at(li, lj) = val;
+        return;
+    }
+    const int axis = ent == E_FACEI ? 0 : 1;
     double w = (double)val;
     if (a.fuse) {
-        double x0 = entity_coord(p, ent, 0, li), y0 = entity_coord(p, ent, 1, lj);
-        if (ent == E_CELL)
-            w = inputs_cell(p, w, x0, y0, a.dt);
-        else if (ent == E_FACEI)
-            w = inputs_face(p, 0, w, x0, y0, a.dt, gi, 0.0);
-        else
-            w = inputs_face(p, 1, w, x0, y0, a.dt, gj, 0.0);
+        if (in_box_idx(p, ent, li, lj) && fabs(w) < fabs(p.src_vel[axis])) w = p.src_vel[axis];
+        if (p.force[axis] != 0.0) w = fma(p.force[axis], a.dt, w);
+        const int per = axis == 0 ? p.per_x : p.per_y, n = axis == 0 ? p.nx : p.ny, g = axis == 0 ? gi : gj;
+        if (!per) {
+            if (g <= 0 && p.bc[axis] == 0) w = 0.0;
+            if (g > n - 1 && p.bc[axis + 2] == 0) w = 0.0;
+        }
     }
-    if (ent == E_CELL)
-        a.qn.at(li, lj) = (float)w;
-    else if (ent == E_FACEI)
+    if (axis == 0)
         a.un.at(li, lj) = w;
     else
         a.vn.at(li, lj) = w;
@@ -443,7 +473,12 @@ cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs) {
         else
             k_advect64<3><<<grd, blk, 0, c->stream>>>(a);
     } else {
-        Adv32 a{p, c->q32[s], c->q32[n], c->u[s], c->v[s], c->u[n], c->v[n], (float)(dt / p.dx), dt, fuse_inputs};
+        // fused inputs with a density-scaled force are applied by the
+        // standalone inputs kernels after the advection
+        Adv32 a{p, c->q32[s], c->q32[n], c->u32, c->v32, c->u[n], c->v[n], (float)(dt / p.dx), dt, fuse_inputs};
+        k_to32<<<grid2(c->u[s].ex, c->u[s].ey, blk), blk, 0, c->stream>>>(c->u[s], c->u32);
+        k_to32<<<grid2(c->v[s].ex, c->v[s].ey, blk), blk, 0, c->stream>>>(c->v[s], c->v32);
+        c->launches += 2;
         if (order == 1)
             k_advect32<1><<<grd, blk, 0, c->stream>>>(a);
         else

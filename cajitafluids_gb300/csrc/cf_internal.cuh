@@ -42,6 +42,10 @@ struct Phys {
     double low[3][2];   // coordinate of local index 0 per entity (spline origin)
     int bc[4];          // left, bottom, right, top
     double bbox[4];     // inflow box x0, y0, x1, y1
+    // per entity (cell, I-face, J-face): local indices [i0, i1) x [j0, j1)
+    // whose coordinates lie in the inflow box (the FP64 test, evaluated once
+    // on the host)
+    int box[3][4];
     double src_q;
     double src_vel[2];
     int src_mode;

@@ -318,6 +318,56 @@ __device__ __forceinline__ void ft_load(const MgLev<T>& L, const MgBc& p, T* xs,
     __syncthreads();
 }
 
+// A tile is interior when its array (tile + halo H) lies in [1, n-1) along
+// both axes: no wrap, no wall, every wall-adjacency bit 0, every transfer
+// weight the interior one.  Those tiles take the index-light paths below.
+template <int TH, int H>
+__device__ __forceinline__ bool ft_interior(int nx, int ny, int i0, int j0) {
+    return i0 - H >= 1 && i0 + FT_W + H <= nx - 1 && j0 - H >= 1 && j0 + TH + H <= ny - 1;
+}
+
+template <typename T, int TH, int H>
+__device__ __forceinline__ void ft_load_int(const MgLev<T>& L, T* xs, T* bs, int i0, int j0, const T* xsrc) {
+    constexpr int W = FT_W + 2 * H, HT = TH + 2 * H;
+    const size_t base = (size_t)(j0 - H) * L.pitch + (i0 - H);
+    for (int q = threadIdx.x; q < W * HT; q += FT_THREADS) {
+        const size_t k = base + (size_t)(q / W) * L.pitch + (q % W);
+        bs[q] = L.b[k];
+        xs[q] = xsrc ? xsrc[k] : T(0);
+    }
+    __syncthreads();
+}
+
+// interior half sweep: warp w takes rows w, w + 8, ...; lane l the cells
+// 2l (+ 64) of the row's colour
+template <typename T, int TH, int H>
+__device__ __forceinline__ void ft_half_int(const MgLev<T>& L, T* xs, const T* bs, int i0, int j0, int c, int h,
+                                            bool first) {
+    constexpr int W = FT_W + 2 * H;
+    const int nrow = TH + 2 * h, hw = FT_W / 2 + h;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const T scale = L.scale, id0 = L.invd[0];
+    for (int rj = warp; rj < nrow; rj += FT_THREADS / 32) {
+        const int gj = j0 - h + rj;
+        const int off = (c + gj + i0 - h) & 1;
+        const int q0 = (rj + H - h) * W + (H - h) + off;
+        for (int pk = lane; pk < hw; pk += 32) {
+            const int q = q0 + 2 * pk;
+            T s;
+            if (first) {
+                s = T(0);
+            } else {
+                s = xs[q - 1] + xs[q + 1];
+                s = s + xs[q - W];
+                s = s + xs[q + W];
+            }
+            T t = mg_fma(scale, s, bs[q]);
+            xs[q] = t * id0;
+        }
+    }
+    __syncthreads();
+}
+
 template <typename T, int TH>
 __global__ void __launch_bounds__(FT_THREADS) k_mg_pre(MgLev<T> F, MgLev<T> C, MgBc p, SolverState* S, int inner) {
     if (!block_live(S, inner)) return;
@@ -325,6 +375,47 @@ __global__ void __launch_bounds__(FT_THREADS) k_mg_pre(MgLev<T> F, MgLev<T> C, M
     __shared__ T xs[W * HT];
     __shared__ T bs[W * HT];  // b, then r in place on the residual ring
     const int i0 = blockIdx.x * FT_W, j0 = blockIdx.y * TH;
+    if (ft_interior<TH, H>(F.nx, F.ny, i0, j0)) {
+        ft_load_int<T, TH, H>(F, xs, bs, i0, j0, nullptr);
+        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 0, 5, true);
+        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 1, 4, false);
+        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 0, 3, false);
+        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 1, 2, false);
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const T d0 = F.diag[0], ms = F.ms;
+        for (int rj = warp; rj < TH + 2; rj += FT_THREADS / 32)
+            for (int ci = lane; ci < FT_W + 2; ci += 32) {
+                const int q = (rj + H - 1) * W + (ci + H - 1);
+                T ax = d0 * xs[q];
+                ax = mg_fma(ms, xs[q - 1], ax);
+                ax = mg_fma(ms, xs[q + 1], ax);
+                ax = mg_fma(ms, xs[q - W], ax);
+                ax = mg_fma(ms, xs[q + W], ax);
+                bs[q] = bs[q] - ax;
+            }
+        __syncthreads();
+        for (int k = threadIdx.x; k < FT_W * TH; k += FT_THREADS) {
+            const int li = k % FT_W, lj = k / FT_W;
+            F.r[(size_t)(j0 + lj) * F.pitch + i0 + li] = xs[(lj + H) * W + li + H];
+        }
+        // restriction with the interior weights 1/4, 3/4, 3/4, 1/4 per axis
+        const T w4[4] = {T(0.25), T(0.75), T(0.75), T(0.25)};
+        for (int k = threadIdx.x; k < (FT_W / 2) * (TH / 2); k += FT_THREADS) {
+            const int ci = k % (FT_W / 2), cj = k / (FT_W / 2);
+            const int qr = (2 * cj - 1 + H) * W + (2 * ci - 1 + H);
+            T acc = T(0);
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const T* row = bs + qr + a * W;
+                T rs = T(0);
+#pragma unroll
+                for (int b = 0; b < 4; ++b) rs = mg_fma(w4[b], row[b], rs);
+                acc = mg_fma(w4[a], rs, acc);
+            }
+            C.b[(size_t)(j0 / 2 + cj) * C.pitch + i0 / 2 + ci] = T(0.25) * acc;
+        }
+        return;
+    }
     ft_load<T, TH, H>(F, p, xs, bs, i0, j0, nullptr);
     ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 0, 5, true);
     ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 1, 4, false);
@@ -379,9 +470,41 @@ template <typename T, int TH>
 __global__ void __launch_bounds__(FT_THREADS) k_mg_post(MgLev<T> C, MgLev<T> F, MgBc p, SolverState* S, int inner) {
     if (!block_live(S, inner)) return;
     constexpr int H = 4, W = FT_W + 2 * H, HT = TH + 2 * H;
+    // coarse cells read by the prolongation of an interior tile's array
+    constexpr int CW = FT_W / 2 + H + 2, CH = TH / 2 + H + 2;
     __shared__ T xs[W * HT];
     __shared__ T bs[W * HT];
+    __shared__ T cs[CW * CH];
     const int i0 = blockIdx.x * FT_W, j0 = blockIdx.y * TH;
+    if (ft_interior<TH, H>(F.nx, F.ny, i0, j0)) {
+        // coarse block from (i0 - H) / 2 - 1, (j0 - H) / 2 - 1
+        const int ci0 = (i0 - H) / 2 - 1, cj0 = (j0 - H) / 2 - 1;
+        for (int q = threadIdx.x; q < CW * CH; q += FT_THREADS)
+            cs[q] = C.x[(size_t)(cj0 + q / CW) * C.pitch + ci0 + q % CW];
+        ft_load_int<T, TH, H>(F, xs, bs, i0, j0, F.r);  // ends with a barrier
+        for (int q = threadIdx.x; q < W * HT; q += FT_THREADS) {
+            const int fx = i0 - H + q % W, fy = j0 - H + q / W;
+            const int I = (fx >> 1) - ci0, NI = I + ((fx & 1) ? 1 : -1);
+            const int J = (fy >> 1) - cj0, NJ = J + ((fy & 1) ? 1 : -1);
+            T row0 = T(0.75) * cs[J * CW + I];
+            row0 = mg_fma(T(0.25), cs[J * CW + NI], row0);
+            T v = T(0.75) * row0;
+            T row1 = T(0.75) * cs[NJ * CW + I];
+            row1 = mg_fma(T(0.25), cs[NJ * CW + NI], row1);
+            v = mg_fma(T(0.25), row1, v);
+            xs[q] = xs[q] + v;
+        }
+        __syncthreads();
+        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 1, 3, false);
+        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 0, 2, false);
+        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 1, 1, false);
+        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 0, 0, false);
+        for (int k = threadIdx.x; k < FT_W * TH; k += FT_THREADS) {
+            const int li = k % FT_W, lj = k / FT_W;
+            F.x[(size_t)(j0 + lj) * F.pitch + i0 + li] = xs[(lj + H) * W + li + H];
+        }
+        return;
+    }
     ft_load<T, TH, H>(F, p, xs, bs, i0, j0, F.r);
     // x += P x_coarse on every cell of the array inside the domain
     for (int q = threadIdx.x; q < W * HT; q += FT_THREADS) {
