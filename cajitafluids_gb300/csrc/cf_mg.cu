@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(MG_BX* MG_BY) k_mg_prolong(MgLev<T> C, MgLev<T
 
 // ---------------------------------------------------------------------------
 // Fused level kernels (temporal blocking in shared memory).  A CTA owns a
-// tile of FT_W x TH fine cells and recomputes a shrinking halo, so that the
+// tile of TW x TH fine cells (both even) and recomputes a shrinking halo, so that the
 // MG_NU = 2 sweep pairs of a level need one pass over memory:
 //   k_mg_pre : x = 4 half sweeps from x = 0 (red, black, red, black),
 //              r = b - A x (in shared memory), b_coarse = R r
@@ -258,7 +258,6 @@ __global__ void __launch_bounds__(MG_BX* MG_BY) k_mg_prolong(MgLev<T> C, MgLev<T
 // k_mg_pre leaves its x in the level's r array (free in this form) and
 // k_mg_post reads it from there and writes x: a CTA of k_mg_post reads its
 // halo from other tiles, which must not be written by the same launch.
-constexpr int FT_W = 64;
 constexpr int FT_THREADS = 256;
 
 // index along an axis after the periodic wrap; -1 beyond a wall
@@ -269,11 +268,11 @@ __device__ __forceinline__ int mg_dom(int g, int n, int per) {
 }
 
 // one half sweep of colour c over the tile grown by h cells; arrays have halo H
-template <typename T, int TH, int H>
+template <typename T, int TW, int TH, int H>
 __device__ __forceinline__ void ft_half(const MgLev<T>& L, const MgBc& p, T* xs, const T* bs, int i0, int j0, int c,
                                         int h, bool first) {
-    constexpr int W = FT_W + 2 * H;
-    const int ncol = FT_W + 2 * h, nrow = TH + 2 * h, hw = ncol / 2;
+    constexpr int W = TW + 2 * H;
+    const int ncol = TW + 2 * h, nrow = TH + 2 * h, hw = ncol / 2;
     const int gi0 = i0 - h;
     for (int k = threadIdx.x; k < hw * nrow; k += FT_THREADS) {
         const int rj = k / hw, pk = k % hw;
@@ -299,10 +298,10 @@ __device__ __forceinline__ void ft_half(const MgLev<T>& L, const MgBc& p, T* xs,
 
 // load x from xsrc (0 when null) and b over the tile with halo H (wrapped; 0
 // beyond walls)
-template <typename T, int TH, int H>
+template <typename T, int TW, int TH, int H>
 __device__ __forceinline__ void ft_load(const MgLev<T>& L, const MgBc& p, T* xs, T* bs, int i0, int j0,
                                         const T* xsrc) {
-    constexpr int W = FT_W + 2 * H, HT = TH + 2 * H;
+    constexpr int W = TW + 2 * H, HT = TH + 2 * H;
     for (int q = threadIdx.x; q < W * HT; q += FT_THREADS) {
         const int li = q % W, lj = q / W;
         const int wi = mg_dom(i0 - H + li, L.nx, p.per_x), wj = mg_dom(j0 - H + lj, L.ny, p.per_y);
@@ -321,14 +320,14 @@ __device__ __forceinline__ void ft_load(const MgLev<T>& L, const MgBc& p, T* xs,
 // A tile is interior when its array (tile + halo H) lies in [1, n-1) along
 // both axes: no wrap, no wall, every wall-adjacency bit 0, every transfer
 // weight the interior one.  Those tiles take the index-light paths below.
-template <int TH, int H>
+template <int TW, int TH, int H>
 __device__ __forceinline__ bool ft_interior(int nx, int ny, int i0, int j0) {
-    return i0 - H >= 1 && i0 + FT_W + H <= nx - 1 && j0 - H >= 1 && j0 + TH + H <= ny - 1;
+    return i0 - H >= 1 && i0 + TW + H <= nx - 1 && j0 - H >= 1 && j0 + TH + H <= ny - 1;
 }
 
-template <typename T, int TH, int H>
+template <typename T, int TW, int TH, int H>
 __device__ __forceinline__ void ft_load_int(const MgLev<T>& L, T* xs, T* bs, int i0, int j0, const T* xsrc) {
-    constexpr int W = FT_W + 2 * H, HT = TH + 2 * H;
+    constexpr int W = TW + 2 * H, HT = TH + 2 * H;
     const size_t base = (size_t)(j0 - H) * L.pitch + (i0 - H);
     for (int q = threadIdx.x; q < W * HT; q += FT_THREADS) {
         const size_t k = base + (size_t)(q / W) * L.pitch + (q % W);
@@ -340,11 +339,11 @@ __device__ __forceinline__ void ft_load_int(const MgLev<T>& L, T* xs, T* bs, int
 
 // interior half sweep: warp w takes rows w, w + 8, ...; lane l the cells
 // 2l (+ 64) of the row's colour
-template <typename T, int TH, int H>
+template <typename T, int TW, int TH, int H>
 __device__ __forceinline__ void ft_half_int(const MgLev<T>& L, T* xs, const T* bs, int i0, int j0, int c, int h,
                                             bool first) {
-    constexpr int W = FT_W + 2 * H;
-    const int nrow = TH + 2 * h, hw = FT_W / 2 + h;
+    constexpr int W = TW + 2 * H;
+    const int nrow = TH + 2 * h, hw = TW / 2 + h;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const T scale = L.scale, id0 = L.invd[0];
     for (int rj = warp; rj < nrow; rj += FT_THREADS / 32) {
@@ -368,23 +367,23 @@ __device__ __forceinline__ void ft_half_int(const MgLev<T>& L, T* xs, const T* b
     __syncthreads();
 }
 
-template <typename T, int TH>
+template <typename T, int TW, int TH>
 __global__ void __launch_bounds__(FT_THREADS) k_mg_pre(MgLev<T> F, MgLev<T> C, MgBc p, SolverState* S, int inner) {
     if (!block_live(S, inner)) return;
-    constexpr int H = 5, W = FT_W + 2 * H, HT = TH + 2 * H;
+    constexpr int H = 5, W = TW + 2 * H, HT = TH + 2 * H;
     __shared__ T xs[W * HT];
     __shared__ T bs[W * HT];  // b, then r in place on the residual ring
-    const int i0 = blockIdx.x * FT_W, j0 = blockIdx.y * TH;
-    if (ft_interior<TH, H>(F.nx, F.ny, i0, j0)) {
-        ft_load_int<T, TH, H>(F, xs, bs, i0, j0, nullptr);
-        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 0, 5, true);
-        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 1, 4, false);
-        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 0, 3, false);
-        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 1, 2, false);
+    const int i0 = blockIdx.x * TW, j0 = blockIdx.y * TH;
+    if (ft_interior<TW, TH, H>(F.nx, F.ny, i0, j0)) {
+        ft_load_int<T, TW, TH, H>(F, xs, bs, i0, j0, nullptr);
+        ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 0, 5, true);
+        ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 1, 4, false);
+        ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 0, 3, false);
+        ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 1, 2, false);
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         const T d0 = F.diag[0], ms = F.ms;
         for (int rj = warp; rj < TH + 2; rj += FT_THREADS / 32)
-            for (int ci = lane; ci < FT_W + 2; ci += 32) {
+            for (int ci = lane; ci < TW + 2; ci += 32) {
                 const int q = (rj + H - 1) * W + (ci + H - 1);
                 T ax = d0 * xs[q];
                 ax = mg_fma(ms, xs[q - 1], ax);
@@ -394,14 +393,14 @@ __global__ void __launch_bounds__(FT_THREADS) k_mg_pre(MgLev<T> F, MgLev<T> C, M
                 bs[q] = bs[q] - ax;
             }
         __syncthreads();
-        for (int k = threadIdx.x; k < FT_W * TH; k += FT_THREADS) {
-            const int li = k % FT_W, lj = k / FT_W;
+        for (int k = threadIdx.x; k < TW * TH; k += FT_THREADS) {
+            const int li = k % TW, lj = k / TW;
             F.r[(size_t)(j0 + lj) * F.pitch + i0 + li] = xs[(lj + H) * W + li + H];
         }
         // restriction with the interior weights 1/4, 3/4, 3/4, 1/4 per axis
         const T w4[4] = {T(0.25), T(0.75), T(0.75), T(0.25)};
-        for (int k = threadIdx.x; k < (FT_W / 2) * (TH / 2); k += FT_THREADS) {
-            const int ci = k % (FT_W / 2), cj = k / (FT_W / 2);
+        for (int k = threadIdx.x; k < (TW / 2) * (TH / 2); k += FT_THREADS) {
+            const int ci = k % (TW / 2), cj = k / (TW / 2);
             const int qr = (2 * cj - 1 + H) * W + (2 * ci - 1 + H);
             T acc = T(0);
 #pragma unroll
@@ -416,14 +415,14 @@ __global__ void __launch_bounds__(FT_THREADS) k_mg_pre(MgLev<T> F, MgLev<T> C, M
         }
         return;
     }
-    ft_load<T, TH, H>(F, p, xs, bs, i0, j0, nullptr);
-    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 0, 5, true);
-    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 1, 4, false);
-    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 0, 3, false);
-    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 1, 2, false);
+    ft_load<T, TW, TH, H>(F, p, xs, bs, i0, j0, nullptr);
+    ft_half<T, TW, TH, H>(F, p, xs, bs, i0, j0, 0, 5, true);
+    ft_half<T, TW, TH, H>(F, p, xs, bs, i0, j0, 1, 4, false);
+    ft_half<T, TW, TH, H>(F, p, xs, bs, i0, j0, 0, 3, false);
+    ft_half<T, TW, TH, H>(F, p, xs, bs, i0, j0, 1, 2, false);
     // residual on the tile grown by 1 (read by the restriction), in place of b
     {
-        const int ncol = FT_W + 2, nrow = TH + 2;
+        const int ncol = TW + 2, nrow = TH + 2;
         for (int k = threadIdx.x; k < ncol * nrow; k += FT_THREADS) {
             const int gi = i0 - 1 + k % ncol, gj = j0 - 1 + k / ncol;
             const int wi = mg_dom(gi, F.nx, p.per_x), wj = mg_dom(gj, F.ny, p.per_y);
@@ -439,13 +438,13 @@ __global__ void __launch_bounds__(FT_THREADS) k_mg_pre(MgLev<T> F, MgLev<T> C, M
     }
     __syncthreads();
     // x on the tile, into the r array (read back by k_mg_post)
-    for (int k = threadIdx.x; k < FT_W * TH; k += FT_THREADS) {
-        const int gi = i0 + k % FT_W, gj = j0 + k / FT_W;
+    for (int k = threadIdx.x; k < TW * TH; k += FT_THREADS) {
+        const int gi = i0 + k % TW, gj = j0 + k / TW;
         if (gi < F.nx && gj < F.ny) F.r[(size_t)gj * F.pitch + gi] = xs[(gj - (j0 - H)) * W + (gi - (i0 - H))];
     }
     // restriction of the coarse cells under the tile
-    for (int k = threadIdx.x; k < (FT_W / 2) * (TH / 2); k += FT_THREADS) {
-        const int I = i0 / 2 + k % (FT_W / 2), J = j0 / 2 + k / (FT_W / 2);
+    for (int k = threadIdx.x; k < (TW / 2) * (TH / 2); k += FT_THREADS) {
+        const int I = i0 / 2 + k % (TW / 2), J = j0 / 2 + k / (TW / 2);
         if (I >= C.nx || J >= C.ny) continue;
         T acc = T(0);
         for (int fy0 = 2 * J - 1; fy0 <= 2 * J + 2; ++fy0) {
@@ -466,22 +465,22 @@ __global__ void __launch_bounds__(FT_THREADS) k_mg_pre(MgLev<T> F, MgLev<T> C, M
     }
 }
 
-template <typename T, int TH>
+template <typename T, int TW, int TH>
 __global__ void __launch_bounds__(FT_THREADS) k_mg_post(MgLev<T> C, MgLev<T> F, MgBc p, SolverState* S, int inner) {
     if (!block_live(S, inner)) return;
-    constexpr int H = 4, W = FT_W + 2 * H, HT = TH + 2 * H;
+    constexpr int H = 4, W = TW + 2 * H, HT = TH + 2 * H;
     // coarse cells read by the prolongation of an interior tile's array
-    constexpr int CW = FT_W / 2 + H + 2, CH = TH / 2 + H + 2;
+    constexpr int CW = TW / 2 + H + 2, CH = TH / 2 + H + 2;
     __shared__ T xs[W * HT];
     __shared__ T bs[W * HT];
     __shared__ T cs[CW * CH];
-    const int i0 = blockIdx.x * FT_W, j0 = blockIdx.y * TH;
-    if (ft_interior<TH, H>(F.nx, F.ny, i0, j0)) {
+    const int i0 = blockIdx.x * TW, j0 = blockIdx.y * TH;
+    if (ft_interior<TW, TH, H>(F.nx, F.ny, i0, j0)) {
         // coarse block from (i0 - H) / 2 - 1, (j0 - H) / 2 - 1
         const int ci0 = (i0 - H) / 2 - 1, cj0 = (j0 - H) / 2 - 1;
         for (int q = threadIdx.x; q < CW * CH; q += FT_THREADS)
             cs[q] = C.x[(size_t)(cj0 + q / CW) * C.pitch + ci0 + q % CW];
-        ft_load_int<T, TH, H>(F, xs, bs, i0, j0, F.r);  // ends with a barrier
+        ft_load_int<T, TW, TH, H>(F, xs, bs, i0, j0, F.r);  // ends with a barrier
         for (int q = threadIdx.x; q < W * HT; q += FT_THREADS) {
             const int fx = i0 - H + q % W, fy = j0 - H + q / W;
             const int I = (fx >> 1) - ci0, NI = I + ((fx & 1) ? 1 : -1);
@@ -495,17 +494,17 @@ __global__ void __launch_bounds__(FT_THREADS) k_mg_post(MgLev<T> C, MgLev<T> F, 
             xs[q] = xs[q] + v;
         }
         __syncthreads();
-        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 1, 3, false);
-        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 0, 2, false);
-        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 1, 1, false);
-        ft_half_int<T, TH, H>(F, xs, bs, i0, j0, 0, 0, false);
-        for (int k = threadIdx.x; k < FT_W * TH; k += FT_THREADS) {
-            const int li = k % FT_W, lj = k / FT_W;
+        ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 1, 3, false);
+        ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 0, 2, false);
+        ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 1, 1, false);
+        ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 0, 0, false);
+        for (int k = threadIdx.x; k < TW * TH; k += FT_THREADS) {
+            const int li = k % TW, lj = k / TW;
             F.x[(size_t)(j0 + lj) * F.pitch + i0 + li] = xs[(lj + H) * W + li + H];
         }
         return;
     }
-    ft_load<T, TH, H>(F, p, xs, bs, i0, j0, F.r);
+    ft_load<T, TW, TH, H>(F, p, xs, bs, i0, j0, F.r);
     // x += P x_coarse on every cell of the array inside the domain
     for (int q = threadIdx.x; q < W * HT; q += FT_THREADS) {
         const int fx = mg_dom(i0 - H + q % W, F.nx, p.per_x), fy = mg_dom(j0 - H + q / W, F.ny, p.per_y);
@@ -525,17 +524,19 @@ __global__ void __launch_bounds__(FT_THREADS) k_mg_post(MgLev<T> C, MgLev<T> F, 
         xs[q] = xs[q] + v;
     }
     __syncthreads();
-    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 1, 3, false);
-    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 0, 2, false);
-    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 1, 1, false);
-    ft_half<T, TH, H>(F, p, xs, bs, i0, j0, 0, 0, false);
-    for (int k = threadIdx.x; k < FT_W * TH; k += FT_THREADS) {
-        const int gi = i0 + k % FT_W, gj = j0 + k / FT_W;
+    ft_half<T, TW, TH, H>(F, p, xs, bs, i0, j0, 1, 3, false);
+    ft_half<T, TW, TH, H>(F, p, xs, bs, i0, j0, 0, 2, false);
+    ft_half<T, TW, TH, H>(F, p, xs, bs, i0, j0, 1, 1, false);
+    ft_half<T, TW, TH, H>(F, p, xs, bs, i0, j0, 0, 0, false);
+    for (int k = threadIdx.x; k < TW * TH; k += FT_THREADS) {
+        const int gi = i0 + k % TW, gj = j0 + k / TW;
         if (gi < F.nx && gj < F.ny) F.x[(size_t)gj * F.pitch + gi] = xs[(gj - (j0 - H)) * W + (gi - (i0 - H))];
     }
 }
 
-// tile heights: FP64 tiles are lower to keep both arrays in 48 KB of shared memory
+// tile shapes: 64 x 32 (FP64: 64 x 24, both arrays in 48 KB of shared
+// memory) on large levels; 32 x 16 on levels with fewer than 1024 large tiles,
+// where more, smaller CTAs shorten the latency-bound passes
 template <typename T>
 struct FtRows {
     static constexpr int value = 32;
@@ -582,14 +583,16 @@ __global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(MgBottom<T> P, 
     if (!block_live(S, inner)) return;
     extern __shared__ __align__(16) unsigned char mg_smem[];
     T* sm = reinterpret_cast<T*>(mg_smem);
-    const int tid = threadIdx.x, nt = blockDim.x;
+    // 32 x 32 threads: tx walks columns (or column pairs), ty rows
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
     auto X = [&](int l) { return sm + P.off[l]; };
     auto B = [&](int l) { return sm + P.off[l] + P.lev[l].nx * P.lev[l].ny; };
     auto R = [&](int l) { return sm + P.off[l] + 2 * P.lev[l].nx * P.lev[l].ny; };
     {
         const MgLev<T>& G = P.lev[0];
         T* b = B(0);
-        for (int k = tid; k < G.nx * G.ny; k += nt) b[k] = G.b[(size_t)(k / G.nx) * G.pitch + (k % G.nx)];
+        for (int gj = ty; gj < G.ny; gj += 32)
+            for (int gi = tx; gi < G.nx; gi += 32) b[gj * G.nx + gi] = G.b[(size_t)gj * G.pitch + gi];
     }
     __syncthreads();
     auto half = [&](int l, int color, bool first) {
@@ -597,12 +600,14 @@ __global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(MgBottom<T> P, 
         T* x = X(l);
         const T* b = B(l);
         const int pairs = (L.nx + 1) / 2;
-        for (int k = tid; k < pairs * L.ny; k += nt) {
-            const int gj = k / pairs, pr = k % pairs;
+        for (int gj = ty; gj < L.ny; gj += 32) {
             const int par = (gj + color) & 1;
-            const int gi = 2 * pr + par, go = 2 * pr + 1 - par;
-            if (gi < L.nx) x[gj * L.nx + gi] = gs_cell(p, x, L.nx, L.ny, gi, gj, b[gj * L.nx + gi], L.scale, L.invd, first);
-            if (first && go < L.nx) x[gj * L.nx + go] = T(0);
+            for (int pr = tx; pr < pairs; pr += 32) {
+                const int gi = 2 * pr + par, go = 2 * pr + 1 - par;
+                if (gi < L.nx)
+                    x[gj * L.nx + gi] = gs_cell(p, x, L.nx, L.ny, gi, gj, b[gj * L.nx + gi], L.scale, L.invd, first);
+                if (first && go < L.nx) x[gj * L.nx + go] = T(0);
+            }
         }
         __syncthreads();
     };
@@ -611,15 +616,16 @@ __global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(MgBottom<T> P, 
         const T* x = X(l);
         const T* b = B(l);
         T* r = R(l);
-        for (int k = tid; k < L.nx * L.ny; k += nt) {
-            const int gi = k % L.nx, gj = k / L.nx;
-            T ax = L.diag[mg_bits(p, L.nx, L.ny, gi, gj)] * x[k];
-            ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi - 1, gj), ax);
-            ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi + 1, gj), ax);
-            ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi, gj - 1), ax);
-            ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi, gj + 1), ax);
-            r[k] = b[k] - ax;
-        }
+        for (int gj = ty; gj < L.ny; gj += 32)
+            for (int gi = tx; gi < L.nx; gi += 32) {
+                const int k = gj * L.nx + gi;
+                T ax = L.diag[mg_bits(p, L.nx, L.ny, gi, gj)] * x[k];
+                ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi - 1, gj), ax);
+                ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi + 1, gj), ax);
+                ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi, gj - 1), ax);
+                ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi, gj + 1), ax);
+                r[k] = b[k] - ax;
+            }
         __syncthreads();
     };
     auto restrict_to = [&](int l) {
@@ -627,53 +633,53 @@ __global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(MgBottom<T> P, 
         const MgLev<T>& C = P.lev[l + 1];
         const T* fr = R(l);
         T* cb = B(l + 1);
-        for (int k = tid; k < C.nx * C.ny; k += nt) {
-            const int I = k % C.nx, J = k / C.nx;
-            T acc = T(0);
-            for (int fy0 = 2 * J - 1; fy0 <= 2 * J + 2; ++fy0) {
-                int fy = fy0;
-                if (fy < 0 || fy >= F.ny) {
-                    if (!p.per_y) continue;
-                    fy = fy < 0 ? fy + F.ny : fy - F.ny;
-                }
-                const T wy = (T)mg_pwq(fy, J, C.ny, p.per_y, p.bc[1], p.bc[3]) * T(0.25);
-                T rs = T(0);
-                for (int fx0 = 2 * I - 1; fx0 <= 2 * I + 2; ++fx0) {
-                    int fx = fx0;
-                    if (fx < 0 || fx >= F.nx) {
-                        if (!p.per_x) continue;
-                        fx = fx < 0 ? fx + F.nx : fx - F.nx;
+        for (int J = ty; J < C.ny; J += 32)
+            for (int I = tx; I < C.nx; I += 32) {
+                T acc = T(0);
+                for (int fy0 = 2 * J - 1; fy0 <= 2 * J + 2; ++fy0) {
+                    int fy = fy0;
+                    if (fy < 0 || fy >= F.ny) {
+                        if (!p.per_y) continue;
+                        fy = fy < 0 ? fy + F.ny : fy - F.ny;
                     }
-                    const T wx = (T)mg_pwq(fx, I, C.nx, p.per_x, p.bc[0], p.bc[2]) * T(0.25);
-                    rs = mg_fma(wx, fr[fy * F.nx + fx], rs);
+                    const T wy = (T)mg_pwq(fy, J, C.ny, p.per_y, p.bc[1], p.bc[3]) * T(0.25);
+                    T rs = T(0);
+                    for (int fx0 = 2 * I - 1; fx0 <= 2 * I + 2; ++fx0) {
+                        int fx = fx0;
+                        if (fx < 0 || fx >= F.nx) {
+                            if (!p.per_x) continue;
+                            fx = fx < 0 ? fx + F.nx : fx - F.nx;
+                        }
+                        const T wx = (T)mg_pwq(fx, I, C.nx, p.per_x, p.bc[0], p.bc[2]) * T(0.25);
+                        rs = mg_fma(wx, fr[fy * F.nx + fx], rs);
+                    }
+                    acc = mg_fma(wy, rs, acc);
                 }
-                acc = mg_fma(wy, rs, acc);
+                cb[J * C.nx + I] = T(0.25) * acc;
             }
-            cb[k] = T(0.25) * acc;
-        }
         __syncthreads();
     };
     auto prolong_from = [&](int l) {  // x_l += P x_{l+1}
         const MgLev<T>& F = P.lev[l];
         const MgLev<T>& C = P.lev[l + 1];
         const T* cx = X(l + 1);
-        T* fx_ = X(l);
-        for (int k = tid; k < F.nx * F.ny; k += nt) {
-            const int fx = k % F.nx, fy = k / F.nx;
-            int I, NI, J, NJ;
-            T wxI, wxN, wyJ, wyN;
-            mg_axis<T>(fx, C.nx, p.per_x, p.bc[0], p.bc[2], I, NI, wxI, wxN);
-            mg_axis<T>(fy, C.ny, p.per_y, p.bc[1], p.bc[3], J, NJ, wyJ, wyN);
-            T row0 = wxI * cx[J * C.nx + I];
-            if (NI >= 0) row0 = mg_fma(wxN, cx[J * C.nx + NI], row0);
-            T v = wyJ * row0;
-            if (NJ >= 0) {
-                T row1 = wxI * cx[NJ * C.nx + I];
-                if (NI >= 0) row1 = mg_fma(wxN, cx[NJ * C.nx + NI], row1);
-                v = mg_fma(wyN, row1, v);
+        T* fxs = X(l);
+        for (int fy = ty; fy < F.ny; fy += 32)
+            for (int fx = tx; fx < F.nx; fx += 32) {
+                int I, NI, J, NJ;
+                T wxI, wxN, wyJ, wyN;
+                mg_axis<T>(fx, C.nx, p.per_x, p.bc[0], p.bc[2], I, NI, wxI, wxN);
+                mg_axis<T>(fy, C.ny, p.per_y, p.bc[1], p.bc[3], J, NJ, wyJ, wyN);
+                T row0 = wxI * cx[J * C.nx + I];
+                if (NI >= 0) row0 = mg_fma(wxN, cx[J * C.nx + NI], row0);
+                T v = wyJ * row0;
+                if (NJ >= 0) {
+                    T row1 = wxI * cx[NJ * C.nx + I];
+                    if (NI >= 0) row1 = mg_fma(wxN, cx[NJ * C.nx + NI], row1);
+                    v = mg_fma(wyN, row1, v);
+                }
+                fxs[fy * F.nx + fx] = fxs[fy * F.nx + fx] + v;
             }
-            fx_[k] = fx_[k] + v;
-        }
         __syncthreads();
     };
     const int nb = P.nlev;
@@ -703,7 +709,8 @@ __global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(MgBottom<T> P, 
     {
         const MgLev<T>& G = P.lev[0];
         const T* x = X(0);
-        for (int k = tid; k < G.nx * G.ny; k += nt) G.x[(size_t)(k / G.nx) * G.pitch + (k % G.nx)] = x[k];
+        for (int gj = ty; gj < G.ny; gj += 32)
+            for (int gi = tx; gi < G.nx; gi += 32) G.x[(size_t)gj * G.pitch + gi] = x[gj * G.nx + gi];
     }
 }
 
@@ -859,10 +866,16 @@ static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, 
     const int lb = bottom_level(lev, nlev, &smem);
     const int top_end = lb < nlev ? lb : nlev - 1;  // levels smoothed by grid kernels on the way down
     constexpr int TH = FtRows<T>::value;
-    auto tiles = [&](const MgLev<T>& L) { return dim3((L.nx + FT_W - 1) / FT_W, (L.ny + TH - 1) / TH); };
+    auto big = [&](const MgLev<T>& L) { return (long long)((L.nx + 63) / 64) * ((L.ny + TH - 1) / TH) >= 1024; };
+    auto tiles = [&](const MgLev<T>& L, int tw, int th) { return dim3((L.nx + tw - 1) / tw, (L.ny + th - 1) / th); };
     for (int l = 0; l < top_end; ++l) {
         if (fused) {
-            k_mg_pre<T, TH><<<tiles(lev[l]), FT_THREADS, 0, c->stream>>>(lev[l], lev[l + 1], p, c->S, inner);
+            if (big(lev[l]))
+                k_mg_pre<T, 64, TH><<<tiles(lev[l], 64, TH), FT_THREADS, 0, c->stream>>>(lev[l], lev[l + 1], p, c->S,
+                                                                                        inner);
+            else
+                k_mg_pre<T, 32, 16><<<tiles(lev[l], 32, 16), FT_THREADS, 0, c->stream>>>(lev[l], lev[l + 1], p, c->S,
+                                                                                        inner);
             ++launches;
             continue;
         }
@@ -899,7 +912,12 @@ static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, 
     }
     for (int l = top_end - 1; l >= 0; --l) {
         if (fused) {
-            k_mg_post<T, TH><<<tiles(lev[l]), FT_THREADS, 0, c->stream>>>(lev[l + 1], lev[l], p, c->S, inner);
+            if (big(lev[l]))
+                k_mg_post<T, 64, TH><<<tiles(lev[l], 64, TH), FT_THREADS, 0, c->stream>>>(lev[l + 1], lev[l], p, c->S,
+                                                                                         inner);
+            else
+                k_mg_post<T, 32, 16><<<tiles(lev[l], 32, 16), FT_THREADS, 0, c->stream>>>(lev[l + 1], lev[l], p, c->S,
+                                                                                         inner);
             ++launches;
             continue;
         }
