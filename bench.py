@@ -306,7 +306,7 @@ def bench_gb300(args, rank, world, dist, device):
         achieved = it_bytes / (it_ms / 1e3) / 1e9
         if mg:
             kname = ("MG-PCG inner iteration: k_tma_dir_matvec32 + k_tma_update32 + gated k_outer_add/"
-                     "k_outer_resid + V-cycle (k_mg_smooth/residual/restrict/prolong, k_mg_coarse) + k_mg_rz32")
+                     "k_outer_resid + V-cycle (k_mg_pre/k_mg_post per level, k_mg_bottom) + k_mg_rz32")
             kern_extra = {}
         else:
             kname = "inner CG iteration (k_tma_dir_matvec32 + k_tma_update32)"
@@ -530,10 +530,10 @@ def bench_reference(args, rank, world, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--skip-cpu", action="store_true")

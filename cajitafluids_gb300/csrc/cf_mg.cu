@@ -750,7 +750,7 @@ static int bottom_level(const MgLev<T>* lev, int nlev, size_t* smem) {
 
 struct MgHierarchy {
     int nlev = 0;
-    int fused = 1;
+    int fused = -1;  // 1: all levels fused, 0: none, -1: by level (see vcycle)
     MgLev<double> d[16];
     MgLev<float> f[16];
     double* z64 = nullptr;
@@ -785,9 +785,6 @@ int mg_setup(cf_ctx* c) {
     if (rc) return rc;
     MgHierarchy* H = new MgHierarchy();
     c->mg = H;
-    // FP32 levels are bound by memory traffic: fused; FP64 levels by the FP64
-    // pipe, where the fused tiles' halo recomputation costs more than it saves
-    H->fused = mixed ? 1 : 0;
     if (const char* e = getenv("CF_MG_FUSED")) H->fused = atoi(e) != 0;
     int nx = c->ph.nx, ny = c->ph.ny;
     for (int l = 0; l < 16 && !rc; ++l) {
@@ -843,8 +840,11 @@ double* mg_z64(cf_ctx* c) { return static_cast<MgHierarchy*>(c->mg)->z64; }
 
 // fused = 1: levels above the bottom solver run the fused pre/post kernels;
 // 0: one launch per half sweep, residual, restriction and prolongation (the
-// same arithmetic).  Default: fused for FP32, level by level for FP64;
-// CF_MG_FUSED=0/1 in the environment overrides it.
+// same arithmetic); -1 (default): fused for FP32 levels, which are bound by
+// memory traffic, and for FP64 levels of at most 2^20 cells, which are bound
+// by launch latency; larger FP64 levels are bound by the FP64 pipe, where the
+// fused tiles' halo recomputation costs more than it saves.  CF_MG_FUSED=0/1
+// in the environment forces one form.
 template <typename T>
 static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, int fused) {
     MgBc p{c->ph.per_x, c->ph.per_y, {c->ph.bc[0], c->ph.bc[1], c->ph.bc[2], c->ph.bc[3]}};
@@ -868,8 +868,12 @@ static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, 
     constexpr int TH = FtRows<T>::value;
     auto big = [&](const MgLev<T>& L) { return (long long)((L.nx + 63) / 64) * ((L.ny + TH - 1) / TH) >= 1024; };
     auto tiles = [&](const MgLev<T>& L, int tw, int th) { return dim3((L.nx + tw - 1) / tw, (L.ny + th - 1) / th); };
+    auto fuse_level = [&](int l) {
+        if (fused >= 0) return fused != 0;
+        return sizeof(T) == 4 || (long long)lev[l].nx * lev[l].ny <= (1ll << 20);
+    };
     for (int l = 0; l < top_end; ++l) {
-        if (fused) {
+        if (fuse_level(l)) {
             if (big(lev[l]))
                 k_mg_pre<T, 64, TH><<<tiles(lev[l], 64, TH), FT_THREADS, 0, c->stream>>>(lev[l], lev[l + 1], p, c->S,
                                                                                         inner);
@@ -911,7 +915,7 @@ static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, 
         }
     }
     for (int l = top_end - 1; l >= 0; --l) {
-        if (fused) {
+        if (fuse_level(l)) {
             if (big(lev[l]))
                 k_mg_post<T, 64, TH><<<tiles(lev[l], 64, TH), FT_THREADS, 0, c->stream>>>(lev[l + 1], lev[l], p, c->S,
                                                                                          inner);
