@@ -318,6 +318,47 @@ __device__ __forceinline__ void put_r32(float* o, int pitch, int nx, int ny, int
     }
 }
 
+// The mixed solution x and right-hand side b are kept as double-float pairs
+// (hi + lo, two FP32 numbers, about 48 significant bits; Dekker 1971): the
+// reliable update r = b - A x then runs on the FP32 pipe instead of GB300's
+// narrow FP64 pipe, with an error (~1e-14 relative to |b| + |A x|) far below
+// what the 1e-8 divergence target needs.  nvcc --fmad=false keeps the
+// error-free transformations exact.
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+    float s = a + b;
+    float bb = s - a;
+    float e = (a - (s - bb)) + (b - bb);
+    return make_float2(s, e);
+}
+__device__ __forceinline__ float2 df_quick(float a, float b) {  // |a| >= |b|
+    float s = a + b;
+    return make_float2(s, b - (s - a));
+}
+__device__ __forceinline__ float2 df_add(float2 x, float2 y) {
+    float2 s = df_two_sum(x.x, y.x);
+    float2 t = df_two_sum(x.y, y.y);
+    s.y = s.y + t.x;
+    s = df_quick(s.x, s.y);
+    s.y = s.y + t.y;
+    return df_quick(s.x, s.y);
+}
+__device__ __forceinline__ float2 df_add_f(float2 x, float e) {
+    float2 s = df_two_sum(x.x, e);
+    s.y = s.y + x.y;
+    return df_quick(s.x, s.y);
+}
+__device__ __forceinline__ float2 df_mul(float2 x, float2 y) {
+    float p = x.x * y.x;
+    float e = fmaf(x.x, y.x, -p);
+    e = fmaf(x.x, y.y, e);
+    e = fmaf(x.y, y.x, e);
+    return df_quick(p, e);
+}
+__device__ __forceinline__ float2 df_split(double v) {
+    float hi = __double2float_rn(v);
+    return make_float2(hi, __double2float_rn(v - (double)hi));
+}
+
 // FP64 init: b, r = b, x = 0, partial r.z and r.r
 __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init64(DivArgs a) {
     SolverState* S = a.S;
@@ -391,8 +432,8 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
                 if (c >= a.nx) continue;
                 double b = div_b(a, c, j);
                 size_t k = (size_t)j * a.pitch + c;
-                a.b[k] = b;
-                a.x[k] = 0.0;
+                reinterpret_cast<float2*>(a.b)[k] = df_split(b);
+                reinterpret_cast<float2*>(a.x)[k] = make_float2(0.f, 0.f);
                 float r = (float)b;
                 put_r32(a.r32, a.pitch32, a.nx, a.ny, a.per_x, a.per_y, c, j, r);
                 a.e32[(ptrdiff_t)j * a.pitch32 + c] = 0.f;
@@ -454,73 +495,115 @@ __device__ __forceinline__ bool outer_due(const SolverState* S) {
     return due != 0;
 }
 
-// Outer refinement, part 1: x += e (FP64 += FP32).  gated = 1 (inside the
-// MG-PCG graph): only while the refinement is due.
-__global__ void k_outer_add(double* x, const float* e, int nx, int ny, int pitch, int pitch32, const SolverState* S,
+// Outer refinement, part 1: x += e (double-float += FP32), e = 0.  gated = 1
+// (inside the MG-PCG graph): only while the refinement is due.
+__global__ void k_outer_add(float2* x, float* e, int nx, int ny, int pitch, int pitch32, const SolverState* S,
                             int gated) {
     if (gated && !outer_due(S)) return;
     int gi = blockIdx.x * blockDim.x + threadIdx.x;
     int gj = blockIdx.y * blockDim.y + threadIdx.y;
     if (gi >= nx || gj >= ny) return;
-    size_t k = (size_t)gj * pitch + gi;
-    x[k] = x[k] + (double)e[(ptrdiff_t)gj * pitch32 + gi];
+    const size_t k = (size_t)gj * pitch + gi;
+    const ptrdiff_t k32 = (ptrdiff_t)gj * pitch32 + gi;
+    x[k] = df_add_f(x[k], e[k32]);
+    e[k32] = 0.f;
 }
 
-// Outer refinement, part 2: r = b - A x in FP64; inner r = (float)r, e = 0.
+// Outer refinement, part 2: r = b - A x in double-float; inner r = hi part.
 struct Outer {
     int nx, ny, per_x, per_y, G, U, pitch, pitch32;
-    Stencil st;
-    const double *x, *b;
-    float *r32, *e32;
+    float dfac[16];  // diagonal / scale by wall-adjacency bits
+    float minv32[16];
+    float2 scale;    // dt / (rho dx^2) as hi + lo
+    const float2 *x, *b;
+    float* r32;
     double *part0, *part1, *part2;
     SolverState* S;
     int gated;  // inside the MG-PCG graph: run only while the refinement is due
 };
 
-__device__ __forceinline__ double xval(const Outer& a, int c, int j) {
+__device__ __forceinline__ float2 xval(const Outer& a, int c, int j) {
     int cc = wrap_index(c, a.nx, a.per_x), jj = wrap_index(j, a.ny, a.per_y);
-    if (cc < 0 || jj < 0) return 0.0;
+    if (cc < 0 || jj < 0) return make_float2(0.f, 0.f);
     return a.x[(size_t)jj * a.pitch + cc];
 }
 
+// x at columns c0, c0 + 1 of row j (wrapped row; 0 beyond a wall or past nx)
+__device__ __forceinline__ float4 xrow2(const Outer& a, const float2* v, int c0, int j) {
+    int jj = wrap_index(j, a.ny, a.per_y);
+    if (jj < 0 || c0 >= a.nx) return make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2* row = v + (size_t)jj * a.pitch + c0;
+    if (c0 + 1 < a.nx) return *reinterpret_cast<const float4*>(row);
+    const float2 x0 = row[0];
+    return make_float4(x0.x, x0.y, 0.f, 0.f);
+}
+
+// a + b for double-float pairs of like magnitude, error ~2^-44 (|a| + |b|)
+__device__ __forceinline__ float2 df_add_s(float2 x, float2 y) {
+    float2 s = df_two_sum(x.x, y.x);
+    s.y = s.y + (x.y + y.y);
+    return df_quick(s.x, s.y);
+}
+
+// r = b - A x at one cell, A x = scale (dfac x_c - (x_W + x_E + x_S + x_N))
+__device__ __forceinline__ float2 df_resid(const Outer& a, int eb, float2 b, float2 c, float2 w, float2 e, float2 s,
+                                           float2 n) {
+    float2 nb = df_add_s(w, e);
+    nb = df_add_s(nb, s);
+    nb = df_add_s(nb, n);
+    float2 t = df_mul(make_float2(a.dfac[eb], 0.f), c);
+    t = df_add_s(t, make_float2(-nb.x, -nb.y));
+    float2 ax = df_mul(a.scale, t);
+    return df_add_s(b, make_float2(-ax.x, -ax.y));
+}
+
+// one warp per unit of 64 columns x 16 rows, lane l on columns 2l, 2l + 1;
+// rows slide through registers, W/E neighbours come by shuffle
 __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
     SolverState* S = a.S;
     if (a.gated && !outer_due(S)) return;
     const int lane = threadIdx.x & 31;
     const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
-    double arr64 = 0.0;
     float arz = 0.f, arr = 0.f;
-    const double ms = a.st.ms;
     if (unit < a.U) {
         const int g = unit % a.G, band = unit / a.G;
         const int c0 = g * CF_UNIT_COLS + 2 * lane;
         const int j0 = band * CF_BAND_ROWS;
         const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
-        for (int j = j0; j < j1; ++j)
-#pragma unroll
-            for (int s = 0; s < 2; ++s) {
-                int c = c0 + s;
-                if (c >= a.nx) continue;
-                int eb = edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y);
-                double ax = a.st.diag[eb] * xval(a, c, j);
-                ax = fma(ms, xval(a, c - 1, j), ax);
-                ax = fma(ms, xval(a, c + 1, j), ax);
-                ax = fma(ms, xval(a, c, j - 1), ax);
-                ax = fma(ms, xval(a, c, j + 1), ax);
-                double r = a.b[(size_t)j * a.pitch + c] - ax;
-                arr64 = fma(r, r, arr64);
-                float r32 = (float)r;
-                put_r32(a.r32, a.pitch32, a.nx, a.ny, a.per_x, a.per_y, c, j, r32);
-                a.e32[(ptrdiff_t)j * a.pitch32 + c] = 0.f;
-                float z = a.st.minv32[eb] * r32;
-                arz = fmaf(r32, z, arz);
-                arr = fmaf(r32, r32, arr);
+        float4 xm = xrow2(a, a.x, c0, j0 - 1), xc = xrow2(a, a.x, c0, j0);
+        for (int j = j0; j < j1; ++j) {
+            const float4 xp = xrow2(a, a.x, c0, j + 1);
+            float2 left = make_float2(__shfl_up_sync(FULLMASK, xc.z, 1), __shfl_up_sync(FULLMASK, xc.w, 1));
+            float2 right = make_float2(__shfl_down_sync(FULLMASK, xc.x, 1), __shfl_down_sync(FULLMASK, xc.y, 1));
+            if (lane == 0) left = xval(a, c0 - 1, j);
+            if (lane == 31 || c0 + 2 >= a.nx) right = xval(a, c0 + 2, j);
+            float2 mid1 = make_float2(xc.z, xc.w);
+            if (c0 + 1 >= a.nx) mid1 = xval(a, c0 + 1, j);  // E neighbour of the last column
+            const float4 bv = xrow2(a, a.b, c0, j);
+            if (c0 < a.nx) {
+                const int eb = edge_bits(c0, j, a.nx, a.ny, a.per_x, a.per_y);
+                const float2 r = df_resid(a, eb, make_float2(bv.x, bv.y), make_float2(xc.x, xc.y), left, mid1,
+                                          make_float2(xm.x, xm.y), make_float2(xp.x, xp.y));
+                put_r32(a.r32, a.pitch32, a.nx, a.ny, a.per_x, a.per_y, c0, j, r.x);
+                arz = fmaf(r.x, a.minv32[eb] * r.x, arz);
+                arr = fmaf(r.x, r.x, arr);
             }
+            if (c0 + 1 < a.nx) {
+                const int eb = edge_bits(c0 + 1, j, a.nx, a.ny, a.per_x, a.per_y);
+                const float2 r = df_resid(a, eb, make_float2(bv.z, bv.w), make_float2(xc.z, xc.w),
+                                          make_float2(xc.x, xc.y), right, make_float2(xm.z, xm.w),
+                                          make_float2(xp.z, xp.w));
+                put_r32(a.r32, a.pitch32, a.nx, a.ny, a.per_x, a.per_y, c0 + 1, j, r.x);
+                arz = fmaf(r.x, a.minv32[eb] * r.x, arz);
+                arr = fmaf(r.x, r.x, arr);
+            }
+            xm = xc;
+            xc = xp;
+        }
     }
-    arr64 = warp_fold(arr64);
     double drz = warp_fold((double)arz), drr = warp_fold((double)arr);
     if (unit < a.U && lane == 0) {
-        a.part0[unit] = arr64;
+        a.part0[unit] = drr;
         a.part1[unit] = drz;
         a.part2[unit] = drr;
     }
@@ -556,6 +639,16 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
             }
         }
     }
+}
+
+// mixed: the double-float solution, in place, to FP64 for the gradient
+__global__ void k_df_to_f64(double* x, int nx, int ny, int pitch) {
+    int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    if (gi >= nx || gj >= ny) return;
+    const size_t k = (size_t)gj * pitch + gi;
+    const float2 v = reinterpret_cast<const float2*>(x)[k];
+    x[k] = (double)v.x + (double)v.y;
 }
 
 // --------------------------------------------------------------------------
@@ -714,11 +807,21 @@ static Outer outer_args(cf_ctx* c, const Stencil& st, int gated) {
     oa.U = c->n_units;
     oa.pitch = c->vpitch;
     oa.pitch32 = c->p32;
-    oa.st = st;
-    oa.x = c->x.a;
-    oa.b = c->b.a;
+    const double scale = -st.ms;
+    for (int b = 0; b < 16; ++b) {
+        int d = 4;  // a SOLID side drops the leg and lowers the diagonal (build_stencil)
+        if ((b & 1) && c->ph.bc[0] == CF_BC_SOLID) --d;
+        if ((b & 2) && c->ph.bc[2] == CF_BC_SOLID) --d;
+        if ((b & 4) && c->ph.bc[1] == CF_BC_SOLID) --d;
+        if ((b & 8) && c->ph.bc[3] == CF_BC_SOLID) --d;
+        oa.dfac[b] = (float)d;
+        oa.minv32[b] = st.minv32[b];
+    }
+    const float hi = (float)scale;
+    oa.scale = make_float2(hi, (float)(scale - (double)hi));
+    oa.x = reinterpret_cast<const float2*>(c->x.a);
+    oa.b = reinterpret_cast<const float2*>(c->b.a);
     oa.r32 = c->r32.a;
-    oa.e32 = c->e32.a;
     oa.part0 = c->partials;
     oa.part1 = c->partials + c->n_units;
     oa.part2 = c->partials + 2 * c->n_units;
@@ -731,7 +834,8 @@ static Outer outer_args(cf_ctx* c, const Stencil& st, int gated) {
 static void launch_outer(cf_ctx* c, const Stencil& st, int gated) {
     Outer oa = outer_args(c, st, gated);
     dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
-    k_outer_add<<<grd, blk, 0, c->stream>>>(c->x.a, c->e32.a, c->ph.nx, c->ph.ny, c->vpitch, c->p32, c->S, gated);
+    k_outer_add<<<grd, blk, 0, c->stream>>>(reinterpret_cast<float2*>(c->x.a), c->e32.a, c->ph.nx, c->ph.ny,
+                                            c->vpitch, c->p32, c->S, gated);
     k_outer_resid<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(oa);
 }
 
@@ -958,6 +1062,11 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
                 if (++launches > max_launch) return fail(c, CF_ERR_NUMERIC, "mixed solver did not stop");
             }
         }
+    }
+    if (mixed) {
+        dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
+        k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, c->ph.nx, c->ph.ny, c->vpitch);
+        c->launches += 1;
     }
     const SolverState* hs = c->hS;
     res->iterations = hs->iter;
