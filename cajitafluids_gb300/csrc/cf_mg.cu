@@ -26,7 +26,7 @@
 namespace cf {
 
 constexpr int MG_NU = 2;
-constexpr int MG_NC = 16;
+constexpr int MG_NC = 8;
 
 template <typename T>
 struct MgLev {
@@ -547,12 +547,21 @@ struct FtRows<double> {
 };
 
 // ---------------------------------------------------------------------------
-// Bottom of the V-cycle in one CTA: every level with at most MG_BOTTOM_MAX
+// Bottom of the V-cycle in one CTA: every level with at most MgBottomMax
 // cells, from the restricted right-hand side of the first of them down to the
 // coarsest and back, in shared memory.  The per-cell arithmetic is the same as
 // in the grid kernels above (same formulas and order), so the result is the
 // same as that of the level-by-level launches; each phase ends at a barrier.
-constexpr int MG_BOTTOM_MAX = 4096;
+// FP32: levels up to 64^2 in the one CTA.  FP64: up to 32^2, because one SM's
+// FP64 pipe would make a 64^2 level slower than a few grid launches.
+template <typename T>
+struct MgBottomMax {
+    static constexpr int value = 4096;
+};
+template <>
+struct MgBottomMax<double> {
+    static constexpr int value = 1024;
+};
 constexpr int MG_BOTTOM_LEVELS = 6;
 constexpr int MG_BOTTOM_THREADS = 1024;
 
@@ -738,7 +747,7 @@ template <typename T>
 static int bottom_level(const MgLev<T>* lev, int nlev, size_t* smem) {
     int lb = nlev;
     for (int l = 0; l < nlev; ++l)
-        if ((long long)lev[l].nx * lev[l].ny <= MG_BOTTOM_MAX && nlev - l <= MG_BOTTOM_LEVELS) {
+        if ((long long)lev[l].nx * lev[l].ny <= MgBottomMax<T>::value && nlev - l <= MG_BOTTOM_LEVELS) {
             lb = l;
             break;
         }

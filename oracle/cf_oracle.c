@@ -624,7 +624,7 @@ static void apply_pressure(orc_state* st, double dt) {
  * The cycle is a symmetric operator, as CG needs. */
 #define MG_MAX 16
 #define MG_NU 2
-#define MG_NC 16
+#define MG_NC 8
 
 typedef struct {
     int nx, ny;
