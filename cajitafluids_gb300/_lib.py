@@ -131,6 +131,7 @@ SIGNATURES = {
     "cf_max_velocity": (ctypes.c_int, [_vp, _dp]),
     "cf_interp_points": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     "cf_trace_points": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_double, _dp]),
+    "cf_cell_velocity": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_ssize_t, ctypes.c_ssize_t]),
     "cf_launch_count": (ctypes.c_longlong, [_vp]),
     "cf_stream": (_vp, [_vp]),
     "cf_timer_start": (ctypes.c_int, [_vp]),

@@ -232,6 +232,15 @@ class Context:
         self._check(self.lib.cf_trace_points(self.h, xy.shape[0], _dptr(xy), float(dt), _dptr(out)))
         return out
 
+    def cell_velocity(self):
+        """Cell-centred (linear) velocity of the current state, as SiloWriter
+        writes it: two (ny, nx) arrays."""
+        ny, nx = self.owned_shape("q")
+        uc = np.empty((ny, nx))
+        vc = np.empty((ny, nx))
+        self._check(self.lib.cf_cell_velocity(self.h, _dptr(uc), _dptr(vc), 1, nx))
+        return uc, vc
+
     @property
     def launches(self) -> int:
         return int(self.lib.cf_launch_count(self.h))

@@ -24,6 +24,7 @@
 
 #include <array>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <iostream>
 #include <memory>
@@ -312,6 +313,52 @@ std::shared_ptr<VelocityCorrectorBase> createVelocityCorrector(const std::shared
     return std::make_shared<VelocityCorrector>(pm, bc, density, delta_t, std::move(solver), std::move(precon));
 }
 
+// src/SiloWriter.hpp: the per-step output.  libsilo is not part of this
+// build, so siloWrite writes the same mesh and variables that writeFile hands
+// to Silo (:61-214: DBPutQuadmesh node coordinates, DBPutQuadvar1 "quantity"
+// and DBPutQuadvar "velocity" (u, v) interpolated to cell centres, zone-
+// centred, owned cells, x fastest) into one raw little-endian file per call:
+//   "CFSILO01" | int32 nx, ny, cycle | float64 time, dt |
+//   float64 X[nx+1] | Y[ny+1] | quantity[nx*ny] | u[nx*ny] | v[nx*ny]
+// named <dir>/CajitaFluids%05d.cfraw (the reference's master-file name,
+// :386-387, with the raw extension).
+template <std::size_t NumSpaceDims>
+class SiloWriter;
+
+template <>
+class SiloWriter<2> {
+  public:
+    SiloWriter(const std::shared_ptr<ProblemManager<2>>& pm, std::string dir = "data")
+        : _pm(pm), _dir(std::move(dir)) {}
+
+    void siloWrite(const char* /*name*/, int time_step, double time, double dt) {
+        cf_ctx* c = _pm->ctx();
+        const auto& mesh = *_pm->mesh();
+        const int nx = mesh.numCell()[0], ny = mesh.numCell()[1];
+        const double h = mesh.cellSize();
+        std::vector<double> q((size_t)nx * ny), u(q.size()), v(q.size()), X(nx + 1), Y(ny + 1);
+        for (int i = 0; i <= nx; ++i) X[i] = mesh.boundingBox()[0] + i * h;
+        for (int j = 0; j <= ny; ++j) Y[j] = mesh.boundingBox()[1] + j * h;
+        check(c, cf_download(c, CF_FIELD_QUANTITY, q.data(), 1, nx), "cf_download");
+        check(c, cf_cell_velocity(c, u.data(), v.data(), 1, nx), "cf_cell_velocity");
+        char path[4096];
+        snprintf(path, sizeof(path), "%s/CajitaFluids%05d.cfraw", _dir.c_str(), time_step);
+        FILE* f = fopen(path, "wb");
+        if (!f) throw std::runtime_error(std::string("cannot open ") + path);
+        const int32_t hdr[3] = {nx, ny, time_step};
+        const double tv[2] = {time, dt};
+        bool ok = fwrite("CFSILO01", 1, 8, f) == 8 && fwrite(hdr, sizeof(int32_t), 3, f) == 3 &&
+                  fwrite(tv, sizeof(double), 2, f) == 2 && fwrite(X.data(), sizeof(double), X.size(), f) == X.size() &&
+                  fwrite(Y.data(), sizeof(double), Y.size(), f) == Y.size();
+        for (const auto* a : {&q, &u, &v}) ok = ok && fwrite(a->data(), sizeof(double), a->size(), f) == a->size();
+        if (fclose(f) != 0 || !ok) throw std::runtime_error(std::string("write failed: ") + path);
+    }
+
+  private:
+    std::shared_ptr<ProblemManager<2>> _pm;
+    std::string _dir;
+};
+
 class SolverBase {
   public:
     virtual ~SolverBase() = default;
@@ -364,16 +411,22 @@ class Solver<2> : public SolverBase {
         if (rc != CF_OK && rc != CF_ERR_NOT_CONVERGED) check(_pm->ctx(), rc, "cf_step");
         _time += _dt;
     }
+    // src/Solver.hpp:149-177, writing through SiloWriter when an output
+    // directory is set (setOutputDirectory)
     void solve(const double t_final, const int write_freq) override {
         int t = 0;
         int num_step = (int)(t_final / _dt);
+        if (_silo) _silo->siloWrite("Mesh", t, _time, _dt);
         setup();
         do {
             if (0 == t % write_freq) printf("Step %d / %d at time = %f\n", t, num_step, _time);
             step();
+            if (_silo && 0 == t % write_freq) _silo->siloWrite("Mesh", t, _time, _dt);
             t++;
         } while (_time < t_final);
     }
+    void setOutputDirectory(const std::string& dir) { _silo = std::make_shared<SiloWriter<2>>(_pm, dir); }
+    const std::shared_ptr<SiloWriter<2>>& siloWriter() const { return _silo; }
 
     // the reference hard-codes tol 1e-6 / max_iter 2000 (src/VelocityCorrector.hpp:103-104)
     void setTolerance(double tol, int max_iter) {
@@ -395,6 +448,7 @@ class Solver<2> : public SolverBase {
     std::shared_ptr<Mesh<2>> _mesh;
     std::shared_ptr<ProblemManager<2>> _pm;
     std::shared_ptr<VelocityCorrector> _vc;
+    std::shared_ptr<SiloWriter<2>> _silo;
     cf_solve_stats _last{};
 };
 

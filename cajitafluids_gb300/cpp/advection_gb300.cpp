@@ -8,7 +8,9 @@
 // Extra options: --steps N runs exactly N steps after setup instead of
 // t_final / dt; --linear samples the advected field linearly; --tol sets the
 // solver tolerance; --out FILE writes the final owned fields as raw FP64
-// ("CFGB" magic, nx, ny, then q, u, v, p in x-fastest order).
+// ("CFGB" magic, nx, ny, then q, u, v, p in x-fastest order); --write-dir DIR
+// turns on the SiloWriter output (DIR/CajitaFluids%05d.cfraw every -w steps,
+// as Solver::solve writes Silo files).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -54,7 +56,7 @@ static void dump(const char* path, const CajitaFluids::ProblemManager<2>& pm) {
 }
 
 int main(int argc, char** argv) {
-    std::string device = "gb300", solver = "PCG", precon = "PFMG", out;
+    std::string device = "gb300", solver = "PCG", precon = "PFMG", out, write_dir;
     double t_final = 4.0, delta_t = 0.005, density = 0.1, gravity = 0.0, quantity = 3.0, tol = 1.0e-6;
     int n = 128, write_freq = 20, steps = -1, order = 3;
     std::array<double, 2> inLocation{{0.2, 0.45}}, inSize{{0.02, 0.1}}, inVelocity{{1.0, 0.0}};
@@ -79,6 +81,7 @@ int main(int argc, char** argv) {
         else if (a == "--linear") order = 1;
         else if (a == "--tol") tol = atof(next());
         else if (a == "--out") out = next();
+        else if (a == "--write-dir") write_dir = next();
         else if (a == "--inflow") {
             inLocation = {{atof(next()), atof(next())}};
             inSize = {{atof(next()), atof(next())}};
@@ -107,11 +110,17 @@ int main(int argc, char** argv) {
         CajitaFluids::Solver<2> s({0, 0, 1.0, 1.0}, {n, n}, density, initializer, bc, source, body, delta_t, solver,
                                   precon, false, {false, false}, order);
         s.setTolerance(tol, 100000);
+        if (!write_dir.empty()) s.setOutputDirectory(write_dir);
         if (steps < 0) {
             s.solve(t_final, write_freq);
         } else {
+            // Solver::solve's loop (src/Solver.hpp:149-177) for a fixed step count
+            if (s.siloWriter()) s.siloWriter()->siloWrite("Mesh", 0, s.time(), s.timeStep());
             s.setup();
-            for (int k = 0; k < steps; ++k) s.step();
+            for (int k = 0; k < steps; ++k) {
+                s.step();
+                if (s.siloWriter() && 0 == k % write_freq) s.siloWriter()->siloWrite("Mesh", k, s.time(), s.timeStep());
+            }
         }
         const cf_solve_stats& st = s.lastStats();
         printf("done: t = %.6f dt = %.6e iterations %d div_l2 %.3e status %d\n", s.time(), s.timeStep(),

@@ -642,6 +642,42 @@ int cf_trace_points(cf_ctx* ctx, int n, const double* xy, double dt, double* out
     return points_call(ctx, n, xy, out, 2, 1, 0, 1, dt);
 }
 
+int cf_cell_velocity(cf_ctx* ctx, double* uc, double* vc, ptrdiff_t si, ptrdiff_t sj) {
+    if (!ctx || !uc || !vc) return CF_ERR_INVALID;
+    CF_GUARD_BEGIN
+    cudaSetDevice(ctx->device);
+    if (si <= 0 || sj <= 0) return fail(ctx, CF_ERR_INVALID, "strides must be positive");
+    const int nx = ctx->ph.nx, ny = ctx->ph.ny;
+    const size_t n = (size_t)nx * ny;
+    int rc = CF_OK;
+    if (!ctx->outbuf) rc = alloc_dev(ctx, ctx->outbuf, 2 * n);
+    if (!rc) rc = cuda_check(ctx, launch_fill_ghosts(ctx), "fill ghosts");
+    if (!rc) rc = cuda_check(ctx, launch_cell_velocity(ctx, ctx->outbuf, ctx->outbuf + n), "cell velocity");
+    if (rc) return rc;
+    double* dst[2] = {uc, vc};
+    std::vector<double> tmp;
+    if (si != 1) tmp.resize(n);
+    for (int f = 0; f < 2; ++f) {
+        const double* src = ctx->outbuf + f * n;
+        if (si == 1) {
+            rc = cuda_check(ctx, cudaMemcpy2DAsync(dst[f], sj * sizeof(double), src, nx * sizeof(double),
+                                                   nx * sizeof(double), ny, cudaMemcpyDefault, ctx->stream),
+                            "cell velocity copy");
+            if (!rc) rc = sync(ctx, "cell velocity copy");
+        } else {
+            rc = cuda_check(ctx, cudaMemcpyAsync(tmp.data(), src, n * sizeof(double), cudaMemcpyDefault, ctx->stream),
+                            "cell velocity copy");
+            if (!rc) rc = sync(ctx, "cell velocity copy");
+            if (!rc)
+                for (int j = 0; j < ny; ++j)
+                    for (int i = 0; i < nx; ++i) dst[f][i * si + j * sj] = tmp[(size_t)j * nx + i];
+        }
+        if (rc) return rc;
+    }
+    return CF_OK;
+    CF_GUARD_END
+}
+
 long long cf_launch_count(const cf_ctx* ctx) { return ctx ? ctx->launches : -1; }
 
 void* cf_stream(const cf_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }

@@ -47,6 +47,7 @@ struct cf_ctx {
 
     void* adjoint = nullptr;  // checkpoints and adjoint buffers (cf_adjoint.cu)
     void* mg = nullptr;       // multigrid hierarchy (cf_mg.cu)
+    double* outbuf = nullptr; // 2 nx ny doubles for cf_cell_velocity, allocated on first use
     cudaGraphExec_t gmg = nullptr;      // batch of MG-PCG iterations
     cudaGraphExec_t gmg_pre = nullptr;  // V-cycle + r.z after the residual is (re)formed
     cf::Stencil gmg_st{};
@@ -76,6 +77,7 @@ cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs);
 cudaError_t launch_add_inputs(cf_ctx* c, double dt);
 cudaError_t launch_interp_points(cf_ctx* c, int field, int order, int n, const double* d_xy, double* d_out);
 cudaError_t launch_trace_points(cf_ctx* c, int n, const double* d_xy, double dt, double* d_out);
+cudaError_t launch_cell_velocity(cf_ctx* c, double* d_uc, double* d_vc);
 cudaError_t launch_max_velocity(cf_ctx* c, double* d_out);
 cudaError_t launch_convert_q(cf_ctx* c, int to_device, int version);
 

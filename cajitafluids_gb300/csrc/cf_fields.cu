@@ -413,6 +413,19 @@ __global__ void k_trace_points(Pts a) {
     a.out[2 * k + 1] = ty;
 }
 
+// SiloWriter::writeFile's cell-centred velocity (src/SiloWriter.hpp:177-191):
+// interpolateVelocity<2, 1> (linear) of u and v at each owned cell centre,
+// written owned-region, x fastest, into uc, vc (pitch nx)
+__global__ void k_cell_velocity(Phys p, Grid<double> u, Grid<double> v, double* uc, double* vc) {
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    if (gi >= p.nx || gj >= p.ny) return;
+    const double x = entity_coord(p, E_CELL, 0, gi + CF_HALO), y = entity_coord(p, E_CELL, 1, gj + CF_HALO);
+    const size_t k = (size_t)gj * p.nx + gi;
+    uc[k] = sample64<1>(u, p.low[E_FACEI][0], p.low[E_FACEI][1], p.rdx, x, y);
+    vc[k] = sample64<1>(v, p.low[E_FACEJ][0], p.low[E_FACEJ][1], p.rdx, x, y);
+}
+
 // max |w| over the owned faces of one axis; non-negative doubles order like
 // their bit patterns, so an integer atomicMax is exact and order-free.
 __global__ void k_max_abs(Grid<double> g, int ox, int oy, unsigned long long* out) {
@@ -511,6 +524,14 @@ cudaError_t launch_interp_points(cf_ctx* c, int field, int order, int n, const d
     Grid<double> f = field == CF_FIELD_QUANTITY ? c->q64[s] : (field == CF_FIELD_U ? c->u[s] : c->v[s]);
     Pts a{c->ph, f, c->u[s], c->v[s], field, order, n, d_xy, d_out, 0.0};
     k_interp_points<<<(n + 127) / 128, 128, 0, c->stream>>>(a);
+    c->launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cell_velocity(cf_ctx* c, double* d_uc, double* d_vc) {
+    const Phys& p = c->ph;
+    dim3 blk(32, 8);
+    k_cell_velocity<<<grid2(p.nx, p.ny, blk), blk, 0, c->stream>>>(p, c->u[c->cur], c->v[c->cur], d_uc, d_vc);
     c->launches += 1;
     return cudaGetLastError();
 }

@@ -203,6 +203,17 @@ int cf_interp_points(cf_ctx* ctx, int field, int order, int n, const double* xy,
 /* TimeIntegrator::rk3 (src/TimeIntegrator.hpp:36-77) of n points */
 int cf_trace_points(cf_ctx* ctx, int n, const double* xy, double dt, double* out);
 
+/* ---- output (replaces the device half of SiloWriter::writeFile) ----
+ * SiloWriter interpolates the face velocities to cell centres for its
+ * "velocity" zonal variable (src/SiloWriter.hpp:177-205:
+ * interpolateVelocity<2, 1> at every owned cell centre).  cf_cell_velocity
+ * fills uc, vc (nx x ny, element (i, j) at base[i*stride_i + j*stride_j]) with
+ * that interpolation of the current velocities (ghosts refreshed first).  The
+ * "quantity" variable is cf_download(CF_FIELD_QUANTITY); the mesh is the node
+ * coordinates lo + i dx.  The C++ mirror's SiloWriter<2> writes these in the
+ * Silo variables' layout to a raw file (libsilo is not part of this build). */
+int cf_cell_velocity(cf_ctx* ctx, double* uc, double* vc, ptrdiff_t stride_i, ptrdiff_t stride_j);
+
 /* ---- instrumentation ---- */
 /* number of kernels this context has launched (graph nodes included) */
 long long cf_launch_count(const cf_ctx* ctx);
