@@ -570,13 +570,14 @@ int cf_backward(cf_ctx* ctx, const double* dL_dq_T, const double* dL_du_T, const
     int rc = check_supported(ctx);
     if (!rc) rc = setup_records(ctx, A);
     if (rc) return rc;
-    SolveOpts so;
+    SolveOpts so{};
     so.tol = A->opts.tol;
     so.abs_tol = 0.0;  // the adjoint right-hand side has its own scale
     so.max_iter = A->opts.max_iter;
     so.inner_tol = 0.1;
     so.max_outer = 200;
     so.precon_none = (!strcmp(A->precon.c_str(), "None") || !strcmp(A->precon.c_str(), "none")) ? 1 : 0;
+    so.precon_mg = (A->precon == "PFMG" || A->precon == "SMG" || A->precon == "MG") ? 1 : 0;
     if (!(so.tol > 0.0)) so.tol = 1e-12;
     // lambda_T
     for (int k = 0; k < 3; ++k) cudaMemsetAsync(grid_base(A->ag[k]), 0, grid_bytes(A->ag[k]), ctx->stream);

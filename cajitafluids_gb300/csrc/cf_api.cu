@@ -162,7 +162,7 @@ void fill_stats(const SolveResult& r, cf_solve_stats* s) {
 }
 
 int do_project(cf_ctx* c, double dt, const cf_solver_opts* opts, cf_solve_stats* stats) {
-    SolveOpts so;
+    SolveOpts so{};
     int rc = parse_opts(c, opts, &so);
     if (rc) return rc;
     if (!(dt > 0.0) || !isfinite(dt)) return fail(c, CF_ERR_INVALID, "dt must be positive and finite");
@@ -318,6 +318,8 @@ int cf_ctx_destroy(cf_ctx* ctx) {
     if (ctx->g32) cudaGraphExecDestroy(ctx->g32);
     if (ctx->gmg) cudaGraphExecDestroy(ctx->gmg);
     if (ctx->gmg_pre) cudaGraphExecDestroy(ctx->gmg_pre);
+    for (cudaGraphExec_t g : ctx->rgx)
+        if (g) cudaGraphExecDestroy(g);
     cf::mg_free(ctx);
     for (void* p : ctx->allocs) cudaFree(p);
     if (ctx->hS) cudaFreeHost(ctx->hS);
@@ -572,7 +574,7 @@ int cf_step(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* opts,
     if (!(dt > 0.0) || !isfinite(dt)) return fail(ctx, CF_ERR_INVALID, "dt must be positive and finite");
     CF_GUARD_BEGIN
     cudaSetDevice(ctx->device);
-    SolveOpts so;
+    SolveOpts so{};
     int rc = parse_opts(ctx, opts, &so);
     if (rc) return rc;
     const bool fuse = !ctx->ph.force_density;

@@ -52,6 +52,12 @@ struct cf_ctx {
     cudaGraphExec_t gmg_pre = nullptr;  // V-cycle + r.z after the residual is (re)formed
     cf::Stencil gmg_st{};
     int gmg_per_iter = 0, gmg_pre_launches = 0;
+    // device-resident projection graphs, one per current buffer (cf_project.cu)
+    cudaGraphExec_t rgx[2] = {nullptr, nullptr};
+    cf::Stencil rg_st[2]{};
+    cf::Phys rg_ph[2]{};
+    int rg_flags[2] = {-1, -1};
+    int rg_head[2] = {0, 0}, rg_trip[2] = {0, 0}, rg_tail[2] = {0, 0};
     // FP32 z = M^-1 r of the mixed MG-PCG, ghost ring as the other FP32 vectors
     cf::Vec32 z32{};
     float* z32b = nullptr;

@@ -73,6 +73,7 @@ struct SolverState {
     double rr_out, inner_tol2, target2, rho_prev;
     int use_abs, restart;
     int refreshed;  // mixed MG: r was just re-formed from the FP64 solution
+    int trips, trip_limit;  // device-resident loop: trips taken, and the bound
     int iter, max_iter, status;
     int inner_iter, inner_status;
     int outer_iter, max_outer;

@@ -31,6 +31,8 @@
 #include <math.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <functional>
 #include <cstring>
 
 #include "cf_ctx.cuh"
@@ -949,6 +951,205 @@ static int read_state(cf_ctx* c) {
     return cuda_check(c, cudaStreamSynchronize(c->stream), "solver state read");
 }
 
+// --------------------------------------------------------------------------
+// Device-resident projection: one CUDA graph per stencil, state setup and
+// current buffer, so that a projection costs one launch and one host
+// synchronisation:
+//   head : divergence + CG init, [MG: V-cycle and r.z]
+//   WHILE (status == RUNNING): kResidentBatch iterations, then k_loop_cond,
+//          which ends the loop, and stops it after trip_limit trips
+//   tail : [mixed: double-float x to FP64], gradient subtraction, ||div u||,
+//          copies of the solver state and the norms to pinned host memory
+static const int kResidentBatch = 16;    // Jacobi-PCG iterations per trip
+static const int kResidentBatchMG = 2;   // MG-PCG iterations per trip
+
+__global__ void k_loop_cond(SolverState* S, cudaGraphConditionalHandle h) {
+    int run = *(volatile int*)&S->status == ST_RUNNING;
+    if (run) {
+        S->trips += 1;
+        if (S->trips > S->trip_limit) {
+            S->status = ST_MAXIT;
+            run = 0;
+        }
+    }
+    cudaGraphSetConditional(h, run ? 1u : 0u);
+}
+
+// kernels of one iteration (per trip: batch of them); returns launches
+static int launch_iterations(cf_ctx* c, const Stencil& st, bool mixed, bool mg, int n) {
+    const int nb = red_blocks(c);
+    const double scale = -st.ms;
+    int k = 0;
+    Cg64 a = cg64_args(c, st);
+    if (mg && !mixed) {
+        a.mg = 1;
+        a.z = mg_z64(c);
+    }
+    for (int i = 0; i < n; ++i) {
+        if (mixed) {
+            if (mg)
+                cg32_launch_pair_mg(c, st);
+            else
+                cg32_launch_iteration(c, st);
+            launch_outer(c, st, 1);
+            k += 4;
+            if (mg) k += cg32_mg_precondition(c, scale);
+        } else {
+            k_cg_dir_matvec64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
+            k_cg_update64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
+            k += 2;
+            if (mg) {
+                k += 1 + mg_vcycle(c, scale);
+                k_mg_rz64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a, 0);
+            }
+        }
+    }
+    return k;
+}
+
+static int capture_graph(cf_ctx* c, cudaGraph_t* g, const std::function<void()>& fn) {
+    int rc = cuda_check(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "capture begin");
+    if (rc) return rc;
+    fn();
+    return cuda_check(c, cudaStreamEndCapture(c->stream, g), "capture end");
+}
+
+static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, bool mg, int cur) {
+    const int nb = red_blocks(c);
+    const double scale = -st.ms;
+    Grid<double> gu = c->u[cur], gv = c->v[cur];
+    cudaGraph_t g = nullptr, head = nullptr, tail = nullptr;
+    int nhead = 0, ntrip = 0, ntail = 0;
+    int rc = cuda_check(c, cudaGraphCreate(&g, 0), "graph create");
+    if (!rc)
+        rc = capture_graph(c, &head, [&] {
+            DivArgs da = div_args(c, st);
+            da.u = gu;
+            da.v = gv;
+            if (mixed)
+                k_div_init_mixed<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
+            else
+                k_div_init64<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
+            nhead = 1;
+            if (mg) {
+                if (mixed) {
+                    nhead += cg32_mg_precondition(c, scale);
+                } else {
+                    Cg64 a = cg64_args(c, st);
+                    a.mg = 1;
+                    a.z = mg_z64(c);
+                    nhead += 1 + mg_vcycle(c, scale);
+                    k_mg_rz64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a, 1);
+                }
+            }
+        });
+    cudaGraphNode_t nh = nullptr, nc = nullptr, nt = nullptr;
+    if (!rc) rc = cuda_check(c, cudaGraphAddChildGraphNode(&nh, g, nullptr, 0, head), "graph head");
+    cudaGraphConditionalHandle h = 0;
+    if (!rc) rc = cuda_check(c, cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault), "handle");
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    if (!rc) rc = cuda_check(c, cudaGraphAddNode(&nc, g, &nh, nullptr, 1, &cp), "graph loop");
+    if (!rc) {
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        rc = cuda_check(c, cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0,
+                                                         cudaStreamCaptureModeThreadLocal),
+                        "capture body");
+        if (!rc) {
+            ntrip = launch_iterations(c, st, mixed, mg, mg ? kResidentBatchMG : kResidentBatch);
+            k_loop_cond<<<1, 1, 0, c->stream>>>(c->S, h);
+            ntrip += 1;
+            rc = cuda_check(c, cudaStreamEndCapture(c->stream, &body), "capture body end");
+        }
+    }
+    if (!rc)
+        rc = capture_graph(c, &tail, [&] {
+            dim3 blk(32, 8);
+            if (mixed) {
+                dim3 grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
+                k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, c->ph.nx, c->ph.ny, c->vpitch);
+                ntail += 1;
+            }
+            Press pa{c->ph, gu, gv, c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx)), 0};
+            dim3 grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
+            k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
+            DivArgs da = div_args(c, st);
+            da.u = gu;
+            da.v = gv;
+            k_div_norms<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
+            ntail += 2;
+            cudaMemcpyAsync(c->hS, c->S, sizeof(SolverState), cudaMemcpyDeviceToHost, c->stream);
+            cudaMemcpyAsync(c->h_out, c->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+        });
+    if (!rc) rc = cuda_check(c, cudaGraphAddChildGraphNode(&nt, g, &nc, 1, tail), "graph tail");
+    if (c->rgx[cur]) {
+        cudaGraphExecDestroy(c->rgx[cur]);
+        c->rgx[cur] = nullptr;
+    }
+    if (!rc) rc = cuda_check(c, cudaGraphInstantiate(&c->rgx[cur], g, 0), "graph instantiate");
+    if (head) cudaGraphDestroy(head);
+    if (tail) cudaGraphDestroy(tail);
+    if (g) cudaGraphDestroy(g);
+    if (rc) return rc;
+    c->rg_head[cur] = nhead;
+    c->rg_trip[cur] = ntrip;
+    c->rg_tail[cur] = ntail;
+    return CF_OK;
+}
+
+static bool resident_enabled() {
+    static int on = -1;
+    if (on < 0) {
+        const char* e = getenv("CF_RESIDENT");
+        on = e ? (atoi(e) != 0) : 1;
+    }
+    return on != 0;
+}
+
+// the projection of the current buffers through the resident graph
+static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, const Stencil& st,
+                            bool mixed, bool mg) {
+    const int cur = c->cur;
+    const int flags = (mixed ? 1 : 0) | (mg ? 2 : 0);
+    int rc = CF_OK;
+    if (!c->rgx[cur] || c->rg_flags[cur] != flags || std::memcmp(&c->rg_st[cur], &st, sizeof(Stencil)) != 0 ||
+        std::memcmp(&c->rg_ph[cur], &c->ph, sizeof(Phys)) != 0) {
+        rc = build_resident(c, st, dt, mixed, mg, cur);
+        if (rc) return rc;
+        c->rg_flags[cur] = flags;
+        c->rg_st[cur] = st;
+        c->rg_ph[cur] = c->ph;
+    }
+    SolverState* h = c->hS;
+    memset(h, 0, sizeof(SolverState));
+    h->tol2 = o.tol * o.tol;
+    h->abs2 = o.abs_tol * o.abs_tol;
+    h->use_abs = o.abs_tol > 0.0 ? 1 : 0;
+    h->area = c->ph.dx * c->ph.dx;
+    h->max_iter = o.max_iter;
+    h->max_outer = o.max_outer;
+    h->inner_tol2 = o.inner_tol * o.inner_tol;
+    h->status = ST_RUNNING;
+    const int batch = mg ? kResidentBatchMG : kResidentBatch;
+    h->trip_limit = (o.max_iter + (mixed ? o.max_outer : 0)) / batch + 4;
+    cudaMemcpyAsync(c->S, h, sizeof(SolverState), cudaMemcpyHostToDevice, c->stream);
+    if ((rc = cuda_check(c, cudaGraphLaunch(c->rgx[cur], c->stream), "graph launch"))) return rc;
+    if ((rc = cuda_check(c, cudaStreamSynchronize(c->stream), "projection"))) return rc;
+    const SolverState* hs = c->hS;
+    c->launches += c->rg_head[cur] + (long long)c->rg_trip[cur] * (hs->trips + 1) + c->rg_tail[cur];
+    res->iterations = hs->iter;
+    res->outer = hs->outer_iter;
+    res->status = hs->status == ST_RUNNING ? ST_MAXIT : hs->status;
+    res->bb = hs->bb;
+    res->rr = hs->rr;
+    res->div_l2 = sqrt(c->h_out[0]) * c->ph.dx;
+    res->div_linf = c->h_out[1];
+    return CF_OK;
+}
+
 int div_norms(cf_ctx* c, double* l2, double* linf) {
     Stencil st{};
     DivArgs a = div_args(c, st);
@@ -971,12 +1172,17 @@ int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res) {
 // applied after the gradient subtraction (see cf_adjoint.cu).
 int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Grid<double> gu, Grid<double> gv,
                   int adjoint) {
-    Stencil st;
+    Stencil st{};
     build_stencil(c, dt, o.precon_none, &st);
     const bool mixed = c->precision == CF_PREC_MIXED;
     const bool mg = o.precon_mg != 0;
     int rc = mg ? mg_setup(c) : CF_OK;
-    if (!rc) rc = mg ? ensure_graph_mg(c, st) : ensure_graph(c, st, mixed);
+    if (rc) return rc;
+    // the resident graph serves plain projections; the adjoint's projection
+    // (other arrays) and profiled runs (events between batches) take the
+    // host-polled batches below
+    if (!adjoint && !c->prof && resident_enabled()) return project_resident(c, dt, o, res, st, mixed, mg);
+    rc = mg ? ensure_graph_mg(c, st) : ensure_graph(c, st, mixed);
     if (rc) return rc;
 
     // solver parameters
