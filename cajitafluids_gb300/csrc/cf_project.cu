@@ -961,7 +961,7 @@ static int read_state(cf_ctx* c) {
 //   tail : [mixed: double-float x to FP64], gradient subtraction, ||div u||,
 //          copies of the solver state and the norms to pinned host memory
 static const int kResidentBatch = 16;    // Jacobi-PCG iterations per trip
-static const int kResidentBatchMG = 2;   // MG-PCG iterations per trip
+static const int kResidentBatchMG = 1;   // MG-PCG iterations per trip
 
 __global__ void k_loop_cond(SolverState* S, cudaGraphConditionalHandle h) {
     int run = *(volatile int*)&S->status == ST_RUNNING;
@@ -987,12 +987,17 @@ static int launch_iterations(cf_ctx* c, const Stencil& st, bool mixed, bool mg, 
     }
     for (int i = 0; i < n; ++i) {
         if (mixed) {
+            // MG: a reliable update follows almost every iteration, so the
+            // gated outer kernels sit in every iteration; Jacobi: once a trip
             if (mg)
                 cg32_launch_pair_mg(c, st);
             else
                 cg32_launch_iteration(c, st);
-            launch_outer(c, st, 1);
-            k += 4;
+            k += 2;
+            if (mg || i == n - 1) {
+                launch_outer(c, st, 1);
+                k += 2;
+            }
             if (mg) k += cg32_mg_precondition(c, scale);
         } else {
             k_cg_dir_matvec64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);

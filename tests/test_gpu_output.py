@@ -48,13 +48,13 @@ def test_cell_velocity_matches_oracle(built, nx, ny, periodic, precision):
     xy = cell_centres(nx, ny, c.dx)
     assert np.array_equal(uc.ravel(), o.sample("u", 1, xy))
     assert np.array_equal(vc.ravel(), o.sample("v", 1, xy))
-    # a uniform flow is reproduced at every cell centre; the last row (u) and
-    # column (v) also touch a wall's zero ghosts with a weight that is zero
-    # up to the rounding of the cell-centre coordinate
+    # a uniform flow is reproduced at every cell centre; cells next to a wall
+    # also touch its zero ghosts, with a weight that is zero only up to the
+    # rounding of the cell-centre coordinate
     for f, val in (("u", 0.75), ("v", -1.25)):
         c.upload(f, np.full(o.shape(f), val))
     uc, vc = c.cell_velocity()
-    assert np.all(uc[:-1, :] == 0.75) and np.all(vc[:, :-1] == -1.25)
+    assert np.all(uc[1:-1, 1:-1] == 0.75) and np.all(vc[1:-1, 1:-1] == -1.25)
     assert np.allclose(uc, 0.75, rtol=1e-14) and np.allclose(vc, -1.25, rtol=1e-14)
 
 
