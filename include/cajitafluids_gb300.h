@@ -224,10 +224,14 @@ void* cf_stream(const cf_ctx* ctx);
 int cf_timer_start(cf_ctx* ctx);
 int cf_timer_stop(cf_ctx* ctx, double* ms);
 
-/* Device-time profile kept by the context while enabled.  The CG solver
- * runs in CUDA-graph batches of CF_CG_BATCH iterations; only batches in
- * which every iteration ran are counted, so solve_ms / solve_iters is the
- * device time of one CG iteration (both kernels). */
+/* Device-time profile kept by the context while enabled.  A projection
+ * normally runs as one device-resident CUDA graph (the PCG iterations in a
+ * conditional loop on the device, one host synchronisation per projection).
+ * While profiling is enabled it runs instead in host-polled CUDA-graph batches
+ * (CF_CG_BATCH Jacobi-PCG or 4 multigrid-PCG iterations) with CUDA events
+ * around each; only batches in which every iteration ran are counted, so
+ * solve_ms / solve_iters is the device time of one PCG iteration (all its
+ * kernels).  The two forms compute the same results. */
 #define CF_CG_BATCH 32
 typedef struct {
     double solve_ms;
