@@ -47,6 +47,9 @@ KERNEL_BYTES_MIXED_ITER = 32.0
 # count.  Measured by this bench's FP64 leg on GB300.
 FP64_ITERS_PER_STEP_4096 = 7890
 MG_NAMES = ("PFMG", "SMG", "MG")
+# DRAM bytes (read + write) of one mixed MG-PCG inner iteration at 4096^2,
+# from an ncu capture of this bench (profiles/traffic_4096_mixed_mg.md)
+MEASURED_TRAFFIC_MG_ITER_4096 = 1.39e9
 
 
 def mg_levels(nx, ny, periodic):
@@ -326,7 +329,11 @@ def bench_gb300(args, rank, world, dist, device):
                       "project_ms_per_step": prof["project_ms"] / max(prof["projects"], 1)},
             "roofline": {"bound": "hbm", "kernel": kname,
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "peak_source": f"hbm_gbs {peak_kind}", "traffic": None,
+                         "peak_source": f"hbm_gbs {peak_kind}",
+                         "traffic": MEASURED_TRAFFIC_MG_ITER_4096 if (mg and w.nx == 4096) else None,
+                         "traffic_source": "ncu dram__bytes_read+write per iteration, "
+                                           "profiles/traffic_4096_mixed_mg.md" if (mg and w.nx == 4096) else None,
+                         "algorithmic_bytes": it_bytes,
                          "algorithmic_bytes_per_cell": it_bytes / ncell, **kern_extra},
             "gpu_launches": launches, "clocks": clk,
             "timing": {"device_ms": ms, "wall_s": t_wall, "workload_gen_s": t_gen},
