@@ -369,6 +369,23 @@ def bench_gb300(args, rank, world, dist, device):
                 h.free()
         cm.close()
 
+    if "warm" in legs and "mixed" in legs:
+        # the same workload with warm-started projections (extension; the
+        # reference cold-starts): steps/s and iterations per step
+        cw = make_context(w, "mixed", device)
+        cw.set_warm_start(True)
+        run_steps(cw, w, args.warmup)
+        wst = []
+        nwarm = min(args.steps, 100)
+        cw.timer_start()
+        run_steps(cw, w, nwarm, wst)
+        msw = cw.timer_stop()
+        cw.close()
+        line["warm_start"] = {"steps_per_s": nwarm / (msw / 1e3),
+                              "cg_inner_iters_per_step": statistics.mean(s["iterations"] for s in wst),
+                              "outer_refinements_per_step": statistics.mean(s["outer_iterations"] for s in wst),
+                              "div_l2_max": max(s["div_l2"] for s in wst), "steps": nwarm}
+
     fstats = []
     k64 = None
     if "fp64" in legs:
@@ -549,8 +566,8 @@ def main():
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--legs", default="mixed,e2e,fp64,adjoint,cpu",
-                    help="comma list of legs to run: mixed (headline), e2e, fp64, adjoint, cpu")
+    ap.add_argument("--legs", default="mixed,e2e,warm,fp64,adjoint,cpu",
+                    help="comma list of legs to run: mixed (headline), e2e, warm, fp64, adjoint, cpu")
     ap.add_argument("--adjoint-size", type=int, default=512)
     ap.add_argument("--adjoint-steps", type=int, default=200)
     ap.add_argument("--adjoint-every", type=int, default=14)

@@ -116,6 +116,7 @@ SIGNATURES = {
     "cf_set_source": (ctypes.c_int, [_vp, _dp, _dp, _dp, ctypes.c_double, ctypes.c_int]),
     "cf_set_body_force": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),
     "cf_set_density": (ctypes.c_int, [_vp, ctypes.c_double]),
+    "cf_set_warm_start": (ctypes.c_int, [_vp, ctypes.c_int]),
     "cf_set_quirks": (ctypes.c_int, [_vp, ctypes.c_uint]),
     "cf_upload": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _pd, _pd]),
     "cf_download": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _pd, _pd]),

@@ -115,6 +115,10 @@ class Context:
     def set_density(self, density: float):
         self._check(self.lib.cf_set_density(self.h, float(density)))
 
+    def set_warm_start(self, on: bool = True):
+        """Start each projection from the previous pressure (extension)."""
+        self._check(self.lib.cf_set_warm_start(self.h, int(bool(on))))
+
     def set_quirks(self, flags: int):
         self._check(self.lib.cf_set_quirks(self.h, int(flags)))
 

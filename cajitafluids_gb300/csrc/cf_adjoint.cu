@@ -358,6 +358,9 @@ int load_state(cf_ctx* c, const double* src) {
 AdjState* adj(cf_ctx* c) { return static_cast<AdjState*>(c->adjoint); }
 
 int check_supported(cf_ctx* c) {
+    // a recomputed segment must repeat the forward exactly; a warm start
+    // would depend on a pressure the checkpoints do not hold
+    if (c->warm) return fail(c, CF_ERR_UNSUPPORTED, "the adjoint needs cold-started projections (warm start is on)");
     const Phys& p = c->ph;
     if (c->precision != CF_PREC_FP64) return fail(c, CF_ERR_UNSUPPORTED, "the adjoint runs on FP64 contexts");
     bool src_active = p.bbox[2] > p.bbox[0] && p.bbox[3] > p.bbox[1];
@@ -512,6 +515,8 @@ int cf_forward_checkpointed(cf_ctx* ctx, int nsteps, int ckpt_every, double dt, 
     if (nsteps <= 0 || ckpt_every <= 0 || !(dt > 0.0) || (value_order != 1 && value_order != 3))
         return fail(ctx, CF_ERR_INVALID, "bad forward_checkpointed arguments");
     if (ctx->precision != CF_PREC_FP64) return fail(ctx, CF_ERR_UNSUPPORTED, "the adjoint runs on FP64 contexts");
+    if (ctx->warm)
+        return fail(ctx, CF_ERR_UNSUPPORTED, "the adjoint needs cold-started projections (warm start is on)");
     cudaSetDevice(ctx->device);
     if (!ctx->adjoint) ctx->adjoint = new AdjState();
     AdjState* A = adj(ctx);

@@ -392,6 +392,12 @@ int cf_set_body_force(cf_ctx* ctx, const double force[2], int density_scaled) {
     return CF_OK;
 }
 
+int cf_set_warm_start(cf_ctx* ctx, int on) {
+    if (!ctx) return CF_ERR_INVALID;
+    ctx->warm = on ? 1 : 0;
+    return CF_OK;
+}
+
 int cf_set_density(cf_ctx* ctx, double density) {
     if (!ctx) return CF_ERR_INVALID;
     if (!(density > 0.0) || !isfinite(density)) return fail(ctx, CF_ERR_INVALID, "density must be positive");

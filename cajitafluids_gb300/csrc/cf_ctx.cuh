@@ -14,6 +14,7 @@ struct cf_ctx {
     cf::Phys ph{};
     int precision = 0;
     double density = 1.0;
+    int warm = 0;  // start each projection from the previous pressure (cf_set_warm_start)
 
     // fields, two versions each (src/ProblemManager.hpp:143-165); index cur is Current
     cf::Grid<double> q64[2]{}, u[2]{}, v[2]{};

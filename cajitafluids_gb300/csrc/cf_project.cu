@@ -278,6 +278,71 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_mg_rz64(Cg64 a, int init) {
     }
 }
 
+// Warm start (FP64): r = b - A x from the previous solution, with A x in the
+// matvec's order (diag x_C, then the W, E, S, N legs), canonical r.z and r.r,
+// and the solver state as the cold init sets it (||b||^2 from k_div_init64).
+__global__ void __launch_bounds__(CF_RED_THREADS) k_warm_resid64(Cg64 a) {
+    SolverState* S = a.S;
+    const int lane = threadIdx.x & 31;
+    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
+    const double ms = a.st.ms;
+    double arz = 0.0, arr = 0.0;
+    if (unit < a.U) {
+        const int g = unit % a.G, band = unit / a.G;
+        const int c0 = g * CF_UNIT_COLS + 2 * lane;
+        const int j0 = band * CF_BAND_ROWS;
+        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
+        auto xv = [&](int c, int j) -> double {
+            int cc = wrap_index(c, a.nx, a.per_x), jj = wrap_index(j, a.ny, a.per_y);
+            if (cc < 0 || jj < 0) return 0.0;
+            return a.x[(size_t)jj * a.pitch + cc];
+        };
+        for (int j = j0; j < j1; ++j)
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                const int c = c0 + s;
+                if (c >= a.nx) continue;
+                const int eb = ebits(a, c, j);
+                double ax = a.st.diag[eb] * xv(c, j);
+                ax = fma(ms, xv(c - 1, j), ax);
+                ax = fma(ms, xv(c + 1, j), ax);
+                ax = fma(ms, xv(c, j - 1), ax);
+                ax = fma(ms, xv(c, j + 1), ax);
+                const size_t k = (size_t)j * a.pitch + c;
+                const double r = a.r[k] - ax;
+                a.r[k] = r;
+                const double z = a.st.minv[eb] * r;
+                arz = fma(r, z, arz);
+                arr = fma(r, r, arr);
+            }
+    }
+    arz = warp_fold(arz);
+    arr = warp_fold(arr);
+    if (unit < a.U && lane == 0) {
+        a.part0[unit] = arz;
+        a.part1[unit] = arr;
+    }
+    if (last_block_arrive(&S->ticket[3])) {
+        double rz = final_tree(a.part0, a.U);
+        double rr = final_tree(a.part1, a.U);
+        if (threadIdx.x == 0) {
+            S->ticket[3] = 0;
+            S->rr = rr;
+            S->rho = rz;
+            S->beta = 0.0;
+            S->iter = 0;
+            if (S->bb == 0.0 || converged(S, rr))
+                S->status = ST_CONVERGED;
+            else if (S->max_iter <= 0)
+                S->status = ST_MAXIT;
+            else if (isnan(rr))
+                S->status = ST_NAN;
+            else
+                S->status = ST_RUNNING;
+        }
+    }
+}
+
 // --------------------------------------------------------------------------
 // Divergence: b = -(1/dx) (u(i+1) - u(i) + v(j+1) - v(j))  (:204-210)
 struct DivArgs {
@@ -290,6 +355,7 @@ struct DivArgs {
     double *part0, *part1, *part2;
     double* out;
     SolverState* S;
+    int warm;  // keep x from the previous solve (warm start) instead of x = 0
 };
 
 __device__ __forceinline__ double div_b(const DivArgs& a, int gi, int gj) {
@@ -380,7 +446,7 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init64(DivArgs a) {
                 double b = div_b(a, c, j);
                 size_t k = (size_t)j * a.pitch + c;
                 a.r[k] = b;
-                a.x[k] = 0.0;
+                if (!a.warm) a.x[k] = 0.0;
                 double z = a.st.minv[edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y)] * b;
                 arz = fma(b, z, arz);
                 arr = fma(b, b, arr);
@@ -435,7 +501,9 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
                 double b = div_b(a, c, j);
                 size_t k = (size_t)j * a.pitch + c;
                 reinterpret_cast<float2*>(a.b)[k] = df_split(b);
-                reinterpret_cast<float2*>(a.x)[k] = make_float2(0.f, 0.f);
+                // x as a double-float pair: 0, or (warm start) the previous
+                // FP64 solution split in place (same 8 bytes per cell)
+                reinterpret_cast<float2*>(a.x)[k] = a.warm ? df_split(a.x[k]) : make_float2(0.f, 0.f);
                 float r = (float)b;
                 put_r32(a.r32, a.pitch32, a.nx, a.ny, a.per_x, a.per_y, c, j, r);
                 a.e32[(ptrdiff_t)j * a.pitch32 + c] = 0.f;
@@ -832,6 +900,19 @@ static Outer outer_args(cf_ctx* c, const Stencil& st, int gated) {
     return oa;
 }
 
+// warm start: the initial residual from the previous solution (after the
+// divergence kernel), FP64 or double-float; returns kernels launched
+static int launch_warm_init(cf_ctx* c, const Stencil& st, bool mixed) {
+    if (mixed) {
+        Outer oa = outer_args(c, st, 0);
+        k_outer_resid<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(oa);
+    } else {
+        Cg64 a = cg64_args(c, st);
+        k_warm_resid64<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(a);
+    }
+    return 1;
+}
+
 // the two outer-refinement kernels; gated = 1 inside the MG-PCG graph
 static void launch_outer(cf_ctx* c, const Stencil& st, int gated) {
     Outer oa = outer_args(c, st, gated);
@@ -1031,11 +1112,13 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
             DivArgs da = div_args(c, st);
             da.u = gu;
             da.v = gv;
+            da.warm = c->warm;
             if (mixed)
                 k_div_init_mixed<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
             else
                 k_div_init64<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
             nhead = 1;
+            if (c->warm) nhead += launch_warm_init(c, st, mixed);
             if (mg) {
                 if (mixed) {
                     nhead += cg32_mg_precondition(c, scale);
@@ -1118,7 +1201,7 @@ static bool resident_enabled() {
 static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, const Stencil& st,
                             bool mixed, bool mg) {
     const int cur = c->cur;
-    const int flags = (mixed ? 1 : 0) | (mg ? 2 : 0);
+    const int flags = (mixed ? 1 : 0) | (mg ? 2 : 0) | (c->warm ? 4 : 0);
     int rc = CF_OK;
     if (!c->rgx[cur] || c->rg_flags[cur] != flags || std::memcmp(&c->rg_st[cur], &st, sizeof(Stencil)) != 0 ||
         std::memcmp(&c->rg_ph[cur], &c->ph, sizeof(Phys)) != 0) {
@@ -1206,10 +1289,13 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     DivArgs da = div_args(c, st);
     da.u = gu;
     da.v = gv;
+    const bool warm = c->warm && !adjoint;
+    da.warm = warm;
     if (c->prof) cudaEventRecord(c->ev[4], c->stream);
     if (!mixed) {
         k_div_init64<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
         c->launches += 1;
+        if (warm) c->launches += launch_warm_init(c, st, false);
         const int batch = mg ? kBatchMG : kBatch;
         cudaGraphExec_t ge = mg ? c->gmg : c->g64;
         const int per_batch = mg ? c->gmg_per_iter * kBatchMG : 2 * kBatch;
@@ -1233,6 +1319,7 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     } else {
         k_div_init_mixed<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
         c->launches += 1;
+        if (warm) c->launches += launch_warm_init(c, st, true);
         if (mg) {
             // MG-PCG: the reliable updates run inside the graph (gated
             // kernels), so the host only polls the status between batches

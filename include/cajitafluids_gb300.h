@@ -149,6 +149,12 @@ int cf_set_source(cf_ctx* ctx, const double location[2], const double size[2],
 int cf_set_body_force(cf_ctx* ctx, const double force[2], int density_scaled);
 /* density used by the VelocityCorrector (src/VelocityCorrector.hpp:72-76) */
 int cf_set_density(cf_ctx* ctx, double density);
+/* Extension: on != 0 starts each projection from the previous pressure (r =
+ * b - A p_prev) instead of the reference's cold start x0 = 0
+ * (src/VelocityCorrector.hpp:272).  Fewer iterations per step; the result
+ * differs from the cold start within the solver tolerance.  The adjoint
+ * (cf_forward_checkpointed / cf_backward) returns CF_ERR_UNSUPPORTED while on. */
+int cf_set_warm_start(cf_ctx* ctx, int on);
 int cf_set_quirks(cf_ctx* ctx, unsigned flags);
 
 /* ---- state (ProblemManager::get / initialize / advance) ---- */

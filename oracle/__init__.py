@@ -28,7 +28,7 @@ class OrcParams(ctypes.Structure):
         ("src_velocity", ctypes.c_double * 2), ("src_mode", ctypes.c_int),
         ("body_force", ctypes.c_double * 2), ("body_density_scaled", ctypes.c_int),
         ("density", ctypes.c_double), ("quirks", ctypes.c_uint), ("precon_none", ctypes.c_int),
-        ("precon_mg", ctypes.c_int),
+        ("precon_mg", ctypes.c_int), ("warm_start", ctypes.c_int),
     ]
 
 
@@ -98,7 +98,7 @@ class Oracle:
 
     def __init__(self, nx, ny, lo=(0.0, 0.0), hi=(1.0, 1.0), periodic=(False, False), bc=(0, 0, 0, 0),
                  source=None, source_mode=0, body=(0.0, 0.0), body_density_scaled=False, density=1.0,
-                 quirks=0, precon_none=False, precon_mg=False):
+                 quirks=0, precon_none=False, precon_mg=False, warm_start=False):
         p = OrcParams()
         p.nx, p.ny = int(nx), int(ny)
         p.lo[:] = list(lo)
@@ -117,6 +117,7 @@ class Oracle:
         p.quirks = int(quirks)
         p.precon_none = int(bool(precon_none))
         p.precon_mg = int(bool(precon_mg))
+        p.warm_start = int(bool(warm_start))
         err = ctypes.create_string_buffer(256)
         self.lib = lib()
         self.h = self.lib.orc_create(ctypes.byref(p), err, 256)

@@ -856,7 +856,7 @@ static int project_mg(orc_state* st, double scale, double tol, double abs_tol, i
     mg_level lev[MG_MAX];
     int nlev = mg_build(st, scale, lev);
     double rr = canon_dot_buf(nx, ny, st->r, st->r, st->partial);
-    double bb = rr, rho = 0.0, beta = 0.0;
+    double bb = canon_dot_buf(nx, ny, st->rhs, st->rhs, st->partial), rho = 0.0, beta = 0.0;
     double tol2 = tol * tol, abs2 = abs_tol * abs_tol;
     int k = 0, status = 0;
 #define MG_CONVERGED(rr) ((rr) <= tol2 * bb || (abs_tol > 0.0 && (rr) * area <= abs2))
@@ -915,18 +915,28 @@ int orc_mg_apply(orc_state* st, double dt, const double* r, double* z) {
  * 158-180, 266-282; Cajita ReferenceConjugateGradient restated).  Stops
  * when ||r||^2 <= tol^2 ||b||^2, or ||r||^2 dx^2 <= abs_tol^2 when
  * abs_tol > 0, checked before each iteration. */
-int orc_project(orc_state* st, double dt, double tol, double abs_tol, int max_iter,
-                orc_solve_stats* stats) {
-    if (st->p.precon_mg) {
-        int nx = st->p.nx, ny = st->p.ny;
-        size_t n = (size_t)nx * ny;
-        double scale = dt / ((st->p.density * st->dx) * st->dx);
-        build_diag(st, dt);
-        divergence(st, st->rhs);
+/* initial residual: cold start x0 = 0, r = b (src/VelocityCorrector.hpp:272);
+ * warm start (extension) keeps x from the previous solve, r = b - A x */
+static void initial_residual(orc_state* st, double scale) {
+    size_t n = (size_t)st->p.nx * st->p.ny;
+    if (st->p.warm_start) {
+        matvec(st, scale, st->x, st->qv);
+        for (size_t k = 0; k < n; ++k) st->r[k] = st->rhs[k] - st->qv[k];
+    } else {
         for (size_t k = 0; k < n; ++k) {
             st->r[k] = st->rhs[k];
             st->x[k] = 0.0;
         }
+    }
+}
+
+int orc_project(orc_state* st, double dt, double tol, double abs_tol, int max_iter,
+                orc_solve_stats* stats) {
+    if (st->p.precon_mg) {
+        double scale = dt / ((st->p.density * st->dx) * st->dx);
+        build_diag(st, dt);
+        divergence(st, st->rhs);
+        initial_residual(st, scale);
         int iters = 0;
         double bb = 0.0, rr = 0.0;
         int status = project_mg(st, scale, tol, abs_tol, max_iter, &iters, &bb, &rr);
@@ -946,15 +956,12 @@ int orc_project(orc_state* st, double dt, double tol, double abs_tol, int max_it
     double area = st->dx * st->dx;
     build_diag(st, dt);
     divergence(st, st->rhs);
+    initial_residual(st, scale);
 #pragma omp parallel for schedule(static)
-    for (size_t k = 0; k < n; ++k) {
-        st->r[k] = st->rhs[k];
-        st->x[k] = 0.0;
-        st->z[k] = st->minv[k] * st->r[k];
-    }
+    for (size_t k = 0; k < n; ++k) st->z[k] = st->minv[k] * st->r[k];
     double rho = canon_dot_buf(nx, ny, st->r, st->z, st->partial);
     double rr = canon_dot_buf(nx, ny, st->r, st->r, st->partial);
-    double bb = rr;
+    double bb = canon_dot_buf(nx, ny, st->rhs, st->rhs, st->partial);
     double beta = 0.0;
     int k = 0, status = 0;
     double tol2 = tol * tol, abs2 = abs_tol * abs_tol;

@@ -40,6 +40,7 @@ typedef struct {
     unsigned quirks;         /* bit 0: fix Q1, bit 1: fix Q3 */
     int precon_none;         /* 1: unpreconditioned CG ("PCG" + "None") */
     int precon_mg;           /* 1: geometric multigrid V-cycle preconditioner */
+    int warm_start;          /* extension: start each solve from the previous pressure */
 } orc_params;
 
 typedef struct {

@@ -11,13 +11,13 @@ FIELDS = ("q", "u", "v")
 
 def make_pair(nx, ny, periodic=(False, False), bc=(0, 0, 0, 0), source=None, source_mode=0, body=(0.0, 0.0),
               body_density_scaled=False, density=0.1, quirks=0, precision="fp64", lo=(0.0, 0.0), hi=None,
-              precon_none=False, precon_mg=False):
+              precon_none=False, precon_mg=False, warm_start=False):
     from oracle import Oracle
     if hi is None:
         hi = (lo[0] + 1.0, lo[1] + ny / nx)
     o = Oracle(nx, ny, lo=lo, hi=hi, periodic=periodic, bc=bc, source=source, source_mode=source_mode, body=body,
                body_density_scaled=body_density_scaled, density=density, quirks=quirks, precon_none=precon_none,
-               precon_mg=precon_mg)
+               precon_mg=precon_mg, warm_start=warm_start)
     c = Context(nx, ny, lo=lo, hi=hi, periodic=periodic, precision=precision)
     c.set_bc(bc)
     if source is not None:
@@ -25,6 +25,8 @@ def make_pair(nx, ny, periodic=(False, False), bc=(0, 0, 0, 0), source=None, sou
     c.set_body_force(body, body_density_scaled)
     c.set_density(density)
     c.set_quirks(quirks)
+    if warm_start:
+        c.set_warm_start(True)
     return o, c
 
 
