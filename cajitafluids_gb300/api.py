@@ -188,6 +188,29 @@ class Context:
         return self._solve_call(self.lib.cf_step, ctypes.c_double(dt), ctypes.c_int(order), opts=opts,
                                 raise_on_maxit=raise_on_maxit)
 
+    def step_host(self, dt: float, order: int, opts: Optional[SolverOptions], q_in, u_in, v_in, q_out=None,
+                  u_out=None, v_out=None, raise_on_maxit=False) -> dict:
+        """cf_step_host: upload q, u, v, one step, download into the outputs
+        (owned shapes, C order, float64; page-locked arrays copy fastest)."""
+        shapes = (self.owned_shape("q"), self.owned_shape("u"), self.owned_shape("v"))
+        ins = []
+        for a, shp in zip((q_in, u_in, v_in), shapes):
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            if a.shape != shp:
+                raise ValueError(f"expected shape {shp}, got {a.shape}")
+            ins.append(a)
+        outs = []
+        for a, shp in zip((q_out, u_out, v_out), shapes):
+            if a is not None and (a.shape != shp or a.dtype != np.float64 or not a.flags.c_contiguous):
+                raise ValueError(f"output must be a C-contiguous float64 array of shape {shp}")
+            outs.append(_dptr(a) if a is not None else None)
+        o = (opts or SolverOptions()).to_c()
+        st = L.SolveStats()
+        allow = () if raise_on_maxit else (L.CF_ERR_NOT_CONVERGED,)
+        self._check(self.lib.cf_step_host(self.h, ctypes.c_double(dt), ctypes.c_int(order), ctypes.byref(o),
+                                          ctypes.byref(st), *[_dptr(a) for a in ins], *outs), allow=allow)
+        return st.as_dict()
+
     # -- adjoint ----------------------------------------------------------------
     def forward_checkpointed(self, nsteps: int, ckpt_every: int, dt: float, order: int = 3,
                              opts: Optional[SolverOptions] = None) -> dict:

@@ -324,6 +324,11 @@ int cf_ctx_destroy(cf_ctx* ctx) {
     for (void* p : ctx->allocs) cudaFree(p);
     if (ctx->hS) cudaFreeHost(ctx->hS);
     if (ctx->h_out) cudaFreeHost(ctx->h_out);
+    if (ctx->stream2) {
+        cudaStreamSynchronize(ctx->stream2);
+        cudaStreamDestroy(ctx->stream2);
+    }
+    if (ctx->ev_adv) cudaEventDestroy(ctx->ev_adv);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return CF_OK;
@@ -594,6 +599,102 @@ int cf_step(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* opts,
     if (!rc && !fuse) rc = cuda_check(ctx, launch_add_inputs(ctx, dt), "add inputs");
     if (rc) return rc;
     return do_project(ctx, dt, opts, stats);
+    CF_GUARD_END
+}
+
+// Solver::step with host buffers in and out (owned arrays, x fastest,
+// contiguous).  Every copy is asynchronous on the context streams; the
+// quantity, final after the advection, is copied out on a second stream while
+// the projection runs; one synchronisation at the end.
+int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* opts, cf_solve_stats* stats,
+                 const double* q_in, const double* u_in, const double* v_in, double* q_out, double* u_out,
+                 double* v_out) {
+    if (!ctx || !q_in || !u_in || !v_in) return CF_ERR_INVALID;
+    if (value_order != 1 && value_order != 3) return fail(ctx, CF_ERR_INVALID, "value_order must be 1 or 3");
+    if (!(dt > 0.0) || !isfinite(dt)) return fail(ctx, CF_ERR_INVALID, "dt must be positive and finite");
+    CF_GUARD_BEGIN
+    cudaSetDevice(ctx->device);
+    SolveOpts so{};
+    int rc = parse_opts(ctx, opts, &so);
+    if (rc) return rc;
+    const bool mixed = ctx->precision == CF_PREC_MIXED;
+    const int nx = ctx->ph.nx, ny = ctx->ph.ny;
+    if (!ctx->stream2) {
+        rc = cuda_check(ctx, cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking), "stream create");
+        if (!rc) rc = cuda_check(ctx, cudaEventCreateWithFlags(&ctx->ev_adv, cudaEventDisableTiming), "event create");
+        if (!rc && mixed) rc = alloc_dev(ctx, ctx->staging2, (size_t)nx * ny);
+        if (rc) return rc;
+    }
+    // uploads into the current buffers
+    const int s0 = ctx->cur;
+    const double* ins[3] = {q_in, u_in, v_in};
+    for (int f = 0; f < 3 && !rc; ++f) {
+        int ox, oy;
+        owned(ctx, f, &ox, &oy);
+        if (f == CF_FIELD_QUANTITY && mixed) {
+            rc = cuda_check(ctx, cudaMemcpyAsync(ctx->staging, ins[f], sizeof(double) * (size_t)ox * oy,
+                                                 cudaMemcpyDefault, ctx->stream), "upload");
+            if (!rc) rc = cuda_check(ctx, launch_convert_q(ctx, 1, s0), "convert");
+        } else {
+            Grid<double> g = f == CF_FIELD_QUANTITY ? ctx->q64[s0] : (f == CF_FIELD_U ? ctx->u[s0] : ctx->v[s0]);
+            rc = cuda_check(ctx, cudaMemcpy2DAsync(&g.at(CF_HALO, CF_HALO), g.pitch * sizeof(double), ins[f],
+                                                   ox * sizeof(double), ox * sizeof(double), oy, cudaMemcpyDefault,
+                                                   ctx->stream),
+                            "upload");
+        }
+    }
+    // advection and inputs (src/Solver.hpp:135-147)
+    const bool fuse = !ctx->ph.force_density;
+    if (!rc) rc = cuda_check(ctx, launch_fill_ghosts(ctx), "fill ghosts");
+    if (!rc) rc = cuda_check(ctx, launch_advect(ctx, dt, value_order, fuse ? 1 : 0), "advect");
+    if (!rc && !fuse) rc = cuda_check(ctx, launch_add_inputs(ctx, dt), "add inputs");
+    if (rc) return rc;
+    const int s1 = ctx->cur;
+    // the quantity is final now: copy it out beside the projection
+    if (q_out) {
+        rc = cuda_check(ctx, cudaEventRecord(ctx->ev_adv, ctx->stream), "event");
+        if (!rc) rc = cuda_check(ctx, cudaStreamWaitEvent(ctx->stream2, ctx->ev_adv, 0), "event wait");
+        if (!rc && mixed) {
+            rc = cuda_check(ctx, launch_q_to_f64(ctx, s1, ctx->staging2, ctx->stream2), "convert");
+            if (!rc)
+                rc = cuda_check(ctx, cudaMemcpyAsync(q_out, ctx->staging2, sizeof(double) * (size_t)nx * ny,
+                                                     cudaMemcpyDefault, ctx->stream2), "download");
+        } else if (!rc) {
+            const Grid<double>& g = ctx->q64[s1];
+            rc = cuda_check(ctx, cudaMemcpy2DAsync(q_out, nx * sizeof(double), &g.at(CF_HALO, CF_HALO),
+                                                   g.pitch * sizeof(double), nx * sizeof(double), ny,
+                                                   cudaMemcpyDefault, ctx->stream2),
+                            "download");
+        }
+        if (rc) return rc;
+    }
+    SolveResult r{};
+    bool deferred = false;
+    rc = project_async(ctx, dt, so, &r, &deferred);
+    double* outs[3] = {nullptr, u_out, v_out};
+    for (int f = 1; f < 3 && !rc; ++f) {
+        if (!outs[f]) continue;
+        int ox, oy;
+        owned(ctx, f, &ox, &oy);
+        const Grid<double>& g = f == CF_FIELD_U ? ctx->u[s1] : ctx->v[s1];
+        rc = cuda_check(ctx, cudaMemcpy2DAsync(outs[f], ox * sizeof(double), &g.at(CF_HALO, CF_HALO),
+                                               g.pitch * sizeof(double), ox * sizeof(double), oy, cudaMemcpyDefault,
+                                               ctx->stream),
+                        "download");
+    }
+    int rc2 = cuda_check(ctx, cudaStreamSynchronize(ctx->stream2), "step_host");
+    int rc1 = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "step_host");
+    if (rc) return rc;
+    if (rc1) return rc1;
+    if (rc2) return rc2;
+    if (deferred) project_collect(ctx, &r);
+    fill_stats(r, stats);
+    rc = status_code(r.status);
+    if (rc == CF_ERR_NOT_CONVERGED)
+        fail(ctx, rc, "pressure solve stopped at max_iter (%d iterations)", r.iterations);
+    else if (rc)
+        fail(ctx, rc, "pressure solve failed (status %d) after %d iterations", r.status, r.iterations);
+    return rc;
     CF_GUARD_END
 }
 

@@ -49,6 +49,11 @@ struct cf_ctx {
     void* adjoint = nullptr;  // checkpoints and adjoint buffers (cf_adjoint.cu)
     void* mg = nullptr;       // multigrid hierarchy (cf_mg.cu)
     double* outbuf = nullptr; // 2 nx ny doubles for cf_cell_velocity, allocated on first use
+    // cf_step_host: a second stream for the quantity's download, which overlaps
+    // the projection, and its staging buffer (nx ny doubles), made on first use
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_adv = nullptr;
+    double* staging2 = nullptr;
     cudaGraphExec_t gmg = nullptr;      // batch of MG-PCG iterations
     cudaGraphExec_t gmg_pre = nullptr;  // V-cycle + r.z after the residual is (re)formed
     cf::Stencil gmg_st{};
@@ -59,6 +64,7 @@ struct cf_ctx {
     cf::Phys rg_ph[2]{};
     int rg_flags[2] = {-1, -1};
     int rg_head[2] = {0, 0}, rg_trip[2] = {0, 0}, rg_tail[2] = {0, 0};
+    int rg_pending = 0;  // buffer of the last resident projection launched
     // FP32 z = M^-1 r of the mixed MG-PCG, ghost ring as the other FP32 vectors
     cf::Vec32 z32{};
     float* z32b = nullptr;
@@ -87,6 +93,7 @@ cudaError_t launch_trace_points(cf_ctx* c, int n, const double* d_xy, double dt,
 cudaError_t launch_cell_velocity(cf_ctx* c, double* d_uc, double* d_vc);
 cudaError_t launch_max_velocity(cf_ctx* c, double* d_out);
 cudaError_t launch_convert_q(cf_ctx* c, int to_device, int version);
+cudaError_t launch_q_to_f64(cf_ctx* c, int version, double* dst, cudaStream_t stream);
 
 // projection (cf_project.cu)
 struct SolveOpts {
@@ -100,6 +107,11 @@ struct SolveResult {
     double bb, rr, div_l2, div_linf;
 };
 int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res);
+// project without the final synchronisation when the device-resident graph
+// serves it (*deferred = true; project_collect fills res after the caller has
+// synchronised the stream), else a plain project (*deferred = false)
+int project_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, bool* deferred);
+void project_collect(cf_ctx* c, SolveResult* res);
 int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Grid<double> gu, Grid<double> gv,
                   int adjoint);
 // FP32 TMA inner CG (cf_cg32.cu)

@@ -556,6 +556,13 @@ cudaError_t launch_max_velocity(cf_ctx* c, double* d_out) {
     return cudaGetLastError();
 }
 
+cudaError_t launch_q_to_f64(cf_ctx* c, int version, double* dst, cudaStream_t stream) {
+    dim3 blk(32, 8);
+    k_q_convert<<<grid2(c->ph.nx, c->ph.ny, blk), blk, 0, stream>>>(c->q32[version], dst, c->ph.nx, c->ph.ny, 0);
+    c->launches += 1;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_convert_q(cf_ctx* c, int to_device, int version) {
     dim3 blk(32, 8);
     k_q_convert<<<grid2(c->ph.nx, c->ph.ny, blk), blk, 0, c->stream>>>(c->q32[version], c->staging, c->ph.nx,

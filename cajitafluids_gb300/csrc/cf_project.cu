@@ -1197,9 +1197,10 @@ static bool resident_enabled() {
     return on != 0;
 }
 
-// the projection of the current buffers through the resident graph
+// the projection of the current buffers through the resident graph; with
+// defer, returns after the launch (project_collect reads the results)
 static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, const Stencil& st,
-                            bool mixed, bool mg) {
+                            bool mixed, bool mg, bool defer = false) {
     const int cur = c->cur;
     const int flags = (mixed ? 1 : 0) | (mg ? 2 : 0) | (c->warm ? 4 : 0);
     int rc = CF_OK;
@@ -1225,7 +1226,15 @@ static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResul
     h->trip_limit = (o.max_iter + (mixed ? o.max_outer : 0)) / batch + 4;
     cudaMemcpyAsync(c->S, h, sizeof(SolverState), cudaMemcpyHostToDevice, c->stream);
     if ((rc = cuda_check(c, cudaGraphLaunch(c->rgx[cur], c->stream), "graph launch"))) return rc;
+    c->rg_pending = cur;
+    if (defer) return CF_OK;
     if ((rc = cuda_check(c, cudaStreamSynchronize(c->stream), "projection"))) return rc;
+    project_collect(c, res);
+    return CF_OK;
+}
+
+void project_collect(cf_ctx* c, SolveResult* res) {
+    const int cur = c->rg_pending;
     const SolverState* hs = c->hS;
     c->launches += c->rg_head[cur] + (long long)c->rg_trip[cur] * (hs->trips + 1) + c->rg_tail[cur];
     res->iterations = hs->iter;
@@ -1235,7 +1244,19 @@ static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResul
     res->rr = hs->rr;
     res->div_l2 = sqrt(c->h_out[0]) * c->ph.dx;
     res->div_linf = c->h_out[1];
-    return CF_OK;
+}
+
+int project_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, bool* deferred) {
+    const bool mixed = c->precision == CF_PREC_MIXED;
+    const bool mg = o.precon_mg != 0;
+    *deferred = false;
+    if (c->prof || !resident_enabled()) return project(c, dt, o, res);
+    Stencil st{};
+    build_stencil(c, dt, o.precon_none, &st);
+    int rc = mg ? mg_setup(c) : CF_OK;
+    if (rc) return rc;
+    *deferred = true;
+    return project_resident(c, dt, o, res, st, mixed, mg, true);
 }
 
 int div_norms(cf_ctx* c, double* l2, double* linf) {

@@ -181,6 +181,18 @@ int cf_setup(cf_ctx* ctx, double dt, const cf_solver_opts* opts, cf_solve_stats*
  * is density scaled. */
 int cf_step(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* opts,
             cf_solve_stats* stats);
+/* Solver::step (as cf_step) with host buffers in and out: q_in, u_in, v_in
+ * are uploaded into the current state, one step runs, and the new q, u, v are
+ * written to q_out, u_out, v_out (any of the outputs may be NULL).  All six
+ * arrays are owned regions, x fastest, contiguous (element (i, j) at
+ * [j * ex + i], ex from cf_owned_extent).  Copies are asynchronous (page-locked
+ * buffers from cf_host_alloc give the full link bandwidth); q_out is copied on
+ * a second stream while the projection runs; the call returns after one final
+ * synchronisation, so the buffers are only touched during the call. */
+int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* opts, cf_solve_stats* stats,
+                 const double* q_in, const double* u_in, const double* v_in, double* q_out, double* u_out,
+                 double* v_out);
+
 /* divergence norms of the current velocity field */
 int cf_div_norms(cf_ctx* ctx, double* l2, double* linf);
 /* max |u|, |v| over owned faces (for CFL time steps) */
