@@ -640,16 +640,20 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
         const int c0 = g * CF_UNIT_COLS + 2 * lane;
         const int j0 = band * CF_BAND_ROWS;
         const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
-        float4 xm = xrow2(a, a.x, c0, j0 - 1), xc = xrow2(a, a.x, c0, j0);
+        // rows j - 1, j, j + 1 in registers; row j + 2 and b of row j + 1 are
+        // fetched one row ahead, so the loads overlap the arithmetic
+        float4 xm = xrow2(a, a.x, c0, j0 - 1), xc = xrow2(a, a.x, c0, j0), xp = xrow2(a, a.x, c0, j0 + 1);
+        float4 bnext = xrow2(a, a.b, c0, j0);
         for (int j = j0; j < j1; ++j) {
-            const float4 xp = xrow2(a, a.x, c0, j + 1);
+            const float4 xpp = xrow2(a, a.x, c0, j + 2);
+            const float4 bv = bnext;
+            if (j + 1 < j1) bnext = xrow2(a, a.b, c0, j + 1);
             float2 left = make_float2(__shfl_up_sync(FULLMASK, xc.z, 1), __shfl_up_sync(FULLMASK, xc.w, 1));
             float2 right = make_float2(__shfl_down_sync(FULLMASK, xc.x, 1), __shfl_down_sync(FULLMASK, xc.y, 1));
             if (lane == 0) left = xval(a, c0 - 1, j);
             if (lane == 31 || c0 + 2 >= a.nx) right = xval(a, c0 + 2, j);
             float2 mid1 = make_float2(xc.z, xc.w);
             if (c0 + 1 >= a.nx) mid1 = xval(a, c0 + 1, j);  // E neighbour of the last column
-            const float4 bv = xrow2(a, a.b, c0, j);
             if (c0 < a.nx) {
                 const int eb = edge_bits(c0, j, a.nx, a.ny, a.per_x, a.per_y);
                 const float2 r = df_resid(a, eb, make_float2(bv.x, bv.y), make_float2(xc.x, xc.y), left, mid1,
@@ -669,6 +673,7 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
             }
             xm = xc;
             xc = xp;
+            xp = xpp;
         }
     }
     double drz = warp_fold((double)arz), drr = warp_fold((double)arr);
