@@ -328,30 +328,32 @@ __device__ __forceinline__ bool ft_interior(int nx, int ny, int i0, int j0) {
 template <typename T, int TW, int TH, int H>
 __device__ __forceinline__ void ft_load_int(const MgLev<T>& L, T* xs, T* bs, int i0, int j0, const T* xsrc) {
     constexpr int W = TW + 2 * H, HT = TH + 2 * H;
-    const size_t base = (size_t)(j0 - H) * L.pitch + (i0 - H);
-    for (int q = threadIdx.x; q < W * HT; q += FT_THREADS) {
-        const size_t k = base + (size_t)(q / W) * L.pitch + (q % W);
-        bs[q] = L.b[k];
-        xs[q] = xsrc ? xsrc[k] : T(0);
-    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const T* b = L.b + (size_t)(j0 - H) * L.pitch + (i0 - H);
+    const T* x = xsrc ? xsrc + (size_t)(j0 - H) * L.pitch + (i0 - H) : nullptr;
+    for (int lj = warp; lj < HT; lj += FT_THREADS / 32)
+        for (int li = lane; li < W; li += 32) {
+            const size_t k = (size_t)lj * L.pitch + li;
+            bs[lj * W + li] = b[k];
+            xs[lj * W + li] = x ? x[k] : T(0);
+        }
     __syncthreads();
 }
 
-// interior half sweep: warp w takes rows w, w + 8, ...; lane l the cells
-// 2l (+ 64) of the row's colour
+// interior half sweep: warp w takes rows w, w + 8, ... (all of one parity, so
+// a lane's cells of the colour sit in one column per row parity); lane l
+// takes the cells 2l (+ 64) of the row's colour
 template <typename T, int TW, int TH, int H>
 __device__ __forceinline__ void ft_half_int(const MgLev<T>& L, T* xs, const T* bs, int i0, int j0, int c, int h,
                                             bool first) {
-    constexpr int W = TW + 2 * H;
+    constexpr int W = TW + 2 * H, RS = FT_THREADS / 32;
     const int nrow = TH + 2 * h, hw = TW / 2 + h;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const T scale = L.scale, id0 = L.invd[0];
-    for (int rj = warp; rj < nrow; rj += FT_THREADS / 32) {
-        const int gj = j0 - h + rj;
-        const int off = (c + gj + i0 - h) & 1;
-        const int q0 = (rj + H - h) * W + (H - h) + off;
-        for (int pk = lane; pk < hw; pk += 32) {
-            const int q = q0 + 2 * pk;
+    const int off = (c + (j0 - h + warp) + i0 - h) & 1;  // rows step by RS (even): fixed parity
+    for (int pk = lane; pk < hw; pk += 32) {
+        int q = (warp + H - h) * W + (H - h) + off + 2 * pk;
+        for (int rj = warp; rj < nrow; rj += RS, q += RS * W) {
             T s;
             if (first) {
                 s = T(0);
@@ -367,13 +369,337 @@ __device__ __forceinline__ void ft_half_int(const MgLev<T>& L, T* xs, const T* b
     __syncthreads();
 }
 
+// ---------------------------------------------------------------------------
+// FP32 register strips for the interior of the large levels.
+//
+// A warp walks one strip of 128 columns (lane l holds columns 4l .. 4l + 3 as
+// a float4) row by row and runs all four half sweeps as a wavefront: at row
+// step t, sweep k works on row t - k + 1, which already has every neighbour
+// value it needs (RB Gauss-Seidel cells of one colour depend only on cells of
+// the other), so each cell value equals that of the tile kernels and of the
+// level-by-level kernels.  Rows live in registers; W/E neighbours across
+// lanes come by shuffle; the rows read from global memory arrive through a
+// per-warp cp.async ring a few rows ahead.  The edge columns and rows of a
+// strip are recomputed by the neighbouring strips (halo 6 | 116 | 6 for the
+// pre-smoothing, which ends with the restriction; 4 | 120 | 4 for the
+// post-smoothing).  Strips cover only cells whose whole read region is inside
+// [1, n-1) on both axes (no wrap, no wall, uniform stencil); the frame around
+// them is done by the tile path in the same launch.
+constexpr int SP_COLS = 128;
+constexpr int SP_PRE_OUT = 116, SP_POST_OUT = 120;
+constexpr int SP_RING = 4;  // rows per warp in flight (one being read, three ahead)
+constexpr unsigned SP_FULL = 0xffffffffu;
+
+// Launch geometry shared by both paths: blocks [0, nframe) are tiles of the
+// frame (all tiles outside [txa, txb) x [tya, tyb)), the rest hold 8 strips
+// each (ns x nr strips, rh rows, the first writing from column x0, row y0).
+struct StripMap {
+    int nframe, ntx, txa, txb, tya, tyb;
+    int ns, nr, rh, x0, y0;
+};
+
+__device__ __forceinline__ void frame_tile(const StripMap& m, int f, int& tx, int& ty) {
+    const int top = m.tya * m.ntx;
+    if (f < top) {
+        ty = f / m.ntx;
+        tx = f - ty * m.ntx;
+        return;
+    }
+    f -= top;
+    const int nty_mid = m.tyb - m.tya, per = m.txa + (m.ntx - m.txb);
+    if (f < nty_mid * per) {
+        ty = m.tya + f / per;
+        const int k = f % per;
+        tx = k < m.txa ? k : m.txb + (k - m.txa);
+        return;
+    }
+    f -= nty_mid * per;
+    ty = m.tyb + f / m.ntx;
+    tx = f % m.ntx;
+}
+
+__device__ __forceinline__ void cpa16(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa8(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa4(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// half sweep of colour c on row j (X), rows j - 1 (Xm) and j + 1 (Xp), b (B);
+// the strip's first column is a multiple of 4, so colour c sits at k = 0, 2
+// when j + c is even and at k = 1, 3 otherwise
+__device__ __forceinline__ void sp_half(float4& X, const float4& Xm, const float4& Xp, const float4& B, int j, int c,
+                                        float scale, float id0) {
+    if (((j + c) & 1) == 0) {
+        const float w = __shfl_up_sync(SP_FULL, X.w, 1);
+        float s = w + X.y;
+        s = s + Xm.x;
+        s = s + Xp.x;
+        X.x = fmaf(scale, s, B.x) * id0;
+        s = X.y + X.w;
+        s = s + Xm.z;
+        s = s + Xp.z;
+        X.z = fmaf(scale, s, B.z) * id0;
+    } else {
+        const float e = __shfl_down_sync(SP_FULL, X.x, 1);
+        float s = X.x + X.z;
+        s = s + Xm.y;
+        s = s + Xp.y;
+        X.y = fmaf(scale, s, B.y) * id0;
+        s = X.z + e;
+        s = s + Xm.w;
+        s = s + Xp.w;
+        X.w = fmaf(scale, s, B.w) * id0;
+    }
+}
+
+// first half sweep from x = 0 (neighbour sum 0)
+__device__ __forceinline__ void sp_first(float4& X, const float4& B, int j, int c, float scale, float id0) {
+    if (((j + c) & 1) == 0) {
+        X.x = fmaf(scale, 0.f, B.x) * id0;
+        X.z = fmaf(scale, 0.f, B.z) * id0;
+    } else {
+        X.y = fmaf(scale, 0.f, B.y) * id0;
+        X.w = fmaf(scale, 0.f, B.w) * id0;
+    }
+}
+
+__device__ __forceinline__ float sp_ax(float d0, float ms, float c, float w, float e, float sth, float nth) {
+    float ax = d0 * c;
+    ax = fmaf(ms, w, ax);
+    ax = fmaf(ms, e, ax);
+    ax = fmaf(ms, sth, ax);
+    return fmaf(ms, nth, ax);
+}
+
+// Pre-smoothing strip: x = 0, (red, black) x 2, x to the r array, r = b - A x,
+// b_coarse = R r.  Output columns [o, o + 116), rows [y0, y0 + rh); coarse
+// cells [o/2, o/2 + 58) x [y0/2, y0/2 + rh/2).  ring: SP_RING x 32 float4.
+__device__ __forceinline__ void strip_pre(const MgLev<float>& F, const MgLev<float>& C, float4* ring, int o, int y0,
+                                          int rh) {
+    const int lane = threadIdx.x & 31;
+    const int s = o - 6;
+    const float* bcol = F.b + s + 4 * lane;
+    const int ya = y0 - 5, yb = y0 + rh + 5;  // rows of b read
+#pragma unroll
+    for (int k = 0; k < SP_RING - 1; ++k) {
+        cpa16(&ring[k * 32 + lane], bcol + (size_t)(ya + k) * F.pitch);
+        cpa_commit();
+    }
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 X0 = z4, X1 = z4, X2 = z4, X3 = z4, X4 = z4, X5 = z4;
+    float4 B0 = z4, B1 = z4, B2 = z4, B3 = z4, B4 = z4;
+    float2 S1 = make_float2(0.f, 0.f), S2 = S1, S3 = S1;
+    const float scale = F.scale, id0 = F.invd[0], d0 = F.diag[0], ms = F.ms;
+    const bool out_lo = lane >= 1 && lane <= 30;
+    for (int t = ya; t < yb; ++t) {
+        const int tn = t + SP_RING - 1;
+        if (tn < yb) cpa16(&ring[((tn - ya) % SP_RING) * 32 + lane], bcol + (size_t)tn * F.pitch);
+        cpa_commit();
+        cpa_wait<SP_RING - 1>();
+        X5 = X4;
+        X4 = X3;
+        X3 = X2;
+        X2 = X1;
+        X1 = X0;
+        X0 = z4;
+        B4 = B3;
+        B3 = B2;
+        B2 = B1;
+        B1 = B0;
+        B0 = ring[((t - ya) % SP_RING) * 32 + lane];
+        sp_first(X0, B0, t, 0, scale, id0);                    // row t
+        sp_half(X1, X2, X0, B1, t - 1, 1, scale, id0);         // row t - 1
+        sp_half(X2, X3, X1, B2, t - 2, 0, scale, id0);         // row t - 2
+        sp_half(X3, X4, X2, B3, t - 3, 1, scale, id0);         // row t - 3: final x
+        const int jx = t - 3;
+        if (jx >= y0 && jx < y0 + rh && out_lo) {
+            float* xr = F.r + (size_t)jx * F.pitch + s + 4 * lane;
+            if (lane == 1)
+                *reinterpret_cast<float2*>(xr + 2) = make_float2(X3.z, X3.w);
+            else if (lane == 30)
+                *reinterpret_cast<float2*>(xr) = make_float2(X3.x, X3.y);
+            else
+                *reinterpret_cast<float4*>(xr) = X3;
+        }
+        // residual of row t - 4 and the restriction's row sums
+        const float w = __shfl_up_sync(SP_FULL, X4.w, 1), e = __shfl_down_sync(SP_FULL, X4.x, 1);
+        float4 R;
+        R.x = B4.x - sp_ax(d0, ms, X4.x, w, X4.y, X5.x, X3.x);
+        R.y = B4.y - sp_ax(d0, ms, X4.y, X4.x, X4.z, X5.y, X3.y);
+        R.z = B4.z - sp_ax(d0, ms, X4.z, X4.y, X4.w, X5.z, X3.z);
+        R.w = B4.w - sp_ax(d0, ms, X4.w, X4.z, e, X5.w, X3.w);
+        const float rl = __shfl_up_sync(SP_FULL, R.w, 1), rr = __shfl_down_sync(SP_FULL, R.x, 1);
+        float2 S0;
+        S0.x = fmaf(0.25f, rl, 0.f);
+        S0.x = fmaf(0.75f, R.x, S0.x);
+        S0.x = fmaf(0.75f, R.y, S0.x);
+        S0.x = fmaf(0.25f, R.z, S0.x);
+        S0.y = fmaf(0.25f, R.y, 0.f);
+        S0.y = fmaf(0.75f, R.z, S0.y);
+        S0.y = fmaf(0.75f, R.w, S0.y);
+        S0.y = fmaf(0.25f, rr, S0.y);
+        const int jr = t - 4;
+        if (!(jr & 1) && jr >= y0 + 2 && jr < y0 + rh + 2 && out_lo) {
+            // coarse row (jr - 2) / 2 from fine rows jr - 3 .. jr
+            float2 acc;
+            acc.x = fmaf(0.25f, S3.x, 0.f);
+            acc.x = fmaf(0.75f, S2.x, acc.x);
+            acc.x = fmaf(0.75f, S1.x, acc.x);
+            acc.x = fmaf(0.25f, S0.x, acc.x);
+            acc.y = fmaf(0.25f, S3.y, 0.f);
+            acc.y = fmaf(0.75f, S2.y, acc.y);
+            acc.y = fmaf(0.75f, S1.y, acc.y);
+            acc.y = fmaf(0.25f, S0.y, acc.y);
+            float* cb = C.b + (size_t)((jr - 2) >> 1) * C.pitch + (s >> 1) + 2 * lane;
+            if (lane == 1)
+                cb[1] = 0.25f * acc.y;
+            else if (lane == 30)
+                cb[0] = 0.25f * acc.x;
+            else
+                *reinterpret_cast<float2*>(cb) = make_float2(0.25f * acc.x, 0.25f * acc.y);
+        }
+        S3 = S2;
+        S2 = S1;
+        S1 = S0;
+    }
+    cpa_wait<0>();
+}
+
+// horizontal prolongation weights of one coarse row for the lane's 4 fine
+// columns (coarse columns I0 - 1 .. I0 + 2, I0 = first column / 2); lanes 0
+// and 31 take the outer neighbours from el and er (the strip's edge columns
+// need them: their x enters the half sweeps of the columns next to them)
+__device__ __forceinline__ float4 sp_hrow(float2 c, float el, float er) {
+    float cl = __shfl_up_sync(SP_FULL, c.y, 1), cr = __shfl_down_sync(SP_FULL, c.x, 1);
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) cl = el;
+    if (lane == 31) cr = er;
+    float4 h;
+    h.x = fmaf(0.25f, cl, 0.75f * c.x);
+    h.y = fmaf(0.25f, c.y, 0.75f * c.x);
+    h.z = fmaf(0.25f, c.x, 0.75f * c.y);
+    h.w = fmaf(0.25f, cr, 0.75f * c.y);
+    return h;
+}
+
+// Post-smoothing strip: x = x_pre + P x_coarse, (black, red) x 2, x written.
+// Output columns [o, o + 120), rows [y0, y0 + rh); y0 even.  ring: SP_RING
+// slots of 32 float4 (b), 32 float4 (x_pre), 32 float2 (coarse row) and the
+// coarse row's two outer neighbours (padded to 16 bytes).
+constexpr int SP_POST_SLOT = 32 * 4 + 32 * 4 + 32 * 2 + 4;  // floats per slot
+__device__ __forceinline__ void strip_post(const MgLev<float>& C, const MgLev<float>& F, float4* ring, int o,
+                                           int y0, int rh) {
+    const int lane = threadIdx.x & 31;
+    const int s = o - 4;
+    const size_t col = (size_t)s + 4 * lane, ccol = (size_t)(s >> 1) + 2 * lane;
+    // coarse column read by this lane for the edge neighbour: I0 - 1 (lane 0), I0 + 2 (lane 31)
+    const size_t ecol = lane == 0 ? ccol - 1 : ccol + 2;
+    const bool edge = lane == 0 || lane == 31;
+    const int ya = y0 - 4, yb = y0 + rh + 4;  // rows read: [ya, yb), ya even
+    float* rg = reinterpret_cast<float*>(ring);
+    auto issue = [&](int row) {
+        float* sl = rg + ((row - ya) % SP_RING) * SP_POST_SLOT;
+        if (row < yb) {
+            cpa16(sl + 4 * lane, F.b + (size_t)row * F.pitch + col);
+            cpa16(sl + 128 + 4 * lane, F.r + (size_t)row * F.pitch + col);
+            if (row & 1) {
+                const float* crow = C.x + (size_t)((row + 1) >> 1) * C.pitch;
+                cpa8(sl + 256 + 2 * lane, crow + ccol);
+                if (edge) cpa4(sl + 320 + (lane >> 4), crow + ecol);
+            }
+        }
+        cpa_commit();
+    };
+#pragma unroll
+    for (int k = 0; k < SP_RING - 1; ++k) issue(ya + k);
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    // horizontal coarse rows: HA = row hi - 1, HB = row hi, hi = (row + 1) / 2
+    auto hrow_direct = [&](int J) {
+        const float* crow = C.x + (size_t)J * C.pitch;
+        const float e = edge ? crow[ecol] : 0.f;
+        return sp_hrow(*reinterpret_cast<const float2*>(crow + ccol), e, e);
+    };
+    float4 HA = hrow_direct(ya / 2 - 1);
+    float4 HB = hrow_direct(ya / 2);
+    float4 X0 = z4, X1 = z4, X2 = z4, X3 = z4, X4 = z4, X5 = z4;
+    float4 B0 = z4, B1 = z4, B2 = z4, B3 = z4, Bn = z4;
+    const float scale = F.scale, id0 = F.invd[0];
+    const bool out = lane >= 1 && lane <= 30;
+    // step t forms x of row t + 1, then sweeps rows t .. t - 3
+    for (int t = ya - 1; t < yb - 1; ++t) {
+        const int row = t + 1;
+        issue(row + SP_RING - 1);
+        cpa_wait<SP_RING - 1>();
+        X5 = X4;
+        X4 = X3;
+        X3 = X2;
+        X2 = X1;
+        X1 = X0;
+        B3 = B2;
+        B2 = B1;
+        B1 = B0;
+        B0 = Bn;
+        const float* sl = rg + ((row - ya) % SP_RING) * SP_POST_SLOT;
+        Bn = *reinterpret_cast<const float4*>(sl + 4 * lane);
+        const float4 xr = *reinterpret_cast<const float4*>(sl + 128 + 4 * lane);
+        if (row & 1) {
+            HA = HB;
+            const float e = edge ? sl[320 + (lane >> 4)] : 0.f;
+            HB = sp_hrow(*reinterpret_cast<const float2*>(sl + 256 + 2 * lane), e, e);
+        }
+        const float4 H0 = (row & 1) ? HA : HB, H1 = (row & 1) ? HB : HA;
+        X0.x = xr.x + fmaf(0.25f, H1.x, 0.75f * H0.x);
+        X0.y = xr.y + fmaf(0.25f, H1.y, 0.75f * H0.y);
+        X0.z = xr.z + fmaf(0.25f, H1.z, 0.75f * H0.z);
+        X0.w = xr.w + fmaf(0.25f, H1.w, 0.75f * H0.w);
+        sp_half(X1, X2, X0, B0, t, 1, scale, id0);          // row t
+        sp_half(X2, X3, X1, B1, t - 1, 0, scale, id0);      // row t - 1
+        sp_half(X3, X4, X2, B2, t - 2, 1, scale, id0);      // row t - 2
+        sp_half(X4, X5, X3, B3, t - 3, 0, scale, id0);      // row t - 3: final x
+        const int jx = t - 3;
+        if (jx >= y0 && jx < y0 + rh && out)
+            *reinterpret_cast<float4*>(F.x + (size_t)jx * F.pitch + col) = X4;
+    }
+    cpa_wait<0>();
+}
+
 template <typename T, int TW, int TH>
-__global__ void __launch_bounds__(FT_THREADS) k_mg_pre(MgLev<T> F, MgLev<T> C, MgBc p, SolverState* S, int inner) {
+__global__ void __launch_bounds__(FT_THREADS) k_mg_pre(MgLev<T> F, MgLev<T> C, MgBc p, SolverState* S, int inner,
+                                                       StripMap m) {
     if (!block_live(S, inner)) return;
     constexpr int H = 5, W = TW + 2 * H, HT = TH + 2 * H;
-    __shared__ T xs[W * HT];
-    __shared__ T bs[W * HT];  // b, then r in place on the residual ring
-    const int i0 = blockIdx.x * TW, j0 = blockIdx.y * TH;
+    constexpr bool STRIPS = sizeof(T) == 4 && TW == 64;
+    constexpr size_t TILE_B = 2 * sizeof(T) * W * HT;
+    constexpr size_t RING_B = STRIPS ? (FT_THREADS / 32) * SP_RING * 32 * sizeof(float4) : 0;
+    __shared__ __align__(16) unsigned char smem[TILE_B > RING_B ? TILE_B : RING_B];
+    if constexpr (STRIPS) {
+        if ((int)blockIdx.x >= m.nframe) {
+            const int warp = threadIdx.x >> 5;
+            const int k = ((int)blockIdx.x - m.nframe) * (FT_THREADS / 32) + warp;
+            if (k >= m.ns * m.nr) return;
+            const int sx = k % m.ns, sy = k / m.ns;
+            strip_pre(F, C, reinterpret_cast<float4*>(smem) + warp * SP_RING * 32, m.x0 + SP_PRE_OUT * sx,
+                      m.y0 + m.rh * sy, m.rh);
+            return;
+        }
+    }
+    T* xs = reinterpret_cast<T*>(smem);
+    T* bs = xs + W * HT;  // b, then r in place on the residual ring
+    int tx, ty;
+    frame_tile(m, blockIdx.x, tx, ty);
+    const int i0 = tx * TW, j0 = ty * TH;
     if (ft_interior<TW, TH, H>(F.nx, F.ny, i0, j0)) {
         ft_load_int<T, TW, TH, H>(F, xs, bs, i0, j0, nullptr);
         ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 0, 5, true);
@@ -466,32 +792,62 @@ __global__ void __launch_bounds__(FT_THREADS) k_mg_pre(MgLev<T> F, MgLev<T> C, M
 }
 
 template <typename T, int TW, int TH>
-__global__ void __launch_bounds__(FT_THREADS) k_mg_post(MgLev<T> C, MgLev<T> F, MgBc p, SolverState* S, int inner) {
+__global__ void __launch_bounds__(FT_THREADS) k_mg_post(MgLev<T> C, MgLev<T> F, MgBc p, SolverState* S, int inner,
+                                                        StripMap m) {
     if (!block_live(S, inner)) return;
     constexpr int H = 4, W = TW + 2 * H, HT = TH + 2 * H;
     // coarse cells read by the prolongation of an interior tile's array
     constexpr int CW = TW / 2 + H + 2, CH = TH / 2 + H + 2;
-    __shared__ T xs[W * HT];
-    __shared__ T bs[W * HT];
-    __shared__ T cs[CW * CH];
-    const int i0 = blockIdx.x * TW, j0 = blockIdx.y * TH;
+    constexpr bool STRIPS = sizeof(T) == 4 && TW == 64;
+    constexpr size_t TILE_B = sizeof(T) * (2 * W * HT + CW * CH);
+    constexpr size_t RING_B = STRIPS ? (FT_THREADS / 32) * SP_RING * SP_POST_SLOT * sizeof(float) : 0;
+    __shared__ __align__(16) unsigned char smem[TILE_B > RING_B ? TILE_B : RING_B];
+    if constexpr (STRIPS) {
+        if ((int)blockIdx.x >= m.nframe) {
+            const int warp = threadIdx.x >> 5;
+            const int k = ((int)blockIdx.x - m.nframe) * (FT_THREADS / 32) + warp;
+            if (k >= m.ns * m.nr) return;
+            const int sx = k % m.ns, sy = k / m.ns;
+            strip_post(C, F, reinterpret_cast<float4*>(smem) + warp * SP_RING * (SP_POST_SLOT / 4), m.x0 + SP_POST_OUT * sx,
+                       m.y0 + m.rh * sy, m.rh);
+            return;
+        }
+    }
+    T* xs = reinterpret_cast<T*>(smem);
+    T* bs = xs + W * HT;
+    T* cs = bs + W * HT;
+    int tx, ty;
+    frame_tile(m, blockIdx.x, tx, ty);
+    const int i0 = tx * TW, j0 = ty * TH;
     if (ft_interior<TW, TH, H>(F.nx, F.ny, i0, j0)) {
         // coarse block from (i0 - H) / 2 - 1, (j0 - H) / 2 - 1
         const int ci0 = (i0 - H) / 2 - 1, cj0 = (j0 - H) / 2 - 1;
-        for (int q = threadIdx.x; q < CW * CH; q += FT_THREADS)
-            cs[q] = C.x[(size_t)(cj0 + q / CW) * C.pitch + ci0 + q % CW];
-        ft_load_int<T, TW, TH, H>(F, xs, bs, i0, j0, F.r);  // ends with a barrier
-        for (int q = threadIdx.x; q < W * HT; q += FT_THREADS) {
-            const int fx = i0 - H + q % W, fy = j0 - H + q / W;
-            const int I = (fx >> 1) - ci0, NI = I + ((fx & 1) ? 1 : -1);
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        for (int cj = warp; cj < CH; cj += FT_THREADS / 32)
+            for (int ci = lane; ci < CW; ci += 32) cs[cj * CW + ci] = C.x[(size_t)(cj0 + cj) * C.pitch + ci0 + ci];
+        __syncthreads();
+        // b, and x (kept in the r array by k_mg_pre) plus the prolongation,
+        // one warp per row
+        const size_t base = (size_t)(j0 - H) * F.pitch + (i0 - H);
+        for (int lj = warp; lj < HT; lj += FT_THREADS / 32) {
+            const int fy = j0 - H + lj;
             const int J = (fy >> 1) - cj0, NJ = J + ((fy & 1) ? 1 : -1);
-            T row0 = T(0.75) * cs[J * CW + I];
-            row0 = mg_fma(T(0.25), cs[J * CW + NI], row0);
-            T v = T(0.75) * row0;
-            T row1 = T(0.75) * cs[NJ * CW + I];
-            row1 = mg_fma(T(0.25), cs[NJ * CW + NI], row1);
-            v = mg_fma(T(0.25), row1, v);
-            xs[q] = xs[q] + v;
+            const T* c0 = cs + J * CW;
+            const T* c1 = cs + NJ * CW;
+            const T* brow = F.b + base + (size_t)lj * F.pitch;
+            const T* xrow = F.r + base + (size_t)lj * F.pitch;
+            for (int li = lane; li < W; li += 32) {
+                const int fx = i0 - H + li;
+                const int I = (fx >> 1) - ci0, NI = I + ((fx & 1) ? 1 : -1);
+                T row0 = T(0.75) * c0[I];
+                row0 = mg_fma(T(0.25), c0[NI], row0);
+                T v = T(0.75) * row0;
+                T row1 = T(0.75) * c1[I];
+                row1 = mg_fma(T(0.25), c1[NI], row1);
+                v = mg_fma(T(0.25), row1, v);
+                bs[lj * W + li] = brow[li];
+                xs[lj * W + li] = xrow[li] + v;
+            }
         }
         __syncthreads();
         ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 1, 3, false);
@@ -760,6 +1116,7 @@ static int bottom_level(const MgLev<T>* lev, int nlev, size_t* smem) {
 struct MgHierarchy {
     int nlev = 0;
     int fused = -1;  // 1: all levels fused, 0: none, -1: by level (see vcycle)
+    int strip_rows = 32;  // rows per FP32 register strip (0: tiles only)
     MgLev<double> d[16];
     MgLev<float> f[16];
     double* z64 = nullptr;
@@ -795,6 +1152,7 @@ int mg_setup(cf_ctx* c) {
     MgHierarchy* H = new MgHierarchy();
     c->mg = H;
     if (const char* e = getenv("CF_MG_FUSED")) H->fused = atoi(e) != 0;
+    if (const char* e = getenv("CF_MG_STRIPS")) H->strip_rows = atoi(e);
     int nx = c->ph.nx, ny = c->ph.ny;
     for (int l = 0; l < 16 && !rc; ++l) {
         if (l == 0) {
@@ -854,8 +1212,42 @@ double* mg_z64(cf_ctx* c) { return static_cast<MgHierarchy*>(c->mg)->z64; }
 // by launch latency; larger FP64 levels are bound by the FP64 pipe, where the
 // fused tiles' halo recomputation costs more than it saves.  CF_MG_FUSED=0/1
 // in the environment forces one form.
+// Launch geometry of a fused pre (or post) launch: tiles of tw x th over the
+// level; with strip_rows > 0 (FP32 64-wide tiles only), register strips of
+// that many rows over the interior and tiles only over the frame around them.
+static StripMap strip_map(int nx, int ny, int tw, int th, int strip_rows, bool pre) {
+    StripMap m{};
+    m.ntx = (nx + tw - 1) / tw;
+    const int nty = (ny + th - 1) / th;
+    m.tya = m.tyb = nty;  // default: every tile in the first band
+    m.nframe = m.ntx * nty;
+    if (strip_rows <= 0 || (strip_rows & 1)) return m;
+    const int out = pre ? SP_PRE_OUT : SP_POST_OUT, hc = pre ? 6 : 4, hr = pre ? 5 : 4;
+    const int x0 = 4 + hc, y0 = 6;  // first strip reads from column 4, row y0 - hr >= 1
+    const int span = nx - 1 - SP_COLS - 4;  // last strip: 4 + out (ns - 1) + 128 <= nx - 1
+    const int ns = span >= 0 ? span / out + 1 : 0;
+    const int nr = (ny - 1 - hr - y0) / strip_rows;  // y0 + rh nr + hr <= ny - 1
+    if (ns < 1 || nr < 1) return m;
+    const int xb = x0 + out * ns, yb = y0 + strip_rows * nr;
+    const int txa = (x0 + tw - 1) / tw, txb = xb / tw, tya = (y0 + th - 1) / th, tyb = yb / th;
+    if (txa >= txb || tya >= tyb) return m;
+    m.txa = txa;
+    m.txb = txb;
+    m.tya = tya;
+    m.tyb = tyb;
+    m.nframe = m.ntx * nty - (txb - txa) * (tyb - tya);
+    m.ns = ns;
+    m.nr = nr;
+    m.rh = strip_rows;
+    m.x0 = x0;
+    m.y0 = y0;
+    return m;
+}
+
+static int launch_blocks(const StripMap& m) { return m.nframe + (m.ns * m.nr + FT_THREADS / 32 - 1) / (FT_THREADS / 32); }
+
 template <typename T>
-static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, int fused) {
+static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, int fused, int strip_rows) {
     MgBc p{c->ph.per_x, c->ph.per_y, {c->ph.bc[0], c->ph.bc[1], c->ph.bc[2], c->ph.bc[3]}};
     double s = scale0;
     for (int l = 0; l < nlev; ++l) {
@@ -876,19 +1268,22 @@ static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, 
     const int top_end = lb < nlev ? lb : nlev - 1;  // levels smoothed by grid kernels on the way down
     constexpr int TH = FtRows<T>::value;
     auto big = [&](const MgLev<T>& L) { return (long long)((L.nx + 63) / 64) * ((L.ny + TH - 1) / TH) >= 1024; };
-    auto tiles = [&](const MgLev<T>& L, int tw, int th) { return dim3((L.nx + tw - 1) / tw, (L.ny + th - 1) / th); };
     auto fuse_level = [&](int l) {
         if (fused >= 0) return fused != 0;
         return sizeof(T) == 4 || (long long)lev[l].nx * lev[l].ny <= (1ll << 20);
     };
+    const int srows = sizeof(T) == 4 ? strip_rows : 0;
     for (int l = 0; l < top_end; ++l) {
         if (fuse_level(l)) {
-            if (big(lev[l]))
-                k_mg_pre<T, 64, TH><<<tiles(lev[l], 64, TH), FT_THREADS, 0, c->stream>>>(lev[l], lev[l + 1], p, c->S,
-                                                                                        inner);
-            else
-                k_mg_pre<T, 32, 16><<<tiles(lev[l], 32, 16), FT_THREADS, 0, c->stream>>>(lev[l], lev[l + 1], p, c->S,
-                                                                                        inner);
+            if (big(lev[l])) {
+                const StripMap m = strip_map(lev[l].nx, lev[l].ny, 64, TH, srows, true);
+                k_mg_pre<T, 64, TH><<<launch_blocks(m), FT_THREADS, 0, c->stream>>>(lev[l], lev[l + 1], p, c->S,
+                                                                                   inner, m);
+            } else {
+                const StripMap m = strip_map(lev[l].nx, lev[l].ny, 32, 16, 0, true);
+                k_mg_pre<T, 32, 16><<<launch_blocks(m), FT_THREADS, 0, c->stream>>>(lev[l], lev[l + 1], p, c->S,
+                                                                                   inner, m);
+            }
             ++launches;
             continue;
         }
@@ -925,12 +1320,15 @@ static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, 
     }
     for (int l = top_end - 1; l >= 0; --l) {
         if (fuse_level(l)) {
-            if (big(lev[l]))
-                k_mg_post<T, 64, TH><<<tiles(lev[l], 64, TH), FT_THREADS, 0, c->stream>>>(lev[l + 1], lev[l], p, c->S,
-                                                                                         inner);
-            else
-                k_mg_post<T, 32, 16><<<tiles(lev[l], 32, 16), FT_THREADS, 0, c->stream>>>(lev[l + 1], lev[l], p, c->S,
-                                                                                         inner);
+            if (big(lev[l])) {
+                const StripMap m = strip_map(lev[l].nx, lev[l].ny, 64, TH, srows, false);
+                k_mg_post<T, 64, TH><<<launch_blocks(m), FT_THREADS, 0, c->stream>>>(lev[l + 1], lev[l], p, c->S,
+                                                                                    inner, m);
+            } else {
+                const StripMap m = strip_map(lev[l].nx, lev[l].ny, 32, 16, 0, false);
+                k_mg_post<T, 32, 16><<<launch_blocks(m), FT_THREADS, 0, c->stream>>>(lev[l + 1], lev[l], p, c->S,
+                                                                                    inner, m);
+            }
             ++launches;
             continue;
         }
@@ -949,8 +1347,8 @@ static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, 
 // returns at once when the solve has stopped.
 int mg_vcycle(cf_ctx* c, double scale0) {
     MgHierarchy* H = static_cast<MgHierarchy*>(c->mg);
-    if (c->precision == CF_PREC_MIXED) return vcycle<float>(c, H->f, H->nlev, scale0, 1, H->fused);
-    return vcycle<double>(c, H->d, H->nlev, scale0, 0, H->fused);
+    if (c->precision == CF_PREC_MIXED) return vcycle<float>(c, H->f, H->nlev, scale0, 1, H->fused, H->strip_rows);
+    return vcycle<double>(c, H->d, H->nlev, scale0, 0, H->fused, 0);
 }
 
 int mg_levels(const cf_ctx* c) { return c->mg ? static_cast<const MgHierarchy*>(c->mg)->nlev : 0; }

@@ -141,3 +141,40 @@ def test_mixed_mg_steps(built):
         assert np.abs(a - b).max() <= 1e-4 * max(np.abs(a).max(), 1e-30), f
     qa, qb = o.get("q"), c.download("q")
     assert np.abs(qa - qb).max() <= 1e-4
+
+
+def _mixed_mg_run(nx, ny, periodic, bc, strips, monkeypatch, seed):
+    from cajitafluids_gb300 import Context
+    monkeypatch.setenv("CF_MG_STRIPS", strips)
+    rng = np.random.default_rng(seed)
+    shapes = {"q": (ny, nx), "u": (ny, nx + (0 if periodic[0] else 1)), "v": (ny + (0 if periodic[1] else 1), nx)}
+    c = Context(nx, ny, hi=(1.0, ny / nx), periodic=periodic, precision="mixed")
+    c.set_bc(bc)
+    for f, shp in shapes.items():
+        c.upload(f, rng.standard_normal(shp))
+    st = [c.project(0.5 / nx, opts(tol=1e-9, max_iter=60, precon="PFMG"))]
+    st.append(c.project(0.5 / nx, opts(tol=1e-11, max_iter=60, precon="PFMG")))
+    out = {f: c.download(f) for f in ("p", "u", "v")}
+    c.close()
+    return st, out
+
+
+@pytest.mark.parametrize("nx,ny,periodic,bc", [
+    (2048, 1024, (True, True), (0, 0, 0, 0)),
+    (2100, 1100, (False, False), (0, 1, 0, 1)),
+    (2176, 1088, (True, False), (1, 0, 1, 0)),
+    (4096, 2048, (True, True), (0, 0, 0, 0)),
+])
+def test_mixed_mg_register_strips(built, monkeypatch, nx, ny, periodic, bc):
+    """The FP32 register strips (interior of the large levels) and the tile
+    kernels compute identical V-cycles: projections with strips of 32 and 8
+    rows equal those with tiles only (CF_MG_STRIPS=0) bit for bit."""
+    ref_st, ref = _mixed_mg_run(nx, ny, periodic, bc, "0", monkeypatch, nx + ny)
+    assert ref_st[0]["iterations"] > 2
+    for strips in ("32", "8"):
+        st, out = _mixed_mg_run(nx, ny, periodic, bc, strips, monkeypatch, nx + ny)
+        for a, b in zip(ref_st, st):
+            assert a["status"] == b["status"] and a["iterations"] == b["iterations"], strips
+            assert a["r_norm"] == b["r_norm"], strips
+        for f in ("p", "u", "v"):
+            assert np.array_equal(ref[f], out[f]), (strips, f)
