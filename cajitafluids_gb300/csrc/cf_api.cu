@@ -278,9 +278,9 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
         // FP32 vectors with a one-cell ghost ring, owned column 0 on 16 bytes
         c->p32 = (int)round_up((size_t)nx + 8, 32);
         size_t n32 = (size_t)c->p32 * (ny + 2);
-        float** bases[4] = {&c->e32b, &c->r32b, &c->pa32b, &c->pb32b};
-        cf::Vec32* vecs[4] = {&c->e32, &c->r32, &c->pa32, &c->pb32};
-        for (int k = 0; k < 4 && !rc; ++k) {
+        float** bases[3] = {&c->r32b, &c->pa32b, &c->pb32b};
+        cf::Vec32* vecs[3] = {&c->r32, &c->pa32, &c->pb32};
+        for (int k = 0; k < 3 && !rc; ++k) {
             rc = alloc_dev(c, *bases[k], n32);
             vecs[k]->a = *bases[k] + c->p32 + 4;
             vecs[k]->pitch = c->p32;

@@ -1,7 +1,7 @@
 // FP32 inner Jacobi-PCG iteration of the mixed-precision projection, fed by
 // TMA.
 //
-// The FP32 solver vectors (e, r, p twice) carry a one-cell ghost ring:
+// The FP32 solver vectors (r, p twice) carry a one-cell ghost ring:
 // element (i, j), i in [-1, nx], j in [-1, ny], lives at
 // base[(j + 1) * pitch + i + 4], so owned column 0 sits on a 16-byte boundary.
 // Wall ghosts stay zero; along a periodic axis the thread that writes an
@@ -17,7 +17,8 @@
 // registers (float4 where a full vector is owned).
 //
 //   K1  p <- M^-1 r + beta p (halo too, in shared memory) ; q <- A p ; p.q
-//   K2  q <- A p (recomputed) ; e += alpha p ; r -= alpha q ; r.z , r.r
+//   K2  q <- A p (recomputed) ; x += alpha p (double-float) ; r -= alpha q ;
+//       r.z , r.r
 //
 // Dot products: FP32 per thread within a tile, FP64 across tiles, warps and
 // CTAs; the last CTA finishes the sum and advances the solver state.
@@ -48,7 +49,9 @@ struct Cg32T {
     int nx, ny, per_x, per_y, tiles_x, tiles, pitch;
     int mg;  // MG-PCG: K1 reads z (minv = 1), K2 leaves beta and rho to k_mg_rz32
     Stencil st;
-    float *e, *r, *pa, *pb;  // element (0, 0)
+    float *r, *pa, *pb;  // element (0, 0)
+    float2* x;           // the solution as double-float pairs (owned cells, row pitch xpitch)
+    int xpitch;
     double *part0, *part1;
     SolverState* S;
 };
@@ -319,10 +322,11 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
 }
 
-// K2: recompute A p, update e and r, r.z and r.r
+// K2: recompute A p, update x (double-float) and r, r.z and r.r.  x is read
+// with plain loads issued before the tile's copies are awaited.
 __global__ void __launch_bounds__(kThreads, 2)
-    k_tma_update32(const __grid_constant__ CUtensorMap map_e, const __grid_constant__ CUtensorMap map_r,
-                   const __grid_constant__ CUtensorMap map_pa, const __grid_constant__ CUtensorMap map_pb, Cg32T a) {
+    k_tma_update32(const __grid_constant__ CUtensorMap map_r, const __grid_constant__ CUtensorMap map_pa,
+                   const __grid_constant__ CUtensorMap map_pb, Cg32T a) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bars[kStages];
     __shared__ double red[kThreads / 32];
@@ -334,7 +338,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ntile = (a.tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
     unsigned char* sb = smem + ((128u - (smem_u32(smem) & 127u)) & 127u);  // TMA wants 128-byte slots
-    auto stage_ptr = [&](int s, int arr) { return reinterpret_cast<float*>(sb + (s * 3 + arr) * kSlot); };
+    auto stage_ptr = [&](int s, int arr) { return reinterpret_cast<float*>(sb + (s * 2 + arr) * kSlot); };
     if (tid == 0) {
         for (int s = 0; s < kStages; ++s) mbar_init(smem_u32(&bars[s]), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -345,10 +349,9 @@ __global__ void __launch_bounds__(kThreads, 2)
         int s = k % kStages;
         int x = (t % a.tiles_x) * kTW, y = (t / a.tiles_x) * kTH;
         uint32_t bar = smem_u32(&bars[s]);
-        mbar_expect_tx(bar, 3 * kBoxBytes);
+        mbar_expect_tx(bar, 2 * kBoxBytes);
         tma_load_2d(smem_u32(stage_ptr(s, 0)), map_p, x, y, bar);
-        tma_load_2d(smem_u32(stage_ptr(s, 1)), &map_e, x, y, bar);
-        tma_load_2d(smem_u32(stage_ptr(s, 2)), &map_r, x, y, bar);
+        tma_load_2d(smem_u32(stage_ptr(s, 1)), &map_r, x, y, bar);
     };
     if (tid == 0)
         for (int k = 0; k < kStages && k < ntile; ++k) issue(k);
@@ -357,15 +360,33 @@ __global__ void __launch_bounds__(kThreads, 2)
         const int s = k % kStages;
         const int t = (int)blockIdx.x + k * (int)gridDim.x;
         const int i0 = (t % a.tiles_x) * kTW, j0 = (t / a.tiles_x) * kTH;
+        const bool inner = interior_tile(a, i0, j0);
+        // x of the lane's cells (i .. i + 3) on its two rows
+        float4 xv[2][2];
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) {
+            const int j = j0 + 2 * warp + rr, i = i0 + 4 * lane;
+            const float2* xp = a.x + (size_t)j * a.xpitch + i;
+            if (inner) {
+                xv[rr][0] = reinterpret_cast<const float4*>(xp)[0];
+                xv[rr][1] = reinterpret_cast<const float4*>(xp)[1];
+            } else {
+                float* xf = reinterpret_cast<float*>(xv[rr]);
+                for (int c = 0; c < 4; ++c) {
+                    const bool in = j < a.ny && i + c < a.nx;
+                    const float2 v = in ? xp[c] : make_float2(0.f, 0.f);
+                    xf[2 * c] = v.x;
+                    xf[2 * c + 1] = v.y;
+                }
+            }
+        }
         bool ok = mbar_wait(smem_u32(&bars[s]), (uint32_t)((k / kStages) & 1), kWaitLimit);
         if (__syncthreads_or(!ok)) {
             abandon(S, bars, k, ntile);
             return;
         }
         const float* P = stage_ptr(s, 0);
-        const float* E = stage_ptr(s, 1);
-        const float* R = stage_ptr(s, 2);
-        const bool inner = interior_tile(a, i0, j0);
+        const float* R = stage_ptr(s, 1);
         float prz = 0.f, prr = 0.f;
 #pragma unroll
         for (int rr = 0; rr < 2; ++rr) {
@@ -373,12 +394,11 @@ __global__ void __launch_bounds__(kThreads, 2)
             float4 pc;
             float4 q = inner ? apply4<true>(a, P, lane, row, i, j, pc) : apply4<false>(a, P, lane, row, i, j, pc);
             const int off = (row + 1) * kBX + 4 + 4 * lane;
-            float4 ev = *reinterpret_cast<const float4*>(E + off);
             float4 rv = *reinterpret_cast<const float4*>(R + off);
-            ev.x = fmaf(alpha, pc.x, ev.x);
-            ev.y = fmaf(alpha, pc.y, ev.y);
-            ev.z = fmaf(alpha, pc.z, ev.z);
-            ev.w = fmaf(alpha, pc.w, ev.w);
+            float2 x0 = df_add_f(make_float2(xv[rr][0].x, xv[rr][0].y), alpha * pc.x);
+            float2 x1 = df_add_f(make_float2(xv[rr][0].z, xv[rr][0].w), alpha * pc.y);
+            float2 x2 = df_add_f(make_float2(xv[rr][1].x, xv[rr][1].y), alpha * pc.z);
+            float2 x3 = df_add_f(make_float2(xv[rr][1].z, xv[rr][1].w), alpha * pc.w);
             rv.x = fmaf(malpha, q.x, rv.x);
             rv.y = fmaf(malpha, q.y, rv.y);
             rv.z = fmaf(malpha, q.z, rv.z);
@@ -388,17 +408,21 @@ __global__ void __launch_bounds__(kThreads, 2)
                 float s2 = fmaf(rv.w, rv.w, fmaf(rv.z, rv.z, fmaf(rv.y, rv.y, rv.x * rv.x)));
                 prr += s2;
                 prz = fmaf(m0, s2, prz);
-                put4(a, a.e, i, j, ev, false);
+                float4* xo = reinterpret_cast<float4*>(a.x + (size_t)j * a.xpitch + i);
+                xo[0] = make_float4(x0.x, x0.y, x1.x, x1.y);
+                xo[1] = make_float4(x2.x, x2.y, x3.x, x3.y);
                 put4(a, a.r, i, j, rv, true);
             } else if (j < a.ny && i < a.nx) {
                 float rvs[4] = {rv.x, rv.y, rv.z, rv.w};
+                const float2 xs[4] = {x0, x1, x2, x3};
+                float2* xo = a.x + (size_t)j * a.xpitch + i;
                 for (int c = 0; c < 4; ++c)
                     if (i + c < a.nx) {
                         float z = a.st.minv32[ebits32t(a, i + c, j)] * rvs[c];
                         prz = fmaf(rvs[c], z, prz);
                         prr = fmaf(rvs[c], rvs[c], prr);
+                        xo[c] = xs[c];
                     }
-                put4(a, a.e, i, j, ev, false);
                 put4(a, a.r, i, j, rv, true);
             }
         }
@@ -529,8 +553,7 @@ static int make_map(cf_ctx* c, CUtensorMap* m, float* base) {
 }
 
 int cg32_setup(cf_ctx* c) {
-    int rc = make_map(c, &c->map_e, c->e32b);
-    if (!rc) rc = make_map(c, &c->map_r, c->r32b);
+    int rc = make_map(c, &c->map_r, c->r32b);
     if (!rc) rc = make_map(c, &c->map_pa, c->pa32b);
     if (!rc) rc = make_map(c, &c->map_pb, c->pb32b);
     if (rc) return rc;
@@ -544,7 +567,7 @@ int cg32_setup(cf_ctx* c) {
                     "smem attribute");
     if (!rc)
         rc = cuda_check(c, cudaFuncSetAttribute(k_tma_update32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                kStages * 3 * kSlot + 128),
+                                                kStages * 2 * kSlot + 128),
                         "smem attribute");
     // persistent grids: as many CTAs as fit on the GPU at once
     int occ1 = 0, occ2 = 0;
@@ -554,7 +577,7 @@ int cg32_setup(cf_ctx* c) {
                         "occupancy");
     if (!rc)
         rc = cuda_check(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_tma_update32, kThreads,
-                                                                         kStages * 3 * kSlot + 128),
+                                                                         kStages * 2 * kSlot + 128),
                         "occupancy");
     if (rc) return rc;
     occ1 = occ1 < 1 ? 1 : occ1;
@@ -588,7 +611,8 @@ static Cg32T cg32_args(cf_ctx* c, const Stencil& st) {
     a.tiles = c->tiles;
     a.pitch = c->p32;
     a.st = st;
-    a.e = c->e32.a;
+    a.x = reinterpret_cast<float2*>(c->x.a);
+    a.xpitch = c->vpitch;
     a.r = c->r32.a;
     a.pa = c->pa32.a;
     a.pb = c->pb32.a;
@@ -601,8 +625,8 @@ static Cg32T cg32_args(cf_ctx* c, const Stencil& st) {
 void cg32_launch_iteration(cf_ctx* c, const Stencil& st) {
     Cg32T a = cg32_args(c, st);
     k_tma_dir_matvec32<<<c->cta32, kThreads, kStages * 2 * kSlot + 128, c->stream>>>(c->map_r, c->map_pa, c->map_pb, a);
-    k_tma_update32<<<c->cta32b, kThreads, kStages * 3 * kSlot + 128, c->stream>>>(c->map_e, c->map_r, c->map_pa,
-                                                                            c->map_pb, a);
+    k_tma_update32<<<c->cta32b, kThreads, kStages * 2 * kSlot + 128, c->stream>>>(c->map_r, c->map_pa, c->map_pb,
+                                                                            a);
 }
 
 // z = V-cycle(r32), its periodic ghosts, rho = r.z; returns kernels launched
@@ -626,8 +650,8 @@ void cg32_launch_pair_mg(cf_ctx* c, const Stencil& st) {
     Cg32T a = cg32_args(c, stz);
     a.mg = 1;
     k_tma_dir_matvec32<<<c->cta32, kThreads, kStages * 2 * kSlot + 128, c->stream>>>(c->map_z, c->map_pa, c->map_pb, a);
-    k_tma_update32<<<c->cta32b, kThreads, kStages * 3 * kSlot + 128, c->stream>>>(c->map_e, c->map_r, c->map_pa,
-                                                                            c->map_pb, a);
+    k_tma_update32<<<c->cta32b, kThreads, kStages * 2 * kSlot + 128, c->stream>>>(c->map_r, c->map_pa, c->map_pb,
+                                                                            a);
 }
 
 }  // namespace cf

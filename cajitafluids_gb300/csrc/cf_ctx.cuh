@@ -27,10 +27,10 @@ struct cf_ctx {
     cf::Vec64 x{}, r{}, pa{}, pb{}, qv{}, b{};
     // FP32 vectors with a one-cell ghost ring: element (i, j) at a[j * p32 + i],
     // storage base = a - p32 - 4 (see cf_cg32.cu)
-    cf::Vec32 e32{}, r32{}, pa32{}, pb32{};
-    float *e32b = nullptr, *r32b = nullptr, *pa32b = nullptr, *pb32b = nullptr;
+    cf::Vec32 r32{}, pa32{}, pb32{};
+    float *r32b = nullptr, *pa32b = nullptr, *pb32b = nullptr;
     int p32 = 0;
-    CUtensorMap map_e{}, map_r{}, map_pa{}, map_pb{};
+    CUtensorMap map_r{}, map_pa{}, map_pb{};
     int tiles_x = 0, tiles = 0, cta32 = 0, cta32b = 0;
     double* partials = nullptr;  // 4 * n_units
     int G = 0, B = 0, n_units = 0;

@@ -170,6 +170,25 @@ __device__ __forceinline__ int wrap_index(int g, int n, int per) {
     return g < 0 ? g + n : g;
 }
 
+// Double-float (hi + lo FP32 pair) error-free sums (Knuth two-sum, Dekker
+// quick two-sum); exact with --fmad=false.
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+    float s = a + b;
+    float bb = s - a;
+    float e = (a - (s - bb)) + (b - bb);
+    return make_float2(s, e);
+}
+__device__ __forceinline__ float2 df_quick(float a, float b) {  // |a| >= |b|
+    float s = a + b;
+    return make_float2(s, b - (s - a));
+}
+// double-float + FP32
+__device__ __forceinline__ float2 df_add_f(float2 x, float e) {
+    float2 s = df_two_sum(x.x, e);
+    s.y = s.y + x.y;
+    return df_quick(s.x, s.y);
+}
+
 }  // namespace cf
 
 // Launch helpers implemented in the .cu files (called by cf_api.cu).

@@ -387,7 +387,7 @@ __device__ __forceinline__ void ft_half_int(const MgLev<T>& L, T* xs, const T* b
 // them is done by the tile path in the same launch.
 constexpr int SP_COLS = 128;
 constexpr int SP_PRE_OUT = 116, SP_POST_OUT = 120;
-constexpr int SP_RING = 4;  // rows per warp in flight (one being read, three ahead)
+constexpr int SP_RING = 3;  // rows per warp in flight (one being read, two ahead); divides 6
 constexpr unsigned SP_FULL = 0xffffffffu;
 
 // Launch geometry shared by both paths: blocks [0, nframe) are tiles of the
@@ -436,12 +436,12 @@ __device__ __forceinline__ void cpa_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// half sweep of colour c on row j (X), rows j - 1 (Xm) and j + 1 (Xp), b (B);
-// the strip's first column is a multiple of 4, so colour c sits at k = 0, 2
-// when j + c is even and at k = 1, 3 otherwise
-__device__ __forceinline__ void sp_half(float4& X, const float4& Xm, const float4& Xp, const float4& B, int j, int c,
+// half sweep of one colour on row j (X), rows j - 1 (Xm) and j + 1 (Xp), b
+// (B); the strip's first column is a multiple of 4, so the colour's cells sit
+// at k = 0, 2 when sel = (j + colour) & 1 is 0 and at k = 1, 3 otherwise
+__device__ __forceinline__ void sp_half(float4& X, const float4& Xm, const float4& Xp, const float4& B, int sel,
                                         float scale, float id0) {
-    if (((j + c) & 1) == 0) {
+    if (sel == 0) {
         const float w = __shfl_up_sync(SP_FULL, X.w, 1);
         float s = w + X.y;
         s = s + Xm.x;
@@ -464,15 +464,17 @@ __device__ __forceinline__ void sp_half(float4& X, const float4& Xm, const float
     }
 }
 
-// first half sweep from x = 0 (neighbour sum 0)
-__device__ __forceinline__ void sp_first(float4& X, const float4& B, int j, int c, float scale, float id0) {
-    if (((j + c) & 1) == 0) {
+// first half sweep from x = 0 (neighbour sum 0); the other colour stays 0
+__device__ __forceinline__ float4 sp_first(const float4& B, int sel, float scale, float id0) {
+    float4 X = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (sel == 0) {
         X.x = fmaf(scale, 0.f, B.x) * id0;
         X.z = fmaf(scale, 0.f, B.z) * id0;
     } else {
         X.y = fmaf(scale, 0.f, B.y) * id0;
         X.w = fmaf(scale, 0.f, B.w) * id0;
     }
+    return X;
 }
 
 __device__ __forceinline__ float sp_ax(float d0, float ms, float c, float w, float e, float sth, float nth) {
@@ -483,96 +485,109 @@ __device__ __forceinline__ float sp_ax(float d0, float ms, float c, float w, flo
     return fmaf(ms, nth, ax);
 }
 
+// The row loops run SP_U steps per trip, fully unrolled, so that a row's
+// registers sit in slot (row - first row) mod SP_U at compile-time indices
+// and the sliding window costs no moves.  Strip heights keep the step counts
+// multiples of SP_U: pre-smoothing walks rh + 10 rows (rh = 2 mod 6),
+// post-smoothing rh + 8 (rh = 4 mod 6).
+constexpr int SP_U = 6;
+
 // Pre-smoothing strip: x = 0, (red, black) x 2, x to the r array, r = b - A x,
 // b_coarse = R r.  Output columns [o, o + 116), rows [y0, y0 + rh); coarse
-// cells [o/2, o/2 + 58) x [y0/2, y0/2 + rh/2).  ring: SP_RING x 32 float4.
+// cells [o/2, o/2 + 58) x [y0/2, y0/2 + rh/2).  y0 even.  ring: SP_RING x 32
+// float4 (rows of b).
 __device__ __forceinline__ void strip_pre(const MgLev<float>& F, const MgLev<float>& C, float4* ring, int o, int y0,
                                           int rh) {
     const int lane = threadIdx.x & 31;
     const int s = o - 6;
     const float* bcol = F.b + s + 4 * lane;
-    const int ya = y0 - 5, yb = y0 + rh + 5;  // rows of b read
+    const int ya = y0 - 5, yb = y0 + rh + 5;  // rows of b read; ya is odd
 #pragma unroll
     for (int k = 0; k < SP_RING - 1; ++k) {
         cpa16(&ring[k * 32 + lane], bcol + (size_t)(ya + k) * F.pitch);
         cpa_commit();
     }
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 X0 = z4, X1 = z4, X2 = z4, X3 = z4, X4 = z4, X5 = z4;
-    float4 B0 = z4, B1 = z4, B2 = z4, B3 = z4, B4 = z4;
-    float2 S1 = make_float2(0.f, 0.f), S2 = S1, S3 = S1;
+    float4 X[SP_U], B[SP_U];
+#pragma unroll
+    for (int k = 0; k < SP_U; ++k) {
+        X[k] = z4;
+        B[k] = z4;
+    }
+    // restriction sums of the coarse row under way (A: two or three fine rows
+    // added) and of the next one (N), over the lane's two coarse columns; fine
+    // rows are added in increasing order, weights 1/4, 3/4, 3/4, 1/4
+    float2 A = make_float2(0.f, 0.f), N = A;
     const float scale = F.scale, id0 = F.invd[0], d0 = F.diag[0], ms = F.ms;
     const bool out_lo = lane >= 1 && lane <= 30;
-    for (int t = ya; t < yb; ++t) {
-        const int tn = t + SP_RING - 1;
-        if (tn < yb) cpa16(&ring[((tn - ya) % SP_RING) * 32 + lane], bcol + (size_t)tn * F.pitch);
-        cpa_commit();
-        cpa_wait<SP_RING - 1>();
-        X5 = X4;
-        X4 = X3;
-        X3 = X2;
-        X2 = X1;
-        X1 = X0;
-        X0 = z4;
-        B4 = B3;
-        B3 = B2;
-        B2 = B1;
-        B1 = B0;
-        B0 = ring[((t - ya) % SP_RING) * 32 + lane];
-        sp_first(X0, B0, t, 0, scale, id0);                    // row t
-        sp_half(X1, X2, X0, B1, t - 1, 1, scale, id0);         // row t - 1
-        sp_half(X2, X3, X1, B2, t - 2, 0, scale, id0);         // row t - 2
-        sp_half(X3, X4, X2, B3, t - 3, 1, scale, id0);         // row t - 3: final x
-        const int jx = t - 3;
-        if (jx >= y0 && jx < y0 + rh && out_lo) {
-            float* xr = F.r + (size_t)jx * F.pitch + s + 4 * lane;
-            if (lane == 1)
-                *reinterpret_cast<float2*>(xr + 2) = make_float2(X3.z, X3.w);
-            else if (lane == 30)
-                *reinterpret_cast<float2*>(xr) = make_float2(X3.x, X3.y);
-            else
-                *reinterpret_cast<float4*>(xr) = X3;
+    for (int tb = ya; tb < yb; tb += SP_U) {
+#pragma unroll
+        for (int u = 0; u < SP_U; ++u) {
+            const int t = tb + u;
+            const int pt = (u + 1) & 1;  // parity of t (tb is odd)
+            const int s0 = u, s1 = (u + 5) % 6, s2 = (u + 4) % 6, s3 = (u + 3) % 6, s4 = (u + 2) % 6,
+                      s5 = (u + 1) % 6;  // slots of rows t .. t - 5
+            const int tn = t + SP_RING - 1;
+            if (tn < yb) cpa16(&ring[((u + SP_RING - 1) % SP_RING) * 32 + lane], bcol + (size_t)tn * F.pitch);
+            cpa_commit();
+            cpa_wait<SP_RING - 1>();
+            B[s0] = ring[(u % SP_RING) * 32 + lane];
+            X[s0] = sp_first(B[s0], pt, scale, id0);                          // row t, colour 0
+            sp_half(X[s1], X[s2], X[s0], B[s1], (pt + 1 + 1) & 1, scale, id0);  // row t - 1, colour 1
+            sp_half(X[s2], X[s3], X[s1], B[s2], (pt + 2) & 1, scale, id0);      // row t - 2, colour 0
+            sp_half(X[s3], X[s4], X[s2], B[s3], (pt + 3 + 1) & 1, scale, id0);  // row t - 3, colour 1: final
+            const int jx = t - 3;
+            if (jx >= y0 && jx < y0 + rh && out_lo) {
+                float* xr = F.r + (size_t)jx * F.pitch + s + 4 * lane;
+                if (lane == 1)
+                    *reinterpret_cast<float2*>(xr + 2) = make_float2(X[s3].z, X[s3].w);
+                else if (lane == 30)
+                    *reinterpret_cast<float2*>(xr) = make_float2(X[s3].x, X[s3].y);
+                else
+                    *reinterpret_cast<float4*>(xr) = X[s3];
+            }
+            // residual of row t - 4 and the restriction's row sums
+            const float4& Xc = X[s4];
+            const float w = __shfl_up_sync(SP_FULL, Xc.w, 1), e = __shfl_down_sync(SP_FULL, Xc.x, 1);
+            float4 R;
+            R.x = B[s4].x - sp_ax(d0, ms, Xc.x, w, Xc.y, X[s5].x, X[s3].x);
+            R.y = B[s4].y - sp_ax(d0, ms, Xc.y, Xc.x, Xc.z, X[s5].y, X[s3].y);
+            R.z = B[s4].z - sp_ax(d0, ms, Xc.z, Xc.y, Xc.w, X[s5].z, X[s3].z);
+            R.w = B[s4].w - sp_ax(d0, ms, Xc.w, Xc.z, e, X[s5].w, X[s3].w);
+            const float rl = __shfl_up_sync(SP_FULL, R.w, 1), rr = __shfl_down_sync(SP_FULL, R.x, 1);
+            float2 rs;  // row sums of row t - 4 under the lane's coarse columns
+            rs.x = fmaf(0.25f, rl, 0.f);
+            rs.x = fmaf(0.75f, R.x, rs.x);
+            rs.x = fmaf(0.75f, R.y, rs.x);
+            rs.x = fmaf(0.25f, R.z, rs.x);
+            rs.y = fmaf(0.25f, R.y, 0.f);
+            rs.y = fmaf(0.75f, R.z, rs.y);
+            rs.y = fmaf(0.75f, R.w, rs.y);
+            rs.y = fmaf(0.25f, rr, rs.y);
+            const int jr = t - 4;
+            if (pt) {
+                // odd fine row 2J + 1: third term of coarse row J, first of J + 1
+                A.x = fmaf(0.75f, rs.x, A.x);
+                A.y = fmaf(0.75f, rs.y, A.y);
+                N.x = fmaf(0.25f, rs.x, 0.f);
+                N.y = fmaf(0.25f, rs.y, 0.f);
+            } else {
+                // even fine row 2J + 2: last term of coarse row J, second of J + 1
+                A.x = fmaf(0.25f, rs.x, A.x);
+                A.y = fmaf(0.25f, rs.y, A.y);
+                if (jr >= y0 + 2 && jr < y0 + rh + 2 && out_lo) {
+                    float* cb = C.b + (size_t)((jr - 2) >> 1) * C.pitch + (s >> 1) + 2 * lane;
+                    if (lane == 1)
+                        cb[1] = 0.25f * A.y;
+                    else if (lane == 30)
+                        cb[0] = 0.25f * A.x;
+                    else
+                        *reinterpret_cast<float2*>(cb) = make_float2(0.25f * A.x, 0.25f * A.y);
+                }
+                A.x = fmaf(0.75f, rs.x, N.x);
+                A.y = fmaf(0.75f, rs.y, N.y);
+            }
         }
-        // residual of row t - 4 and the restriction's row sums
-        const float w = __shfl_up_sync(SP_FULL, X4.w, 1), e = __shfl_down_sync(SP_FULL, X4.x, 1);
-        float4 R;
-        R.x = B4.x - sp_ax(d0, ms, X4.x, w, X4.y, X5.x, X3.x);
-        R.y = B4.y - sp_ax(d0, ms, X4.y, X4.x, X4.z, X5.y, X3.y);
-        R.z = B4.z - sp_ax(d0, ms, X4.z, X4.y, X4.w, X5.z, X3.z);
-        R.w = B4.w - sp_ax(d0, ms, X4.w, X4.z, e, X5.w, X3.w);
-        const float rl = __shfl_up_sync(SP_FULL, R.w, 1), rr = __shfl_down_sync(SP_FULL, R.x, 1);
-        float2 S0;
-        S0.x = fmaf(0.25f, rl, 0.f);
-        S0.x = fmaf(0.75f, R.x, S0.x);
-        S0.x = fmaf(0.75f, R.y, S0.x);
-        S0.x = fmaf(0.25f, R.z, S0.x);
-        S0.y = fmaf(0.25f, R.y, 0.f);
-        S0.y = fmaf(0.75f, R.z, S0.y);
-        S0.y = fmaf(0.75f, R.w, S0.y);
-        S0.y = fmaf(0.25f, rr, S0.y);
-        const int jr = t - 4;
-        if (!(jr & 1) && jr >= y0 + 2 && jr < y0 + rh + 2 && out_lo) {
-            // coarse row (jr - 2) / 2 from fine rows jr - 3 .. jr
-            float2 acc;
-            acc.x = fmaf(0.25f, S3.x, 0.f);
-            acc.x = fmaf(0.75f, S2.x, acc.x);
-            acc.x = fmaf(0.75f, S1.x, acc.x);
-            acc.x = fmaf(0.25f, S0.x, acc.x);
-            acc.y = fmaf(0.25f, S3.y, 0.f);
-            acc.y = fmaf(0.75f, S2.y, acc.y);
-            acc.y = fmaf(0.75f, S1.y, acc.y);
-            acc.y = fmaf(0.25f, S0.y, acc.y);
-            float* cb = C.b + (size_t)((jr - 2) >> 1) * C.pitch + (s >> 1) + 2 * lane;
-            if (lane == 1)
-                cb[1] = 0.25f * acc.y;
-            else if (lane == 30)
-                cb[0] = 0.25f * acc.x;
-            else
-                *reinterpret_cast<float2*>(cb) = make_float2(0.25f * acc.x, 0.25f * acc.y);
-        }
-        S3 = S2;
-        S2 = S1;
-        S1 = S0;
     }
     cpa_wait<0>();
 }
@@ -609,8 +624,8 @@ __device__ __forceinline__ void strip_post(const MgLev<float>& C, const MgLev<fl
     const bool edge = lane == 0 || lane == 31;
     const int ya = y0 - 4, yb = y0 + rh + 4;  // rows read: [ya, yb), ya even
     float* rg = reinterpret_cast<float*>(ring);
-    auto issue = [&](int row) {
-        float* sl = rg + ((row - ya) % SP_RING) * SP_POST_SLOT;
+    auto issue = [&](int row, int slot) {
+        float* sl = rg + slot * SP_POST_SLOT;
         if (row < yb) {
             cpa16(sl + 4 * lane, F.b + (size_t)row * F.pitch + col);
             cpa16(sl + 128 + 4 * lane, F.r + (size_t)row * F.pitch + col);
@@ -623,60 +638,65 @@ __device__ __forceinline__ void strip_post(const MgLev<float>& C, const MgLev<fl
         cpa_commit();
     };
 #pragma unroll
-    for (int k = 0; k < SP_RING - 1; ++k) issue(ya + k);
+    for (int k = 0; k < SP_RING - 1; ++k) issue(ya + k, k);
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    // horizontal coarse rows: HA = row hi - 1, HB = row hi, hi = (row + 1) / 2
     auto hrow_direct = [&](int J) {
         const float* crow = C.x + (size_t)J * C.pitch;
         const float e = edge ? crow[ecol] : 0.f;
         return sp_hrow(*reinterpret_cast<const float2*>(crow + ccol), e, e);
     };
-    float4 HA = hrow_direct(ya / 2 - 1);
-    float4 HB = hrow_direct(ya / 2);
-    float4 X0 = z4, X1 = z4, X2 = z4, X3 = z4, X4 = z4, X5 = z4;
-    float4 B0 = z4, B1 = z4, B2 = z4, B3 = z4, Bn = z4;
+    // horizontal coarse rows by slot (J - ya / 2) mod 3
+    float4 H[3];
+    H[0] = hrow_direct(ya / 2);
+    H[1] = z4;
+    H[2] = hrow_direct(ya / 2 - 1);
+    float4 X[SP_U], B[SP_U];
+#pragma unroll
+    for (int k = 0; k < SP_U; ++k) {
+        X[k] = z4;
+        B[k] = z4;
+    }
     const float scale = F.scale, id0 = F.invd[0];
     const bool out = lane >= 1 && lane <= 30;
     // step t forms x of row t + 1, then sweeps rows t .. t - 3
-    for (int t = ya - 1; t < yb - 1; ++t) {
-        const int row = t + 1;
-        issue(row + SP_RING - 1);
-        cpa_wait<SP_RING - 1>();
-        X5 = X4;
-        X4 = X3;
-        X3 = X2;
-        X2 = X1;
-        X1 = X0;
-        B3 = B2;
-        B2 = B1;
-        B1 = B0;
-        B0 = Bn;
-        const float* sl = rg + ((row - ya) % SP_RING) * SP_POST_SLOT;
-        Bn = *reinterpret_cast<const float4*>(sl + 4 * lane);
-        const float4 xr = *reinterpret_cast<const float4*>(sl + 128 + 4 * lane);
-        if (row & 1) {
-            HA = HB;
-            const float e = edge ? sl[320 + (lane >> 4)] : 0.f;
-            HB = sp_hrow(*reinterpret_cast<const float2*>(sl + 256 + 2 * lane), e, e);
+    for (int tb = ya - 1; tb < yb - 1; tb += SP_U) {
+#pragma unroll
+        for (int u = 0; u < SP_U; ++u) {
+            const int t = tb + u, row = t + 1;
+            const int pr = u & 1;  // parity of row (ya is even)
+            const int s0 = u, s1 = (u + 5) % 6, s2 = (u + 4) % 6, s3 = (u + 3) % 6, s4 = (u + 2) % 6,
+                      s5 = (u + 1) % 6;  // slots of rows t + 1 .. t - 4
+            issue(row + SP_RING - 1, (u + SP_RING - 1) % SP_RING);
+            cpa_wait<SP_RING - 1>();
+            const float* sl = rg + (u % SP_RING) * SP_POST_SLOT;
+            B[s0] = *reinterpret_cast<const float4*>(sl + 4 * lane);
+            const float4 xr = *reinterpret_cast<const float4*>(sl + 128 + 4 * lane);
+            const int ch = ((u + 1) >> 1) % 3, cl = (ch + 2) % 3;  // slots of coarse rows hi, hi - 1
+            if (pr) {
+                const float e = edge ? sl[320 + (lane >> 4)] : 0.f;
+                H[ch] = sp_hrow(*reinterpret_cast<const float2*>(sl + 256 + 2 * lane), e, e);
+            }
+            const float4 H0 = pr ? H[cl] : H[ch], H1 = pr ? H[ch] : H[cl];  // rows J, NJ
+            float4& X0 = X[s0];
+            X0.x = xr.x + fmaf(0.25f, H1.x, 0.75f * H0.x);
+            X0.y = xr.y + fmaf(0.25f, H1.y, 0.75f * H0.y);
+            X0.z = xr.z + fmaf(0.25f, H1.z, 0.75f * H0.z);
+            X0.w = xr.w + fmaf(0.25f, H1.w, 0.75f * H0.w);
+            // row t has parity 1 - pr
+            sp_half(X[s1], X[s2], X[s0], B[s1], (pr + 1 + 1) & 1, scale, id0);  // row t, colour 1
+            sp_half(X[s2], X[s3], X[s1], B[s2], (pr + 2) & 1, scale, id0);      // row t - 1, colour 0
+            sp_half(X[s3], X[s4], X[s2], B[s3], (pr + 3 + 1) & 1, scale, id0);  // row t - 2, colour 1
+            sp_half(X[s4], X[s5], X[s3], B[s4], (pr + 4) & 1, scale, id0);      // row t - 3, colour 0: final
+            const int jx = t - 3;
+            if (jx >= y0 && jx < y0 + rh && out)
+                *reinterpret_cast<float4*>(F.x + (size_t)jx * F.pitch + col) = X[s4];
         }
-        const float4 H0 = (row & 1) ? HA : HB, H1 = (row & 1) ? HB : HA;
-        X0.x = xr.x + fmaf(0.25f, H1.x, 0.75f * H0.x);
-        X0.y = xr.y + fmaf(0.25f, H1.y, 0.75f * H0.y);
-        X0.z = xr.z + fmaf(0.25f, H1.z, 0.75f * H0.z);
-        X0.w = xr.w + fmaf(0.25f, H1.w, 0.75f * H0.w);
-        sp_half(X1, X2, X0, B0, t, 1, scale, id0);          // row t
-        sp_half(X2, X3, X1, B1, t - 1, 0, scale, id0);      // row t - 1
-        sp_half(X3, X4, X2, B2, t - 2, 1, scale, id0);      // row t - 2
-        sp_half(X4, X5, X3, B3, t - 3, 0, scale, id0);      // row t - 3: final x
-        const int jx = t - 3;
-        if (jx >= y0 && jx < y0 + rh && out)
-            *reinterpret_cast<float4*>(F.x + (size_t)jx * F.pitch + col) = X4;
     }
     cpa_wait<0>();
 }
 
 template <typename T, int TW, int TH>
-__global__ void __launch_bounds__(FT_THREADS) k_mg_pre(MgLev<T> F, MgLev<T> C, MgBc p, SolverState* S, int inner,
+__global__ void __launch_bounds__(FT_THREADS, 3) k_mg_pre(MgLev<T> F, MgLev<T> C, MgBc p, SolverState* S, int inner,
                                                        StripMap m) {
     if (!block_live(S, inner)) return;
     constexpr int H = 5, W = TW + 2 * H, HT = TH + 2 * H;
@@ -792,7 +812,7 @@ __global__ void __launch_bounds__(FT_THREADS) k_mg_pre(MgLev<T> F, MgLev<T> C, M
 }
 
 template <typename T, int TW, int TH>
-__global__ void __launch_bounds__(FT_THREADS) k_mg_post(MgLev<T> C, MgLev<T> F, MgBc p, SolverState* S, int inner,
+__global__ void __launch_bounds__(FT_THREADS, 3) k_mg_post(MgLev<T> C, MgLev<T> F, MgBc p, SolverState* S, int inner,
                                                         StripMap m) {
     if (!block_live(S, inner)) return;
     constexpr int H = 4, W = TW + 2 * H, HT = TH + 2 * H;
@@ -1221,14 +1241,18 @@ static StripMap strip_map(int nx, int ny, int tw, int th, int strip_rows, bool p
     const int nty = (ny + th - 1) / th;
     m.tya = m.tyb = nty;  // default: every tile in the first band
     m.nframe = m.ntx * nty;
-    if (strip_rows <= 0 || (strip_rows & 1)) return m;
-    const int out = pre ? SP_PRE_OUT : SP_POST_OUT, hc = pre ? 6 : 4, hr = pre ? 5 : 4;
+    if (strip_rows <= 0) return m;
+    // strip height nearest to strip_rows with rh + 2 hr a multiple of SP_U
+    const int hr = pre ? 5 : 4, want = (SP_U - (2 * hr) % SP_U) % SP_U;
+    const int dn = strip_rows - (((strip_rows - want) % SP_U) + SP_U) % SP_U, up = dn + SP_U;
+    const int rh = dn >= 2 && strip_rows - dn < up - strip_rows ? dn : up;
+    const int out = pre ? SP_PRE_OUT : SP_POST_OUT, hc = pre ? 6 : 4;
     const int x0 = 4 + hc, y0 = 6;  // first strip reads from column 4, row y0 - hr >= 1
     const int span = nx - 1 - SP_COLS - 4;  // last strip: 4 + out (ns - 1) + 128 <= nx - 1
     const int ns = span >= 0 ? span / out + 1 : 0;
-    const int nr = (ny - 1 - hr - y0) / strip_rows;  // y0 + rh nr + hr <= ny - 1
+    const int nr = (ny - 1 - hr - y0) / rh;  // y0 + rh nr + hr <= ny - 1
     if (ns < 1 || nr < 1) return m;
-    const int xb = x0 + out * ns, yb = y0 + strip_rows * nr;
+    const int xb = x0 + out * ns, yb = y0 + rh * nr;
     const int txa = (x0 + tw - 1) / tw, txb = xb / tw, tya = (y0 + th - 1) / th, tyb = yb / th;
     if (txa >= txb || tya >= tyb) return m;
     m.txa = txa;
@@ -1238,7 +1262,7 @@ static StripMap strip_map(int nx, int ny, int tw, int th, int strip_rows, bool p
     m.nframe = m.ntx * nty - (txb - txa) * (tyb - tya);
     m.ns = ns;
     m.nr = nr;
-    m.rh = strip_rows;
+    m.rh = rh;
     m.x0 = x0;
     m.y0 = y0;
     return m;

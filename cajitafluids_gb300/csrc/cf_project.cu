@@ -351,7 +351,7 @@ struct DivArgs {
     double mscale;  // -(1/dx)
     Stencil st;
     double *x, *r, *b;
-    float *r32, *e32;
+    float* r32;
     double *part0, *part1, *part2;
     double* out;
     SolverState* S;
@@ -392,27 +392,12 @@ __device__ __forceinline__ void put_r32(float* o, int pitch, int nx, int ny, int
 // narrow FP64 pipe, with an error (~1e-14 relative to |b| + |A x|) far below
 // what the 1e-8 divergence target needs.  nvcc --fmad=false keeps the
 // error-free transformations exact.
-__device__ __forceinline__ float2 df_two_sum(float a, float b) {
-    float s = a + b;
-    float bb = s - a;
-    float e = (a - (s - bb)) + (b - bb);
-    return make_float2(s, e);
-}
-__device__ __forceinline__ float2 df_quick(float a, float b) {  // |a| >= |b|
-    float s = a + b;
-    return make_float2(s, b - (s - a));
-}
 __device__ __forceinline__ float2 df_add(float2 x, float2 y) {
     float2 s = df_two_sum(x.x, y.x);
     float2 t = df_two_sum(x.y, y.y);
     s.y = s.y + t.x;
     s = df_quick(s.x, s.y);
     s.y = s.y + t.y;
-    return df_quick(s.x, s.y);
-}
-__device__ __forceinline__ float2 df_add_f(float2 x, float e) {
-    float2 s = df_two_sum(x.x, e);
-    s.y = s.y + x.y;
     return df_quick(s.x, s.y);
 }
 __device__ __forceinline__ float2 df_mul(float2 x, float2 y) {
@@ -506,7 +491,6 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
                 reinterpret_cast<float2*>(a.x)[k] = a.warm ? df_split(a.x[k]) : make_float2(0.f, 0.f);
                 float r = (float)b;
                 put_r32(a.r32, a.pitch32, a.nx, a.ny, a.per_x, a.per_y, c, j, r);
-                a.e32[(ptrdiff_t)j * a.pitch32 + c] = 0.f;
                 float z = a.st.minv32[edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y)] * r;
                 abb = fma(b, b, abb);
                 arz = fmaf(r, z, arz);
@@ -565,21 +549,8 @@ __device__ __forceinline__ bool outer_due(const SolverState* S) {
     return due != 0;
 }
 
-// Outer refinement, part 1: x += e (double-float += FP32), e = 0.  gated = 1
-// (inside the MG-PCG graph): only while the refinement is due.
-__global__ void k_outer_add(float2* x, float* e, int nx, int ny, int pitch, int pitch32, const SolverState* S,
-                            int gated) {
-    if (gated && !outer_due(S)) return;
-    int gi = blockIdx.x * blockDim.x + threadIdx.x;
-    int gj = blockIdx.y * blockDim.y + threadIdx.y;
-    if (gi >= nx || gj >= ny) return;
-    const size_t k = (size_t)gj * pitch + gi;
-    const ptrdiff_t k32 = (ptrdiff_t)gj * pitch32 + gi;
-    x[k] = df_add_f(x[k], e[k32]);
-    e[k32] = 0.f;
-}
-
-// Outer refinement, part 2: r = b - A x in double-float; inner r = hi part.
+// Outer refinement (reliable update): r = b - A x in double-float, x as the
+// inner iterations left it; inner r = hi part.
 struct Outer {
     int nx, ny, per_x, per_y, G, U, pitch, pitch32;
     float dfac[16];  // diagonal / scale by wall-adjacency bits
@@ -840,7 +811,6 @@ static DivArgs div_args(cf_ctx* c, const Stencil& st) {
     a.r = c->r.a;
     a.b = c->b.a;
     a.r32 = c->r32.a;
-    a.e32 = c->e32.a;
     a.part0 = c->partials;
     a.part1 = c->partials + c->n_units;
     a.part2 = c->partials + 2 * c->n_units;
@@ -918,12 +888,9 @@ static int launch_warm_init(cf_ctx* c, const Stencil& st, bool mixed) {
     return 1;
 }
 
-// the two outer-refinement kernels; gated = 1 inside the MG-PCG graph
+// the outer refinement; gated = 1 inside the MG-PCG graph
 static void launch_outer(cf_ctx* c, const Stencil& st, int gated) {
     Outer oa = outer_args(c, st, gated);
-    dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
-    k_outer_add<<<grd, blk, 0, c->stream>>>(reinterpret_cast<float2*>(c->x.a), c->e32.a, c->ph.nx, c->ph.ny,
-                                            c->vpitch, c->p32, c->S, gated);
     k_outer_resid<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(oa);
 }
 
@@ -996,7 +963,7 @@ static int ensure_graph_mg(cf_ctx* c, const Stencil& st) {
             if (mixed) {
                 cg32_launch_pair_mg(c, st);
                 launch_outer(c, st, 1);
-                per = 4 + cg32_mg_precondition(c, scale);
+                per = 3 + cg32_mg_precondition(c, scale);
             } else {
                 k_cg_dir_matvec64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
                 k_cg_update64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
@@ -1082,7 +1049,7 @@ static int launch_iterations(cf_ctx* c, const Stencil& st, bool mixed, bool mg, 
             k += 2;
             if (mg || i == n - 1) {
                 launch_outer(c, st, 1);
-                k += 2;
+                k += 1;
             }
             if (mg) k += cg32_mg_precondition(c, scale);
         } else {
@@ -1381,7 +1348,7 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
                 }
                 if (c->hS->status != ST_RUNNING) break;
                 launch_outer(c, st, 0);
-                c->launches += 2;
+                c->launches += 1;
                 if ((rc = read_state(c))) return rc;
                 if (++launches > max_launch) return fail(c, CF_ERR_NUMERIC, "mixed solver did not stop");
             }
