@@ -631,7 +631,9 @@ void cg32_launch_iteration(cf_ctx* c, const Stencil& st) {
 
 // z = V-cycle(r32), its periodic ghosts, rho = r.z; returns kernels launched
 int cg32_mg_precondition(cf_ctx* c, double scale) {
-    int n = mg_vcycle(c, scale);
+    bool done = false;
+    int n = mg_vcycle(c, scale, &done);
+    if (done) return n;  // r.z, the scalars and z's ghosts came with the finest post-smoothing
     if (c->ph.per_x || c->ph.per_y) {
         int m = c->ph.nx > c->ph.ny ? c->ph.nx : c->ph.ny;
         k_z32_ghosts<<<(m + 255) / 256, 256, 0, c->stream>>>(c->z32.a, c->ph.nx, c->ph.ny, c->p32, c->ph.per_x,

@@ -124,7 +124,11 @@ int div_norms(cf_ctx* c, double* l2, double* linf);
 // multigrid preconditioner (cf_mg.cu)
 int mg_setup(cf_ctx* c);
 void mg_free(cf_ctx* c);
-int mg_vcycle(cf_ctx* c, double scale0);  // returns kernels launched
+// Enqueues one V-cycle, returns kernels launched.  Mixed precision with
+// rz_done non-null: the finest post-smoothing kernel also forms rho = r.z,
+// the CG scalars and z's periodic ghosts when the level runs fused (*rz_done
+// tells whether it did).
+int mg_vcycle(cf_ctx* c, double scale0, bool* rz_done = nullptr);
 int mg_levels(const cf_ctx* c);
 double* mg_z64(cf_ctx* c);
 }  // namespace cf

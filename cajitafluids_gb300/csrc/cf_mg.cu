@@ -398,6 +398,58 @@ struct StripMap {
     int ns, nr, rh, x0, y0;
 };
 
+// Epilogue of the finest FP32 post-smoothing (mixed MG-PCG): rho = r.z over
+// the level (r = the level's b, z = its x), the CG scalars updated as by
+// k_mg_rz32, and the periodic ghost copies of z written with the edge cells.
+// Partials: one per frame tile (slot = block) and one per strip (slot =
+// nframe + strip); the last block to finish folds them in a fixed order.
+struct RzEpi {
+    int on;
+    double* part;
+};
+
+__device__ __forceinline__ void rz_finish(const RzEpi& E, SolverState* S, int nparts) {
+    if (last_block_arrive(&S->ticket[7])) {
+        const double rz = final_tree(E.part, nparts);
+        if (threadIdx.x == 0) {
+            S->ticket[7] = 0;
+            const double den = S->refreshed ? S->rho_prev : S->rho_in;
+            S->refreshed = 0;
+            S->beta_in = den != 0.0 ? rz / den : 0.0;
+            S->rho_in = rz;
+            if (isnan(rz))
+                S->status = ST_NAN;
+            else if (!(rz > 0.0))
+                S->inner_status = ST_BREAKDOWN;  // FP32 noise floor: refine and restart
+        }
+    }
+}
+
+// sum over the block's threads in a fixed order (FT_THREADS = CF_RED_THREADS)
+__device__ __forceinline__ double block_total(double v) {
+    __shared__ double ws[FT_THREADS / 32];
+    v = warp_fold(v);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = ws[0];
+#pragma unroll
+    for (int k = 1; k < FT_THREADS / 32; ++k) t = t + ws[k];
+    __syncthreads();
+    return t;
+}
+
+// cell (i, j) lies in the region written by the strips
+__device__ __forceinline__ bool in_strips(const StripMap& m, int i, int j) {
+    return m.ns > 0 && i >= m.x0 && i < m.x0 + SP_POST_OUT * m.ns && j >= m.y0 && j < m.y0 + m.rh * m.nr;
+}
+
+// a frame tile's share of r.z, then the fold by the last block
+__device__ __forceinline__ void post_epilogue(const RzEpi& E, SolverState* S, int nparts, double v) {
+    const double t = block_total(v);
+    if (threadIdx.x == 0) E.part[blockIdx.x] = t;
+    rz_finish(E, S, nparts);
+}
+
 __device__ __forceinline__ void frame_tile(const StripMap& m, int f, int& tx, int& ty) {
     const int top = m.tya * m.ntx;
     if (f < top) {
@@ -614,8 +666,9 @@ __device__ __forceinline__ float4 sp_hrow(float2 c, float el, float er) {
 // slots of 32 float4 (b), 32 float4 (x_pre), 32 float2 (coarse row) and the
 // coarse row's two outer neighbours (padded to 16 bytes).
 constexpr int SP_POST_SLOT = 32 * 4 + 32 * 4 + 32 * 2 + 4;  // floats per slot
-__device__ __forceinline__ void strip_post(const MgLev<float>& C, const MgLev<float>& F, float4* ring, int o,
-                                           int y0, int rh) {
+__device__ __forceinline__ float strip_post(const MgLev<float>& C, const MgLev<float>& F, float4* ring, int o,
+                                            int y0, int rh) {
+    float rz = 0.f;  // b.x over the cells this lane writes
     const int lane = threadIdx.x & 31;
     const int s = o - 4;
     const size_t col = (size_t)s + 4 * lane, ccol = (size_t)(s >> 1) + 2 * lane;
@@ -688,11 +741,17 @@ __device__ __forceinline__ void strip_post(const MgLev<float>& C, const MgLev<fl
             sp_half(X[s3], X[s4], X[s2], B[s3], (pr + 3 + 1) & 1, scale, id0);  // row t - 2, colour 1
             sp_half(X[s4], X[s5], X[s3], B[s4], (pr + 4) & 1, scale, id0);      // row t - 3, colour 0: final
             const int jx = t - 3;
-            if (jx >= y0 && jx < y0 + rh && out)
+            if (jx >= y0 && jx < y0 + rh && out) {
                 *reinterpret_cast<float4*>(F.x + (size_t)jx * F.pitch + col) = X[s4];
+                rz = fmaf(B[s4].x, X[s4].x, rz);
+                rz = fmaf(B[s4].y, X[s4].y, rz);
+                rz = fmaf(B[s4].z, X[s4].z, rz);
+                rz = fmaf(B[s4].w, X[s4].w, rz);
+            }
         }
     }
     cpa_wait<0>();
+    return rz;
 }
 
 template <typename T, int TW, int TH>
@@ -813,7 +872,7 @@ __global__ void __launch_bounds__(FT_THREADS, 3) k_mg_pre(MgLev<T> F, MgLev<T> C
 
 template <typename T, int TW, int TH>
 __global__ void __launch_bounds__(FT_THREADS, 3) k_mg_post(MgLev<T> C, MgLev<T> F, MgBc p, SolverState* S, int inner,
-                                                        StripMap m) {
+                                                           StripMap m, RzEpi E) {
     if (!block_live(S, inner)) return;
     constexpr int H = 4, W = TW + 2 * H, HT = TH + 2 * H;
     // coarse cells read by the prolongation of an interior tile's array
@@ -822,14 +881,22 @@ __global__ void __launch_bounds__(FT_THREADS, 3) k_mg_post(MgLev<T> C, MgLev<T> 
     constexpr size_t TILE_B = sizeof(T) * (2 * W * HT + CW * CH);
     constexpr size_t RING_B = STRIPS ? (FT_THREADS / 32) * SP_RING * SP_POST_SLOT * sizeof(float) : 0;
     __shared__ __align__(16) unsigned char smem[TILE_B > RING_B ? TILE_B : RING_B];
+    const int nparts = m.nframe + m.ns * m.nr;
     if constexpr (STRIPS) {
         if ((int)blockIdx.x >= m.nframe) {
             const int warp = threadIdx.x >> 5;
             const int k = ((int)blockIdx.x - m.nframe) * (FT_THREADS / 32) + warp;
-            if (k >= m.ns * m.nr) return;
-            const int sx = k % m.ns, sy = k / m.ns;
-            strip_post(C, F, reinterpret_cast<float4*>(smem) + warp * SP_RING * (SP_POST_SLOT / 4), m.x0 + SP_POST_OUT * sx,
-                       m.y0 + m.rh * sy, m.rh);
+            float rz = 0.f;
+            if (k < m.ns * m.nr) {
+                const int sx = k % m.ns, sy = k / m.ns;
+                rz = strip_post(C, F, reinterpret_cast<float4*>(smem) + warp * SP_RING * (SP_POST_SLOT / 4),
+                                m.x0 + SP_POST_OUT * sx, m.y0 + m.rh * sy, m.rh);
+            }
+            if (E.on) {
+                const double d = warp_fold((double)rz);
+                if (k < m.ns * m.nr && (threadIdx.x & 31) == 0) E.part[m.nframe + k] = d;
+                rz_finish(E, S, nparts);
+            }
             return;
         }
     }
@@ -874,10 +941,14 @@ __global__ void __launch_bounds__(FT_THREADS, 3) k_mg_post(MgLev<T> C, MgLev<T> 
         ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 0, 2, false);
         ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 1, 1, false);
         ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 0, 0, false);
+        T rz = T(0);
         for (int k = threadIdx.x; k < TW * TH; k += FT_THREADS) {
             const int li = k % TW, lj = k / TW;
-            F.x[(size_t)(j0 + lj) * F.pitch + i0 + li] = xs[(lj + H) * W + li + H];
+            const int q = (lj + H) * W + li + H;
+            F.x[(size_t)(j0 + lj) * F.pitch + i0 + li] = xs[q];
+            if (E.on && !in_strips(m, i0 + li, j0 + lj)) rz = mg_fma(bs[q], xs[q], rz);
         }
+        if (E.on) post_epilogue(E, S, nparts, (double)rz);
         return;
     }
     ft_load<T, TW, TH, H>(F, p, xs, bs, i0, j0, F.r);
@@ -904,10 +975,29 @@ __global__ void __launch_bounds__(FT_THREADS, 3) k_mg_post(MgLev<T> C, MgLev<T> 
     ft_half<T, TW, TH, H>(F, p, xs, bs, i0, j0, 0, 2, false);
     ft_half<T, TW, TH, H>(F, p, xs, bs, i0, j0, 1, 1, false);
     ft_half<T, TW, TH, H>(F, p, xs, bs, i0, j0, 0, 0, false);
+    T rz = T(0);
     for (int k = threadIdx.x; k < TW * TH; k += FT_THREADS) {
         const int gi = i0 + k % TW, gj = j0 + k / TW;
-        if (gi < F.nx && gj < F.ny) F.x[(size_t)gj * F.pitch + gi] = xs[(gj - (j0 - H)) * W + (gi - (i0 - H))];
+        if (gi < F.nx && gj < F.ny) {
+            const int q = (gj - (j0 - H)) * W + (gi - (i0 - H));
+            const T v = xs[q];
+            T* row = F.x + (size_t)gj * F.pitch;
+            row[gi] = v;
+            if (E.on) {
+                if (!in_strips(m, gi, gj)) rz = mg_fma(bs[q], v, rz);
+                // ghost copies along periodic axes (the finest level's x has a ghost ring)
+                if (p.per_x) {
+                    if (gi == 0) row[F.nx] = v;
+                    if (gi == F.nx - 1) row[-1] = v;
+                }
+                if (p.per_y) {
+                    if (gj == 0) F.x[(ptrdiff_t)F.ny * F.pitch + gi] = v;
+                    if (gj == F.ny - 1) F.x[-(ptrdiff_t)F.pitch + gi] = v;
+                }
+            }
+        }
     }
+    if (E.on) post_epilogue(E, S, nparts, (double)rz);
 }
 
 // tile shapes: 64 x 32 (FP64: 64 x 24, both arrays in 48 KB of shared
@@ -1137,6 +1227,7 @@ struct MgHierarchy {
     int nlev = 0;
     int fused = -1;  // 1: all levels fused, 0: none, -1: by level (see vcycle)
     int strip_rows = 32;  // rows per FP32 register strip (0: tiles only)
+    int rz_fused = 1;     // mixed: r.z and z's ghosts in the finest post-smoothing kernel
     MgLev<double> d[16];
     MgLev<float> f[16];
     double* z64 = nullptr;
@@ -1173,6 +1264,7 @@ int mg_setup(cf_ctx* c) {
     c->mg = H;
     if (const char* e = getenv("CF_MG_FUSED")) H->fused = atoi(e) != 0;
     if (const char* e = getenv("CF_MG_STRIPS")) H->strip_rows = atoi(e);
+    if (const char* e = getenv("CF_MG_RZ_FUSED")) H->rz_fused = atoi(e) != 0;
     int nx = c->ph.nx, ny = c->ph.ny;
     for (int l = 0; l < 16 && !rc; ++l) {
         if (l == 0) {
@@ -1271,7 +1363,8 @@ static StripMap strip_map(int nx, int ny, int tw, int th, int strip_rows, bool p
 static int launch_blocks(const StripMap& m) { return m.nframe + (m.ns * m.nr + FT_THREADS / 32 - 1) / (FT_THREADS / 32); }
 
 template <typename T>
-static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, int fused, int strip_rows) {
+static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, int fused, int strip_rows,
+                  double* epi_part, bool* epi_done) {
     MgBc p{c->ph.per_x, c->ph.per_y, {c->ph.bc[0], c->ph.bc[1], c->ph.bc[2], c->ph.bc[3]}};
     double s = scale0;
     for (int l = 0; l < nlev; ++l) {
@@ -1344,14 +1437,19 @@ static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, 
     }
     for (int l = top_end - 1; l >= 0; --l) {
         if (fuse_level(l)) {
+            RzEpi E{0, epi_part};
+            if (l == 0 && epi_part) {
+                E.on = 1;
+                *epi_done = true;
+            }
             if (big(lev[l])) {
                 const StripMap m = strip_map(lev[l].nx, lev[l].ny, 64, TH, srows, false);
                 k_mg_post<T, 64, TH><<<launch_blocks(m), FT_THREADS, 0, c->stream>>>(lev[l + 1], lev[l], p, c->S,
-                                                                                    inner, m);
+                                                                                    inner, m, E);
             } else {
                 const StripMap m = strip_map(lev[l].nx, lev[l].ny, 32, 16, 0, false);
                 k_mg_post<T, 32, 16><<<launch_blocks(m), FT_THREADS, 0, c->stream>>>(lev[l + 1], lev[l], p, c->S,
-                                                                                    inner, m);
+                                                                                    inner, m, E);
             }
             ++launches;
             continue;
@@ -1369,10 +1467,17 @@ static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, 
 // Enqueue z = V-cycle(r) at stencil scale scale0 (FP64: z64 <- r; mixed:
 // z32 <- r32) and return the number of kernels launched.  Every kernel
 // returns at once when the solve has stopped.
-int mg_vcycle(cf_ctx* c, double scale0) {
+int mg_vcycle(cf_ctx* c, double scale0, bool* rz_done) {
     MgHierarchy* H = static_cast<MgHierarchy*>(c->mg);
-    if (c->precision == CF_PREC_MIXED) return vcycle<float>(c, H->f, H->nlev, scale0, 1, H->fused, H->strip_rows);
-    return vcycle<double>(c, H->d, H->nlev, scale0, 0, H->fused, 0);
+    bool done = false;
+    int n;
+    if (c->precision == CF_PREC_MIXED)
+        n = vcycle<float>(c, H->f, H->nlev, scale0, 1, H->fused, H->strip_rows,
+                          rz_done && H->rz_fused ? c->partials : nullptr, &done);
+    else
+        n = vcycle<double>(c, H->d, H->nlev, scale0, 0, H->fused, 0, nullptr, &done);
+    if (rz_done) *rz_done = done;
+    return n;
 }
 
 int mg_levels(const cf_ctx* c) { return c->mg ? static_cast<const MgHierarchy*>(c->mg)->nlev : 0; }

@@ -143,9 +143,10 @@ def test_mixed_mg_steps(built):
     assert np.abs(qa - qb).max() <= 1e-4
 
 
-def _mixed_mg_run(nx, ny, periodic, bc, strips, monkeypatch, seed):
+def _mixed_mg_run(nx, ny, periodic, bc, strips, monkeypatch, seed, rz_fused="0"):
     from cajitafluids_gb300 import Context
     monkeypatch.setenv("CF_MG_STRIPS", strips)
+    monkeypatch.setenv("CF_MG_RZ_FUSED", rz_fused)
     rng = np.random.default_rng(seed)
     shapes = {"q": (ny, nx), "u": (ny, nx + (0 if periodic[0] else 1)), "v": (ny + (0 if periodic[1] else 1), nx)}
     c = Context(nx, ny, hi=(1.0, ny / nx), periodic=periodic, precision="mixed")
@@ -168,7 +169,9 @@ def _mixed_mg_run(nx, ny, periodic, bc, strips, monkeypatch, seed):
 def test_mixed_mg_register_strips(built, monkeypatch, nx, ny, periodic, bc):
     """The FP32 register strips (interior of the large levels) and the tile
     kernels compute identical V-cycles: projections with strips of 32 and 8
-    rows equal those with tiles only (CF_MG_STRIPS=0) bit for bit."""
+    rows equal those with tiles only (CF_MG_STRIPS=0) bit for bit.  r.z is
+    formed by its own kernel here (CF_MG_RZ_FUSED=0): the fused form sums in
+    an order that follows the tiling."""
     ref_st, ref = _mixed_mg_run(nx, ny, periodic, bc, "0", monkeypatch, nx + ny)
     assert ref_st[0]["iterations"] > 2
     for strips in ("32", "8"):
@@ -178,3 +181,24 @@ def test_mixed_mg_register_strips(built, monkeypatch, nx, ny, periodic, bc):
             assert a["r_norm"] == b["r_norm"], strips
         for f in ("p", "u", "v"):
             assert np.array_equal(ref[f], out[f]), (strips, f)
+
+
+@pytest.mark.parametrize("nx,ny,periodic,bc", [
+    (2048, 1024, (True, True), (0, 0, 0, 0)),
+    (2100, 1100, (False, False), (0, 1, 0, 1)),
+    (200, 136, (True, False), (0, 0, 0, 1)),
+    (96, 64, (True, True), (0, 0, 0, 0)),
+])
+def test_mixed_mg_rz_fused(built, monkeypatch, nx, ny, periodic, bc):
+    """r.z, the CG scalars and z's periodic ghosts formed by the finest
+    post-smoothing kernel (default) agree with the separate kernels up to the
+    order of the FP32 sums: same iteration counts (within one), same
+    projected velocities to FP32 accuracy."""
+    ref_st, ref = _mixed_mg_run(nx, ny, periodic, bc, "32", monkeypatch, nx + ny, rz_fused="0")
+    st, out = _mixed_mg_run(nx, ny, periodic, bc, "32", monkeypatch, nx + ny, rz_fused="1")
+    for a, b in zip(ref_st, st):
+        assert a["status"] == b["status"]
+        assert abs(a["iterations"] - b["iterations"]) <= 1
+    for f in ("u", "v"):
+        d = np.abs(ref[f] - out[f]).max()
+        assert d <= 1e-6 * np.abs(ref[f]).max(), (f, d)
