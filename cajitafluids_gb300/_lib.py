@@ -132,6 +132,7 @@ SIGNATURES = {
                                     ctypes.POINTER(SolveStats), _dp, _dp, _dp, _dp, _dp, _dp]),
     "cf_div_norms": (ctypes.c_int, [_vp, _dp, _dp]),
     "cf_max_velocity": (ctypes.c_int, [_vp, _dp]),
+    "cf_test_conversions": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_float), _dp]),
     "cf_interp_points": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     "cf_trace_points": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_double, _dp]),
     "cf_cell_velocity": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_ssize_t, ctypes.c_ssize_t]),

@@ -241,6 +241,16 @@ class Context:
         self._check(self.lib.cf_div_norms(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def test_conversions(self, d: np.ndarray):
+        """The device's integer-pipe FP64 -> FP32 and FP32 -> FP64 conversions of d."""
+        d = np.ascontiguousarray(d, dtype=np.float64).ravel()
+        f = np.empty(d.size, dtype=np.float32)
+        w = np.empty(d.size, dtype=np.float64)
+        self._check(self.lib.cf_test_conversions(self.h, d.size, d.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                 f.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                 w.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return f, w
+
     def max_velocity(self) -> float:
         a = ctypes.c_double()
         self._check(self.lib.cf_max_velocity(self.h, ctypes.byref(a)))

@@ -704,6 +704,28 @@ int cf_div_norms(cf_ctx* ctx, double* l2, double* linf) {
     return div_norms(ctx, l2, linf);
 }
 
+int cf_test_conversions(cf_ctx* ctx, int n, const double* d, float* f, double* w) {
+    if (!ctx || n < 0 || (n > 0 && (!d || !f || !w))) return CF_ERR_INVALID;
+    if (n == 0) return CF_OK;
+    CF_GUARD_BEGIN
+    cudaSetDevice(ctx->device);
+    double *dd = nullptr, *dw = nullptr;
+    float* df = nullptr;
+    int rc = cuda_check(ctx, cudaMalloc(&dd, sizeof(double) * n), "alloc");
+    if (!rc) rc = cuda_check(ctx, cudaMalloc(&dw, sizeof(double) * n), "alloc");
+    if (!rc) rc = cuda_check(ctx, cudaMalloc(&df, sizeof(float) * n), "alloc");
+    if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(dd, d, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream), "copy");
+    if (!rc) rc = cuda_check(ctx, launch_test_convert(ctx, n, dd, df, dw), "convert");
+    if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(f, df, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(w, dw, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    if (!rc) rc = sync(ctx, "conversions");
+    cudaFree(dd);
+    cudaFree(dw);
+    cudaFree(df);
+    return rc;
+    CF_GUARD_END
+}
+
 int cf_max_velocity(cf_ctx* ctx, double* umax) {
     if (!ctx || !umax) return CF_ERR_INVALID;
     cudaSetDevice(ctx->device);

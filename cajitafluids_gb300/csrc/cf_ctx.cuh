@@ -92,6 +92,7 @@ cudaError_t launch_interp_points(cf_ctx* c, int field, int order, int n, const d
 cudaError_t launch_trace_points(cf_ctx* c, int n, const double* d_xy, double dt, double* d_out);
 cudaError_t launch_cell_velocity(cf_ctx* c, double* d_uc, double* d_vc);
 cudaError_t launch_max_velocity(cf_ctx* c, double* d_out);
+cudaError_t launch_test_convert(cf_ctx* c, int n, const double* d, float* f, double* w);
 cudaError_t launch_convert_q(cf_ctx* c, int to_device, int version);
 cudaError_t launch_q_to_f64(cf_ctx* c, int version, double* dst, cudaStream_t stream);
 

@@ -216,7 +216,7 @@ __global__ void k_to32(Grid<double> src, Grid<float> dst) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= src.ex || j >= src.ey) return;
-    dst.at(i, j) = (float)src.at(i, j);
+    dst.at(i, j) = d2f_rn(src.at(i, j));
 }
 
 __device__ __forceinline__ bool in_box_idx(const Phys& p, int ent, int li, int lj) {
@@ -540,6 +540,22 @@ cudaError_t launch_trace_points(cf_ctx* c, int n, const double* d_xy, double dt,
     int s = c->cur;
     Pts a{c->ph, c->u[s], c->u[s], c->v[s], 0, 1, n, d_xy, d_out, dt};
     k_trace_points<<<(n + 127) / 128, 128, 0, c->stream>>>(a);
+    c->launches += 1;
+    return cudaGetLastError();
+}
+
+// test export: the integer-pipe conversions applied to n values
+__global__ void k_test_convert(int n, const double* d, float* f, double* w) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float v = d2f_rn(d[k]);
+    f[k] = v;
+    w[k] = f2d_exact(v);
+}
+
+cudaError_t launch_test_convert(cf_ctx* c, int n, const double* d, float* f, double* w) {
+    if (n <= 0) return cudaSuccess;
+    k_test_convert<<<(n + 255) / 256, 256, 0, c->stream>>>(n, d, f, w);
     c->launches += 1;
     return cudaGetLastError();
 }

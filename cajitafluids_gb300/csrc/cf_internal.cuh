@@ -170,6 +170,43 @@ __device__ __forceinline__ int wrap_index(int g, int n, int per) {
     return g < 0 ? g + n : g;
 }
 
+// FP32 <-> FP64 conversions by bit manipulation on the integer pipe (GB300's
+// FP64 pipe, which executes the hardware conversions, is narrow).  Straight
+// from the IEEE 754 binary32/binary64 layouts: a normal binary32 widens
+// exactly by re-biasing the exponent (+896) and shifting the significand by
+// 29 bits; a binary64 in the binary32 normal range narrows by keeping the top
+// 23 significand bits and rounding on the 29 dropped ones, to nearest with
+// ties to even (a carry out of the significand increments the exponent,
+// which is the correctly rounded result up to infinity).  Zeros take the same
+// path; a warp holding any other special value (subnormal, infinity, NaN,
+// out of range) uses the hardware conversion.
+__device__ __forceinline__ double f2d_exact(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    const bool fast = e != 0xffu && (e != 0u || m == 0u);
+    if (__all_sync(__activemask(), fast)) {
+        const unsigned hi = (u & 0x80000000u) | (e == 0u ? 0u : ((e + 896u) << 20) | (m >> 3));
+        const unsigned lo = m << 29;
+        return __hiloint2double((int)hi, (int)lo);
+    }
+    return (double)f;
+}
+
+__device__ __forceinline__ float d2f_rn(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    const bool zero = (hi & 0x7fffffffu) == 0u && lo == 0u;
+    const bool fast = zero || (e >= 897u && e <= 1150u);
+    if (__all_sync(__activemask(), fast)) {
+        const unsigned m23 = ((hi & 0xfffffu) << 3) | (lo >> 29);
+        const unsigned rest = lo & 0x1fffffffu, half = 0x10000000u;
+        const unsigned up = (rest > half || (rest == half && (m23 & 1u))) ? 1u : 0u;
+        const unsigned fb = (hi & 0x80000000u) | (zero ? 0u : (((e - 896u) << 23) | m23) + up);
+        return __uint_as_float(fb);
+    }
+    return __double2float_rn(d);
+}
+
 // Double-float (hi + lo FP32 pair) error-free sums (Knuth two-sum, Dekker
 // quick two-sum); exact with --fmad=false.
 __device__ __forceinline__ float2 df_two_sum(float a, float b) {

@@ -356,6 +356,8 @@ struct DivArgs {
     double* out;
     SolverState* S;
     int warm;  // keep x from the previous solve (warm start) instead of x = 0
+    int mixed;        // k_div_norms: squares and magnitudes in FP32
+    float mscale32;   // -(1/dx) in FP32
 };
 
 __device__ __forceinline__ double div_b(const DivArgs& a, int gi, int gj) {
@@ -408,8 +410,8 @@ __device__ __forceinline__ float2 df_mul(float2 x, float2 y) {
     return df_quick(p, e);
 }
 __device__ __forceinline__ float2 df_split(double v) {
-    float hi = __double2float_rn(v);
-    return make_float2(hi, __double2float_rn(v - (double)hi));
+    const float hi = d2f_rn(v);
+    return make_float2(hi, d2f_rn(v - f2d_exact(hi)));
 }
 
 // FP64 init: b, r = b, x = 0, partial r.z and r.r
@@ -465,14 +467,14 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init64(DivArgs a) {
     }
 }
 
-// Mixed init: b (FP64, kept for the outer residual), x = 0, inner r = (float)b,
-// e = 0; partial b.b (FP64), inner r.z and r.r (FP32 per lane, FP64 beyond).
+// Mixed init: b (double-float, kept for the outer residual), x = 0, inner
+// r = hi part of b; partial b.b (the tolerance base), inner r.z and r.r
+// (FP32 per lane, FP64 beyond).
 __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
     SolverState* S = a.S;
     const int lane = threadIdx.x & 31;
     const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
-    double abb = 0.0;
-    float arz = 0.f, arr = 0.f;
+    float abb = 0.f, arz = 0.f, arr = 0.f;
     if (unit < a.U) {
         const int g = unit % a.G, band = unit / a.G;
         const int c0 = g * CF_UNIT_COLS + 2 * lane;
@@ -483,24 +485,25 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
             for (int s = 0; s < 2; ++s) {
                 int c = c0 + s;
                 if (c >= a.nx) continue;
-                double b = div_b(a, c, j);
-                size_t k = (size_t)j * a.pitch + c;
-                reinterpret_cast<float2*>(a.b)[k] = df_split(b);
+                const double b = div_b(a, c, j);
+                const size_t k = (size_t)j * a.pitch + c;
+                const float2 bs = df_split(b);
+                reinterpret_cast<float2*>(a.b)[k] = bs;
                 // x as a double-float pair: 0, or (warm start) the previous
                 // FP64 solution split in place (same 8 bytes per cell)
                 reinterpret_cast<float2*>(a.x)[k] = a.warm ? df_split(a.x[k]) : make_float2(0.f, 0.f);
-                float r = (float)b;
+                const float r = bs.x;
                 put_r32(a.r32, a.pitch32, a.nx, a.ny, a.per_x, a.per_y, c, j, r);
                 float z = a.st.minv32[edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y)] * r;
-                abb = fma(b, b, abb);
+                abb = fmaf(r, r, abb);
                 arz = fmaf(r, z, arz);
                 arr = fmaf(r, r, arr);
             }
     }
-    abb = warp_fold(abb);
+    const double dbb = warp_fold((double)abb);
     double drz = warp_fold((double)arz), drr = warp_fold((double)arr);
     if (unit < a.U && lane == 0) {
-        a.part0[unit] = abb;
+        a.part0[unit] = dbb;
         a.part1[unit] = drz;
         a.part2[unit] = drr;
     }
@@ -694,7 +697,7 @@ __global__ void k_df_to_f64(double* x, int nx, int ny, int pitch) {
     if (gi >= nx || gj >= ny) return;
     const size_t k = (size_t)gj * pitch + gi;
     const float2 v = reinterpret_cast<const float2*>(x)[k];
-    x[k] = (double)v.x + (double)v.y;
+    x[k] = f2d_exact(v.x) + f2d_exact(v.y);
 }
 
 // --------------------------------------------------------------------------
@@ -759,6 +762,7 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_norms(DivArgs a) {
     const int lane = threadIdx.x & 31;
     const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
     double ass = 0.0, amx = 0.0;
+    float fss = 0.f, fmx = 0.f;
     if (unit < a.U) {
         const int g = unit % a.G, band = unit / a.G;
         const int c0 = g * CF_UNIT_COLS + 2 * lane;
@@ -769,10 +773,27 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_norms(DivArgs a) {
             for (int s = 0; s < 2; ++s) {
                 int c = c0 + s;
                 if (c >= a.nx) continue;
-                double b = div_b(a, c, j);
-                ass = fma(b, b, ass);
-                amx = fmax(amx, fabs(b));
+                if (a.mixed) {
+                    // the FP64 divergence sum, then its square and magnitude in FP32
+                    int ie = c + 1, jn = j + 1;
+                    if (a.per_x && ie == a.nx) ie = 0;
+                    if (a.per_y && jn == a.ny) jn = 0;
+                    double t = a.u.at(ie + CF_HALO, j + CF_HALO) - a.u.at(c + CF_HALO, j + CF_HALO);
+                    t = t + a.v.at(c + CF_HALO, jn + CF_HALO);
+                    t = t - a.v.at(c + CF_HALO, j + CF_HALO);
+                    const float bf = d2f_rn(t) * a.mscale32;
+                    fss = fmaf(bf, bf, fss);
+                    fmx = fmaxf(fmx, fabsf(bf));
+                } else {
+                    double b = div_b(a, c, j);
+                    ass = fma(b, b, ass);
+                    amx = fmax(amx, fabs(b));
+                }
             }
+    }
+    if (a.mixed) {
+        ass = (double)fss;
+        amx = (double)fmx;
     }
     ass = warp_fold(ass);
     amx = warp_max(amx);
@@ -806,6 +827,8 @@ static DivArgs div_args(cf_ctx* c, const Stencil& st) {
     a.u = c->u[c->cur];
     a.v = c->v[c->cur];
     a.mscale = -(1.0 / c->ph.dx);
+    a.mixed = c->precision == CF_PREC_MIXED;
+    a.mscale32 = (float)a.mscale;
     a.st = st;
     a.x = c->x.a;
     a.r = c->r.a;

@@ -220,6 +220,10 @@ int cf_backward(cf_ctx* ctx, const double* dL_dq_T, const double* dL_du_T, const
 int cf_interp_points(cf_ctx* ctx, int field, int order, int n, const double* xy, double* out);
 /* TimeIntegrator::rk3 (src/TimeIntegrator.hpp:36-77) of n points */
 int cf_trace_points(cf_ctx* ctx, int n, const double* xy, double dt, double* out);
+/* the device's FP64 -> FP32 (round to nearest even) and FP32 -> FP64
+ * conversions of the mixed-precision kernels, applied to d[n]: f = narrowed,
+ * w = f widened (no counterpart in the reference) */
+int cf_test_conversions(cf_ctx* ctx, int n, const double* d, float* f, double* w);
 
 /* ---- output (replaces the device half of SiloWriter::writeFile) ----
  * SiloWriter interpolates the face velocities to cell centres for its
