@@ -170,6 +170,26 @@ __device__ __forceinline__ int wrap_index(int g, int n, int per) {
     return g < 0 ? g + n : g;
 }
 
+// Asynchronous global -> shared copies (cp.async, completion by groups per
+// thread: a thread that reads back only what it copied needs no barrier).
+__device__ __forceinline__ void cpa16(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa8(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa4(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // FP32 <-> FP64 conversions by bit manipulation on the integer pipe (GB300's
 // FP64 pipe, which executes the hardware conversions, is narrow).  Straight
 // from the IEEE 754 binary32/binary64 layouts: a normal binary32 widens

@@ -470,24 +470,6 @@ __device__ __forceinline__ void frame_tile(const StripMap& m, int f, int& tx, in
     tx = f % m.ntx;
 }
 
-__device__ __forceinline__ void cpa16(void* dst, const void* src) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cpa8(void* dst, const void* src) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cpa4(void* dst, const void* src) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cpa_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
 // half sweep of one colour on row j (X), rows j - 1 (Xm) and j + 1 (Xp), b
 // (B); the strip's first column is a multiple of 4, so the colour's cells sit
 // at k = 0, 2 when sel = (j + colour) & 1 is 0 and at k = 1, 3 otherwise

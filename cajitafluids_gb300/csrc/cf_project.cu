@@ -601,6 +601,88 @@ __device__ __forceinline__ float2 df_resid(const Outer& a, int eb, float2 b, flo
     return df_add_s(b, make_float2(-ax.x, -ax.y));
 }
 
+// interior cell: wall-adjacency bits 0, so the diagonal factor is 4 and
+// 4 x is exact
+__device__ __forceinline__ float2 df_resid_int(const Outer& a, float2 b, float2 c, float2 w, float2 e, float2 s,
+                                               float2 n) {
+    float2 nb = df_add_s(w, e);
+    nb = df_add_s(nb, s);
+    nb = df_add_s(nb, n);
+    float2 t = df_add_s(make_float2(4.f * c.x, 4.f * c.y), make_float2(-nb.x, -nb.y));
+    float2 ax = df_mul(a.scale, t);
+    return df_add_s(b, make_float2(-ax.x, -ax.y));
+}
+
+// Interior unit (every cell and neighbour inside the domain, no wrap, no
+// wall): the same arithmetic without the boundary logic.  The rows arrive
+// through a per-warp cp.async ring OR_RING - 1 rows ahead (group k: x of
+// row j0 - 1 + k, and for the unit's own rows b and the outer columns'
+// neighbours of lanes 0 and 31); each lane reads back only what it copied.
+constexpr int OR_RING = 4;
+constexpr int OR_SLOT = 64 * 2 + 64 * 2 + 8;  // floats: x row, b row, two edge pairs (16-byte multiple)
+__device__ __forceinline__ void outer_unit_interior(const Outer& a, float* ring, int lane, int c0, int j0, int j1,
+                                                    float& arz, float& arr) {
+    const float m0 = a.minv32[0];
+    const bool edge = lane == 0 || lane == 31;
+    const int ec = lane == 0 ? c0 - 1 : c0 + 2;  // outer neighbour column of lanes 0 and 31
+    const int eo = 256 + (lane == 31 ? 2 : 0);
+    const int last = j1;                         // groups cover rows j0 - 1 .. j1
+    auto issue = [&](int k) {
+        const int row = j0 - 1 + k;
+        float* sl = ring + (k % OR_RING) * OR_SLOT;
+        if (row <= last) {
+            const size_t o = (size_t)row * a.pitch;
+            cpa16(sl + 4 * lane, a.x + o + c0);
+            if (row >= j0 && row < j1) {
+                cpa16(sl + 128 + 4 * lane, a.b + o + c0);
+                if (edge) cpa8(sl + eo, a.x + o + ec);
+            }
+        }
+        cpa_commit();
+    };
+    auto xrow = [&](int k) { return *reinterpret_cast<const float4*>(ring + (k % OR_RING) * OR_SLOT + 4 * lane); };
+    auto brow = [&](int k) {
+        return *reinterpret_cast<const float4*>(ring + (k % OR_RING) * OR_SLOT + 128 + 4 * lane);
+    };
+    auto erow = [&](int k) {
+        return edge ? *reinterpret_cast<const float2*>(ring + (k % OR_RING) * OR_SLOT + eo) : make_float2(0.f, 0.f);
+    };
+#pragma unroll
+    for (int k = 0; k < OR_RING - 1; ++k) issue(k);
+    issue(OR_RING - 1);
+    cpa_wait<OR_RING - 1>();
+    float4 xm = xrow(0);  // row j0 - 1
+    issue(OR_RING);
+    cpa_wait<OR_RING - 1>();
+    float4 xc = xrow(1), bv = brow(1);  // row j0
+    float2 ev = erow(1);
+    for (int j = j0; j < j1; ++j) {
+        const int k = j - j0 + 2;  // group of row j + 1
+        issue(k + OR_RING - 1);
+        cpa_wait<OR_RING - 1>();
+        const float4 xp = xrow(k), bn = brow(k);
+        const float2 en = erow(k);
+        float2 left = make_float2(__shfl_up_sync(FULLMASK, xc.z, 1), __shfl_up_sync(FULLMASK, xc.w, 1));
+        float2 right = make_float2(__shfl_down_sync(FULLMASK, xc.x, 1), __shfl_down_sync(FULLMASK, xc.y, 1));
+        if (lane == 0) left = ev;
+        if (lane == 31) right = ev;
+        const float2 r0 = df_resid_int(a, make_float2(bv.x, bv.y), make_float2(xc.x, xc.y), left,
+                                       make_float2(xc.z, xc.w), make_float2(xm.x, xm.y), make_float2(xp.x, xp.y));
+        const float2 r1 = df_resid_int(a, make_float2(bv.z, bv.w), make_float2(xc.z, xc.w), make_float2(xc.x, xc.y),
+                                       right, make_float2(xm.z, xm.w), make_float2(xp.z, xp.w));
+        *reinterpret_cast<float2*>(a.r32 + (ptrdiff_t)j * a.pitch32 + c0) = make_float2(r0.x, r1.x);
+        arz = fmaf(r0.x, m0 * r0.x, arz);
+        arr = fmaf(r0.x, r0.x, arr);
+        arz = fmaf(r1.x, m0 * r1.x, arz);
+        arr = fmaf(r1.x, r1.x, arr);
+        xm = xc;
+        xc = xp;
+        bv = bn;
+        ev = en;
+    }
+    cpa_wait<0>();
+}
+
 // one warp per unit of 64 columns x 16 rows, lane l on columns 2l, 2l + 1;
 // rows slide through registers, W/E neighbours come by shuffle
 __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
@@ -609,11 +691,19 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
     const int lane = threadIdx.x & 31;
     const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
     float arz = 0.f, arr = 0.f;
-    if (unit < a.U) {
-        const int g = unit % a.G, band = unit / a.G;
+    const int g = unit % a.G, band = unit / a.G;
+    const int j0u = band * CF_BAND_ROWS, j1u = min(j0u + CF_BAND_ROWS, a.ny);
+    // rows j0u - 1 .. j1u + 1 and columns g * 64 - 1 .. g * 64 + 64 are read
+    const bool interior = unit < a.U && g * CF_UNIT_COLS >= 1 && (g + 1) * CF_UNIT_COLS + 1 <= a.nx &&
+                          j0u >= 1 && j1u + 2 <= a.ny;
+    __shared__ __align__(16) float ring[CF_RED_WARPS * OR_RING * OR_SLOT];
+    if (interior) {
+        outer_unit_interior(a, ring + (threadIdx.x >> 5) * OR_RING * OR_SLOT, lane, g * CF_UNIT_COLS + 2 * lane, j0u,
+                            j1u, arz, arr);
+    } else if (unit < a.U) {
         const int c0 = g * CF_UNIT_COLS + 2 * lane;
-        const int j0 = band * CF_BAND_ROWS;
-        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
+        const int j0 = j0u;
+        const int j1 = j1u;
         // rows j - 1, j, j + 1 in registers; row j + 2 and b of row j + 1 are
         // fetched one row ahead, so the loads overlap the arithmetic
         float4 xm = xrow2(a, a.x, c0, j0 - 1), xc = xrow2(a, a.x, c0, j0), xp = xrow2(a, a.x, c0, j0 + 1);
