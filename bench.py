@@ -33,14 +33,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "steps/s at 4096² mixed-prec vs FP64 at ‖div u‖≤1e-8; adjoint/forward ratio"
-# Algorithmic bytes per cell per CG iteration (minimal compulsory traffic):
-# FP64 CG 88 B (r, p read twice-free form: SpMV 2 + update 6 + direction 3
-# words), mixed inner FP32 CG 44 B.
-ALG_BYTES_FP64_ITER = 88.0
-ALG_BYTES_MIXED_ITER = 44.0
-# bytes the kernels of this build must move per cell per iteration
-KERNEL_BYTES_FP64_ITER = 80.0
-KERNEL_BYTES_MIXED_ITER = 32.0
+# bytes the inner Jacobi-PCG kernels of this build move per cell per
+# iteration (mixed: K1 R r, p, W p at 4 B; K2 R p, r, W r at 4 B, R/W the
+# double-float x at 8 B)
+KERNEL_BYTES_MIXED_ITER = 40.0
 # Jacobi-PCG iterations per step of this workload in FP64 (the FP64 GPU path
 # and the CPU oracle are bit-identical, so they take the same count); with
 # --precon Diagonal the reference arm extrapolates its sampled CG cost to this
@@ -49,7 +45,7 @@ FP64_ITERS_PER_STEP_4096 = 7890
 MG_NAMES = ("PFMG", "SMG", "MG")
 # DRAM bytes (read + write) of one mixed MG-PCG inner iteration at 4096^2,
 # from an ncu capture of this bench (profiles/traffic_4096_mixed_mg.md)
-MEASURED_TRAFFIC_MG_ITER_4096 = 1.39e9
+MEASURED_TRAFFIC_MG_ITER_4096 = 1.19e9
 
 
 def mg_levels(nx, ny, periodic):
@@ -65,27 +61,33 @@ def mg_levels(nx, ny, periodic):
     return lv
 
 
-def alg_bytes_per_iter(nx, ny, periodic, precon, word, outer_frac=0.0):
-    """Algorithmic (minimal compulsory) bytes of one PCG iteration.
+def alg_bytes_per_iter(nx, ny, periodic, precon, word, outer_frac=0.0, mixed=False):
+    """Algorithmic (minimal compulsory) bytes of one PCG iteration, per the
+    stage table of the measurement plan (full-grid arrays of `word` bytes,
+    ghosts ignored).
 
-    Jacobi: 11 full-grid words per cell (SpMV + dot: R p, W Ap; update + dot:
-    R x, p, r, Ap, W x, r; direction: R z, p, W p; M^-1 from wall flags).
-    MG: the same 11 words with z read instead of recomputed, plus r.z (2 words)
-    and the V-cycle: per non-coarsest level 8 red/black half sweeps of 1.5
-    words each (other colour read, own b read, own x written), residual 3,
-    restriction 1.25, prolongation 2.25 words per cell of that level; the
-    one-CTA coarsest level 2 words.  Mixed: plus the FP64 reliable update
-    (R x, e, W x; R x, b, W r32, e32 = 44 B per cell) on the fraction of
-    iterations that run it."""
+    Jacobi: 11 arrays per cell (SpMV + dot: R p, W Ap; update + dot: R x, p,
+    r, Ap, W x, r; direction: R r, p, W p; M^-1 from wall flags).
+    MG: direction + SpMV (R z, p, W p) 3, update (R p, r, x, W r, x) 5, and
+    per V-cycle level above the coarsest 5.5 arrays of that level's cells
+    (pre-smoothing: R b, W x, W coarse b at 1/4; post-smoothing: R b, x,
+    coarse x at 1/4, W x), the coarsest level 2; FP64 adds r.z (R r, z) 2,
+    mixed forms r.z with the finest post-smoothing.  Mixed: the solution x
+    is a double-float pair (8 bytes) in the update, and the reliable update
+    (R x, b at 8 bytes, W r at 4 = 20 B per cell) runs on the fraction
+    outer_frac of the iterations."""
     n = nx * ny
     if precon not in MG_NAMES:
-        return 11 * word * n
-    b = 13 * word * n
+        return 11 * word * n + outer_frac * 20.0 * n
+    xw = 8 if mixed else word
+    b = 3 * word * n + (3 * word + 2 * xw) * n
+    if not mixed:
+        b += 2 * word * n
     lv = mg_levels(nx, ny, periodic)
     for a, c in lv[:-1]:
-        b += 18.5 * word * a * c
+        b += 5.5 * word * a * c
     b += 2 * word * lv[-1][0] * lv[-1][1]
-    return b + outer_frac * 44.0 * n
+    return b + outer_frac * 20.0 * n
 
 
 def env_int(name, default):
@@ -309,11 +311,12 @@ def bench_gb300(args, rank, world, dist, device):
         it_ms = prof["solve_ms"] / prof["solve_iters"] if prof["solve_iters"] else float("nan")
         iters = statistics.mean(s["iterations"] for s in stats)
         outers = statistics.mean(s["outer_iterations"] for s in stats)
-        it_bytes = alg_bytes_per_iter(w.nx, w.ny, w.periodic, w.precon, 4, min(outers / max(iters, 1), 1.0))
+        it_bytes = alg_bytes_per_iter(w.nx, w.ny, w.periodic, w.precon, 4, min(outers / max(iters, 1), 1.0),
+                                      mixed=True)
         achieved = it_bytes / (it_ms / 1e3) / 1e9
         if mg:
-            kname = ("MG-PCG inner iteration: k_tma_dir_matvec32 + k_tma_update32 + gated k_outer_add/"
-                     "k_outer_resid + V-cycle (k_mg_pre/k_mg_post per level, k_mg_bottom) + k_mg_rz32")
+            kname = ("MG-PCG inner iteration: k_tma_dir_matvec32 + k_tma_update32 + gated k_outer_resid + "
+                     "V-cycle (k_mg_pre/k_mg_post per level with r.z in the finest post-smoothing, k_mg_bottom)")
             kern_extra = {}
         else:
             kname = "inner CG iteration (k_tma_dir_matvec32 + k_tma_update32)"
