@@ -20,11 +20,32 @@ static __constant__ double ENT_OFF_D[3][2] = {{0.5, 0.5}, {0.0, 0.5}, {0.5, 0.0}
 // Ghost fill: the one-GPU form of Cajita's advection halo gather
 // (src/ProblemManager.hpp:173-176, 394-398).  Wall ghosts keep their
 // construction zeros; periodic ghosts copy the wrapped owned entity.
+// One thread per ghost cell: thread t walks the frame around the owned
+// block [H, H + nox) x [H, H + noy): the H rows above it, then per owned row
+// its left and right ghosts, then the rows below it.
+__device__ __forceinline__ int ghost_count(int ex, int ey, int nox, int noy) {
+    return CF_HALO * ex + noy * (ex - nox) + (ey - CF_HALO - noy) * ex;
+}
+
 template <typename T>
 __global__ void k_fill_ghosts(Grid<T> g, int nox, int noy, int per_x, int per_y) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.ex || j >= g.ey) return;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ghost_count(g.ex, g.ey, nox, noy)) return;
+    int i, j;
+    const int top = CF_HALO * g.ex, midw = g.ex - nox, mid = noy * midw;
+    if (t < top) {
+        j = t / g.ex;
+        i = t - j * g.ex;
+    } else if (t < top + mid) {
+        t -= top;
+        j = CF_HALO + t / midw;
+        const int k = t % midw;
+        i = k < CF_HALO ? k : nox + k;
+    } else {
+        t -= top + mid;
+        j = CF_HALO + noy + t / g.ex;
+        i = t % g.ex;
+    }
     int gi = i - CF_HALO, gj = j - CF_HALO;
     bool in_x = gi >= 0 && gi < nox, in_y = gj >= 0 && gj < noy;
     if (in_x && in_y) return;
@@ -463,13 +484,21 @@ cudaError_t launch_fill_ghosts(cf_ctx* c) {
     int s = c->cur;
     int nqx = p.nx, nqy = p.ny;
     int nux = p.per_x ? p.nx : p.nx + 1, nvy = p.per_y ? p.ny : p.ny + 1;
+    auto frame = [&](int ex, int ey, int nox, int noy) {
+        const int n = CF_HALO * ex + noy * (ex - nox) + (ey - CF_HALO - noy) * ex;
+        return (n + 255) / 256;
+    };
     if (c->precision == CF_PREC_FP64) {
-        k_fill_ghosts<double><<<grid2(c->q64[s].ex, c->q64[s].ey, blk), blk, 0, c->stream>>>(c->q64[s], nqx, nqy, p.per_x, p.per_y);
+        const Grid<double>& g = c->q64[s];
+        k_fill_ghosts<double><<<frame(g.ex, g.ey, nqx, nqy), 256, 0, c->stream>>>(g, nqx, nqy, p.per_x, p.per_y);
     } else {
-        k_fill_ghosts<float><<<grid2(c->q32[s].ex, c->q32[s].ey, blk), blk, 0, c->stream>>>(c->q32[s], nqx, nqy, p.per_x, p.per_y);
+        const Grid<float>& g = c->q32[s];
+        k_fill_ghosts<float><<<frame(g.ex, g.ey, nqx, nqy), 256, 0, c->stream>>>(g, nqx, nqy, p.per_x, p.per_y);
     }
-    k_fill_ghosts<double><<<grid2(c->u[s].ex, c->u[s].ey, blk), blk, 0, c->stream>>>(c->u[s], nux, p.ny, p.per_x, p.per_y);
-    k_fill_ghosts<double><<<grid2(c->v[s].ex, c->v[s].ey, blk), blk, 0, c->stream>>>(c->v[s], p.nx, nvy, p.per_x, p.per_y);
+    k_fill_ghosts<double><<<frame(c->u[s].ex, c->u[s].ey, nux, p.ny), 256, 0, c->stream>>>(c->u[s], nux, p.ny, p.per_x,
+                                                                                       p.per_y);
+    k_fill_ghosts<double><<<frame(c->v[s].ex, c->v[s].ey, p.nx, nvy), 256, 0, c->stream>>>(c->v[s], p.nx, nvy, p.per_x,
+                                                                                       p.per_y);
     c->launches += 3;
     return cudaGetLastError();
 }
