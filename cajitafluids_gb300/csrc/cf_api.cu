@@ -427,6 +427,7 @@ int cf_upload(cf_ctx* ctx, int field, const double* host, ptrdiff_t si, ptrdiff_
     if (si <= 0 || sj <= 0) return fail(ctx, CF_ERR_INVALID, "strides must be positive");
     int s = ctx->cur;
     bool q32 = field == CF_FIELD_QUANTITY && ctx->precision == CF_PREC_MIXED;
+    if (field != CF_FIELD_QUANTITY) ctx->uv32 = 0;
     Grid<double> g = field == CF_FIELD_QUANTITY ? ctx->q64[s] : (field == CF_FIELD_U ? ctx->u[s] : ctx->v[s]);
     int rc;
     if (si == 1 && !q32) {
@@ -628,6 +629,7 @@ int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* 
     // uploads into the current buffers
     const int s0 = ctx->cur;
     const double* ins[3] = {q_in, u_in, v_in};
+    ctx->uv32 = 0;
     for (int f = 0; f < 3 && !rc; ++f) {
         int ox, oy;
         owned(ctx, f, &ox, &oy);

@@ -15,6 +15,9 @@ struct cf_ctx {
     int precision = 0;
     double density = 1.0;
     int warm = 0;  // start each projection from the previous pressure (cf_set_warm_start)
+    // mixed: u32/v32 hold the FP32 copies of the owned u, v of the current
+    // state (written by the last gradient subtraction; ghosts not yet filled)
+    int uv32 = 0;
 
     // fields, two versions each (src/ProblemManager.hpp:143-165); index cur is Current
     cf::Grid<double> q64[2]{}, u[2]{}, v[2]{};

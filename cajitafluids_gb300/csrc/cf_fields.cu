@@ -518,9 +518,25 @@ cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs) {
         // fused inputs with a density-scaled force are applied by the
         // standalone inputs kernels after the advection
         Adv32 a{p, c->q32[s], c->q32[n], c->u32, c->v32, c->u[n], c->v[n], (float)(dt / p.dx), dt, fuse_inputs};
-        k_to32<<<grid2(c->u[s].ex, c->u[s].ey, blk), blk, 0, c->stream>>>(c->u[s], c->u32);
-        k_to32<<<grid2(c->v[s].ex, c->v[s].ey, blk), blk, 0, c->stream>>>(c->v[s], c->v32);
-        c->launches += 2;
+        if (c->uv32) {
+            // the last gradient subtraction left the owned FP32 copies: only their ghosts
+            const int nux = p.per_x ? p.nx : p.nx + 1, nvy = p.per_y ? p.ny : p.ny + 1;
+            if (p.per_x || p.per_y) {
+                auto frame = [&](const Grid<float>& g, int nox, int noy) {
+                    return (CF_HALO * g.ex + noy * (g.ex - nox) + (g.ey - CF_HALO - noy) * g.ex + 255) / 256;
+                };
+                k_fill_ghosts<float><<<frame(c->u32, nux, p.ny), 256, 0, c->stream>>>(c->u32, nux, p.ny, p.per_x,
+                                                                                     p.per_y);
+                k_fill_ghosts<float><<<frame(c->v32, p.nx, nvy), 256, 0, c->stream>>>(c->v32, p.nx, nvy, p.per_x,
+                                                                                     p.per_y);
+                c->launches += 2;
+            }
+        } else {
+            k_to32<<<grid2(c->u[s].ex, c->u[s].ey, blk), blk, 0, c->stream>>>(c->u[s], c->u32);
+            k_to32<<<grid2(c->v[s].ex, c->v[s].ey, blk), blk, 0, c->stream>>>(c->v[s], c->v32);
+            c->launches += 2;
+        }
+        c->uv32 = 0;  // the advection writes the next u, v
         if (order == 1)
             k_advect32<1><<<grd, blk, 0, c->stream>>>(a);
         else
@@ -534,6 +550,7 @@ cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs) {
 cudaError_t launch_add_inputs(cf_ctx* c, double dt) {
     const Phys& p = c->ph;
     int s = c->cur;
+    c->uv32 = 0;  // writes u, v
     dim3 blk(32, 8);
     if (c->precision == CF_PREC_FP64) {
         Inp<double> a{p, c->q64[s], c->u[s], c->v[s], dt};

@@ -801,6 +801,10 @@ struct Press {
     int pitch;
     double ms;    // -(dt / (density dx))
     int adjoint;  // 1: transpose of the projection (masks applied by the caller, none here)
+    // mixed: every value written to u, v also goes, rounded to FP32, to these
+    // copies (the next FP32 advection's velocity arrays)
+    Grid<float> u32, v32;
+    int w32;
 };
 
 __device__ __forceinline__ double pval(const Press& a, int gi, int gj) {
@@ -830,6 +834,7 @@ __global__ void k_apply_pressure(Press a) {
             if (!fix_q1 && !p.per_y && gj == 0 && gi < p.nx && p.bc[1] == 0) w = 0.0;
         }
         u = w;
+        if (a.w32) a.u32.at(gi + CF_HALO, gj + CF_HALO) = d2f_rn(w);
     } else {
         double& v = a.v.at(gi + CF_HALO, gj + CF_HALO);
         double d = pval(a, gi, gj) - pval(a, gi, gj - 1);
@@ -840,9 +845,11 @@ __global__ void k_apply_pressure(Press a) {
                 if (gj > p.ny - 1 && p.bc[3] == 0) w = 0.0;
             } else if (gj > p.ny - 1 && p.bc[3] == 0) {
                 a.u.at(gi + CF_HALO, gj + CF_HALO) = 0.0;  // u ghost row ny
+                if (a.w32) a.u32.at(gi + CF_HALO, gj + CF_HALO) = 0.f;
             }
         }
         v = w;
+        if (a.w32) a.v32.at(gi + CF_HALO, gj + CF_HALO) = d2f_rn(w);
     }
 }
 
@@ -1246,7 +1253,8 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
                 k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, c->ph.nx, c->ph.ny, c->vpitch);
                 ntail += 1;
             }
-            Press pa{c->ph, gu, gv, c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx)), 0};
+            Press pa{c->ph, gu, gv, c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx)), 0, c->u32, c->v32,
+                     mixed ? 1 : 0};
             dim3 grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
             k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
             DivArgs da = div_args(c, st);
@@ -1311,6 +1319,7 @@ static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResul
     h->trip_limit = (o.max_iter + (mixed ? o.max_outer : 0)) / batch + 4;
     cudaMemcpyAsync(c->S, h, sizeof(SolverState), cudaMemcpyHostToDevice, c->stream);
     if ((rc = cuda_check(c, cudaGraphLaunch(c->rgx[cur], c->stream), "graph launch"))) return rc;
+    if (mixed) c->uv32 = 1;  // the graph's gradient subtraction wrote the FP32 velocity copies
     c->rg_pending = cur;
     if (defer) return CF_OK;
     if ((rc = cuda_check(c, cudaStreamSynchronize(c->stream), "projection"))) return rc;
@@ -1480,10 +1489,13 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     res->rr = hs->rr;
 
     // gradient subtraction
-    Press pa{c->ph, gu, gv, c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx)), adjoint};
+    const bool w32 = mixed && !adjoint && gu.o == c->u[c->cur].o && gv.o == c->v[c->cur].o;
+    Press pa{c->ph, gu, gv, c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx)), adjoint, c->u32, c->v32,
+             w32 ? 1 : 0};
     dim3 blk(32, 8), grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
     k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
     c->launches += 1;
+    c->uv32 = w32 ? 1 : 0;
     if ((rc = cuda_check(c, cudaGetLastError(), "apply pressure"))) return rc;
     if (c->prof) cudaEventRecord(c->ev[5], c->stream);
     if (adjoint) return cuda_check(c, cudaStreamSynchronize(c->stream), "adjoint projection");
