@@ -308,8 +308,32 @@ __global__ void __launch_bounds__(256) k_advect32(Adv32 a) {
     float ox_e = ent == E_FACEI ? 0.f : 0.5f;
     float oy_e = ent == E_FACEJ ? 0.f : 0.5f;
     float uox = ox_e, uoy = oy_e - 0.5f, vox = ox_e - 0.5f, voy = oy_e;
-    float v0x = lin32(a.u, li, lj, uox, uoy);
-    float v0y = lin32(a.v, li, lj, vox, voy);
+    // first RK stage at the entity itself: the linear samples' integer cells
+    // and fractions (0 or 1/2) are known, so the taps are read directly with
+    // the same arithmetic (a zero-weight row is dropped: it only could turn a
+    // -0 into +0, which no later step can tell apart)
+    float v0x, v0y;
+    {
+        const float* u0 = &a.u.at(li, lj);
+        const float* w0 = &a.v.at(li, lj);
+        const int pu = a.u.pitch, pv = a.v.pitch;
+        if (ent == E_CELL) {
+            v0x = fmaf(0.5f, __ldg(u0 + 1) - __ldg(u0), __ldg(u0));
+            v0y = fmaf(0.5f, __ldg(w0 + pv) - __ldg(w0), __ldg(w0));
+        } else if (ent == E_FACEI) {
+            v0x = __ldg(u0);
+            const float* r0 = w0 - 1;
+            const float s0 = fmaf(0.5f, __ldg(r0 + 1) - __ldg(r0), __ldg(r0));
+            const float s1 = fmaf(0.5f, __ldg(r0 + pv + 1) - __ldg(r0 + pv), __ldg(r0 + pv));
+            v0y = fmaf(0.5f, s1 - s0, s0);
+        } else {
+            const float* r0 = u0 - pu;
+            const float s0 = fmaf(0.5f, __ldg(r0 + 1) - __ldg(r0), __ldg(r0));
+            const float s1 = fmaf(0.5f, __ldg(r0 + pu + 1) - __ldg(r0 + pu), __ldg(r0 + pu));
+            v0x = fmaf(0.5f, s1 - s0, s0);
+            v0y = __ldg(w0);
+        }
+    }
     float h1 = -0.5f * a.c, h2 = -0.75f * a.c;
     float d1x = h1 * v0x, d1y = h1 * v0y;
     float v1x = lin32(a.u, li, lj, uox + d1x, uoy + d1y);
