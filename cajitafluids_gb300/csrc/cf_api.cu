@@ -329,6 +329,8 @@ int cf_ctx_destroy(cf_ctx* ctx) {
         cudaStreamDestroy(ctx->stream2);
     }
     if (ctx->ev_adv) cudaEventDestroy(ctx->ev_adv);
+    if (ctx->ev_uv) cudaEventDestroy(ctx->ev_uv);
+    if (ctx->ev_q) cudaEventDestroy(ctx->ev_q);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return CF_OK;
@@ -623,32 +625,46 @@ int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* 
     if (!ctx->stream2) {
         rc = cuda_check(ctx, cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking), "stream create");
         if (!rc) rc = cuda_check(ctx, cudaEventCreateWithFlags(&ctx->ev_adv, cudaEventDisableTiming), "event create");
+        if (!rc) rc = cuda_check(ctx, cudaEventCreateWithFlags(&ctx->ev_uv, cudaEventDisableTiming), "event create");
+        if (!rc) rc = cuda_check(ctx, cudaEventCreateWithFlags(&ctx->ev_q, cudaEventDisableTiming), "event create");
         if (!rc && mixed) rc = alloc_dev(ctx, ctx->staging2, (size_t)nx * ny);
         if (rc) return rc;
     }
-    // uploads into the current buffers
+    // Uploads into the current buffers: u and v first on the main stream; the
+    // quantity once they are in (they share the link), on the second stream,
+    // while the velocities' own advection runs on the main one.
     const int s0 = ctx->cur;
-    const double* ins[3] = {q_in, u_in, v_in};
     ctx->uv32 = 0;
-    for (int f = 0; f < 3 && !rc; ++f) {
+    for (int f = CF_FIELD_U; f <= CF_FIELD_V && !rc; ++f) {
         int ox, oy;
         owned(ctx, f, &ox, &oy);
-        if (f == CF_FIELD_QUANTITY && mixed) {
-            rc = cuda_check(ctx, cudaMemcpyAsync(ctx->staging, ins[f], sizeof(double) * (size_t)ox * oy,
-                                                 cudaMemcpyDefault, ctx->stream), "upload");
-            if (!rc) rc = cuda_check(ctx, launch_convert_q(ctx, 1, s0), "convert");
-        } else {
-            Grid<double> g = f == CF_FIELD_QUANTITY ? ctx->q64[s0] : (f == CF_FIELD_U ? ctx->u[s0] : ctx->v[s0]);
-            rc = cuda_check(ctx, cudaMemcpy2DAsync(&g.at(CF_HALO, CF_HALO), g.pitch * sizeof(double), ins[f],
-                                                   ox * sizeof(double), ox * sizeof(double), oy, cudaMemcpyDefault,
-                                                   ctx->stream),
-                            "upload");
-        }
+        Grid<double> g = f == CF_FIELD_U ? ctx->u[s0] : ctx->v[s0];
+        rc = cuda_check(ctx, cudaMemcpy2DAsync(&g.at(CF_HALO, CF_HALO), g.pitch * sizeof(double),
+                                               f == CF_FIELD_U ? u_in : v_in, ox * sizeof(double), ox * sizeof(double),
+                                               oy, cudaMemcpyDefault, ctx->stream),
+                        "upload");
     }
-    // advection and inputs (src/Solver.hpp:135-147)
+    if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->ev_uv, ctx->stream), "event");
+    if (!rc) rc = cuda_check(ctx, cudaStreamWaitEvent(ctx->stream2, ctx->ev_uv, 0), "event wait");
+    if (!rc && mixed) {
+        rc = cuda_check(ctx, cudaMemcpyAsync(ctx->staging, q_in, sizeof(double) * (size_t)nx * ny, cudaMemcpyDefault,
+                                             ctx->stream2), "upload");
+        if (!rc) rc = cuda_check(ctx, launch_convert_q(ctx, 1, s0, ctx->stream2), "convert");
+    } else if (!rc) {
+        const Grid<double>& g = ctx->q64[s0];
+        rc = cuda_check(ctx, cudaMemcpy2DAsync(&g.at(CF_HALO, CF_HALO), g.pitch * sizeof(double), q_in,
+                                               nx * sizeof(double), nx * sizeof(double), ny, cudaMemcpyDefault,
+                                               ctx->stream2),
+                        "upload");
+    }
+    if (!rc) rc = cuda_check(ctx, launch_fill_ghosts(ctx, GHOSTS_Q, ctx->stream2), "fill ghosts");
+    if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->ev_q, ctx->stream2), "event");
+    // advection and inputs (src/Solver.hpp:135-147): u and v, then q once it is in
     const bool fuse = !ctx->ph.force_density;
-    if (!rc) rc = cuda_check(ctx, launch_fill_ghosts(ctx), "fill ghosts");
-    if (!rc) rc = cuda_check(ctx, launch_advect(ctx, dt, value_order, fuse ? 1 : 0), "advect");
+    if (!rc) rc = cuda_check(ctx, launch_fill_ghosts(ctx, GHOSTS_UV), "fill ghosts");
+    if (!rc) rc = cuda_check(ctx, launch_advect(ctx, dt, value_order, fuse ? 1 : 0, 1, 2, true, false), "advect");
+    if (!rc) rc = cuda_check(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_q, 0), "event wait");
+    if (!rc) rc = cuda_check(ctx, launch_advect(ctx, dt, value_order, fuse ? 1 : 0, 0, 1, false, true), "advect");
     if (!rc && !fuse) rc = cuda_check(ctx, launch_add_inputs(ctx, dt), "add inputs");
     if (rc) return rc;
     const int s1 = ctx->cur;

@@ -56,6 +56,7 @@ struct cf_ctx {
     // the projection, and its staging buffer (nx ny doubles), made on first use
     cudaStream_t stream2 = nullptr;
     cudaEvent_t ev_adv = nullptr;
+    cudaEvent_t ev_uv = nullptr, ev_q = nullptr;  // cf_step_host: velocities in, quantity in
     double* staging2 = nullptr;
     cudaGraphExec_t gmg = nullptr;      // batch of MG-PCG iterations
     cudaGraphExec_t gmg_pre = nullptr;  // V-cycle + r.z after the residual is (re)formed
@@ -88,15 +89,20 @@ int cuda_check(cf_ctx* c, cudaError_t e, const char* what);
 void build_stencil(const cf_ctx* c, double dt, int precon_none, Stencil* st);
 
 // launchers (cf_fields.cu)
-cudaError_t launch_fill_ghosts(cf_ctx* c);
-cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs);
+// ghost fills: what = GHOSTS_Q | GHOSTS_UV, on stream (null: the context's)
+enum { GHOSTS_Q = 1, GHOSTS_UV = 2, GHOSTS_ALL = 3 };
+cudaError_t launch_fill_ghosts(cf_ctx* c, int what = GHOSTS_ALL, cudaStream_t stream = nullptr);
+// advection of entities [ent0, ent0 + nent) (0 q, 1 u, 2 v); prep: make the
+// FP32 velocity copies first (mixed); advance: switch to the new state after
+cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs, int ent0 = 0, int nent = 3,
+                          bool prep = true, bool advance = true);
 cudaError_t launch_add_inputs(cf_ctx* c, double dt);
 cudaError_t launch_interp_points(cf_ctx* c, int field, int order, int n, const double* d_xy, double* d_out);
 cudaError_t launch_trace_points(cf_ctx* c, int n, const double* d_xy, double dt, double* d_out);
 cudaError_t launch_cell_velocity(cf_ctx* c, double* d_uc, double* d_vc);
 cudaError_t launch_max_velocity(cf_ctx* c, double* d_out);
 cudaError_t launch_test_convert(cf_ctx* c, int n, const double* d, float* f, double* w);
-cudaError_t launch_convert_q(cf_ctx* c, int to_device, int version);
+cudaError_t launch_convert_q(cf_ctx* c, int to_device, int version, cudaStream_t stream = nullptr);
 cudaError_t launch_q_to_f64(cf_ctx* c, int version, double* dst, cudaStream_t stream);
 
 // projection (cf_project.cu)

@@ -184,12 +184,13 @@ struct Adv64 {
     Grid<double> q, u, v, qn, un, vn;
     double dt;
     int fuse;
+    int ent0;  // entity of blockIdx.z == 0 (a launch may cover a subset)
 };
 
 template <int ORDER>
 __global__ void __launch_bounds__(256) k_advect64(Adv64 a) {
     const Phys& p = a.p;
-    int ent = blockIdx.z;
+    int ent = blockIdx.z + a.ent0;
     int gi = blockIdx.x * blockDim.x + threadIdx.x;
     int gj = blockIdx.y * blockDim.y + threadIdx.y;
     int ox = p.nx + ((ent == E_FACEI && !p.per_x) ? 1 : 0);
@@ -230,6 +231,7 @@ struct Adv32 {
     float c;      // dt / dx
     double dt;
     int fuse;
+    int ent0;     // entity of blockIdx.z == 0 (a launch may cover a subset)
 };
 
 // FP32 copy of a ghosted FP64 array (ghosts included)
@@ -297,7 +299,7 @@ __device__ __forceinline__ float cub32(const Grid<T>& g, int bi, int bj, float f
 template <int ORDER>
 __global__ void __launch_bounds__(256) k_advect32(Adv32 a) {
     const Phys& p = a.p;
-    int ent = blockIdx.z;
+    int ent = blockIdx.z + a.ent0;
     int gi = blockIdx.x * blockDim.x + threadIdx.x;
     int gj = blockIdx.y * blockDim.y + threadIdx.y;
     int ox = p.nx + ((ent == E_FACEI && !p.per_x) ? 1 : 0);
@@ -501,10 +503,10 @@ static inline dim3 grid2(int ex, int ey, dim3 blk, int z = 1) {
     return dim3((ex + blk.x - 1) / blk.x, (ey + blk.y - 1) / blk.y, z);
 }
 
-cudaError_t launch_fill_ghosts(cf_ctx* c) {
+cudaError_t launch_fill_ghosts(cf_ctx* c, int what, cudaStream_t stream) {
     const Phys& p = c->ph;
     if (!p.per_x && !p.per_y) return cudaSuccess;  // wall ghosts are never written
-    dim3 blk(32, 8);
+    if (!stream) stream = c->stream;
     int s = c->cur;
     int nqx = p.nx, nqy = p.ny;
     int nux = p.per_x ? p.nx : p.nx + 1, nvy = p.per_y ? p.ny : p.ny + 1;
@@ -512,28 +514,34 @@ cudaError_t launch_fill_ghosts(cf_ctx* c) {
         const int n = CF_HALO * ex + noy * (ex - nox) + (ey - CF_HALO - noy) * ex;
         return (n + 255) / 256;
     };
-    if (c->precision == CF_PREC_FP64) {
-        const Grid<double>& g = c->q64[s];
-        k_fill_ghosts<double><<<frame(g.ex, g.ey, nqx, nqy), 256, 0, c->stream>>>(g, nqx, nqy, p.per_x, p.per_y);
-    } else {
-        const Grid<float>& g = c->q32[s];
-        k_fill_ghosts<float><<<frame(g.ex, g.ey, nqx, nqy), 256, 0, c->stream>>>(g, nqx, nqy, p.per_x, p.per_y);
+    if (what & GHOSTS_Q) {
+        if (c->precision == CF_PREC_FP64) {
+            const Grid<double>& g = c->q64[s];
+            k_fill_ghosts<double><<<frame(g.ex, g.ey, nqx, nqy), 256, 0, stream>>>(g, nqx, nqy, p.per_x, p.per_y);
+        } else {
+            const Grid<float>& g = c->q32[s];
+            k_fill_ghosts<float><<<frame(g.ex, g.ey, nqx, nqy), 256, 0, stream>>>(g, nqx, nqy, p.per_x, p.per_y);
+        }
+        c->launches += 1;
     }
-    k_fill_ghosts<double><<<frame(c->u[s].ex, c->u[s].ey, nux, p.ny), 256, 0, c->stream>>>(c->u[s], nux, p.ny, p.per_x,
-                                                                                       p.per_y);
-    k_fill_ghosts<double><<<frame(c->v[s].ex, c->v[s].ey, p.nx, nvy), 256, 0, c->stream>>>(c->v[s], p.nx, nvy, p.per_x,
-                                                                                       p.per_y);
-    c->launches += 3;
+    if (what & GHOSTS_UV) {
+        k_fill_ghosts<double><<<frame(c->u[s].ex, c->u[s].ey, nux, p.ny), 256, 0, stream>>>(c->u[s], nux, p.ny,
+                                                                                         p.per_x, p.per_y);
+        k_fill_ghosts<double><<<frame(c->v[s].ex, c->v[s].ey, p.nx, nvy), 256, 0, stream>>>(c->v[s], p.nx, nvy,
+                                                                                         p.per_x, p.per_y);
+        c->launches += 2;
+    }
     return cudaGetLastError();
 }
 
-cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs) {
+cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs, int ent0, int nent, bool prep,
+                          bool advance) {
     const Phys& p = c->ph;
     int s = c->cur, n = 1 - s;
     dim3 blk(32, 8);
-    dim3 grd = grid2(p.nx + 1, p.ny + 1, blk, 3);
+    dim3 grd = grid2(p.nx + 1, p.ny + 1, blk, nent);
     if (c->precision == CF_PREC_FP64) {
-        Adv64 a{p, c->q64[s], c->u[s], c->v[s], c->q64[n], c->u[n], c->v[n], dt, fuse_inputs};
+        Adv64 a{p, c->q64[s], c->u[s], c->v[s], c->q64[n], c->u[n], c->v[n], dt, fuse_inputs, ent0};
         if (order == 1)
             k_advect64<1><<<grd, blk, 0, c->stream>>>(a);
         else
@@ -541,8 +549,10 @@ cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs) {
     } else {
         // fused inputs with a density-scaled force are applied by the
         // standalone inputs kernels after the advection
-        Adv32 a{p, c->q32[s], c->q32[n], c->u32, c->v32, c->u[n], c->v[n], (float)(dt / p.dx), dt, fuse_inputs};
-        if (c->uv32) {
+        Adv32 a{p, c->q32[s], c->q32[n], c->u32, c->v32, c->u[n], c->v[n], (float)(dt / p.dx), dt, fuse_inputs, ent0};
+        if (!prep) {
+            // the FP32 velocity copies were prepared by an earlier part of this advection
+        } else if (c->uv32) {
             // the last gradient subtraction left the owned FP32 copies: only their ghosts
             const int nux = p.per_x ? p.nx : p.nx + 1, nvy = p.per_y ? p.ny : p.ny + 1;
             if (p.per_x || p.per_y) {
@@ -560,14 +570,16 @@ cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs) {
             k_to32<<<grid2(c->v[s].ex, c->v[s].ey, blk), blk, 0, c->stream>>>(c->v[s], c->v32);
             c->launches += 2;
         }
-        c->uv32 = 0;  // the advection writes the next u, v
         if (order == 1)
             k_advect32<1><<<grd, blk, 0, c->stream>>>(a);
         else
             k_advect32<3><<<grd, blk, 0, c->stream>>>(a);
     }
     c->launches += 1;
-    c->cur = n;  // ProblemManager::advance for q, u, v
+    if (advance) {
+        c->uv32 = 0;  // the advection wrote the next u, v
+        c->cur = n;   // ProblemManager::advance for q, u, v
+    }
     return cudaGetLastError();
 }
 
@@ -649,10 +661,11 @@ cudaError_t launch_q_to_f64(cf_ctx* c, int version, double* dst, cudaStream_t st
     return cudaGetLastError();
 }
 
-cudaError_t launch_convert_q(cf_ctx* c, int to_device, int version) {
+cudaError_t launch_convert_q(cf_ctx* c, int to_device, int version, cudaStream_t stream) {
     dim3 blk(32, 8);
-    k_q_convert<<<grid2(c->ph.nx, c->ph.ny, blk), blk, 0, c->stream>>>(c->q32[version], c->staging, c->ph.nx,
-                                                                       c->ph.ny, to_device);
+    if (!stream) stream = c->stream;
+    k_q_convert<<<grid2(c->ph.nx, c->ph.ny, blk), blk, 0, stream>>>(c->q32[version], c->staging, c->ph.nx, c->ph.ny,
+                                                                    to_device);
     c->launches += 1;
     return cudaGetLastError();
 }
