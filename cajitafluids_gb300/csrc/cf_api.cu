@@ -331,6 +331,7 @@ int cf_ctx_destroy(cf_ctx* ctx) {
     if (ctx->ev_adv) cudaEventDestroy(ctx->ev_adv);
     if (ctx->ev_uv) cudaEventDestroy(ctx->ev_uv);
     if (ctx->ev_q) cudaEventDestroy(ctx->ev_q);
+    if (ctx->ev_press) cudaEventDestroy(ctx->ev_press);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return CF_OK;
@@ -689,6 +690,13 @@ int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* 
     SolveResult r{};
     bool deferred = false;
     rc = project_async(ctx, dt, so, &r, &deferred);
+    // the resident projection records ev_press after the gradient subtraction:
+    // u and v go out on the second stream from there, beside the norms
+    cudaStream_t out_stream = ctx->stream;
+    if (!rc && deferred && (u_out || v_out)) {
+        rc = cuda_check(ctx, cudaStreamWaitEvent(ctx->stream2, ctx->ev_press, 0), "event wait");
+        out_stream = ctx->stream2;
+    }
     double* outs[3] = {nullptr, u_out, v_out};
     for (int f = 1; f < 3 && !rc; ++f) {
         if (!outs[f]) continue;
@@ -697,7 +705,7 @@ int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* 
         const Grid<double>& g = f == CF_FIELD_U ? ctx->u[s1] : ctx->v[s1];
         rc = cuda_check(ctx, cudaMemcpy2DAsync(outs[f], ox * sizeof(double), &g.at(CF_HALO, CF_HALO),
                                                g.pitch * sizeof(double), ox * sizeof(double), oy, cudaMemcpyDefault,
-                                               ctx->stream),
+                                               out_stream),
                         "download");
     }
     int rc2 = cuda_check(ctx, cudaStreamSynchronize(ctx->stream2), "step_host");

@@ -57,6 +57,7 @@ struct cf_ctx {
     cudaStream_t stream2 = nullptr;
     cudaEvent_t ev_adv = nullptr;
     cudaEvent_t ev_uv = nullptr, ev_q = nullptr;  // cf_step_host: velocities in, quantity in
+    cudaEvent_t ev_press = nullptr;  // recorded by the resident projection right after the gradient subtraction
     double* staging2 = nullptr;
     cudaGraphExec_t gmg = nullptr;      // batch of MG-PCG iterations
     cudaGraphExec_t gmg_pre = nullptr;  // V-cycle + r.z after the residual is (re)formed

@@ -1193,6 +1193,10 @@ static int capture_graph(cf_ctx* c, cudaGraph_t* g, const std::function<void()>&
 }
 
 static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, bool mg, int cur) {
+    if (!c->ev_press) {
+        int rc0 = cuda_check(c, cudaEventCreateWithFlags(&c->ev_press, cudaEventDisableTiming), "event create");
+        if (rc0) return rc0;
+    }
     const int nb = red_blocks(c);
     const double scale = -st.ms;
     Grid<double> gu = c->u[cur], gv = c->v[cur];
@@ -1257,6 +1261,8 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
                      mixed ? 1 : 0};
             dim3 grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
             k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
+            // u, v are final here: a caller may copy them out beside the norms
+            cudaEventRecordWithFlags(c->ev_press, c->stream, cudaEventRecordExternal);
             DivArgs da = div_args(c, st);
             da.u = gu;
             da.v = gv;
