@@ -358,6 +358,7 @@ struct DivArgs {
     int warm;  // keep x from the previous solve (warm start) instead of x = 0
     int mixed;        // k_div_norms: squares and magnitudes in FP32
     float mscale32;   // -(1/dx) in FP32
+    float2 mscale2;   // -(1/dx) as a double-float pair
 };
 
 __device__ __forceinline__ double div_b(const DivArgs& a, int gi, int gj) {
@@ -485,9 +486,16 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
             for (int s = 0; s < 2; ++s) {
                 int c = c0 + s;
                 if (c >= a.nx) continue;
-                const double b = div_b(a, c, j);
+                // the divergence sum in FP64 (it cancels), its scale -1/dx as
+                // a double-float product on the FP32 pipe
+                int ie = c + 1, jn = j + 1;
+                if (a.per_x && ie == a.nx) ie = 0;
+                if (a.per_y && jn == a.ny) jn = 0;
+                double t = a.u.at(ie + CF_HALO, j + CF_HALO) - a.u.at(c + CF_HALO, j + CF_HALO);
+                t = t + a.v.at(c + CF_HALO, jn + CF_HALO);
+                t = t - a.v.at(c + CF_HALO, j + CF_HALO);
                 const size_t k = (size_t)j * a.pitch + c;
-                const float2 bs = df_split(b);
+                const float2 bs = df_mul(a.mscale2, df_split(t));
                 reinterpret_cast<float2*>(a.b)[k] = bs;
                 // x as a double-float pair: 0, or (warm start) the previous
                 // FP64 solution split in place (same 8 bytes per cell)
@@ -926,6 +934,7 @@ static DivArgs div_args(cf_ctx* c, const Stencil& st) {
     a.mscale = -(1.0 / c->ph.dx);
     a.mixed = c->precision == CF_PREC_MIXED;
     a.mscale32 = (float)a.mscale;
+    a.mscale2 = make_float2(a.mscale32, (float)(a.mscale - (double)a.mscale32));
     a.st = st;
     a.x = c->x.a;
     a.r = c->r.a;
