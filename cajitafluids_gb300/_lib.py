@@ -128,6 +128,8 @@ SIGNATURES = {
     "cf_setup": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolveStats)]),
     "cf_step": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(SolverOpts),
                                ctypes.POINTER(SolveStats)]),
+    "cf_steps": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.POINTER(SolverOpts),
+                                ctypes.POINTER(SolveStats), ctypes.POINTER(ctypes.c_int)]),
     "cf_step_host": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(SolverOpts),
                                     ctypes.POINTER(SolveStats), _dp, _dp, _dp, _dp, _dp, _dp]),
     "cf_div_norms": (ctypes.c_int, [_vp, _dp, _dp]),

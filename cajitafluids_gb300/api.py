@@ -188,6 +188,21 @@ class Context:
         return self._solve_call(self.lib.cf_step, ctypes.c_double(dt), ctypes.c_int(order), opts=opts,
                                 raise_on_maxit=raise_on_maxit)
 
+    def steps(self, nsteps: int, dt: float, order: int = 3, opts: Optional[SolverOptions] = None,
+              raise_on_maxit=False) -> dict:
+        """cf_steps: nsteps steps with one synchronisation; the last step's
+        solve statistics plus "unconverged", the number of steps whose
+        pressure solve did not converge."""
+        o = (opts or SolverOptions()).to_c()
+        st = L.SolveStats()
+        bad = ctypes.c_int(0)
+        allow = () if raise_on_maxit else (L.CF_ERR_NOT_CONVERGED,)
+        self._check(self.lib.cf_steps(self.h, int(nsteps), ctypes.c_double(dt), ctypes.c_int(order), ctypes.byref(o),
+                                      ctypes.byref(st), ctypes.byref(bad)), allow=allow)
+        d = st.as_dict()
+        d["unconverged"] = bad.value
+        return d
+
     def step_host(self, dt: float, order: int, opts: Optional[SolverOptions], q_in, u_in, v_in, q_out=None,
                   u_out=None, v_out=None, raise_on_maxit=False) -> dict:
         """cf_step_host: upload q, u, v, one step, download into the outputs

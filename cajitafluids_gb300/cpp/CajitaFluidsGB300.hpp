@@ -22,6 +22,7 @@
 // std::runtime_error for an invalid backend, src/Solver.hpp:305-348).
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstdint>
@@ -412,18 +413,37 @@ class Solver<2> : public SolverBase {
         _time += _dt;
     }
     // src/Solver.hpp:149-177, writing through SiloWriter when an output
-    // directory is set (setOutputDirectory)
+    // directory is set (setOutputDirectory).  The same steps, prints and
+    // writes as the reference's do-while loop; the steps between two output
+    // points go to the device in one cf_steps call (no host synchronisation
+    // between them).
     void solve(const double t_final, const int write_freq) override {
-        int t = 0;
         int num_step = (int)(t_final / _dt);
-        if (_silo) _silo->siloWrite("Mesh", t, _time, _dt);
+        if (_silo) _silo->siloWrite("Mesh", 0, _time, _dt);
         setup();
-        do {
-            if (0 == t % write_freq) printf("Step %d / %d at time = %f\n", t, num_step, _time);
-            step();
-            if (_silo && 0 == t % write_freq) _silo->siloWrite("Mesh", t, _time, _dt);
-            t++;
-        } while (_time < t_final);
+        // the loop's step count: time accumulates one dt at a time until t_final
+        int total = 0;
+        for (double tm = _time; total == 0 || tm < t_final; ++total) tm += _dt;
+        int t = 0;
+        while (t < total) {
+            if (0 == t % write_freq) {
+                printf("Step %d / %d at time = %f\n", t, num_step, _time);
+                steps(1);
+                if (_silo) _silo->siloWrite("Mesh", t, _time, _dt);
+                t += 1;
+            } else {
+                const int next = std::min(total, (t / write_freq + 1) * write_freq);
+                steps(next - t);
+                t = next;
+            }
+        }
+    }
+    // n steps in one device-side loop (cf_steps)
+    void steps(int n) {
+        int bad = 0;
+        int rc = cf_steps(_pm->ctx(), n, _dt, _order, &_vc->options(), &_last, &bad);
+        if (rc != CF_OK && rc != CF_ERR_NOT_CONVERGED) check(_pm->ctx(), rc, "cf_steps");
+        for (int k = 0; k < n; ++k) _time += _dt;
     }
     void setOutputDirectory(const std::string& dir) { _silo = std::make_shared<SiloWriter<2>>(_pm, dir); }
     const std::shared_ptr<SiloWriter<2>>& siloWriter() const { return _silo; }

@@ -295,6 +295,8 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
     c->staging_elems = (size_t)(nx + 1) * (ny + 1);
     if (!rc) rc = alloc_dev(c, c->staging, c->staging_elems);
     if (!rc) rc = cuda_check(c, cudaMallocHost(&c->hS, sizeof(SolverState)), "cudaMallocHost");
+    if (!rc) rc = cuda_check(c, cudaMallocHost(&c->hP, sizeof(SolverState)), "cudaMallocHost");
+    if (!rc) rc = alloc_dev(c, c->d_tally, 2);
     if (!rc) rc = cuda_check(c, cudaMallocHost(&c->h_out, 4 * sizeof(double)), "cudaMallocHost");
     if (!rc && c->precision == CF_PREC_MIXED) rc = cg32_setup(c);
     for (int k = 0; k < 8 && !rc; ++k) rc = cuda_check(c, cudaEventCreate(&c->ev[k]), "event create");
@@ -323,6 +325,7 @@ int cf_ctx_destroy(cf_ctx* ctx) {
     cf::mg_free(ctx);
     for (void* p : ctx->allocs) cudaFree(p);
     if (ctx->hS) cudaFreeHost(ctx->hS);
+    if (ctx->hP) cudaFreeHost(ctx->hP);
     if (ctx->h_out) cudaFreeHost(ctx->h_out);
     if (ctx->stream2) {
         cudaStreamSynchronize(ctx->stream2);
@@ -603,6 +606,63 @@ int cf_step(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* opts,
     if (!rc && !fuse) rc = cuda_check(ctx, launch_add_inputs(ctx, dt), "add inputs");
     if (rc) return rc;
     return do_project(ctx, dt, opts, stats);
+    CF_GUARD_END
+}
+
+// Solver::solve's step loop (src/Solver.hpp:149-177) on the device: nsteps
+// advections and projections enqueued back to back, the projections'
+// parameters written once, one synchronisation at the end.  Each projection
+// adds to a device tally when it does not converge.
+int cf_steps(cf_ctx* ctx, int nsteps, double dt, int value_order, const cf_solver_opts* opts,
+             cf_solve_stats* stats, int* unconverged) {
+    if (!ctx || nsteps < 0) return CF_ERR_INVALID;
+    if (value_order != 1 && value_order != 3) return fail(ctx, CF_ERR_INVALID, "value_order must be 1 or 3");
+    if (!(dt > 0.0) || !isfinite(dt)) return fail(ctx, CF_ERR_INVALID, "dt must be positive and finite");
+    if (unconverged) *unconverged = 0;
+    if (nsteps == 0) return CF_OK;
+    CF_GUARD_BEGIN
+    cudaSetDevice(ctx->device);
+    SolveOpts so{};
+    int rc = parse_opts(ctx, opts, &so);
+    if (rc) return rc;
+    if (ctx->prof || !resident_projection()) {
+        // host-polled projections: one step at a time
+        int bad = 0, worst = CF_OK;
+        for (int k = 0; k < nsteps; ++k) {
+            int r = cf_step(ctx, dt, value_order, opts, stats);
+            if (r == CF_ERR_NOT_CONVERGED || r == CF_ERR_NUMERIC || r == CF_ERR_TIMEOUT) {
+                ++bad;
+                worst = r;
+            } else if (r) {
+                return r;
+            }
+        }
+        if (unconverged) *unconverged = bad;
+        return worst;
+    }
+    const bool fuse = !ctx->ph.force_density;
+    rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_tally, 0, 2 * sizeof(int), ctx->stream), "tally");
+    SolveResult r{};
+    bool deferred = false;
+    for (int k = 0; k < nsteps && !rc; ++k) {
+        rc = cuda_check(ctx, launch_fill_ghosts(ctx), "fill ghosts");
+        if (!rc) rc = cuda_check(ctx, launch_advect(ctx, dt, value_order, fuse ? 1 : 0), "advect");
+        if (!rc && !fuse) rc = cuda_check(ctx, launch_add_inputs(ctx, dt), "add inputs");
+        if (!rc) rc = project_async(ctx, dt, so, &r, &deferred, k > 0);
+    }
+    int tally[2] = {0, 0};
+    if (!rc)
+        rc = cuda_check(ctx, cudaMemcpyAsync(tally, ctx->d_tally, sizeof(tally), cudaMemcpyDeviceToHost, ctx->stream),
+                        "tally");
+    const int rc1 = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "steps");
+    if (rc) return rc;
+    if (rc1) return rc1;
+    if (deferred) project_collect(ctx, &r);
+    fill_stats(r, stats);
+    if (unconverged) *unconverged = tally[0];
+    if (tally[0] == 0) return CF_OK;
+    const int code = status_code(tally[1]);
+    return fail(ctx, code, "%d of %d pressure solves did not converge (worst status %d)", tally[0], nsteps, tally[1]);
     CF_GUARD_END
 }
 

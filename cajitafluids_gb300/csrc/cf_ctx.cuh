@@ -38,7 +38,9 @@ struct cf_ctx {
     double* partials = nullptr;  // 4 * n_units
     int G = 0, B = 0, n_units = 0;
     cf::SolverState* S = nullptr;   // device
-    cf::SolverState* hS = nullptr;  // pinned host mirror
+    cf::SolverState* hS = nullptr;  // pinned host mirror (solver state copied back)
+    cf::SolverState* hP = nullptr;  // pinned solver parameters copied in (not overwritten by a projection)
+    int* d_tally = nullptr;         // resident projections: [0] solves that did not converge, [1] worst status
     double* d_out = nullptr;        // small device output slots
     double* h_out = nullptr;        // pinned host mirror
     double* staging = nullptr;      // FP64 staging for conversions / strided copies
@@ -121,7 +123,9 @@ int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res);
 // project without the final synchronisation when the device-resident graph
 // serves it (*deferred = true; project_collect fills res after the caller has
 // synchronised the stream), else a plain project (*deferred = false)
-int project_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, bool* deferred);
+bool resident_projection();  // device-resident projection graphs in use (CF_RESIDENT=0 turns them off)
+int project_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, bool* deferred,
+                  bool params_ready = false);
 void project_collect(cf_ctx* c, SolveResult* res);
 int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Grid<double> gu, Grid<double> gv,
                   int adjoint);

@@ -1145,6 +1145,16 @@ static int read_state(cf_ctx* c) {
 static const int kResidentBatch = 16;    // Jacobi-PCG iterations per trip
 static const int kResidentBatchMG = 1;   // MG-PCG iterations per trip
 
+// after each resident projection: count the solves that did not converge
+// (a solve still RUNNING stopped at the trip limit) and keep the worst status
+__global__ void k_step_tally(const SolverState* S, int* tally) {
+    int st = S->status == ST_RUNNING ? ST_MAXIT : S->status;
+    if (st != ST_CONVERGED) {
+        tally[0] += 1;
+        if (st > tally[1]) tally[1] = st;
+    }
+}
+
 __global__ void k_loop_cond(SolverState* S, cudaGraphConditionalHandle h) {
     int run = *(volatile int*)&S->status == ST_RUNNING;
     if (run) {
@@ -1276,7 +1286,8 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
             da.u = gu;
             da.v = gv;
             k_div_norms<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
-            ntail += 2;
+            k_step_tally<<<1, 1, 0, c->stream>>>(c->S, c->d_tally);
+            ntail += 3;
             cudaMemcpyAsync(c->hS, c->S, sizeof(SolverState), cudaMemcpyDeviceToHost, c->stream);
             cudaMemcpyAsync(c->h_out, c->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
         });
@@ -1305,10 +1316,12 @@ static bool resident_enabled() {
     return on != 0;
 }
 
+bool resident_projection() { return resident_enabled(); }
+
 // the projection of the current buffers through the resident graph; with
 // defer, returns after the launch (project_collect reads the results)
 static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, const Stencil& st,
-                            bool mixed, bool mg, bool defer = false) {
+                            bool mixed, bool mg, bool defer = false, bool params_ready = false) {
     const int cur = c->cur;
     const int flags = (mixed ? 1 : 0) | (mg ? 2 : 0) | (c->warm ? 4 : 0);
     int rc = CF_OK;
@@ -1320,18 +1333,24 @@ static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResul
         c->rg_st[cur] = st;
         c->rg_ph[cur] = c->ph;
     }
-    SolverState* h = c->hS;
-    memset(h, 0, sizeof(SolverState));
-    h->tol2 = o.tol * o.tol;
-    h->abs2 = o.abs_tol * o.abs_tol;
-    h->use_abs = o.abs_tol > 0.0 ? 1 : 0;
-    h->area = c->ph.dx * c->ph.dx;
-    h->max_iter = o.max_iter;
-    h->max_outer = o.max_outer;
-    h->inner_tol2 = o.inner_tol * o.inner_tol;
-    h->status = ST_RUNNING;
-    const int batch = mg ? kResidentBatchMG : kResidentBatch;
-    h->trip_limit = (o.max_iter + (mixed ? o.max_outer : 0)) / batch + 4;
+    // The parameters go in from their own pinned buffer: the tail copies the
+    // final state back into hS, and a caller that enqueues several steps
+    // without synchronising (params_ready: the same parameters, written once)
+    // must not have a later step read an earlier step's final state.
+    SolverState* h = c->hP;
+    if (!params_ready) {
+        memset(h, 0, sizeof(SolverState));
+        h->tol2 = o.tol * o.tol;
+        h->abs2 = o.abs_tol * o.abs_tol;
+        h->use_abs = o.abs_tol > 0.0 ? 1 : 0;
+        h->area = c->ph.dx * c->ph.dx;
+        h->max_iter = o.max_iter;
+        h->max_outer = o.max_outer;
+        h->inner_tol2 = o.inner_tol * o.inner_tol;
+        h->status = ST_RUNNING;
+        const int batch = mg ? kResidentBatchMG : kResidentBatch;
+        h->trip_limit = (o.max_iter + (mixed ? o.max_outer : 0)) / batch + 4;
+    }
     cudaMemcpyAsync(c->S, h, sizeof(SolverState), cudaMemcpyHostToDevice, c->stream);
     if ((rc = cuda_check(c, cudaGraphLaunch(c->rgx[cur], c->stream), "graph launch"))) return rc;
     if (mixed) c->uv32 = 1;  // the graph's gradient subtraction wrote the FP32 velocity copies
@@ -1355,7 +1374,7 @@ void project_collect(cf_ctx* c, SolveResult* res) {
     res->div_linf = c->h_out[1];
 }
 
-int project_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, bool* deferred) {
+int project_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, bool* deferred, bool params_ready) {
     const bool mixed = c->precision == CF_PREC_MIXED;
     const bool mg = o.precon_mg != 0;
     *deferred = false;
@@ -1365,7 +1384,7 @@ int project_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, bo
     int rc = mg ? mg_setup(c) : CF_OK;
     if (rc) return rc;
     *deferred = true;
-    return project_resident(c, dt, o, res, st, mixed, mg, true);
+    return project_resident(c, dt, o, res, st, mixed, mg, true, params_ready);
 }
 
 int div_norms(cf_ctx* c, double* l2, double* linf) {

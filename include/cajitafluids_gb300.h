@@ -193,6 +193,15 @@ int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* 
                  const double* q_in, const double* u_in, const double* v_in, double* q_out, double* u_out,
                  double* v_out);
 
+/* Solver::solve's step loop (src/Solver.hpp:149-177) on the device: nsteps
+ * calls' worth of cf_step enqueued back to back with one synchronisation at
+ * the end.  stats: the last step's solve.  *unconverged (may be NULL): how
+ * many of the steps' pressure solves did not converge.  Returns CF_OK when
+ * all converged, else the code of the worst failure (CF_ERR_NOT_CONVERGED,
+ * CF_ERR_NUMERIC, CF_ERR_TIMEOUT); the state has advanced nsteps either way. */
+int cf_steps(cf_ctx* ctx, int nsteps, double dt, int value_order, const cf_solver_opts* opts,
+             cf_solve_stats* stats, int* unconverged);
+
 /* divergence norms of the current velocity field */
 int cf_div_norms(cf_ctx* ctx, double* l2, double* linf);
 /* max |u|, |v| over owned faces (for CFL time steps) */
