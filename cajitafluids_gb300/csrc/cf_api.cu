@@ -296,7 +296,7 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
     if (!rc) rc = alloc_dev(c, c->staging, c->staging_elems);
     if (!rc) rc = cuda_check(c, cudaMallocHost(&c->hS, sizeof(SolverState)), "cudaMallocHost");
     if (!rc) rc = cuda_check(c, cudaMallocHost(&c->hP, sizeof(SolverState)), "cudaMallocHost");
-    if (!rc) rc = alloc_dev(c, c->d_tally, 2);
+    if (!rc) rc = alloc_dev(c, c->d_tally, 4);
     if (!rc) rc = cuda_check(c, cudaMallocHost(&c->h_out, 4 * sizeof(double)), "cudaMallocHost");
     if (!rc && c->precision == CF_PREC_MIXED) rc = cg32_setup(c);
     for (int k = 0; k < 8 && !rc; ++k) rc = cuda_check(c, cudaEventCreate(&c->ev[k]), "event create");
@@ -641,7 +641,7 @@ int cf_steps(cf_ctx* ctx, int nsteps, double dt, int value_order, const cf_solve
         return worst;
     }
     const bool fuse = !ctx->ph.force_density;
-    rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_tally, 0, 2 * sizeof(int), ctx->stream), "tally");
+    rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_tally, 0, 3 * sizeof(int), ctx->stream), "tally");
     SolveResult r{};
     bool deferred = false;
     for (int k = 0; k < nsteps && !rc; ++k) {
@@ -650,14 +650,14 @@ int cf_steps(cf_ctx* ctx, int nsteps, double dt, int value_order, const cf_solve
         if (!rc && !fuse) rc = cuda_check(ctx, launch_add_inputs(ctx, dt), "add inputs");
         if (!rc) rc = project_async(ctx, dt, so, &r, &deferred, k > 0);
     }
-    int tally[2] = {0, 0};
+    int tally[3] = {0, 0, 0};
     if (!rc)
         rc = cuda_check(ctx, cudaMemcpyAsync(tally, ctx->d_tally, sizeof(tally), cudaMemcpyDeviceToHost, ctx->stream),
                         "tally");
     const int rc1 = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "steps");
     if (rc) return rc;
     if (rc1) return rc1;
-    if (deferred) project_collect(ctx, &r);
+    if (deferred) project_collect(ctx, &r, nsteps, tally[2]);
     fill_stats(r, stats);
     if (unconverged) *unconverged = tally[0];
     if (tally[0] == 0) return CF_OK;

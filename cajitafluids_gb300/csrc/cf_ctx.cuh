@@ -40,7 +40,7 @@ struct cf_ctx {
     cf::SolverState* S = nullptr;   // device
     cf::SolverState* hS = nullptr;  // pinned host mirror (solver state copied back)
     cf::SolverState* hP = nullptr;  // pinned solver parameters copied in (not overwritten by a projection)
-    int* d_tally = nullptr;         // resident projections: [0] solves that did not converge, [1] worst status
+    int* d_tally = nullptr;         // resident projections: [0] unconverged solves, [1] worst status, [2] trips
     double* d_out = nullptr;        // small device output slots
     double* h_out = nullptr;        // pinned host mirror
     double* staging = nullptr;      // FP64 staging for conversions / strided copies
@@ -126,7 +126,9 @@ int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res);
 bool resident_projection();  // device-resident projection graphs in use (CF_RESIDENT=0 turns them off)
 int project_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, bool* deferred,
                   bool params_ready = false);
-void project_collect(cf_ctx* c, SolveResult* res);
+// results of the last deferred resident projection; launch counts for it,
+// or (nproj > 0) for nproj projections with trips loop trips in all
+void project_collect(cf_ctx* c, SolveResult* res, int nproj = 0, long long trips = 0);
 int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Grid<double> gu, Grid<double> gv,
                   int adjoint);
 // FP32 TMA inner CG (cf_cg32.cu)

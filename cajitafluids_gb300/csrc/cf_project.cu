@@ -1147,12 +1147,14 @@ static const int kResidentBatchMG = 1;   // MG-PCG iterations per trip
 
 // after each resident projection: count the solves that did not converge
 // (a solve still RUNNING stopped at the trip limit) and keep the worst status
+// (tally[2]: loop trips + 1 summed over the projections, for launch counts)
 __global__ void k_step_tally(const SolverState* S, int* tally) {
     int st = S->status == ST_RUNNING ? ST_MAXIT : S->status;
     if (st != ST_CONVERGED) {
         tally[0] += 1;
         if (st > tally[1]) tally[1] = st;
     }
+    tally[2] += S->trips + 1;
 }
 
 __global__ void k_loop_cond(SolverState* S, cudaGraphConditionalHandle h) {
@@ -1361,10 +1363,13 @@ static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResul
     return CF_OK;
 }
 
-void project_collect(cf_ctx* c, SolveResult* res) {
+void project_collect(cf_ctx* c, SolveResult* res, int nproj, long long trips) {
     const int cur = c->rg_pending;
     const SolverState* hs = c->hS;
-    c->launches += c->rg_head[cur] + (long long)c->rg_trip[cur] * (hs->trips + 1) + c->rg_tail[cur];
+    if (nproj <= 0)
+        c->launches += c->rg_head[cur] + (long long)c->rg_trip[cur] * (hs->trips + 1) + c->rg_tail[cur];
+    else  // nproj projections with trips loop trips (+1 each) in all
+        c->launches += (long long)nproj * (c->rg_head[cur] + c->rg_tail[cur]) + (long long)c->rg_trip[cur] * trips;
     res->iterations = hs->iter;
     res->outer = hs->outer_iter;
     res->status = hs->status == ST_RUNNING ? ST_MAXIT : hs->status;
