@@ -62,21 +62,56 @@ __global__ void k_fill_ghosts(Grid<T> g, int nox, int noy, int per_x, int per_y)
 
 // --------------------------------------------------------------------------
 // FP64 spline sample (Cajita B-spline order 1 / 3, evaluated separably).
+//
+// The clamp of the logical coordinate to [lo, hi] (lo, hi small non-negative
+// integers), its integer part and that part as a double are done on the
+// integer pipe: for doubles of one sign the IEEE 754 bit patterns order like
+// the values (a set sign bit makes the signed pattern negative; patterns
+// above +infinity's are NaNs), the integer part of x in [0, 2^31) is the
+// significand with the hidden bit shifted right by 52 - exponent, and an int
+// k > 0 is exactly the double with exponent 31 - clz(k) and k's bits below
+// its top one as the significand.  The results are those of fmin/fmax, the
+// truncating conversion and the int-to-double conversion, which run on
+// GB300's narrow FP64 pipe.
+__device__ __forceinline__ double exact_double(int k) {  // k >= 0
+    if (k == 0) return 0.0;
+    const int e = 31 - __clz(k);
+    const unsigned long long m = ((unsigned long long)(unsigned)k << (52 - e)) & 0xFFFFFFFFFFFFFull;
+    return __longlong_as_double((long long)(((unsigned long long)(e + 1023) << 52) | m));
+}
+
+// fmin(fmax(x, lo), hi) for lo <= hi non-negative (NaN -> lo, as fmax gives)
+__device__ __forceinline__ double clamp_bits(double x, double lo, double hi) {
+    const long long b = __double_as_longlong(x);
+    if (b < __double_as_longlong(lo) || b > 0x7FF0000000000000LL) return lo;
+    if (b > __double_as_longlong(hi)) return hi;
+    return x;
+}
+
+// (int)x for x in [0, 2^31)
+__device__ __forceinline__ int trunc_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)(b >> 52) - 1023;
+    if (e < 0) return 0;
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    return (int)(m >> (52 - e));
+}
+
 template <int ORDER>
 __device__ __forceinline__ void weights64(double xi, int ext, int& k0, double* w) {
     if (ORDER == 1) {
-        xi = fmin(fmax(xi, 0.0), (double)(ext - 1));
-        int k = (int)xi;
+        xi = clamp_bits(xi, 0.0, exact_double(ext - 1));
+        int k = trunc_bits(xi);
         if (k > ext - 2) k = ext - 2;
-        double t = xi - (double)k;
+        double t = xi - exact_double(k);
         w[0] = 1.0 - t;
         w[1] = t;
         k0 = k;
     } else {
-        xi = fmin(fmax(xi, 1.0), (double)(ext - 2));
-        int k = (int)xi;
+        xi = clamp_bits(xi, 1.0, exact_double(ext - 2));
+        int k = trunc_bits(xi);
         if (k > ext - 3) k = ext - 3;
-        double t = xi - (double)k;
+        double t = xi - exact_double(k);
         double s = 1.0 - t;
         double t2 = t * t;
         double t3 = t2 * t;
@@ -111,7 +146,7 @@ __device__ double sample64(const Grid<double>& g, double lx, double ly, double r
 }
 
 __device__ __forceinline__ double entity_coord(const Phys& p, int ent, int axis, int idx) {
-    double t = (double)idx + ENT_OFF_D[ent][axis];
+    double t = exact_double(idx) + ENT_OFF_D[ent][axis];
     return p.gl[axis] + t * p.dx;
 }
 
@@ -148,6 +183,23 @@ __device__ __forceinline__ bool in_box(const Phys& p, double x, double y) {
     return x >= p.bbox[0] && x < p.bbox[2] && y >= p.bbox[1] && y < p.bbox[3];
 }
 
+// the box test on local indices (ranges the host evaluated with the same
+// FP64 coordinate test, src/InflowSource.hpp:78-88)
+__device__ __forceinline__ bool in_box_idx(const Phys& p, int ent, int li, int lj) {
+    return li >= p.box[ent][0] && li < p.box[ent][1] && lj >= p.box[ent][2] && lj < p.box[ent][3];
+}
+
+__device__ __forceinline__ double inputs_cell_in(const Phys& p, double q, bool inbox, double dt) {
+    if (inbox) {
+        if (p.src_mode == 0) {
+            if (q < p.src_q) q = p.src_q;
+        } else {
+            q = fma(p.src_q, dt, q);
+        }
+    }
+    return q;
+}
+
 __device__ __forceinline__ double inputs_cell(const Phys& p, double q, double x, double y, double dt) {
     if (in_box(p, x, y)) {
         if (p.src_mode == 0) {
@@ -160,6 +212,22 @@ __device__ __forceinline__ double inputs_cell(const Phys& p, double q, double x,
 }
 
 // axis 0: I-face (u), axis 1: J-face (v); rho is used only with a density-scaled force.
+__device__ __forceinline__ double inputs_face_in(const Phys& p, int axis, double w, bool inbox, double dt, int gidx,
+                                                 double rho) {
+    if (inbox && fabs(w) < fabs(p.src_vel[axis])) w = p.src_vel[axis];
+    if (p.force_density)
+        w = fma(p.force[axis] * rho, dt, w);
+    else
+        w = fma(p.force[axis], dt, w);
+    int per = axis == 0 ? p.per_x : p.per_y;
+    int n = axis == 0 ? p.nx : p.ny;
+    if (!per) {
+        if (gidx <= 0 && p.bc[axis] == 0) w = 0.0;
+        if (gidx > n - 1 && p.bc[axis + 2] == 0) w = 0.0;
+    }
+    return w;
+}
+
 __device__ __forceinline__ double inputs_face(const Phys& p, int axis, double w, double x, double y,
                                               double dt, int gidx, double rho) {
     if (in_box(p, x, y) && fabs(w) < fabs(p.src_vel[axis])) w = p.src_vel[axis];
@@ -204,12 +272,13 @@ __global__ void __launch_bounds__(256) k_advect64(Adv64 a) {
     rk3_64(p, a.u, a.v, a.dt, x0, y0, tx, ty);
     double val = sample64<ORDER>(f, p.low[ent][0], p.low[ent][1], p.rdx, tx, ty);
     if (a.fuse) {
+        const bool inbox = in_box_idx(p, ent, gi + CF_HALO, gj + CF_HALO);
         if (ent == E_CELL)
-            val = inputs_cell(p, val, x0, y0, a.dt);
+            val = inputs_cell_in(p, val, inbox, a.dt);
         else if (ent == E_FACEI)
-            val = inputs_face(p, 0, val, x0, y0, a.dt, gi, 0.0);
+            val = inputs_face_in(p, 0, val, inbox, a.dt, gi, 0.0);
         else
-            val = inputs_face(p, 1, val, x0, y0, a.dt, gj, 0.0);
+            val = inputs_face_in(p, 1, val, inbox, a.dt, gj, 0.0);
     }
     fn.at(gi + CF_HALO, gj + CF_HALO) = val;
 }
@@ -242,9 +311,6 @@ __global__ void k_to32(Grid<double> src, Grid<float> dst) {
     dst.at(i, j) = d2f_rn(src.at(i, j));
 }
 
-__device__ __forceinline__ bool in_box_idx(const Phys& p, int ent, int li, int lj) {
-    return li >= p.box[ent][0] && li < p.box[ent][1] && lj >= p.box[ent][2] && lj < p.box[ent][3];
-}
 
 template <typename T>
 __device__ __forceinline__ float lin32(const Grid<T>& g, int bi, int bj, float fx, float fy) {
