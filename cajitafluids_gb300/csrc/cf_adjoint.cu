@@ -58,7 +58,8 @@ struct Samp {
 };
 
 // Weights, derivative weights and the sample value / gradient, in the same
-// arithmetic as the forward sample (cf_fields.cu).
+// arithmetic as the forward sample (cf_fields.cu; clamps, integer parts and
+// int-to-double conversions on the integer pipe, exact).
 template <int ORDER>
 __device__ void samp(const Grid<double>& g, double lx, double ly, double rdx, double x, double y, Samp& s) {
     constexpr int n = ORDER == 1 ? 2 : 4;
@@ -70,24 +71,24 @@ __device__ void samp(const Grid<double>& g, double lx, double ly, double rdx, do
     for (int d = 0; d < 2; ++d) {
         double v = xi[d];
         if (ORDER == 1) {
-            double lo = 0.0, hi = (double)(ext[d] - 1);
-            clamped[d] = !(v >= lo && v <= hi);
-            v = fmin(fmax(v, lo), hi);
-            int k = (int)v;
+            double lo = 0.0, hi = exact_double(ext[d] - 1);
+            clamped[d] = outside_bits(v, lo, hi);
+            v = clamp_bits(v, lo, hi);
+            int k = trunc_bits(v);
             if (k > ext[d] - 2) k = ext[d] - 2;
-            double t = v - (double)k;
+            double t = v - exact_double(k);
             w[d][0] = 1.0 - t;
             w[d][1] = t;
             dw[d][0] = -1.0;
             dw[d][1] = 1.0;
             k0[d] = k;
         } else {
-            double lo = 1.0, hi = (double)(ext[d] - 2);
-            clamped[d] = !(v >= lo && v <= hi);
-            v = fmin(fmax(v, lo), hi);
-            int k = (int)v;
+            double lo = 1.0, hi = exact_double(ext[d] - 2);
+            clamped[d] = outside_bits(v, lo, hi);
+            v = clamp_bits(v, lo, hi);
+            int k = trunc_bits(v);
             if (k > ext[d] - 3) k = ext[d] - 3;
-            double t = v - (double)k;
+            double t = v - exact_double(k);
             double sm = 1.0 - t, t2 = t * t, t3 = t2 * t, s3 = (sm * sm) * sm;
             w[d][0] = s3 * (1.0 / 6.0);
             w[d][1] = fma(0.5, t3, -t2) + (2.0 / 3.0);

@@ -227,6 +227,53 @@ __device__ __forceinline__ float d2f_rn(double d) {
     return __double2float_rn(d);
 }
 
+// Spline-coordinate helpers for the FP64 samplers.
+// The clamp of the logical coordinate to [lo, hi] (lo, hi small non-negative
+// integers), its integer part and that part as a double are done on the
+// integer pipe: for doubles of one sign the IEEE 754 bit patterns order like
+// the values (a set sign bit makes the signed pattern negative; patterns
+// above +infinity's are NaNs), the integer part of x in [0, 2^31) is the
+// significand with the hidden bit shifted right by 52 - exponent, and an int
+// k > 0 is exactly the double with exponent 31 - clz(k) and k's bits below
+// its top one as the significand.  The results are those of fmin/fmax, the
+// truncating conversion and the int-to-double conversion, which run on
+// GB300's narrow FP64 pipe.
+__device__ __forceinline__ double exact_double(int k) {  // k >= 0
+    if (k == 0) return 0.0;
+    const int e = 31 - __clz(k);
+    const unsigned long long m = ((unsigned long long)(unsigned)k << (52 - e)) & 0xFFFFFFFFFFFFFull;
+    return __longlong_as_double((long long)(((unsigned long long)(e + 1023) << 52) | m));
+}
+
+// x's bit pattern for ordered comparisons with non-negative bounds (-0 as +0)
+__device__ __forceinline__ long long order_bits(double x) {
+    const long long b = __double_as_longlong(x);
+    return b == (long long)0x8000000000000000ull ? 0 : b;
+}
+
+// !(lo <= x && x <= hi) for lo <= hi non-negative (true for NaN)
+__device__ __forceinline__ bool outside_bits(double x, double lo, double hi) {
+    const long long b = order_bits(x);
+    return b < __double_as_longlong(lo) || b > __double_as_longlong(hi);
+}
+
+// fmin(fmax(x, lo), hi) for lo <= hi non-negative (NaN -> lo, as fmax gives)
+__device__ __forceinline__ double clamp_bits(double x, double lo, double hi) {
+    const long long b = order_bits(x);
+    if (b < __double_as_longlong(lo) || b > 0x7FF0000000000000LL) return lo;
+    if (b > __double_as_longlong(hi)) return hi;
+    return x;
+}
+
+// (int)x for x in [0, 2^31)
+__device__ __forceinline__ int trunc_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)(b >> 52) - 1023;
+    if (e < 0) return 0;
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    return (int)(m >> (52 - e));
+}
+
 // Double-float (hi + lo FP32 pair) error-free sums (Knuth two-sum, Dekker
 // quick two-sum); exact with --fmad=false.
 __device__ __forceinline__ float2 df_two_sum(float a, float b) {
