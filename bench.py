@@ -166,9 +166,17 @@ def make_context(w, precision, device):
     return c
 
 
+# Mixed MG-PCG reliable-update threshold of this workload: 0.5, i.e. a
+# double-float residual after every iteration (each cuts the residual by more
+# than half): 5 iterations and 5 updates per step at 4096^2 instead of 6 and 4
+# with the library's default 0.1 (4.08 vs 4.38 ms per step, GB300).
+MG_INNER_TOL = 0.5
+
+
 def solver_opts(w):
     from cajitafluids_gb300 import SolverOptions
-    return SolverOptions(tol=w.tol, abs_tol=w.abs_tol, max_iter=w.max_iter, precon=w.precon)
+    inner = MG_INNER_TOL if w.precon in MG_NAMES else 0.0
+    return SolverOptions(tol=w.tol, abs_tol=w.abs_tol, max_iter=w.max_iter, precon=w.precon, inner_tol=inner)
 
 
 def run_steps(c, w, n, stats=None):
@@ -275,6 +283,7 @@ def bench_gb300(args, rank, world, dist, device):
                                f"FP64 outer refinement), cubic, {pc_text}, ||div u||_L2 <= {w.abs_tol:g}",
                    "nx": w.nx, "ny": w.ny, "periodic": True, "precision": "mixed", "value_order": w.order,
                    "dt": w.dt, "abs_tol_div_l2": w.abs_tol, "solver": "PCG", "precon": w.precon,
+                   "reliable_update_threshold": solver_opts(w).inner_tol or 0.1,
                    "mg_levels": len(mg_levels(w.nx, w.ny, w.periodic)) if mg else None,
                    "parallelism": f"replicas x{world}",
                    "l2_policy": "inputs larger than L2 (state + solver vectors ~1 GB)"},
