@@ -255,7 +255,9 @@ __global__ void __launch_bounds__(256) k_advect64(Adv64 a) {
 // (the entity's local index) plus a small FP32 displacement in cell units,
 // so FP32 keeps full relative precision at any grid size.  u and v are
 // stored in FP64 (the projection works on them in FP64) and read here from
-// FP32 copies made once per step (k_to32), so no sample converts; q is FP32.
+// FP32 copies, so no sample converts: the gradient subtraction writes them,
+// or (after an upload or inputs) k_to32 makes them from the FP64 arrays;
+// q is FP32.
 // The inputs epilogue tests the inflow box on integer index ranges that the
 // host evaluated with the FP64 coordinate test, and works in FP64 only where
 // the FP64 result needs it (inside the box, a non-zero body force).
