@@ -15,6 +15,10 @@ struct cf_ctx {
     int precision = 0;
     double density = 1.0;
     int warm = 0;  // start each projection from the previous pressure (cf_set_warm_start)
+    // mixed MG-PCG with a reliable update after every iteration (threshold >=
+    // 0.5): the inner step only advances x (set per projection from its options)
+    int x_only = 0;
+    int gmg_xonly = -1;  // x_only of the cached host-polled MG graphs
     // mixed: u32/v32 hold the FP32 copies of the owned u, v of the current
     // state (written by the last gradient subtraction; ghosts not yet filled)
     int uv32 = 0;

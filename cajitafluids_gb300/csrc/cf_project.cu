@@ -1079,7 +1079,8 @@ static int capture(cf_ctx* c, cudaGraphExec_t* ge, F&& fn) {
 // K1 (z-mode), K2, V-cycle, r.z; gmg_pre = V-cycle and r.z after the
 // residual was formed (cold start, and after each reliable update).
 static int ensure_graph_mg(cf_ctx* c, const Stencil& st) {
-    if (c->gmg && c->gmg_pre && std::memcmp(&c->gmg_st, &st, sizeof(Stencil)) == 0) return CF_OK;
+    if (c->gmg && c->gmg_pre && c->gmg_xonly == c->x_only && std::memcmp(&c->gmg_st, &st, sizeof(Stencil)) == 0)
+        return CF_OK;
     const bool mixed = c->precision == CF_PREC_MIXED;
     const int nb = red_blocks(c);
     const double scale = -st.ms;
@@ -1112,6 +1113,7 @@ static int ensure_graph_mg(cf_ctx* c, const Stencil& st) {
         });
     if (rc) return rc;
     c->gmg_st = st;
+    c->gmg_xonly = c->x_only;
     c->gmg_per_iter = per;
     c->gmg_pre_launches = pre;
     return CF_OK;
@@ -1325,7 +1327,8 @@ bool resident_projection() { return resident_enabled(); }
 static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, const Stencil& st,
                             bool mixed, bool mg, bool defer = false, bool params_ready = false) {
     const int cur = c->cur;
-    const int flags = (mixed ? 1 : 0) | (mg ? 2 : 0) | (c->warm ? 4 : 0);
+    c->x_only = (mixed && mg && o.inner_tol >= 0.5) ? 1 : 0;
+    const int flags = (mixed ? 1 : 0) | (mg ? 2 : 0) | (c->warm ? 4 : 0) | (c->x_only ? 8 : 0);
     int rc = CF_OK;
     if (!c->rgx[cur] || c->rg_flags[cur] != flags || std::memcmp(&c->rg_st[cur], &st, sizeof(Stencil)) != 0 ||
         std::memcmp(&c->rg_ph[cur], &c->ph, sizeof(Phys)) != 0) {
@@ -1420,6 +1423,7 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     const bool mg = o.precon_mg != 0;
     int rc = mg ? mg_setup(c) : CF_OK;
     if (rc) return rc;
+    c->x_only = (mixed && mg && o.inner_tol >= 0.5) ? 1 : 0;
     // the resident graph serves plain projections; the adjoint's projection
     // (other arrays) and profiled runs (events between batches) take the
     // host-polled batches below

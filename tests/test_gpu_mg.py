@@ -202,3 +202,33 @@ def test_mixed_mg_rz_fused(built, monkeypatch, nx, ny, periodic, bc):
     for f in ("u", "v"):
         d = np.abs(ref[f] - out[f]).max()
         assert d <= 1e-6 * np.abs(ref[f]).max(), (f, d)
+
+
+@pytest.mark.parametrize("nx,ny,periodic,bc", [
+    (256, 256, (True, True), (0, 0, 0, 0)),
+    (192, 128, (False, False), (0, 1, 0, 1)),
+])
+def test_mixed_mg_update_every_iteration(built, nx, ny, periodic, bc):
+    """Reliable-update threshold >= 0.5: the inner step only advances x and
+    every iteration ends with the double-float residual.  Same results, bit
+    for bit, as the full inner step at a threshold just below 0.5 whenever
+    that run also updated after every iteration."""
+    from cajitafluids_gb300 import Context
+    rng = np.random.default_rng(nx * ny)
+    shapes = {"q": (ny, nx), "u": (ny, nx + (0 if periodic[0] else 1)), "v": (ny + (0 if periodic[1] else 1), nx)}
+    state = {f: rng.standard_normal(shp) for f, shp in shapes.items()}
+    runs = []
+    for itol in (0.49, 0.5):
+        c = Context(nx, ny, hi=(1.0, ny / nx), periodic=periodic, precision="mixed")
+        c.set_bc(bc)
+        for f, a in state.items():
+            c.upload(f, a)
+        st = c.project(0.5 / nx, opts(tol=1e-9, max_iter=200, precon="PFMG", inner_tol=itol))
+        runs.append((st, {f: c.download(f) for f in ("p", "u", "v")}))
+        c.close()
+    (sa, fa), (sb, fb) = runs
+    assert sb["status"] == 0 and sb["outer_iterations"] >= sb["iterations"]
+    assert sa["outer_iterations"] >= sa["iterations"], "the comparison run did not update every iteration"
+    assert sa["iterations"] == sb["iterations"] and sa["r_norm"] == sb["r_norm"]
+    for f in ("p", "u", "v"):
+        assert np.array_equal(fa[f], fb[f]), f
