@@ -112,7 +112,9 @@ typedef struct {
     double abs_tol;
     int max_iter;        /* FP64 CG iterations, or total FP32 iterations (mixed) */
     double inner_tol;    /* mixed: FP32 residual reduction that triggers an FP64
-                            reliable update (0 = 0.1) */
+                            reliable update (0 = 0.1); with PFMG/SMG/MG, 0.5 or
+                            more updates after every iteration (the inner step
+                            then only advances x) */
     int max_outer;       /* mixed: limit on FP64 reliable updates (0 = 200) */
 } cf_solver_opts;
 
