@@ -75,12 +75,19 @@ def alg_bytes_per_iter(nx, ny, periodic, precon, word, outer_frac=0.0, mixed=Fal
     mixed forms r.z with the finest post-smoothing.  Mixed: the solution x
     is a double-float pair (8 bytes) in the update, and the reliable update
     (R x, b at 8 bytes, W r at 4 = 20 B per cell) runs on the fraction
-    outer_frac of the iterations."""
+    outer_frac of the iterations; when that is every iteration, the update
+    replaces r, so the inner step needs only R p and R/W x."""
     n = nx * ny
     if precon not in MG_NAMES:
         return 11 * word * n + outer_frac * 20.0 * n
     xw = 8 if mixed else word
-    b = 3 * word * n + (3 * word + 2 * xw) * n
+    b = 3 * word * n
+    if mixed and outer_frac >= 1.0:
+        # an update after every iteration replaces r: the inner step only
+        # advances x (R p, R/W x)
+        b += (word + 2 * xw) * n
+    else:
+        b += (3 * word + 2 * xw) * n
     if not mixed:
         b += 2 * word * n
     lv = mg_levels(nx, ny, periodic)
