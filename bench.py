@@ -45,7 +45,7 @@ FP64_ITERS_PER_STEP_4096 = 7890
 MG_NAMES = ("PFMG", "SMG", "MG")
 # DRAM bytes (read + write) of one mixed MG-PCG inner iteration at 4096^2,
 # from an ncu capture of this bench (profiles/traffic_4096_mixed_mg.md)
-MEASURED_TRAFFIC_MG_ITER_4096 = 1.30e9
+MEASURED_TRAFFIC_MG_ITER_4096 = 1.17e9
 
 
 def mg_levels(nx, ny, periodic):
@@ -336,8 +336,9 @@ def bench_gb300(args, rank, world, dist, device):
                                       mixed=True)
         achieved = it_bytes / (it_ms / 1e3) / 1e9
         if mg:
-            kname = ("MG-PCG inner iteration: k_tma_dir_matvec32 + k_tma_update32 + gated k_outer_resid + "
-                     "V-cycle (k_mg_pre/k_mg_post per level with r.z in the finest post-smoothing, k_mg_bottom)")
+            kname = ("MG-PCG inner iteration: k_tma_dir_matvec32 + k_x_update32 (k_tma_update32 below an update "
+                     "threshold of 0.5) + gated k_outer_resid + V-cycle (k_mg_pre/k_mg_post per level with r.z in "
+                     "the finest post-smoothing, k_mg_bottom)")
             kern_extra = {}
         else:
             kname = "inner CG iteration (k_tma_dir_matvec32 + k_tma_update32)"
