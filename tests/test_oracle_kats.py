@@ -11,7 +11,10 @@ the hot path must satisfy:
   * the discrete divergence of a streamfunction MAC field vanishes;
   * the 5-point matrix equals BoundaryCondition::build_matrix entry for
     entry and is symmetric; CG matches a sparse direct solve;
-  * the fixed-order dot product agrees with numpy's.
+  * the fixed-order dot product agrees with numpy's;
+  * the inputs (inflow box at entity positions, body force, SOLID walls), the
+    rk3 trace with and without quirk Q3, the divergence of an affine field and
+    the gradient subtraction with quirk Q1.
 """
 import numpy as np
 import pytest
@@ -275,3 +278,172 @@ def test_zero_rhs_takes_no_iterations():
     o = Oracle(16, 16)
     st = o.project(0.01)
     assert st["iterations"] == 0 and st["status"] == 0
+
+
+# ---- inputs, trace and gradient known answers (the spec of Solver::_addInputs,
+# TimeIntegrator::rk3 and VelocityCorrector::_applyPressure) ----
+FREE, SOLID = 1, 0
+
+
+def _random_state(o, rng, lo=-3.0, hi=3.0):
+    q = rng.uniform(0.0, 5.0, o.shape("q"))
+    u = rng.uniform(lo, hi, o.shape("u"))
+    v = rng.uniform(lo, hi, o.shape("v"))
+    o.set("q", q)
+    o.set("u", u)
+    o.set("v", v)
+    return q, u, v
+
+
+def test_inflow_source_tests_the_box_at_entity_positions():
+    """InflowSource<2> (src/InflowSource.hpp:30-98): the half-open box
+    [x0, x0+w) x [y0, y0+h) is tested at the cell centre for q and at the face
+    centres for u and v; q becomes max(q, Q), a face velocity is replaced by the
+    source's only where it is smaller in magnitude; not a rate."""
+    n = 16
+    dx = 1.0 / n
+    src = ((0.25, 0.5), (0.25, 0.25), (2.0, -1.5), 3.0)
+    o = Oracle(n, n, bc=(FREE,) * 4, source=src)
+    rng = np.random.default_rng(21)
+    q, u, v = _random_state(o, rng)
+    u[8:12, 4] = u[8:12, 8] = 0.0       # faces on the box's left and right edges
+    o.set("u", u)
+    o.add_inputs(0.125)
+
+    def inside(x, y):
+        return (x >= 0.25) & (x < 0.5) & (y >= 0.5) & (y < 0.75)
+
+    jc, ic = np.mgrid[0:n, 0:n]
+    mq = inside((ic + 0.5) * dx, (jc + 0.5) * dx)
+    eq = np.where(mq, np.maximum(q, 3.0), q)
+    ju, iu = np.mgrid[0:n, 0:n + 1]
+    mu = inside(iu * dx, (ju + 0.5) * dx) & (np.abs(u) < 2.0)
+    eu = np.where(mu, 2.0, u)
+    jv, iv = np.mgrid[0:n + 1, 0:n]
+    mv = inside((iv + 0.5) * dx, jv * dx) & (np.abs(v) < 1.5)
+    ev = np.where(mv, -1.5, v)
+    assert np.array_equal(o.get("q"), eq)
+    assert np.array_equal(o.get("u"), eu)
+    assert np.array_equal(o.get("v"), ev)
+    # the box's left edge (x = 0.25) is inside, its right edge (x = 0.5) outside
+    assert (o.get("u")[8:12, 4] == 2.0).all()
+    assert (o.get("u")[8:12, 8] == 0.0).all()
+
+
+def test_body_force_adds_f_dt_on_every_face():
+    """BodyForce<2> (src/BodyForce.hpp:30-69): u += f_x dt and v += f_y dt on
+    every owned face, wall faces included, not scaled by the quantity."""
+    n = 12
+    f = (0.5, -9.81)
+    dt = 0.01
+    o = Oracle(n, n, bc=(FREE,) * 4, body=f)
+    rng = np.random.default_rng(22)
+    q, u, v = _random_state(o, rng)
+    o.add_inputs(dt)
+    assert np.allclose(o.get("u"), u + f[0] * dt, rtol=0, atol=1e-15)
+    assert np.allclose(o.get("v"), v + f[1] * dt, rtol=0, atol=1e-15)
+    assert np.array_equal(o.get("q"), q)
+
+
+@pytest.mark.parametrize("bc", [(SOLID,) * 4, (SOLID, FREE, FREE, SOLID), (FREE, SOLID, SOLID, FREE)])
+def test_solid_walls_zero_their_normal_faces(bc):
+    """BoundaryCondition<2>::operator() (src/BoundaryConditions.hpp:102-129):
+    with sides ordered [left, bottom, right, top], a SOLID side zeroes the
+    normal velocity on its wall faces (u at gi = 0 or N, v at gj = 0 or N); a
+    FREE side and every interior face are untouched."""
+    n = 10
+    o = Oracle(n, n, bc=bc)
+    rng = np.random.default_rng(23)
+    _, u, v = _random_state(o, rng)
+    o.add_inputs(0.01)
+    eu, ev = u.copy(), v.copy()
+    if bc[0] == SOLID:
+        eu[:, 0] = 0.0
+    if bc[2] == SOLID:
+        eu[:, n] = 0.0
+    if bc[1] == SOLID:
+        ev[0, :] = 0.0
+    if bc[3] == SOLID:
+        ev[n, :] = 0.0
+    assert np.array_equal(o.get("u"), eu)
+    assert np.array_equal(o.get("v"), ev)
+
+
+@pytest.mark.parametrize("fix_q3", [False, True])
+def test_rk3_third_stage_uses_v0(fix_q3):
+    """TimeIntegrator::rk3 (src/TimeIntegrator.hpp:36-77) on the shear field
+    u = a y, v = b x, which linear interpolation reproduces exactly: the third
+    stage starts from x0 - 3/4 dt v0 (quirk Q3, :57-58); with the fix it starts
+    from x0 - 3/4 dt v1 (Ralston's third-order scheme)."""
+    n = 32
+    dx = 1.0 / n
+    a, b = 1.7, -2.3
+    o = Oracle(n, n, periodic=(False, False), quirks=2 if fix_q3 else 0)
+    ju, iu = np.mgrid[0:n, 0:n + 1]
+    jv, iv = np.mgrid[0:n + 1, 0:n]
+    o.set("u", a * (ju + 0.5) * dx)
+    o.set("v", b * (iv + 0.5) * dx)
+    o.fill_ghosts()
+
+    def vel(p):
+        return np.stack([a * p[:, 1], b * p[:, 0]], axis=1)
+
+    rng = np.random.default_rng(24)
+    x0 = rng.uniform(0.3, 0.7, (64, 2))
+    dt = 0.05
+    v0 = vel(x0)
+    v1 = vel(x0 - 0.5 * dt * v0)
+    v2 = vel(x0 - 0.75 * dt * (v1 if fix_q3 else v0))
+    expect = x0 - dt * (2.0 / 9.0 * v0 + 3.0 / 9.0 * v1 + 4.0 / 9.0 * v2)
+    got = o.trace(x0, dt)
+    assert np.abs(got - expect).max() < 1e-13
+    other = x0 - dt * (2.0 / 9.0 * v0 + 3.0 / 9.0 * v1
+                       + 4.0 / 9.0 * vel(x0 - 0.75 * dt * (v0 if fix_q3 else v1)))
+    assert np.abs(got - other).max() > 1e-7
+
+
+def test_divergence_of_an_affine_field():
+    """_buildRHS (src/VelocityCorrector.hpp:182-212): u = alpha x, v = beta y
+    has discrete divergence alpha + beta in every cell; the L2 norm is taken
+    with the cell area, so it equals |alpha + beta| on the unit box."""
+    n = 24
+    dx = 1.0 / n
+    alpha, beta = 0.75, -2.0
+    o = Oracle(n, n, bc=(FREE,) * 4)
+    ju, iu = np.mgrid[0:n, 0:n + 1]
+    jv, iv = np.mgrid[0:n + 1, 0:n]
+    o.set("u", alpha * iu * dx)
+    o.set("v", beta * jv * dx)
+    l2, linf = o.div_norms()
+    assert linf == pytest.approx(abs(alpha + beta), rel=1e-12)
+    assert l2 == pytest.approx(abs(alpha + beta), rel=1e-12)
+
+
+def test_apply_pressure_subtracts_the_face_gradient():
+    """_applyPressure (src/VelocityCorrector.hpp:214-264) with SOLID walls and
+    quirk Q1 kept: every owned face gets u -= dt/(rho dx) (p(i) - p(i-1)),
+    physical ghosts of p are 0, so the bottom wall's v becomes
+    v - scale p(i, 0) and the top wall's v + scale p(i, N-1); u's bottom row is
+    then zeroed by the J-face condition applied to u (:260)."""
+    n = 16
+    dx = 1.0 / n
+    dt, rho = 0.02, 1.3
+    o = Oracle(n, n, density=rho)
+    rng = np.random.default_rng(25)
+    _, u, v = _random_state(o, rng)
+    o.project(dt, tol=1e-10, max_iter=5000)
+    p = o.get("p")
+    s = dt / (rho * dx)
+    pz = np.zeros((n + 2, n + 2))
+    pz[1:-1, 1:-1] = p
+    eu = u - s * (pz[1:-1, 1:] - pz[1:-1, :-1])
+    ev = v - s * (pz[1:, 1:-1] - pz[:-1, 1:-1])
+    eu[:, 0] = 0.0          # I-face condition on the SOLID left and right walls
+    eu[:, n] = 0.0
+    eu[0, :] = 0.0          # Q1: the J-face condition applied to u
+    tol = 1e-12 * (np.abs(u).max() + s * np.abs(p).max())
+    assert np.abs(o.get("u") - eu).max() <= tol
+    assert np.abs(o.get("v") - ev).max() <= tol
+    vn = o.get("v")
+    assert np.abs(vn[0] - (v[0] - s * p[0])).max() <= tol
+    assert np.abs(vn[n] - (v[n] + s * p[n - 1])).max() <= tol
