@@ -369,6 +369,18 @@ class SolverBase {
 };
 
 // src/Solver.hpp:55-279.
+// src/Solver.hpp:96-106: dt is limited to one cell per step at the inflow
+// speed plus sqrt(|f| dx); the limited step is fixed for the run, because the
+// pressure matrix is built with it.
+inline double limitTimeStep(double delta_t, double cell_size, const InflowSource<2>& source,
+                            const BodyForce<2>& body) {
+    double forcemax = std::sqrt(body._force[0] * body._force[0] + body._force[1] * body._force[1]);
+    double umax = std::fmax(std::fabs(source._velocity[0]), std::fabs(source._velocity[1])) +
+                  std::sqrt(forcemax * cell_size);
+    if ((umax > 0) && (delta_t > cell_size / umax)) return cell_size / umax;
+    return delta_t;
+}
+
 template <std::size_t NumSpaceDim>
 class Solver;
 
@@ -383,14 +395,9 @@ class Solver<2> : public SolverBase {
            std::array<bool, 2> periodic = {{false, false}}, int value_order = 3)
         : _density(density), _bc(bc), _source(source), _body(body), _dt(delta_t), _time(0.0), _order(value_order) {
         _mesh = std::make_shared<Mesh<2>>(global_bounding_box, global_num_cell, 3, periodic);
-        // src/Solver.hpp:96-106: limit dt to one cell per step at the inflow speed
-        double forcemax = std::sqrt(body._force[0] * body._force[0] + body._force[1] * body._force[1]);
-        double umax = std::fmax(std::fabs(source._velocity[0]), std::fabs(source._velocity[1])) +
-                      std::sqrt(forcemax * _mesh->cellSize());
-        if ((umax > 0) && (_dt > _mesh->cellSize() / umax)) {
-            _dt = _mesh->cellSize() / umax;
+        _dt = limitTimeStep(delta_t, _mesh->cellSize(), source, body);
+        if (_dt != delta_t)
             std::cerr << "Reducting timestep to " << _dt << " given mesh size and inflow velocity.\n";
-        }
         _bc.min = _mesh->minDomainGlobalCellIndex();
         _bc.max = _mesh->maxDomainGlobalCellIndex();
         _pm = std::make_shared<ProblemManager<2>>(_mesh, create_functor, mixed);
