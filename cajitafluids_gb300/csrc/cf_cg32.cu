@@ -658,10 +658,14 @@ __global__ void __launch_bounds__(256) k_x_update32(Cg32T a) {
     const float* p = (it & 1) ? a.pa : a.pb;
     const float alpha = (float)S->alpha_in;
     const int nq = (a.nx + 3) / 4;  // column quads per row
-    const long long total = (long long)nq * a.ny;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int j = (int)(t / nq), i = 4 * (int)(t % nq);
+    // grid-stride walk over (row j, quad q) without a division per element:
+    // the stride splits once into whole rows dj and a remainder dq < nq
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const int dj = (int)(stride / nq), dq = (int)(stride % nq);
+    int j = (int)(t0 / nq), q = (int)(t0 % nq);
+    while (j < a.ny) {
+        const int i = 4 * q;
         const float* pr = p + (ptrdiff_t)j * a.pitch + i;
         float2* xr = a.x + (size_t)j * a.xpitch + i;
         if (i + 3 < a.nx) {
@@ -675,6 +679,12 @@ __global__ void __launch_bounds__(256) k_x_update32(Cg32T a) {
             reinterpret_cast<float4*>(xr)[1] = make_float4(r2.x, r2.y, r3.x, r3.y);
         } else {
             for (int k = 0; i + k < a.nx; ++k) xr[k] = df_add_f(xr[k], alpha * pr[k]);
+        }
+        q += dq;
+        j += dj;
+        if (q >= nq) {
+            q -= nq;
+            ++j;
         }
     }
     if (last_block_arrive(&S->ticket[6])) {
