@@ -20,13 +20,15 @@
 // p ping-pongs between two buffers because K1 recomputes the new direction
 // on its halo from the old one.
 //
-// Mixed precision: Jacobi-PCG on FP32 vectors (e, r, p) with FP64 scalars,
-// 32 bytes per cell per iteration (A p is recomputed in K2 instead of
-// stored), with reliable updates (residual replacement, van der Vorst & Ye
-// 2000): whenever the recursive FP32 residual has fallen by a factor delta
-// since the last update, x += e in FP64, r = b - A x is formed in FP64 and
-// replaces the FP32 residual, and the iteration continues with the same
-// search direction.  Convergence is judged only on the FP64 residual.
+// Mixed precision: PCG on FP32 vectors (r, p twice; z for the multigrid
+// preconditioner) with FP64 scalars; K2 adds alpha p into x kept as a
+// double-float pair (40 bytes per cell per Jacobi-PCG iteration: A p is
+// recomputed in K2 instead of stored).  Reliable updates (residual
+// replacement, van der Vorst & Ye 2000): whenever the recursive FP32 residual
+// has fallen by a factor delta since the last update, r = b - A x is formed
+// in double-float from x and the double-float b and replaces the FP32
+// residual, and the iteration continues with the same search direction.
+// Convergence is judged only on the residual of a reliable update.
 #include <cuda_runtime.h>
 #include <math.h>
 
