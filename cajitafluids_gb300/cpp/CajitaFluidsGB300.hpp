@@ -368,7 +368,6 @@ class SolverBase {
     virtual void solve(const double t_final, const int write_freq) = 0;
 };
 
-// src/Solver.hpp:55-279.
 // src/Solver.hpp:96-106: dt is limited to one cell per step at the inflow
 // speed plus sqrt(|f| dx); the limited step is fixed for the run, because the
 // pressure matrix is built with it.
@@ -381,6 +380,7 @@ inline double limitTimeStep(double delta_t, double cell_size, const InflowSource
     return delta_t;
 }
 
+// src/Solver.hpp:55-279.
 template <std::size_t NumSpaceDim>
 class Solver;
 
