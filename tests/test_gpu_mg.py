@@ -85,6 +85,26 @@ def test_full_steps_config0_mg(built):
     assert np.array_equal(o.get("p"), c.download("p"))
 
 
+def test_full_steps_config1_size(built):
+    """The 1024^2 workload with all walls SOLID, the config-0 inflow, gravity
+    scaled by the quantity (extension Q5), cubic values and tol 1e-10: setup
+    and three steps bit for bit, with the divergence norms of every step."""
+    n = 1024
+    o, c = make_pair(n, n, source=INFLOW, body=(0.0, -9.8), body_density_scaled=True, density=0.1,
+                     precon_mg=True)
+    dt = 0.5 * (1.0 / n) / 3.0
+    so = o.setup(dt, tol=1e-10, max_iter=500)
+    sg = c.setup(dt, opts(tol=1e-10, max_iter=500, precon="PFMG"))
+    assert so["iterations"] == sg["iterations"]
+    for k in range(3):
+        so = o.step(dt, 3, tol=1e-10, max_iter=500)
+        sg = c.step(dt, 3, opts(tol=1e-10, max_iter=500, precon="PFMG"))
+        assert sg["status"] == 0 and so["iterations"] == sg["iterations"], k
+        assert so["div_l2"] == sg["div_l2"] and so["div_linf"] == sg["div_linf"], k
+    assert_fields_equal(o, c, tag="1024^2 steps")
+    assert np.array_equal(o.get("p"), c.download("p"))
+
+
 def test_mg_max_iter_and_zero_rhs(built):
     rng = np.random.default_rng(8)
     o, c = make_pair(64, 64, precon_mg=True)
