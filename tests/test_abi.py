@@ -51,3 +51,15 @@ def test_error_codes_match_header():
         m = re.search(r"#define\s+%s\s+\((-?\d+)\)" % name, text)
         assert m, name
         assert int(m.group(1)) == getattr(L, name)
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    """Without libcfgpu.so the binding raises; nothing falls back to a CPU
+    path (run in a fresh interpreter, since the library is cached once
+    loaded)."""
+    import sys
+    code = ("from cajitafluids_gb300 import _lib\n"
+            f"_lib.load({str(tmp_path / 'libcfgpu.so')!r})\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT, timeout=120)
+    assert r.returncode != 0
+    assert "OSError" in r.stderr and "no CPU fallback" in r.stderr
