@@ -23,6 +23,7 @@ CF_ERR_MESH = -7
 CF_ERR_TOO_LARGE = -8
 CF_ERR_TIMEOUT = -9
 CF_NOALLOC_MAX_UNITS = 65536
+CF_STRIP_FIELDS = 18
 
 ERROR_NAMES = {
     CF_ERR_INVALID: "CF_ERR_INVALID",
@@ -135,6 +136,8 @@ SIGNATURES = {
     "cf_div_norms": (ctypes.c_int, [_vp, _dp, _dp]),
     "cf_max_velocity": (ctypes.c_int, [_vp, _dp]),
     "cf_test_conversions": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_float), _dp]),
+    "cf_test_strip_geometry": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_int, _ip, _ip, ctypes.c_int]),
     "cf_interp_points": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     "cf_trace_points": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_double, _dp]),
     "cf_cell_velocity": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_ssize_t, ctypes.c_ssize_t]),

@@ -812,6 +812,14 @@ int cf_test_conversions(cf_ctx* ctx, int n, const double* d, float* f, double* w
     CF_GUARD_END
 }
 
+int cf_test_strip_geometry(int nx, int ny, int tile_w, int tile_h, int strip_rows, int pre, int* fields,
+                           int* frame_xy, int cap) {
+    if (nx < 1 || ny < 1 || (tile_w != 32 && tile_w != 64) || tile_h < 2 || (tile_h & 1) || strip_rows < 0 ||
+        !fields || cap < 0 || (cap > 0 && !frame_xy) || (strip_rows > 0 && tile_w != 64))
+        return CF_ERR_INVALID;
+    return cf::mg_strip_geometry(nx, ny, tile_w, tile_h, strip_rows, pre, fields, frame_xy, cap);
+}
+
 int cf_max_velocity(cf_ctx* ctx, double* umax) {
     if (!ctx || !umax) return CF_ERR_INVALID;
     cudaSetDevice(ctx->device);

@@ -151,6 +151,7 @@ void mg_free(cf_ctx* c);
 // tells whether it did).
 int mg_vcycle(cf_ctx* c, double scale0, bool* rz_done = nullptr);
 int mg_levels(const cf_ctx* c);
+int mg_strip_geometry(int nx, int ny, int tw, int th, int strip_rows, int pre, int* fields, int* frame_xy, int cap);
 double* mg_z64(cf_ctx* c);
 }  // namespace cf
 

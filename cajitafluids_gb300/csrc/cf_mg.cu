@@ -450,7 +450,7 @@ __device__ __forceinline__ void post_epilogue(const RzEpi& E, SolverState* S, in
     rz_finish(E, S, nparts);
 }
 
-__device__ __forceinline__ void frame_tile(const StripMap& m, int f, int& tx, int& ty) {
+__host__ __device__ __forceinline__ void frame_tile(const StripMap& m, int f, int& tx, int& ty) {
     const int top = m.tya * m.ntx;
     if (f < top) {
         ty = f / m.ntx;
@@ -1343,6 +1343,20 @@ static StripMap strip_map(int nx, int ny, int tw, int th, int strip_rows, bool p
 }
 
 static int launch_blocks(const StripMap& m) { return m.nframe + (m.ns * m.nr + FT_THREADS / 32 - 1) / (FT_THREADS / 32); }
+
+// The launch geometry above, on the host, for tests: the StripMap fields, the
+// strip shape constants and the tile of every frame block (host arithmetic
+// only; nothing is launched).
+int mg_strip_geometry(int nx, int ny, int tw, int th, int strip_rows, int pre, int* fields, int* frame_xy, int cap) {
+    const StripMap m = strip_map(nx, ny, tw, th, strip_rows, pre != 0);
+    const int v[CF_STRIP_FIELDS] = {m.nframe, m.ntx, m.txa, m.txb, m.tya, m.tyb, m.ns, m.nr, m.rh, m.x0, m.y0,
+                                    pre ? SP_PRE_OUT : SP_POST_OUT, pre ? 6 : 4, pre ? 5 : 4, SP_COLS, SP_U,
+                                    FT_THREADS / 32, launch_blocks(m)};
+    for (int k = 0; k < CF_STRIP_FIELDS; ++k) fields[k] = v[k];
+    if (frame_xy)
+        for (int f = 0; f < m.nframe && f < cap; ++f) frame_tile(m, f, frame_xy[2 * f], frame_xy[2 * f + 1]);
+    return CF_OK;
+}
 
 template <typename T>
 static int vcycle(cf_ctx* c, MgLev<T>* lev, int nlev, double scale0, int inner, int fused, int strip_rows,

@@ -236,6 +236,20 @@ int cf_trace_points(cf_ctx* ctx, int n, const double* xy, double dt, double* out
  * w = f widened (no counterpart in the reference) */
 int cf_test_conversions(cf_ctx* ctx, int n, const double* d, float* f, double* w);
 
+/* launch geometry of the fused multigrid pre-smoothing (pre != 0) or
+ * post-smoothing kernel on an nx x ny level with tile_w x tile_h tiles
+ * (tile_w 32 or 64) and register strips of about strip_rows rows (0: tiles
+ * only), computed on the host without a device (no counterpart in the
+ * reference).  fields[CF_STRIP_FIELDS]: frame blocks, tiles per row, the
+ * strip-covered tile rectangle [txa, txb) x [tya, tyb), strips per row and
+ * rows of strips, strip height, first written column and row, columns written
+ * per strip, column halo, row halo, columns read per strip, row unroll, strips
+ * per block, blocks launched.  frame_xy (optional, 2 * cap ints) receives the
+ * tile (x, y) of each frame block. */
+#define CF_STRIP_FIELDS 18
+int cf_test_strip_geometry(int nx, int ny, int tile_w, int tile_h, int strip_rows, int pre, int* fields,
+                           int* frame_xy, int cap);
+
 /* ---- output (replaces the device half of SiloWriter::writeFile) ----
  * SiloWriter interpolates the face velocities to cell centres for its
  * "velocity" zonal variable (src/SiloWriter.hpp:177-205:
