@@ -691,6 +691,13 @@ int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* 
         if (!rc && mixed) rc = alloc_dev(ctx, ctx->staging2, (size_t)nx * ny);
         if (rc) return rc;
     }
+    // on an error after copies were queued, wait for both streams before
+    // returning, so that no copy touches the caller's buffers after the call
+    auto drain = [ctx](int code) {
+        cudaStreamSynchronize(ctx->stream2);
+        cudaStreamSynchronize(ctx->stream);
+        return code;
+    };
     // Uploads into the current buffers: u and v first on the main stream; the
     // quantity once they are in (they share the link), on the second stream,
     // while the velocities' own advection runs on the main one.
@@ -727,7 +734,7 @@ int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* 
     if (!rc) rc = cuda_check(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_q, 0), "event wait");
     if (!rc) rc = cuda_check(ctx, launch_advect(ctx, dt, value_order, fuse ? 1 : 0, 0, 1, false, true), "advect");
     if (!rc && !fuse) rc = cuda_check(ctx, launch_add_inputs(ctx, dt), "add inputs");
-    if (rc) return rc;
+    if (rc) return drain(rc);
     const int s1 = ctx->cur;
     // the quantity is final now: copy it out beside the projection
     if (q_out) {
@@ -745,7 +752,7 @@ int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* 
                                                    cudaMemcpyDefault, ctx->stream2),
                             "download");
         }
-        if (rc) return rc;
+        if (rc) return drain(rc);
     }
     SolveResult r{};
     bool deferred = false;
