@@ -4,8 +4,8 @@
 
 The reference (Kokkos + Cabana/Cajita + HYPRE + MPI) cannot be built or
 imported here, so the fixtures are oracle outputs: they pin the oracle
-against regressions (tests/test_oracle_golden.py, bit for bit) and give the
-GPU path fixed expected values (tests/test_gpu_golden.py, bit for bit).
+against regressions and give the GPU path fixed expected values
+(tests/test_golden.py, bit for bit).
 Every input is generated from a seed below.
 """
 import os
@@ -56,6 +56,24 @@ def periodic_small(n=32, steps=6, seed=5):
                 v=o.get("v"), p=o.get("p"), iterations=np.array(its))
 
 
+def walls_buoyancy_mg(n=48, steps=6):
+    """Walls, the config-0 inflow, gravity scaled by the quantity (extension
+    Q5), cubic values, PCG + the multigrid preconditioner (the PFMG name),
+    from a zero state."""
+    dt = 0.5 * (1.0 / n) / 3.0
+    o = Oracle(n, n, source=INFLOW, body=(0.0, -9.8), body_density_scaled=True, density=0.1, precon_mg=True)
+    its, div = [], []
+    s = o.setup(dt, tol=1e-10, max_iter=500)
+    its.append(s["iterations"])
+    div.append(s["div_l2"])
+    for _ in range(steps):
+        s = o.step(dt, 3, tol=1e-10, max_iter=500)
+        its.append(s["iterations"])
+        div.append(s["div_l2"])
+    return dict(n=n, dt=dt, steps=steps, order=3, tol=1e-10, q=o.get("q"), u=o.get("u"), v=o.get("v"),
+                p=o.get("p"), iterations=np.array(its), div_l2=np.array(div))
+
+
 def interpolation_kat(n=24, seed=9):
     """Spline samples of seeded fields at seeded points, both orders."""
     rng = np.random.default_rng(seed)
@@ -80,6 +98,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "config0_32.npz"), **config0_small())
     np.savez_compressed(os.path.join(HERE, "periodic_spectral_32.npz"), **periodic_small())
     np.savez_compressed(os.path.join(HERE, "interp_kat_24.npz"), **interpolation_kat())
+    np.savez_compressed(os.path.join(HERE, "walls_buoyancy_mg_48.npz"), **walls_buoyancy_mg())
     print("wrote", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))
 
 

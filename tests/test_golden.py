@@ -59,6 +59,21 @@ def test_oracle_reproduces_periodic_fixture(built):
         assert np.array_equal(o.get(f), g[f]), f
 
 
+def test_oracle_reproduces_walls_buoyancy_mg_fixture(built):
+    """Walls, inflow, gravity scaled by the quantity, cubic values, PCG with
+    the multigrid preconditioner: iterations, divergence norms and fields."""
+    g = _load("walls_buoyancy_mg_48.npz")
+    n = int(g["n"])
+    dt, tol = float(g["dt"]), float(g["tol"])
+    o = Oracle(n, n, source=INFLOW, body=(0.0, -9.8), body_density_scaled=True, density=0.1, precon_mg=True)
+    st = [o.setup(dt, tol=tol, max_iter=500)]
+    st += [o.step(dt, int(g["order"]), tol=tol, max_iter=500) for _ in range(int(g["steps"]))]
+    assert np.array_equal([s["iterations"] for s in st], g["iterations"])
+    assert np.array_equal([s["div_l2"] for s in st], g["div_l2"])
+    for f in ("q", "u", "v", "p"):
+        assert np.array_equal(o.get(f), g[f]), f
+
+
 def test_oracle_reproduces_interpolation_fixture(built):
     g = _load("interp_kat_24.npz")
     n = int(g["n"])
