@@ -44,7 +44,8 @@ KERNEL_BYTES_MIXED_ITER = 40.0
 FP64_ITERS_PER_STEP_4096 = 7890
 MG_NAMES = ("PFMG", "SMG", "MG")
 # DRAM bytes (read + write) of one mixed MG-PCG inner iteration at 4096^2,
-# from an ncu capture of this bench (profiles/traffic_4096_mixed_mg.md)
+# from an ncu capture of this bench's kernels (dram__bytes_read.sum +
+# dram__bytes_write.sum summed over the kernels of one iteration)
 MEASURED_TRAFFIC_MG_ITER_4096 = 1.17e9
 
 
@@ -359,8 +360,8 @@ def bench_gb300(args, rank, world, dist, device):
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": f"hbm_gbs {peak_kind}",
                          "traffic": MEASURED_TRAFFIC_MG_ITER_4096 if (mg and w.nx == 4096) else None,
-                         "traffic_source": "ncu dram__bytes_read+write per iteration, "
-                                           "profiles/traffic_4096_mixed_mg.md" if (mg and w.nx == 4096) else None,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, summed over the "
+                                           "kernels of one inner iteration" if (mg and w.nx == 4096) else None,
                          "algorithmic_bytes": it_bytes,
                          "algorithmic_bytes_per_cell": it_bytes / ncell, **kern_extra},
             "gpu_launches": launches, "clocks": clk,

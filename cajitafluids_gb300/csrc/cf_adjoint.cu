@@ -168,21 +168,20 @@ __global__ void k_adj_records(AdjRec a) {
     samp<1>(a.u, ulx, uly, p.rdx, x0, y0, s0u);
     samp<1>(a.v, vlx, vly, p.rdx, x0, y0, s0v);
     const double h1 = 0.5 * dt, h2 = 0.75 * dt;
-    double x1 = fma(-h1, s0u.val, x0), y1 = fma(-h1, s0v.val, y0);
+    // the forward's operation order (one rounding per operation)
+    double x1 = __dsub_rn(x0, __dmul_rn(h1, s0u.val)), y1 = __dsub_rn(y0, __dmul_rn(h1, s0v.val));
     samp<1>(a.u, ulx, uly, p.rdx, x1, y1, s1u);
     samp<1>(a.v, vlx, vly, p.rdx, x1, y1, s1v);
     const bool ralston = (p.quirks & 2u) != 0;
     double sx = ralston ? s1u.val : s0u.val, sy = ralston ? s1v.val : s0v.val;
-    double x2 = fma(-h2, sx, x0), y2 = fma(-h2, sy, y0);
+    double x2 = __dsub_rn(x0, __dmul_rn(h2, sx)), y2 = __dsub_rn(y0, __dmul_rn(h2, sy));
     samp<1>(a.u, ulx, uly, p.rdx, x2, y2, s2u);
     samp<1>(a.v, vlx, vly, p.rdx, x2, y2, s2v);
-    double ax = (2.0 / 9.0) * s0u.val;
-    ax = fma(3.0 / 9.0, s1u.val, ax);
-    ax = fma(4.0 / 9.0, s2u.val, ax);
-    double ay = (2.0 / 9.0) * s0v.val;
-    ay = fma(3.0 / 9.0, s1v.val, ay);
-    ay = fma(4.0 / 9.0, s2v.val, ay);
-    double tx = fma(-dt, ax, x0), ty = fma(-dt, ay, y0);
+    double ax = __dadd_rn(__dmul_rn(2.0 / 9.0, s0u.val), __dmul_rn(3.0 / 9.0, s1u.val));
+    ax = __dadd_rn(ax, __dmul_rn(4.0 / 9.0, s2u.val));
+    double ay = __dadd_rn(__dmul_rn(2.0 / 9.0, s0v.val), __dmul_rn(3.0 / 9.0, s1v.val));
+    ay = __dadd_rn(ay, __dmul_rn(4.0 / 9.0, s2v.val));
+    double tx = __dsub_rn(x0, __dmul_rn(dt, ax)), ty = __dsub_rn(y0, __dmul_rn(dt, ay));
     if (a.order == 1)
         samp<1>(f, p.low[ent][0], p.low[ent][1], p.rdx, tx, ty, sf);
     else

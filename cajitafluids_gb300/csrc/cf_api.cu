@@ -82,8 +82,14 @@ int alloc_grid(cf_ctx* c, Grid<T>& g, int ex, int ey) {
     return CF_OK;
 }
 
+// Host-side failure injection for tests: when positive, the n-th device
+// allocation from now on fails as if cudaMalloc had run out of memory.
+static int g_fail_alloc_in = 0;
+
 template <typename T>
 int alloc_dev(cf_ctx* c, T*& ptr, size_t n) {
+    if (g_fail_alloc_in > 0 && --g_fail_alloc_in == 0)
+        return fail(c, CF_ERR_NOMEM, "cudaMalloc of %zu bytes failed: injected failure", n * sizeof(T));
     void* base = nullptr;
     cudaError_t e = cudaMalloc(&base, n * sizeof(T) + 256);
     if (e != cudaSuccess) return fail(c, CF_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(e));
@@ -213,7 +219,7 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
     if (d->nx <= 0 || d->ny <= 0 || d->nx > (1 << 16) || d->ny > (1 << 16)) return CF_ERR_INVALID;
     if (d->precision != CF_PREC_FP64 && d->precision != CF_PREC_MIXED) return CF_ERR_INVALID;
     if (!(d->hi[0] > d->lo[0]) || !(d->hi[1] > d->lo[1])) return CF_ERR_INVALID;
-    // src/Mesh.hpp:472-486: uniform cell size from x, every extent divisible by it
+    // src/Mesh.hpp:49-64: uniform cell size from x, every extent divisible by it
     double dx = (d->hi[0] - d->lo[0]) / d->nx;
     for (int k = 0; k < 2; ++k) {
         int n = k == 0 ? d->nx : d->ny;
@@ -666,6 +672,39 @@ int cf_steps(cf_ctx* ctx, int nsteps, double dt, int value_order, const cf_solve
     CF_GUARD_END
 }
 
+// The second stream, the events and (mixed) the quantity's download staging
+// of cf_step_host.  Each member is created into a local and stored only once
+// it exists, so a failure leaves the members made so far valid and the rest
+// null; the next call creates only what is missing.
+static int step_host_resources(cf_ctx* ctx, bool mixed) {
+    if (!ctx->stream2) {
+        cudaStream_t s = nullptr;
+        int rc = cuda_check(ctx, cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream create");
+        if (rc) return rc;
+        ctx->stream2 = s;
+    }
+    cudaEvent_t* evs[3] = {&ctx->ev_adv, &ctx->ev_uv, &ctx->ev_q};
+    for (cudaEvent_t* ev : evs) {
+        if (*ev) continue;
+        cudaEvent_t e = nullptr;
+        int rc = cuda_check(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event create");
+        if (rc) return rc;
+        *ev = e;
+    }
+    if (mixed && !ctx->staging2) {
+        double* p = nullptr;
+        int rc = alloc_dev(ctx, p, (size_t)ctx->ph.nx * ctx->ph.ny);
+        if (rc) return rc;
+        ctx->staging2 = p;
+    }
+    return CF_OK;
+}
+
+int cf_test_fail_alloc(int nth) {
+    g_fail_alloc_in = nth > 0 ? nth : 0;
+    return CF_OK;
+}
+
 // Solver::step with host buffers in and out (owned arrays, x fastest,
 // contiguous).  Every copy is asynchronous on the context streams; the
 // quantity, final after the advection, is copied out on a second stream while
@@ -683,14 +722,11 @@ int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* 
     if (rc) return rc;
     const bool mixed = ctx->precision == CF_PREC_MIXED;
     const int nx = ctx->ph.nx, ny = ctx->ph.ny;
-    if (!ctx->stream2) {
-        rc = cuda_check(ctx, cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking), "stream create");
-        if (!rc) rc = cuda_check(ctx, cudaEventCreateWithFlags(&ctx->ev_adv, cudaEventDisableTiming), "event create");
-        if (!rc) rc = cuda_check(ctx, cudaEventCreateWithFlags(&ctx->ev_uv, cudaEventDisableTiming), "event create");
-        if (!rc) rc = cuda_check(ctx, cudaEventCreateWithFlags(&ctx->ev_q, cudaEventDisableTiming), "event create");
-        if (!rc && mixed) rc = alloc_dev(ctx, ctx->staging2, (size_t)nx * ny);
-        if (rc) return rc;
-    }
+    // lazy set-up: each member is created on its own when it is missing, so a
+    // call that failed part way (out of memory, say) leaves the others valid
+    // and the next call creates what is still missing
+    rc = step_host_resources(ctx, mixed);
+    if (rc) return rc;
     // on an error after copies were queued, wait for both streams before
     // returning, so that no copy touches the caller's buffers after the call
     auto drain = [ctx](int code) {

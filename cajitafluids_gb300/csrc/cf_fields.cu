@@ -124,24 +124,25 @@ __device__ void rk3_64(const Phys& p, const Grid<double>& u, const Grid<double>&
     const double vlx = p.low[E_FACEJ][0], vly = p.low[E_FACEJ][1];
     double v0x = sample64<1>(u, ulx, uly, p.rdx, x0, y0);
     double v0y = sample64<1>(v, vlx, vly, p.rdx, x0, y0);
+    // the reference's stage expressions as written, one rounding per
+    // operation: x0 - 0.5 * dt * v0 is x0 - ((0.5 * dt) * v0)
     double h1 = 0.5 * dt;
-    double x1 = fma(-h1, v0x, x0), y1 = fma(-h1, v0y, y0);
+    double x1 = __dsub_rn(x0, __dmul_rn(h1, v0x)), y1 = __dsub_rn(y0, __dmul_rn(h1, v0y));
     double v1x = sample64<1>(u, ulx, uly, p.rdx, x1, y1);
     double v1y = sample64<1>(v, vlx, vly, p.rdx, x1, y1);
     double h2 = 0.75 * dt;
     bool ralston = (p.quirks & 2u) != 0;
     double sx = ralston ? v1x : v0x, sy = ralston ? v1y : v0y;
-    double x2 = fma(-h2, sx, x0), y2 = fma(-h2, sy, y0);
+    double x2 = __dsub_rn(x0, __dmul_rn(h2, sx)), y2 = __dsub_rn(y0, __dmul_rn(h2, sy));
     double v2x = sample64<1>(u, ulx, uly, p.rdx, x2, y2);
     double v2y = sample64<1>(v, vlx, vly, p.rdx, x2, y2);
-    double ax = (2.0 / 9.0) * v0x;
-    ax = fma(3.0 / 9.0, v1x, ax);
-    ax = fma(4.0 / 9.0, v2x, ax);
-    double ay = (2.0 / 9.0) * v0y;
-    ay = fma(3.0 / 9.0, v1y, ay);
-    ay = fma(4.0 / 9.0, v2y, ay);
-    tx = fma(-dt, ax, x0);
-    ty = fma(-dt, ay, y0);
+    // x0 - dt * ((2/9) v0 + (3/9) v1 + (4/9) v2), summed left to right
+    double ax = __dadd_rn(__dmul_rn(2.0 / 9.0, v0x), __dmul_rn(3.0 / 9.0, v1x));
+    ax = __dadd_rn(ax, __dmul_rn(4.0 / 9.0, v2x));
+    double ay = __dadd_rn(__dmul_rn(2.0 / 9.0, v0y), __dmul_rn(3.0 / 9.0, v1y));
+    ay = __dadd_rn(ay, __dmul_rn(4.0 / 9.0, v2y));
+    tx = __dsub_rn(x0, __dmul_rn(dt, ax));
+    ty = __dsub_rn(y0, __dmul_rn(dt, ay));
 }
 
 // --------------------------------------------------------------------------
@@ -161,7 +162,7 @@ __device__ __forceinline__ double inputs_cell_in(const Phys& p, double q, bool i
         if (p.src_mode == 0) {
             if (q < p.src_q) q = p.src_q;
         } else {
-            q = fma(p.src_q, dt, q);
+            q = __dadd_rn(q, __dmul_rn(p.src_q, dt));  // rate form (extension)
         }
     }
     return q;
@@ -172,7 +173,7 @@ __device__ __forceinline__ double inputs_cell(const Phys& p, double q, double x,
         if (p.src_mode == 0) {
             if (q < p.src_q) q = p.src_q;
         } else {
-            q = fma(p.src_q, dt, q);
+            q = __dadd_rn(q, __dmul_rn(p.src_q, dt));  // rate form (extension)
         }
     }
     return q;
@@ -182,10 +183,12 @@ __device__ __forceinline__ double inputs_cell(const Phys& p, double q, double x,
 __device__ __forceinline__ double inputs_face_in(const Phys& p, int axis, double w, bool inbox, double dt, int gidx,
                                                  double rho) {
     if (inbox && fabs(w) < fabs(p.src_vel[axis])) w = p.src_vel[axis];
+    // ux += _force[0] * delta_t (src/BodyForce.hpp:52, 61); the density-scaled
+    // form (extension) scales the force first
     if (p.force_density)
-        w = fma(p.force[axis] * rho, dt, w);
+        w = __dadd_rn(w, __dmul_rn(__dmul_rn(p.force[axis], rho), dt));
     else
-        w = fma(p.force[axis], dt, w);
+        w = __dadd_rn(w, __dmul_rn(p.force[axis], dt));
     int per = axis == 0 ? p.per_x : p.per_y;
     int n = axis == 0 ? p.nx : p.ny;
     if (!per) {
@@ -198,10 +201,12 @@ __device__ __forceinline__ double inputs_face_in(const Phys& p, int axis, double
 __device__ __forceinline__ double inputs_face(const Phys& p, int axis, double w, double x, double y,
                                               double dt, int gidx, double rho) {
     if (in_box(p, x, y) && fabs(w) < fabs(p.src_vel[axis])) w = p.src_vel[axis];
+    // ux += _force[0] * delta_t (src/BodyForce.hpp:52, 61); the density-scaled
+    // form (extension) scales the force first
     if (p.force_density)
-        w = fma(p.force[axis] * rho, dt, w);
+        w = __dadd_rn(w, __dmul_rn(__dmul_rn(p.force[axis], rho), dt));
     else
-        w = fma(p.force[axis], dt, w);
+        w = __dadd_rn(w, __dmul_rn(p.force[axis], dt));
     int per = axis == 0 ? p.per_x : p.per_y;
     int n = axis == 0 ? p.nx : p.ny;
     if (!per) {
@@ -397,7 +402,7 @@ __global__ void __launch_bounds__(256) k_advect32(Adv32 a) {
                 const float qf = (float)p.src_q;
                 if (val < qf) val = qf;
             } else {
-                val = (float)fma(p.src_q, a.dt, (double)val);
+                val = (float)__dadd_rn((double)val, __dmul_rn(p.src_q, a.dt));
             }
         }
         a.qn.at(li, lj) = val;
@@ -407,7 +412,7 @@ __global__ void __launch_bounds__(256) k_advect32(Adv32 a) {
     double w = (double)val;
     if (a.fuse) {
         if (in_box_idx(p, ent, li, lj) && fabs(w) < fabs(p.src_vel[axis])) w = p.src_vel[axis];
-        if (p.force[axis] != 0.0) w = fma(p.force[axis], a.dt, w);
+        if (p.force[axis] != 0.0) w = __dadd_rn(w, __dmul_rn(p.force[axis], a.dt));
         const int per = axis == 0 ? p.per_x : p.per_y, n = axis == 0 ? p.nx : p.ny, g = axis == 0 ? gi : gj;
         if (!per) {
             if (g <= 0 && p.bc[axis] == 0) w = 0.0;

@@ -8,9 +8,10 @@
 // would synchronise the device.  The regular entry point needs a cf_ctx,
 // and creating one allocates every field and solver vector.
 //
-// The variant computes exactly what cf_div_norms computes (same per-cell
-// divergence, same fixed reduction order, so the results are bit for bit
-// equal) but keeps its reduction scratch -- one partial sum and one partial
+// The variant computes what cf_div_norms computes for an FP64 context (same
+// per-cell divergence, same fixed reduction order, so the results are bit
+// for bit equal; a mixed context squares in FP32 and can differ in the last
+// bits of the L2 norm) but keeps its reduction scratch -- one partial sum and one partial
 // max per 64 x 16-cell unit, plus the last-block ticket -- in the
 // file-scope device array below, which every GPU that loads this library
 // holds until the process exits (1 MiB).
@@ -34,7 +35,9 @@ double* g_scratch_addr[kMaxDevices] = {};
 
 // Once per device, with that device current: the device address of the
 // scratch array (the host-side symbol is only a stand-in, never a pointer a
-// kernel may use).
+// kernel may use).  The cached address is that of the primary context's
+// module; it goes stale after cudaDeviceReset, which callers must not mix
+// with this entry point.
 int scratch_for_current_device(double** out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return CF_ERR_CUDA;

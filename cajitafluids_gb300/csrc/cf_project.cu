@@ -834,8 +834,10 @@ __global__ void k_apply_pressure(Press a) {
     const bool fix_q1 = (p.quirks & 1u) != 0;
     if (axis == 0) {
         double& u = a.u.at(gi + CF_HALO, gj + CF_HALO);
+        // u -= scale * (p(i) - p(i-1)) (src/VelocityCorrector.hpp:245), one
+        // rounding per operation; ms = -scale, so u + ms*d gives those bits
         double d = pval(a, gi, gj) - pval(a, gi - 1, gj);
-        double w = fma(a.ms, d, u);
+        double w = __dadd_rn(u, __dmul_rn(a.ms, d));
         if (!a.adjoint) {
             if (!p.per_x) {
                 if (gi <= 0 && p.bc[0] == 0) w = 0.0;
@@ -848,7 +850,7 @@ __global__ void k_apply_pressure(Press a) {
     } else {
         double& v = a.v.at(gi + CF_HALO, gj + CF_HALO);
         double d = pval(a, gi, gj) - pval(a, gi, gj - 1);
-        double w = fma(a.ms, d, v);
+        double w = __dadd_rn(v, __dmul_rn(a.ms, d));  // :256
         if (!p.per_y && !a.adjoint) {
             if (fix_q1) {
                 if (gj <= 0 && p.bc[1] == 0) w = 0.0;

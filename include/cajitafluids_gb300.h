@@ -49,7 +49,7 @@ extern "C" {
 #define CF_ERR_NOT_CONVERGED (-4) /* solver stopped at max_iter; state is consistent */
 #define CF_ERR_NUMERIC (-5)       /* NaN/Inf or CG breakdown; state is consistent */
 #define CF_ERR_NOMEM (-6)         /* device allocation failed */
-#define CF_ERR_MESH (-7)          /* extent not evenly divisible (src/Mesh.hpp:478-486) */
+#define CF_ERR_MESH (-7)          /* extent not evenly divisible (src/Mesh.hpp:49-64) */
 #define CF_ERR_TIMEOUT (-9)       /* a bounded device-side wait ran out; state is consistent */
 
 /* fields */
@@ -250,6 +250,11 @@ int cf_test_conversions(cf_ctx* ctx, int n, const double* d, float* f, double* w
 int cf_test_strip_geometry(int nx, int ny, int tile_w, int tile_h, int strip_rows, int pre, int* fields,
                            int* frame_xy, int cap);
 
+/* Test hook (host-side failure injection, no GPU fault): with nth > 0 the
+ * nth device allocation of the library from now on fails as an out-of-memory
+ * cudaMalloc would (CF_ERR_NOMEM); 0 switches the injection off. */
+int cf_test_fail_alloc(int nth);
+
 /* ---- output (replaces the device half of SiloWriter::writeFile) ----
  * SiloWriter interpolates the face velocities to cell centres for its
  * "velocity" zonal variable (src/SiloWriter.hpp:177-205:
@@ -311,13 +316,20 @@ int cf_host_free(void* ptr);
  * u: device pointer to u(0, 0) of the owned I-faces, u(gi, gj) at
  *    u[gj * u_pitch + gi], (nx + 1 - periodic_x) x ny values; v likewise
  *    for the J-faces, nx x (ny + 1 - periodic_y).  out: device pointer to two
- *    doubles, written with the same values cf_div_norms returns (L2 norm with
- *    unit-area cells, max |div u|).  stream: a cudaStream_t (NULL = default
+ *    doubles: the L2 norm of div u with unit-area cells and max |div u|,
+ *    equal bit for bit to what cf_div_norms returns for an FP64 context
+ *    holding the same u and v (a mixed-precision context squares the
+ *    divergence in FP32 before its FP64 sum, so its L2 norm can differ in
+ *    the last bits).  stream: a cudaStream_t (NULL = default
  *    stream).  The call only enqueues work; read out after the stream.
  * Limits: at most CF_NOALLOC_MAX_UNITS units of 64 x 16 cells (8192 x 8192
  * cells); larger grids return CF_ERR_TOO_LARGE without touching the GPU.
  * The first call on each device looks up the scratch address on that
- * device (make that first call before any stream capture).  All calls share
+ * device (make that first call before any stream capture) and keeps it for
+ * the rest of the process: that address belongs to the CUDA runtime's
+ * primary context of the device, so calls must run with that context
+ * current, and not after cudaDeviceReset on that device (the library's
+ * device module, and with it the scratch array, may then sit elsewhere).  All calls share
  * the one scratch array: calls that overlap on the GPU (different streams,
  * or threads without ordering) race and give wrong results. */
 #define CF_ERR_TOO_LARGE (-8)

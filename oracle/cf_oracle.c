@@ -8,8 +8,15 @@
  *
  * Evaluation-order contract (shared with the CUDA FP64 kernels, written
  * independently there):
- *   - every fused multiply-add is an explicit fma(); nothing else is
- *     contracted (build with -ffp-contract=off);
+ *   - arithmetic the reference writes out in its own files (the rk3 stages,
+ *     the body force, the divergence, the gradient subtraction, the matrix
+ *     entries) is evaluated as written: C++ precedence, left to right, one
+ *     rounding per operation, no contraction (build with -ffp-contract=off);
+ *     the reference's own code compiled the same way gives the same bits
+ *     (oracle/refshim and tests/test_reference_pin.py);
+ *   - in the parts the reference delegates to Cajita (spline weights and
+ *     sums, the conjugate-gradient recurrences), every fused multiply-add is
+ *     an explicit fma();
  *   - dot products are summed in a fixed blocked order: the owned cell grid
  *     is cut into units of 64 columns x 16 rows; unit u = band * G + g;
  *     inside a unit, "lane" l (0..31) owns columns 64g+2l and 64g+2l+1 and
@@ -82,7 +89,8 @@ int orc_threads(void) {
 #endif
 }
 
-/* Mesh construction: src/Mesh.hpp:469-500. */
+/* Mesh construction: the uniform cell size and its extent check,
+ * src/Mesh.hpp:49-64. */
 orc_state* orc_create(const orc_params* prm, char* err, int errlen) {
     if (prm->nx <= 0 || prm->ny <= 0) {
         snprintf(err, errlen, "cell counts must be positive");
@@ -292,22 +300,24 @@ static void rk3_trace(const orc_state* st, double dt, const double x0[2], double
     double v0[2], v1[2], v2[2], x1[2], x2[2];
     v0[0] = sample_grid(st, u, E_FACEI, 1, x0[0], x0[1]);
     v0[1] = sample_grid(st, v, E_FACEJ, 1, x0[0], x0[1]);
+    /* the reference's expressions as written, one rounding per operation:
+     * x0 - 0.5 * dt * v0 parses as x0 - ((0.5 * dt) * v0) (:48-49) */
     double h1 = 0.5 * dt;
-    x1[0] = fma(-h1, v0[0], x0[0]);
-    x1[1] = fma(-h1, v0[1], x0[1]);
+    x1[0] = x0[0] - h1 * v0[0];
+    x1[1] = x0[1] - h1 * v0[1];
     v1[0] = sample_grid(st, u, E_FACEI, 1, x1[0], x1[1]);
     v1[1] = sample_grid(st, v, E_FACEJ, 1, x1[0], x1[1]);
     double h2 = 0.75 * dt;
     const double* vs = (st->p.quirks & 2u) ? v1 : v0;
-    x2[0] = fma(-h2, vs[0], x0[0]);
-    x2[1] = fma(-h2, vs[1], x0[1]);
+    x2[0] = x0[0] - h2 * vs[0];
+    x2[1] = x0[1] - h2 * vs[1];
     v2[0] = sample_grid(st, u, E_FACEI, 1, x2[0], x2[1]);
     v2[1] = sample_grid(st, v, E_FACEJ, 1, x2[0], x2[1]);
+    /* x0 - dt * ((2/9) v0 + (3/9) v1 + (4/9) v2), summed left to right (:62-65) */
     for (int d = 0; d < 2; ++d) {
-        double a = (2.0 / 9.0) * v0[d];
-        a = fma(3.0 / 9.0, v1[d], a);
-        a = fma(4.0 / 9.0, v2[d], a);
-        tr[d] = fma(-dt, a, x0[d]);
+        double a = (2.0 / 9.0) * v0[d] + (3.0 / 9.0) * v1[d];
+        a = a + (4.0 / 9.0) * v2[d];
+        tr[d] = x0[d] - dt * a;
     }
 }
 
@@ -376,7 +386,7 @@ void orc_add_inputs(orc_state* st, double dt) {
                 if (p->src_mode == 0) {
                     if (*qq < p->src_quantity) *qq = p->src_quantity;
                 } else {
-                    *qq = fma(p->src_quantity, dt, *qq);
+                    *qq = *qq + p->src_quantity * dt; /* rate form (extension) */
                 }
             }
         }
@@ -387,11 +397,13 @@ void orc_add_inputs(orc_state* st, double dt) {
             double y = entity_coord(st, E_FACEI, 1, gj + HALO);
             double* uu = at(u, gi + HALO, gj + HALO);
             if (in_box(p, x, y) && fabs(*uu) < fabs(p->src_velocity[0])) *uu = p->src_velocity[0];
+            /* ux += _force[0] * delta_t (src/BodyForce.hpp:52); the
+             * density-scaled form (extension) scales the force first */
             if (p->body_density_scaled) {
                 double rho = (cell_value(st, gi - 1, gj) + cell_value(st, gi, gj)) * 0.5;
-                *uu = fma(p->body_force[0] * rho, dt, *uu);
+                *uu = *uu + (p->body_force[0] * rho) * dt;
             } else {
-                *uu = fma(p->body_force[0], dt, *uu);
+                *uu = *uu + p->body_force[0] * dt;
             }
             if (!p->periodic[0]) {
                 if (gi <= 0 && p->bc_type[0] == SOLID) *uu = 0.0;
@@ -407,9 +419,9 @@ void orc_add_inputs(orc_state* st, double dt) {
             if (in_box(p, x, y) && fabs(*vv) < fabs(p->src_velocity[1])) *vv = p->src_velocity[1];
             if (p->body_density_scaled) {
                 double rho = (cell_value(st, gi, gj - 1) + cell_value(st, gi, gj)) * 0.5;
-                *vv = fma(p->body_force[1] * rho, dt, *vv);
+                *vv = *vv + (p->body_force[1] * rho) * dt;
             } else {
-                *vv = fma(p->body_force[1], dt, *vv);
+                *vv = *vv + p->body_force[1] * dt; /* src/BodyForce.hpp:61 */
             }
             if (!p->periodic[1]) {
                 if (gj <= 0 && p->bc_type[1] == SOLID) *vv = 0.0;
@@ -581,7 +593,6 @@ static void apply_pressure(orc_state* st, double dt) {
     const orc_params* p = &st->p;
     int nx = p->nx, ny = p->ny;
     double scale = dt / (p->density * st->dx);
-    double ms = -scale;
     grid_t* u = &st->f[ORC_U][0];
     grid_t* v = &st->f[ORC_V][0];
     int oxu = owned_count(st, ORC_U, 0);
@@ -589,7 +600,7 @@ static void apply_pressure(orc_state* st, double dt) {
         for (int gi = 0; gi < oxu; ++gi) {
             double d = vec_at(st, st->x, gi, gj) - vec_at(st, st->x, gi - 1, gj);
             double* uu = at(u, gi + HALO, gj + HALO);
-            *uu = fma(ms, d, *uu);
+            *uu = *uu - scale * d; /* u -= scale * (p(i) - p(i-1)), :245 */
             if (!p->periodic[0]) {
                 if (gi <= 0 && p->bc_type[0] == SOLID) *uu = 0.0;
                 if (gi > nx - 1 && p->bc_type[2] == SOLID) *uu = 0.0;
@@ -601,7 +612,7 @@ static void apply_pressure(orc_state* st, double dt) {
         for (int gi = 0; gi < nx; ++gi) {
             double d = vec_at(st, st->x, gi, gj) - vec_at(st, st->x, gi, gj - 1);
             double* vv = at(v, gi + HALO, gj + HALO);
-            *vv = fma(ms, d, *vv);
+            *vv = *vv - scale * d; /* :256 */
             if (p->periodic[1]) continue;
             /* the J-face condition, applied to u (reference) or v (fixed) */
             double* tgt = fix_q1 ? vv : at(u, gi + HALO, gj + HALO);

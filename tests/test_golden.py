@@ -130,3 +130,25 @@ def test_gpu_reproduces_interpolation_fixture(built):
         for order in (1, 3):
             assert np.array_equal(c.interp_points(f, order, g["xy"]), g[f"{f}_o{order}"])
     assert np.array_equal(c.trace_points(g["xy"], 0.01), g["trace"])
+
+
+@pytest.mark.gpu
+def test_gpu_reproduces_walls_buoyancy_mg_fixture(built):
+    """Walls, inflow, gravity scaled by the quantity, cubic values and the
+    multigrid-preconditioned CG on the GPU: iterations, divergence norms and
+    fields bit for bit."""
+    from cajitafluids_gb300 import Context, SolverOptions
+    g = _load("walls_buoyancy_mg_48.npz")
+    n = int(g["n"])
+    dt, tol = float(g["dt"]), float(g["tol"])
+    c = Context(n, n)
+    c.set_source(*INFLOW)
+    c.set_body_force((0.0, -9.8), True)
+    c.set_density(0.1)
+    o = SolverOptions(tol=tol, max_iter=500, precon="PFMG")
+    st = [c.setup(dt, o)]
+    st += [c.step(dt, int(g["order"]), o) for _ in range(int(g["steps"]))]
+    assert np.array_equal([s["iterations"] for s in st], g["iterations"])
+    assert np.array_equal([s["div_l2"] for s in st], g["div_l2"])
+    for f in ("q", "u", "v", "p"):
+        assert np.array_equal(c.download(f), g[f]), f

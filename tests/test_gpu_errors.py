@@ -19,7 +19,7 @@ def test_invalid_arguments(built):
     assert lib.cf_ctx_create(None, ctypes.byref(h)) == L.CF_ERR_INVALID
     d = L.GridDesc(0, 8, (ctypes.c_double * 2)(0, 0), (ctypes.c_double * 2)(1, 1), (ctypes.c_int * 2)(0, 0), 0, 0)
     assert lib.cf_ctx_create(ctypes.byref(d), ctypes.byref(h)) == L.CF_ERR_INVALID
-    # extent not divisible by the uniform cell size (src/Mesh.hpp:478-486)
+    # extent not divisible by the uniform cell size (src/Mesh.hpp:49-64)
     d = L.GridDesc(8, 8, (ctypes.c_double * 2)(0, 0), (ctypes.c_double * 2)(1, 2), (ctypes.c_int * 2)(0, 0), 0, 0)
     assert lib.cf_ctx_create(ctypes.byref(d), ctypes.byref(h)) == L.CF_ERR_MESH
     assert lib.cf_step(None, 0.1, 3, None, None) == L.CF_ERR_INVALID

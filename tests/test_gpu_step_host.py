@@ -51,3 +51,34 @@ def test_step_host_outputs_optional_and_shapes_checked(built):
     assert np.array_equal(qo, c.download("q"))
     with pytest.raises(ValueError):
         c.step_host(0.001, 3, opts(), st["q"], st["v"], st["u"])
+
+
+def test_step_host_failed_setup_is_retried(built):
+    """A first cf_step_host whose lazy set-up fails (an out-of-memory
+    cudaMalloc, injected on the host) returns CF_ERR_NOMEM and leaves no
+    half-made state: the next call creates what is missing and matches a
+    context that never failed, bit for bit."""
+    from cajitafluids_gb300 import _lib as L
+    from cajitafluids_gb300.api import CfError
+    lib = L.load()
+    rng = np.random.default_rng(5)
+    o, a = make_pair(48, 48, source=INFLOW, precision="mixed")
+    b = make_pair(48, 48, source=INFLOW, precision="mixed")[1]
+    st = random_state(o, rng, scale=0.2)
+    dt = 0.5 / 48 / 3.0
+    so = opts(tol=1e-9, precon="PFMG")
+    outs_a = [np.empty(a.owned_shape(f)) for f in ("q", "u", "v")]
+    outs_b = [np.empty(b.owned_shape(f)) for f in ("q", "u", "v")]
+    # the mixed context's first cf_step_host allocates one staging buffer
+    lib.cf_test_fail_alloc(1)
+    try:
+        with pytest.raises(CfError) as e:
+            a.step_host(dt, 3, so, st["q"], st["u"], st["v"], *outs_a)
+        assert e.value.code == L.CF_ERR_NOMEM
+    finally:
+        lib.cf_test_fail_alloc(0)
+    sa = a.step_host(dt, 3, so, st["q"], st["u"], st["v"], *outs_a)
+    sb = b.step_host(dt, 3, so, st["q"], st["u"], st["v"], *outs_b)
+    assert sa["iterations"] == sb["iterations"]
+    for x, y in zip(outs_a, outs_b):
+        assert np.array_equal(x, y)
