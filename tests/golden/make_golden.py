@@ -1,12 +1,17 @@
-"""Generates the golden fixtures in this directory from the CPU oracle.
+"""Generates the golden fixtures in this directory.
 
     python tests/golden/make_golden.py
 
-The reference (Kokkos + Cabana/Cajita + HYPRE + MPI) cannot be built or
-imported here, so the fixtures are oracle outputs: they pin the oracle
-against regressions and give the GPU path fixed expected values
-(tests/test_golden.py, bit for bit).
-Every input is generated from a seed below.
+reference_*.npz come from the reference's own code: its src/*.hpp compiled
+unchanged against the serial Kokkos/Cajita/MPI stand-ins in oracle/refshim
+and run through createSolver("serial", ...) with the "Reference" solver
+(oracle/reference.py).  They are written only where the reference's sources
+are present; elsewhere the committed files are kept.  The other fixtures
+are outputs of the CPU oracle, which equals the reference's code bit for
+bit where both run (tests/test_reference_pin.py) and extends it to the
+multigrid preconditioner, periodic axes and linear values.  All of them
+give the GPU path fixed expected values (tests/test_golden.py, bit for
+bit).  Every input is generated from a seed below.
 """
 import os
 import sys
@@ -94,7 +99,43 @@ def interpolation_kat(n=24, seed=9):
     return out
 
 
+def reference_config0(n=64, steps=6):
+    """The config-0 problem (walls, zero start, the inflow box, Q = 1,
+    v = 3) run by the reference's own Solver<2>: setup + steps, cubic values
+    and tol 1e-6 / 2000 iterations as the reference hard-codes them."""
+    from oracle import reference as R
+    dt = 0.5 * (1.0 / n) / 3.0
+    prm = R.params(n, n, source=INFLOW, density=0.1, dt=dt)
+    r = R.run(prm, steps=steps)
+    return dict(n=n, dt=dt, steps=steps, density=0.1, q=r["q"], u=r["u"], v=r["v"], p=r["p"],
+                iterations=r["iterations"])
+
+
+def reference_random_walls_gravity(n=40, steps=4, seed=11):
+    """A seeded random state, a FREE bottom wall, gravity and the inflow,
+    run by the reference's own Solver<2>."""
+    from oracle import reference as R
+    rng = np.random.default_rng(seed)
+    q0 = rng.uniform(0.0, 1.0, (n, n))
+    u0 = rng.standard_normal((n, n + 1)) * 0.3
+    v0 = rng.standard_normal((n + 1, n)) * 0.3
+    dt = 0.25 / n
+    bc = (0, 1, 0, 0)
+    body = (0.0, -2.0)
+    prm = R.params(n, n, bc=bc, source=INFLOW, body=body, density=0.1, dt=dt)
+    r = R.run(prm, q0, u0, v0, steps=steps)
+    return dict(n=n, dt=dt, steps=steps, density=0.1, bc=np.array(bc), body=np.array(body), q0=q0, u0=u0, v0=v0,
+                q=r["q"], u=r["u"], v=r["v"], p=r["p"], iterations=r["iterations"])
+
+
 def main():
+    from oracle import reference as R
+    if R.available():
+        np.savez_compressed(os.path.join(HERE, "reference_config0_64.npz"), **reference_config0())
+        np.savez_compressed(os.path.join(HERE, "reference_random_walls_gravity_40.npz"),
+                            **reference_random_walls_gravity())
+    else:
+        print("the reference's sources are not on this machine: reference_*.npz kept as committed")
     np.savez_compressed(os.path.join(HERE, "config0_32.npz"), **config0_small())
     np.savez_compressed(os.path.join(HERE, "periodic_spectral_32.npz"), **periodic_small())
     np.savez_compressed(os.path.join(HERE, "interp_kat_24.npz"), **interpolation_kat())

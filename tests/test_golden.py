@@ -1,6 +1,9 @@
 """Committed golden fixtures (tests/golden/*.npz, made by make_golden.py).
 
-CPU: the oracle reproduces them bit for bit (it is deterministic and
+reference_*.npz hold the reference's own results (its src/*.hpp compiled
+unchanged against the stand-ins in oracle/refshim); the others are oracle
+outputs.
+CPU: the oracle reproduces all of them bit for bit (it is deterministic and
 contraction-free, so x86 and Arm give the same bits).
 GPU: the FP64 CUDA path reproduces them bit for bit through the C ABI.
 """
@@ -150,5 +153,60 @@ def test_gpu_reproduces_walls_buoyancy_mg_fixture(built):
     st += [c.step(dt, int(g["order"]), o) for _ in range(int(g["steps"]))]
     assert np.array_equal([s["iterations"] for s in st], g["iterations"])
     assert np.array_equal([s["div_l2"] for s in st], g["div_l2"])
+    for f in ("q", "u", "v", "p"):
+        assert np.array_equal(c.download(f), g[f]), f
+
+
+# ---- fixtures written by the reference's own code ----------------------------
+# The reference hard-codes cubic values and a Jacobi-preconditioned CG with
+# tolerance 1e-6 and 2000 iterations (src/TimeIntegrator.hpp:112-113,
+# src/VelocityCorrector.hpp:103-104, 158-180).
+REF_FIXTURES = ("reference_config0_64.npz", "reference_random_walls_gravity_40.npz")
+
+
+def _ref_setup(g):
+    bc = tuple(int(b) for b in g["bc"]) if "bc" in g else (0, 0, 0, 0)
+    body = tuple(float(b) for b in g["body"]) if "body" in g else (0.0, 0.0)
+    return bc, body
+
+
+@pytest.mark.parametrize("name", REF_FIXTURES)
+def test_oracle_reproduces_reference_fixture(built, name):
+    g = _load(name)
+    n = int(g["n"])
+    dt = float(g["dt"])
+    bc, body = _ref_setup(g)
+    o = Oracle(n, n, bc=bc, source=INFLOW, body=body, density=float(g["density"]))
+    for f in ("q", "u", "v"):
+        if f + "0" in g:
+            o.set(f, g[f + "0"])
+    its = [o.setup(dt, tol=1e-6, max_iter=2000)["iterations"]]
+    its += [o.step(dt, 3, tol=1e-6, max_iter=2000)["iterations"] for _ in range(int(g["steps"]))]
+    assert np.array_equal(its, g["iterations"])
+    for f in ("q", "u", "v", "p"):
+        assert np.array_equal(o.get(f), g[f]), f
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", REF_FIXTURES)
+def test_gpu_reproduces_reference_fixture(built, name):
+    """The CUDA FP64 step equals the reference's own step bit for bit."""
+    from cajitafluids_gb300 import Context, SolverOptions
+    g = _load(name)
+    n = int(g["n"])
+    dt = float(g["dt"])
+    bc, body = _ref_setup(g)
+    c = Context(n, n)
+    c.set_bc(bc)
+    c.set_source(*INFLOW)
+    c.set_body_force(body)
+    c.set_density(float(g["density"]))
+    for f in ("q", "u", "v"):
+        if f + "0" in g:
+            c.upload(f, g[f + "0"])
+    o = SolverOptions(solver="Reference", tol=1e-6, max_iter=2000)
+    its = [c.setup(dt, o)["iterations"]]
+    its += [c.step(dt, 3, o)["iterations"] for _ in range(int(g["steps"]))]
+    assert np.array_equal(its, g["iterations"])
     for f in ("q", "u", "v", "p"):
         assert np.array_equal(c.download(f), g[f]), f
