@@ -297,14 +297,12 @@ def bench_gb300(args, rank, world, dist, device):
                    "l2_policy": "inputs larger than L2 (state + solver vectors ~1 GB)"},
         "adjoint_forward_ratio": None,
     }
-    q_mixed_w = None
     value = None
     stats = []
     if "mixed" in legs:
         # ---- mixed precision (headline) ----
         cm = make_context(w, "mixed", device)
         run_steps(cm, w, args.warmup)
-        q_mixed_w = cm.download("q")
         l0 = cm.launches
         clocks = ClockSampler(device)
         barrier_sync(dist)
@@ -422,7 +420,6 @@ def bench_gb300(args, rank, world, dist, device):
         # ---- plain FP64 on the same steps ----
         cf = make_context(w, "fp64", device)
         run_steps(cf, w, args.warmup, fstats)
-        q64_w = cf.download("q")
         barrier_sync(dist)
         cf.timer_start()
         run_steps(cf, w, args.fp64_steps, fstats)
@@ -443,10 +440,12 @@ def bench_gb300(args, rank, world, dist, device):
                         "div_l2_max": max(s["div_l2"] for s in fstats) if fstats else None}
         if value and value64:
             line["mixed_vs_fp64"] = value / value64
-        if q_mixed_w is not None:
-            err = q_mixed_w - q64_w
-            line["scalar_error_vs_fp64"] = {"after_steps": args.warmup, "linf": float(np.abs(err).max()),
-                                            "l2": float(np.sqrt(np.mean(err * err)))}
+
+    if "accuracy" in legs:
+        line["scalar_error_vs_fp64"] = bench_accuracy(args, w, device)
+
+    if "configs" in legs:
+        line["configs_0_1"] = bench_configs(args, device)
 
     if "adjoint" in legs:
         line["adjoint"] = bench_adjoint(args, device, dist)
@@ -465,6 +464,70 @@ def bench_gb300(args, rank, world, dist, device):
         line["cpu_baseline"] = {"value": 1.0 / statistics.mean(per_step), "unit": "steps/s", "cores": cores,
                                 "kind": "port", "cpu": cpu_model(), "sample": sample, **detail}
     return line
+
+
+def bench_accuracy(args, w, device):
+    """The workload's full run (config 2: 200 steps) in mixed precision and
+    in FP64 from the same initial state: the scalar's L-inf and RMS error
+    of the mixed run against the FP64 run every 20 steps, and the largest
+    ||div u||_L2 after any projection of either run."""
+    n = max(1, args.accuracy_steps)
+    cm = make_context(w, "mixed", device)
+    cf = make_context(w, "fp64", device)
+    o = solver_opts(w)
+    every = []
+    div_m, div_f = 0.0, 0.0
+    for s in range(1, n + 1):
+        div_m = max(div_m, cm.step(w.dt, w.order, o, raise_on_maxit=True)["div_l2"])
+        div_f = max(div_f, cf.step(w.dt, w.order, o, raise_on_maxit=True)["div_l2"])
+        if s % 20 == 0 or s == n:
+            err = cm.download("q") - cf.download("q")
+            every.append({"step": s, "linf": float(np.abs(err).max()), "l2": float(np.sqrt(np.mean(err * err)))})
+    cm.close()
+    cf.close()
+    last = every[-1]
+    return {"after_steps": n, "linf": last["linf"], "l2": last["l2"], "target_linf": 1e-6,
+            "meets_target": last["linf"] <= 1e-6, "every_20_steps": every,
+            "div_l2_max_mixed": div_m, "div_l2_max_fp64": div_f,
+            "run": f"{w.nx}^2 from the workload's initial state, {n} steps each, mixed and FP64"}
+
+
+def bench_configs(args, device):
+    """Configs 0 and 1 of the benchmark plan at full size and length, FP64,
+    Jacobi-PCG (the reference's own solver form), one cf_step per step:
+    steps/s, CG iterations per step and ||div u||_L2 after every projection
+    (setup's included).  Their fields equal the oracle's bit for bit (the
+    GPU tests check all 100 steps of config 0 and the first two of config
+    1); here they are only run and measured."""
+    from cajitafluids_gb300 import Context, SolverOptions
+    from cajitafluids_gb300.workloads import config0, config1
+    out = {}
+    for name, w, max_iter in (("config0", config0(), 20000), ("config1", config1(), 50000)):
+        c = Context(w.nx, w.ny)
+        c.set_bc(w.bc)
+        c.set_source(*w.source, mode=w.source_mode)
+        c.set_body_force(w.body, w.body_density_scaled)
+        c.set_density(w.density)
+        o = SolverOptions(tol=w.tol, max_iter=max_iter, precon="Diagonal")
+        st = [c.setup(w.dt, o, raise_on_maxit=True)]
+        c.timer_start()
+        t0 = time.perf_counter()
+        for _ in range(w.steps):
+            st.append(c.step(w.dt, w.order, o, raise_on_maxit=True))
+        ms = c.timer_stop()
+        wall = time.perf_counter() - t0
+        c.close()
+        div = [s["div_l2"] for s in st]
+        out[name] = {"workload": f"{w.nx}^2 walls, inflow, " + ("gravity scaled by the quantity, " if w.body_density_scaled
+                                                                  else "") +
+                                 f"{'cubic' if w.order == 3 else 'linear'} values, FP64 PCG + Diagonal to {w.tol:g}, "
+                                 f"setup + {w.steps} steps",
+                     "steps": w.steps, "steps_per_s": w.steps / (max(ms, wall * 1e3) / 1e3),
+                     "cg_iters_per_step": statistics.mean(s["iterations"] for s in st[1:]),
+                     "all_converged": all(s["status"] == 0 for s in st),
+                     "div_l2_max": max(div), "div_l2_last": div[-1],
+                     "div_l2_every_projection": [float(f"{d:.3g}") for d in div]}
+    return out
 
 
 def bench_adjoint(args, device, dist):
@@ -596,12 +659,15 @@ def main():
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--legs", default="mixed,e2e,warm,fp64,adjoint,cpu",
-                    help="comma list of legs to run: mixed (headline), e2e, warm, fp64, adjoint, cpu")
+    ap.add_argument("--legs", default="mixed,e2e,warm,fp64,accuracy,configs,adjoint,cpu",
+                    help="comma list of legs to run: mixed (headline), e2e, warm, fp64, accuracy, configs, "
+                         "adjoint, cpu")
+    ap.add_argument("--accuracy-steps", type=int, default=200,
+                    help="steps of the mixed-vs-FP64 accuracy run (the workload's full run length)")
     ap.add_argument("--adjoint-size", type=int, default=512)
     ap.add_argument("--adjoint-steps", type=int, default=200)
     ap.add_argument("--adjoint-every", type=int, default=14)
-    ap.add_argument("--adjoint-fd", type=int, default=0, help="central-difference checks of the gradient")
+    ap.add_argument("--adjoint-fd", type=int, default=2, help="central-difference checks of the gradient")
     ap.add_argument("--ref-iters", type=int, default=12000)
     ap.add_argument("--precon", default="PFMG",
                     help="PCG preconditioner: PFMG/SMG/MG (geometric multigrid, the reference CLI default), "

@@ -119,6 +119,11 @@ class Context:
         """Start each projection from the previous pressure (extension)."""
         self._check(self.lib.cf_set_warm_start(self.h, int(bool(on))))
 
+    def set_graphs(self, on: bool = True):
+        """CUDA graphs for the pressure solve (default), or every kernel
+        launched on its own (same results)."""
+        self._check(self.lib.cf_set_graphs(self.h, int(bool(on))))
+
     def set_quirks(self, flags: int):
         self._check(self.lib.cf_set_quirks(self.h, int(flags)))
 

@@ -415,6 +415,18 @@ int cf_set_warm_start(cf_ctx* ctx, int on) {
     return CF_OK;
 }
 
+int cf_set_graphs(cf_ctx* ctx, int on) {
+    if (!ctx) return CF_ERR_INVALID;
+    ctx->direct = on ? 0 : 1;
+    return CF_OK;
+}
+
+int cf_test_stall_wait(cf_ctx* ctx, int on) {
+    if (!ctx) return CF_ERR_INVALID;
+    ctx->test_stall = on ? 1 : 0;
+    return CF_OK;
+}
+
 int cf_set_density(cf_ctx* ctx, double density) {
     if (!ctx) return CF_ERR_INVALID;
     if (!(density > 0.0) || !isfinite(density)) return fail(ctx, CF_ERR_INVALID, "density must be positive");

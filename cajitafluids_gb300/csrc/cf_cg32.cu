@@ -44,6 +44,11 @@ constexpr int kSlot = 9856;              // 128-byte aligned slot
 constexpr int kStages = 3;
 constexpr int kThreads = 256;
 constexpr unsigned kWaitLimit = 1u << 22;
+// the drain after a timeout waits longer than any tile wait: a CTA must not
+// exit while one of its bulk copies may still be writing its shared memory
+constexpr unsigned kDrainLimit = 1u << 24;
+// the stalled wait of the timeout-path test (cf_test_stall_wait)
+constexpr unsigned kStallLimit = 1u << 10;
 
 struct Cg32T {
     int nx, ny, per_x, per_y, tiles_x, tiles, pitch;
@@ -200,12 +205,13 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
     return t;
 }
 
-// Timeout path: record the status and wait (bounded) for this CTA's copies.
+// Timeout path: record the status and wait (bounded, with the longer drain
+// limit) for this CTA's copies still in flight.
 __device__ void abandon(SolverState* S, const uint64_t* bars, int kfirst, int ktiles) {
     if (threadIdx.x == 0) {
         atomicExch(&S->status, (int)ST_TIMEOUT);
         for (int k = kfirst; k < ktiles && k < kfirst + kStages; ++k)
-            mbar_wait(smem_u32(&bars[k % kStages]), (uint32_t)((k / kStages) & 1), kWaitLimit >> 4);
+            mbar_wait(smem_u32(&bars[k % kStages]), (uint32_t)((k / kStages) & 1), kDrainLimit);
     }
     __syncthreads();
 }
@@ -216,11 +222,14 @@ __global__ void __launch_bounds__(kThreads, 2)
                        const __grid_constant__ CUtensorMap map_pb, Cg32T a) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bars[kStages];
+    // test knob: an mbarrier that nothing arrives on (cf_test_stall_wait)
+    __shared__ __align__(8) uint64_t never;
     __shared__ double red[kThreads / 32];
     SolverState* S = a.S;
     if (!running(S)) return;
     const int it = S->inner_iter;
     const bool first = it == 0 || S->restart;
+    const bool stall = S->test_stall != 0 && blockIdx.x == 0;
     const float beta = (float)S->beta_in;
     const CUtensorMap* map_old = (it & 1) ? &map_pb : &map_pa;
     float* pnew = (it & 1) ? a.pa : a.pb;
@@ -230,6 +239,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     auto stage_ptr = [&](int s, int arr) { return reinterpret_cast<float*>(sb + (s * 2 + arr) * kSlot); };
     if (tid == 0) {
         for (int s = 0; s < kStages; ++s) mbar_init(smem_u32(&bars[s]), 1);
+        mbar_init(smem_u32(&never), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -249,7 +259,11 @@ __global__ void __launch_bounds__(kThreads, 2)
         const int s = k % kStages;
         const int t = (int)blockIdx.x + k * (int)gridDim.x;
         const int i0 = (t % a.tiles_x) * kTW, j0 = (t / a.tiles_x) * kTH;
-        bool ok = mbar_wait(smem_u32(&bars[s]), (uint32_t)((k / kStages) & 1), kWaitLimit);
+        // with the test knob, block 0's first wait is on the barrier nothing
+        // arrives on, with a short limit: it times out, and the drain below
+        // waits for the real copies of stages 0..2
+        bool ok = (stall && k == 0) ? mbar_wait(smem_u32(&never), 0u, kStallLimit)
+                                    : mbar_wait(smem_u32(&bars[s]), (uint32_t)((k / kStages) & 1), kWaitLimit);
         if (__syncthreads_or(!ok)) {
             abandon(S, bars, k, ntile);
             return;

@@ -81,6 +81,12 @@ struct cf_ctx {
     float* z32b = nullptr;
     CUtensorMap map_z{};
     long long launches = 0;
+    // cf_set_graphs(ctx, 0): every kernel is issued on its own (no CUDA graphs,
+    // host-polled projection); the results are the same bits
+    int direct = 0;
+    // cf_test_stall_wait: the inner FP32 CG's first tile wait of block 0
+    // waits on an mbarrier nothing arrives on (timeout-path test)
+    int test_stall = 0;
     // profiling (cf_profile_enable)
     int prof = 0;
     cf_profile pd{};

@@ -77,6 +77,7 @@ struct SolverState {
     int iter, max_iter, status;
     int inner_iter, inner_status;
     int outer_iter, max_outer;
+    int test_stall;  // test knob (cf_test_stall_wait): see k_tma_dir_matvec32
     unsigned int ticket[8];
 };
 

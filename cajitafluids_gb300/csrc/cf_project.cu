@@ -1030,6 +1030,69 @@ static void launch_outer(cf_ctx* c, const Stencil& st, int gated) {
 static const int kBatch = CF_CG_BATCH;  // CG iterations per graph launch
 static const int kBatchMG = 4;          // MG-PCG iterations per graph launch
 
+// kBatch Jacobi-PCG iterations (the body of the batch graph)
+static void batch_cg(cf_ctx* c, const Stencil& st, bool mixed) {
+    if (mixed) {
+        for (int i = 0; i < kBatch; ++i) cg32_launch_iteration(c, st);
+    } else {
+        const int nb = red_blocks(c);
+        Cg64 a = cg64_args(c, st);
+        for (int i = 0; i < kBatch; ++i) {
+            k_cg_dir_matvec64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
+            k_cg_update64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
+        }
+    }
+}
+
+// kBatchMG MG-PCG iterations: K1 (z-mode), K2, V-cycle, r.z (mixed: the
+// gated reliable update too); returns the kernels of one iteration
+static int batch_mg(cf_ctx* c, const Stencil& st) {
+    const bool mixed = c->precision == CF_PREC_MIXED;
+    const int nb = red_blocks(c);
+    const double scale = -st.ms;
+    Cg64 a = cg64_args(c, st);
+    a.mg = 1;
+    a.z = mixed ? nullptr : mg_z64(c);
+    int per = 0;
+    for (int i = 0; i < kBatchMG; ++i) {
+        if (mixed) {
+            cg32_launch_pair_mg(c, st);
+            launch_outer(c, st, 1);
+            per = 3 + cg32_mg_precondition(c, scale);
+        } else {
+            k_cg_dir_matvec64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
+            k_cg_update64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
+            per = 3 + mg_vcycle(c, scale);
+            k_mg_rz64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a, 0);
+        }
+    }
+    return per;
+}
+
+// V-cycle and r.z after the residual was (re)formed; returns kernels launched
+static int batch_mg_pre(cf_ctx* c, const Stencil& st) {
+    const bool mixed = c->precision == CF_PREC_MIXED;
+    const double scale = -st.ms;
+    if (mixed) return cg32_mg_precondition(c, scale);
+    Cg64 a = cg64_args(c, st);
+    a.mg = 1;
+    a.z = mg_z64(c);
+    const int pre = 1 + mg_vcycle(c, scale);
+    k_mg_rz64<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(a, 1);
+    return pre;
+}
+
+// One batch of the host-polled projection: the captured graph, or, with
+// graphs off (cf_set_graphs), the same kernels issued one by one.
+template <typename F>
+static int launch_batch(cf_ctx* c, cudaGraphExec_t ge, F&& issue) {
+    if (c->direct) {
+        issue();
+        return cuda_check(c, cudaGetLastError(), "kernel launch");
+    }
+    return cuda_check(c, cudaGraphLaunch(ge, c->stream), "graph launch");
+}
+
 // Build (or reuse) the graph of kBatch iterations for the current stencil.
 static int ensure_graph(cf_ctx* c, const Stencil& st, bool mixed) {
     cudaGraphExec_t& ge = mixed ? c->g32 : c->g64;
@@ -1042,16 +1105,7 @@ static int ensure_graph(cf_ctx* c, const Stencil& st, bool mixed) {
     cudaGraph_t g;
     int rc = cuda_check(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "capture begin");
     if (rc) return rc;
-    int nb = red_blocks(c);
-    if (mixed) {
-        for (int i = 0; i < kBatch; ++i) cg32_launch_iteration(c, st);
-    } else {
-        Cg64 a = cg64_args(c, st);
-        for (int i = 0; i < kBatch; ++i) {
-            k_cg_dir_matvec64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
-            k_cg_update64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
-        }
-    }
+    batch_cg(c, st, mixed);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if ((rc = cuda_check(c, e, "capture end"))) return rc;
     e = cudaGraphInstantiate(&ge, g, 0);
@@ -1085,36 +1139,9 @@ static int capture(cf_ctx* c, cudaGraphExec_t* ge, F&& fn) {
 static int ensure_graph_mg(cf_ctx* c, const Stencil& st) {
     if (c->gmg && c->gmg_pre && c->gmg_xonly == c->x_only && std::memcmp(&c->gmg_st, &st, sizeof(Stencil)) == 0)
         return CF_OK;
-    const bool mixed = c->precision == CF_PREC_MIXED;
-    const int nb = red_blocks(c);
-    const double scale = -st.ms;
-    Cg64 a = cg64_args(c, st);
-    a.mg = 1;
-    a.z = mixed ? nullptr : mg_z64(c);
     int per = 0, pre = 0;
-    int rc = capture(c, &c->gmg, [&] {
-        for (int i = 0; i < kBatchMG; ++i) {
-            if (mixed) {
-                cg32_launch_pair_mg(c, st);
-                launch_outer(c, st, 1);
-                per = 3 + cg32_mg_precondition(c, scale);
-            } else {
-                k_cg_dir_matvec64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
-                k_cg_update64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
-                per = 3 + mg_vcycle(c, scale);
-                k_mg_rz64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a, 0);
-            }
-        }
-    });
-    if (!rc)
-        rc = capture(c, &c->gmg_pre, [&] {
-            if (mixed) {
-                pre = cg32_mg_precondition(c, scale);
-            } else {
-                pre = 1 + mg_vcycle(c, scale);
-                k_mg_rz64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a, 1);
-            }
-        });
+    int rc = capture(c, &c->gmg, [&] { per = batch_mg(c, st); });
+    if (!rc) rc = capture(c, &c->gmg_pre, [&] { pre = batch_mg_pre(c, st); });
     if (rc) return rc;
     c->gmg_st = st;
     c->gmg_xonly = c->x_only;
@@ -1359,6 +1386,7 @@ static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResul
         h->status = ST_RUNNING;
         const int batch = mg ? kResidentBatchMG : kResidentBatch;
         h->trip_limit = (o.max_iter + (mixed ? o.max_outer : 0)) / batch + 4;
+        h->test_stall = c->test_stall;
     }
     cudaMemcpyAsync(c->S, h, sizeof(SolverState), cudaMemcpyHostToDevice, c->stream);
     if ((rc = cuda_check(c, cudaGraphLaunch(c->rgx[cur], c->stream), "graph launch"))) return rc;
@@ -1390,7 +1418,7 @@ int project_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, bo
     const bool mixed = c->precision == CF_PREC_MIXED;
     const bool mg = o.precon_mg != 0;
     *deferred = false;
-    if (c->prof || !resident_enabled()) return project(c, dt, o, res);
+    if (c->prof || c->direct || !resident_enabled()) return project(c, dt, o, res);
     Stencil st{};
     build_stencil(c, dt, o.precon_none, &st);
     int rc = mg ? mg_setup(c) : CF_OK;
@@ -1431,7 +1459,8 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     // the resident graph serves plain projections; the adjoint's projection
     // (other arrays) and profiled runs (events between batches) take the
     // host-polled batches below
-    if (!adjoint && !c->prof && resident_enabled()) return project_resident(c, dt, o, res, st, mixed, mg);
+    if (!adjoint && !c->prof && !c->direct && resident_enabled())
+        return project_resident(c, dt, o, res, st, mixed, mg);
     rc = mg ? ensure_graph_mg(c, st) : ensure_graph(c, st, mixed);
     if (rc) return rc;
 
@@ -1446,6 +1475,7 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     h->max_outer = o.max_outer;
     h->inner_tol2 = o.inner_tol * o.inner_tol;
     h->status = ST_RUNNING;
+    h->test_stall = c->test_stall;
     cudaMemcpyAsync(c->S, h, sizeof(SolverState), cudaMemcpyHostToDevice, c->stream);
     int nb = red_blocks(c);
     DivArgs da = div_args(c, st);
@@ -1462,7 +1492,7 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
         cudaGraphExec_t ge = mg ? c->gmg : c->g64;
         const int per_batch = mg ? c->gmg_per_iter * kBatchMG : 2 * kBatch;
         if (mg) {
-            if ((rc = cuda_check(c, cudaGraphLaunch(c->gmg_pre, c->stream), "graph launch"))) return rc;
+            if ((rc = launch_batch(c, c->gmg_pre, [&] { batch_mg_pre(c, st); }))) return rc;
             c->launches += c->gmg_pre_launches;
         }
         int max_launch = o.max_iter / batch + 3;
@@ -1474,7 +1504,11 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
             if (c->hS->status != ST_RUNNING) break;
             if (l >= max_launch) return fail(c, CF_ERR_NUMERIC, "solver did not stop after %d batches", l);
             if (c->prof) cudaEventRecord(c->ev[0], c->stream);
-            if ((rc = cuda_check(c, cudaGraphLaunch(ge, c->stream), "graph launch"))) return rc;
+            if (mg)
+                rc = launch_batch(c, ge, [&] { batch_mg(c, st); });
+            else
+                rc = launch_batch(c, ge, [&] { batch_cg(c, st, false); });
+            if (rc) return rc;
             if (c->prof) cudaEventRecord(c->ev[1], c->stream);
             c->launches += per_batch;
         }
@@ -1485,7 +1519,7 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
         if (mg) {
             // MG-PCG: the reliable updates run inside the graph (gated
             // kernels), so the host only polls the status between batches
-            if ((rc = cuda_check(c, cudaGraphLaunch(c->gmg_pre, c->stream), "graph launch"))) return rc;
+            if ((rc = launch_batch(c, c->gmg_pre, [&] { batch_mg_pre(c, st); }))) return rc;
             c->launches += c->gmg_pre_launches;
             int max_launch = (o.max_iter + o.max_outer) / kBatchMG + 3;
             int prev_iter = 0;
@@ -1496,7 +1530,7 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
                 if (c->hS->status != ST_RUNNING) break;
                 if (l >= max_launch) return fail(c, CF_ERR_NUMERIC, "mixed MG solver did not stop");
                 if (c->prof) cudaEventRecord(c->ev[0], c->stream);
-                if ((rc = cuda_check(c, cudaGraphLaunch(c->gmg, c->stream), "graph launch"))) return rc;
+                if ((rc = launch_batch(c, c->gmg, [&] { batch_mg(c, st); }))) return rc;
                 if (c->prof) cudaEventRecord(c->ev[1], c->stream);
                 c->launches += c->gmg_per_iter * kBatchMG;
             }
@@ -1509,7 +1543,7 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
                     if (++launches > max_launch) return fail(c, CF_ERR_NUMERIC, "mixed solver did not stop");
                     int prev_iter = c->hS->iter;
                     if (c->prof) cudaEventRecord(c->ev[0], c->stream);
-                    if ((rc = cuda_check(c, cudaGraphLaunch(c->g32, c->stream), "graph launch"))) return rc;
+                    if ((rc = launch_batch(c, c->g32, [&] { batch_cg(c, st, true); }))) return rc;
                     if (c->prof) cudaEventRecord(c->ev[1], c->stream);
                     c->launches += 2 * kBatch;
                     if ((rc = read_state(c))) return rc;

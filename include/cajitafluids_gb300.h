@@ -158,6 +158,13 @@ int cf_set_density(cf_ctx* ctx, double density);
  * (cf_forward_checkpointed / cf_backward) returns CF_ERR_UNSUPPORTED while on. */
 int cf_set_warm_start(cf_ctx* ctx, int on);
 int cf_set_quirks(cf_ctx* ctx, unsigned flags);
+/* Launch mode (no counterpart in the reference; Kokkos launches every
+ * parallel_for on its own).  on = 1 (default): the pressure solve runs as
+ * CUDA graphs (one device-resident graph per projection, or host-polled
+ * graph batches).  on = 0: every kernel of the solve is launched on its own
+ * and the host polls the solver state between batches, for tools that list
+ * kernel launches one by one.  The results are the same bits either way. */
+int cf_set_graphs(cf_ctx* ctx, int on);
 
 /* ---- state (ProblemManager::get / initialize / advance) ---- */
 int cf_upload(cf_ctx* ctx, int field, const double* host, ptrdiff_t stride_i, ptrdiff_t stride_j);
@@ -254,6 +261,12 @@ int cf_test_strip_geometry(int nx, int ny, int tile_w, int tile_h, int strip_row
  * nth device allocation of the library from now on fails as an out-of-memory
  * cudaMalloc would (CF_ERR_NOMEM); 0 switches the injection off. */
 int cf_test_fail_alloc(int nth);
+/* Test hook (timeout path, no GPU fault): with on != 0, the first tile wait
+ * of one CTA of the mixed-precision inner CG waits on an mbarrier that
+ * nothing arrives on, with a short limit; it times out, the CTA waits for
+ * its own bulk copies in flight and returns, and the projection returns
+ * CF_ERR_TIMEOUT.  The context stays usable; 0 switches the hook off. */
+int cf_test_stall_wait(cf_ctx* ctx, int on);
 
 /* ---- output (replaces the device half of SiloWriter::writeFile) ----
  * SiloWriter interpolates the face velocities to cell centres for its

@@ -1,6 +1,7 @@
 """Generates the golden fixtures in this directory.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py           # the small fixtures
+    python tests/golden/make_golden.py --long    # also the full-length config 0 / config 1 runs
 
 reference_*.npz come from the reference's own code: its src/*.hpp compiled
 unchanged against the serial Kokkos/Cajita/MPI stand-ins in oracle/refshim
@@ -128,7 +129,53 @@ def reference_random_walls_gravity(n=40, steps=4, seed=11):
                 q=r["q"], u=r["u"], v=r["v"], p=r["p"], iterations=r["iterations"])
 
 
+def field_digest(arrays) -> str:
+    """SHA-256 over the bytes of float64 arrays: equal digests mean equal
+    bits, so a long run is compared bit for bit without storing its fields."""
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a, dtype=np.float64).tobytes())
+    return h.hexdigest()
+
+
+def config0_full(steps=100):
+    """Config 0 at its full size and length: 256^2, walls, zero start, the
+    inflow box, linear values, Jacobi-PCG to 1e-8; setup + 100 steps.
+    Stored as the iteration count and ||div u|| of every projection and a
+    digest of the final q, u, v, p."""
+    from cajitafluids_gb300.workloads import config0
+    w = config0(steps=steps)
+    o = Oracle(w.nx, w.ny, source=w.source, density=w.density)
+    st = [o.setup(w.dt, tol=w.tol, max_iter=20000)]
+    st += [o.step(w.dt, w.order, tol=w.tol, max_iter=20000) for _ in range(steps)]
+    return dict(n=w.nx, steps=steps, dt=w.dt, tol=w.tol, order=w.order,
+                iterations=np.array([x["iterations"] for x in st]), div_l2=np.array([x["div_l2"] for x in st]),
+                div_linf=np.array([x["div_linf"] for x in st]),
+                digest=field_digest([o.get(f) for f in ("q", "u", "v", "p")]), q_sum=float(o.get("q").sum()))
+
+
+def config1_head(steps=2):
+    """Config 1's problem (1024^2, walls, inflow, gravity scaled by the
+    quantity, cubic values, Jacobi-PCG to 1e-10): setup + the first steps
+    the oracle affords (about a minute per projection on 8 cores)."""
+    from cajitafluids_gb300.workloads import config1
+    w = config1(steps=steps)
+    o = Oracle(w.nx, w.ny, source=w.source, body=w.body, body_density_scaled=w.body_density_scaled,
+               density=w.density)
+    st = [o.setup(w.dt, tol=w.tol, max_iter=50000)]
+    st += [o.step(w.dt, w.order, tol=w.tol, max_iter=50000) for _ in range(steps)]
+    return dict(n=w.nx, steps=steps, dt=w.dt, tol=w.tol, order=w.order,
+                iterations=np.array([x["iterations"] for x in st]), div_l2=np.array([x["div_l2"] for x in st]),
+                div_linf=np.array([x["div_linf"] for x in st]),
+                digest=field_digest([o.get(f) for f in ("q", "u", "v", "p")]), q_sum=float(o.get("q").sum()))
+
+
 def main():
+    if "--long" in sys.argv:
+        # full-length runs: several minutes of oracle time
+        np.savez_compressed(os.path.join(HERE, "config0_256_full.npz"), **config0_full())
+        np.savez_compressed(os.path.join(HERE, "config1_1024_head.npz"), **config1_head())
     from oracle import reference as R
     if R.available():
         np.savez_compressed(os.path.join(HERE, "reference_config0_64.npz"), **reference_config0())

@@ -5,7 +5,8 @@ Checks:
     q(T) is linear in q(0) and <q_T(dq), y> must equal <dq, J^T y> to
     round-off (the transpose of the interpolation scatter);
   * central finite differences of the FP64 forward on seeded directions in
-    q(0), u(0), v(0) and the inflow rate, for a loss that mixes the scalar
+    q(0), u(0), v(0) and the inflow rate, with the Jacobi ("Diagonal") and
+    the multigrid ("PFMG") preconditioner, for a loss that mixes the scalar
     misfit 1/2 |q(T) - target|^2 with linear terms in u(T), v(T);
     tolerance 1e-5 relative to the directional derivative (the CG solves run
     to a relative residual of 1e-13 so the forward is smooth to far below
@@ -27,6 +28,11 @@ pytestmark = pytest.mark.gpu
 N = 48
 STEPS = 8
 OPTS = SolverOptions(tol=1e-13, max_iter=20000)
+PRECONS = ("Diagonal", "PFMG")
+
+
+def opts_for(precon):
+    return SolverOptions(tol=1e-13, max_iter=20000, precon=precon)
 
 
 def make_ctx(rate=0.0, periodic=False):
@@ -48,30 +54,32 @@ def dt_for(u, v):
     return 0.4 / N / max(np.abs(u).max(), np.abs(v).max())
 
 
-def run(c, q, u, v, dt, every=3):
+def run(c, q, u, v, dt, every=3, opts=OPTS):
     c.upload("q", q)
     c.upload("u", u)
     c.upload("v", v)
-    c.forward_checkpointed(STEPS, every, dt, 3, OPTS)
+    c.forward_checkpointed(STEPS, every, dt, 3, opts)
     return c.download("q"), c.download("u"), c.download("v")
 
 
-def test_dot_product_test_scalar_transport():
+@pytest.mark.parametrize("precon", PRECONS)
+def test_dot_product_test_scalar_transport(precon):
     q, u, v = initial()
     dt = dt_for(u, v)
     c = make_ctx()
     rng = np.random.default_rng(0)
     dq = rng.standard_normal(q.shape)
     y = rng.standard_normal(q.shape)
-    q1, _, _ = run(c, dq, u, v, dt)
+    q1, _, _ = run(c, dq, u, v, dt, opts=opts_for(precon))
     g = c.backward(y)
     lhs = float(np.sum(q1 * y))
     rhs = float(np.sum(dq * g["q"]))
     assert abs(lhs - rhs) <= 1e-12 * (abs(lhs) + np.sum(np.abs(q1 * y)))
 
 
+@pytest.mark.parametrize("precon", PRECONS)
 @pytest.mark.parametrize("periodic", [False, True])
-def test_gradient_matches_central_differences(periodic):
+def test_gradient_matches_central_differences(periodic, precon):
     q0, u0, v0 = initial(periodic)
     dt = dt_for(u0, v0)
     rate = 0.0 if periodic else 2.0
@@ -84,7 +92,7 @@ def test_gradient_matches_central_differences(periodic):
     def loss(q, u, v, r=rate):
         if not periodic:
             c.set_source((0.45, 0.10), (0.10, 0.05), (0.0, 0.0), r, mode=1)
-        qT, uT, vT = run(c, q, u, v, dt)
+        qT, uT, vT = run(c, q, u, v, dt, opts=opts_for(precon))
         return 0.5 * float(np.sum((qT - target) ** 2)) + float(np.sum(cu * uT)) + float(np.sum(cv * vT)), qT
 
     L0, qT = loss(q0, u0, v0)

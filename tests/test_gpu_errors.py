@@ -124,3 +124,39 @@ def test_mixed_context_roundtrip(built):
     with pytest.raises(CfError) as e:
         c.interp_points("q", 3, np.zeros((1, 2)))
     assert e.value.code == L.CF_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("precon", ["Diagonal", "PFMG"])
+@pytest.mark.parametrize("graphs", [True, False])
+def test_device_wait_timeout_is_reported_and_context_usable(built, precon, graphs):
+    """The mixed inner CG's bounded mbarrier waits: with the test hook one
+    CTA's first tile wait is on a barrier that nothing arrives on, so it runs
+    out (no GPU fault: the CTA records the timeout, waits for its own copies
+    and returns).  The projection returns CF_ERR_TIMEOUT; with the hook off
+    the same context projects the same state to the same bits as a fresh
+    context."""
+    lib = L.load()
+    n = 256
+    rng = np.random.default_rng(8)
+    o, a = make_pair(n, n, precision="mixed")
+    b = make_pair(n, n, precision="mixed")[1]
+    a.set_graphs(graphs)
+    st = random_state(o, rng, smooth=True)
+    so = opts(tol=1e-8, max_iter=5000, precon=precon)
+    load_state(o, a, st)
+    assert lib.cf_test_stall_wait(a.h, 1) == L.CF_OK
+    try:
+        with pytest.raises(CfError) as e:
+            a.project(0.002, so, raise_on_maxit=True)
+        assert e.value.code == L.CF_ERR_TIMEOUT
+        assert "timed out" in str(e.value)
+    finally:
+        lib.cf_test_stall_wait(a.h, 0)
+    for f in ("q", "u", "v"):
+        a.upload(f, st[f])
+        b.upload(f, st[f])
+    sa = a.project(0.002, so, raise_on_maxit=True)
+    sb = b.project(0.002, so, raise_on_maxit=True)
+    assert sa["iterations"] == sb["iterations"] and sa["div_l2"] == sb["div_l2"]
+    for f in ("p", "u", "v"):
+        assert np.array_equal(a.download(f), b.download(f)), f
