@@ -555,14 +555,18 @@ def bench_adjoint(args, device, dist):
     c = fresh()
     c.step(w.dt, w.order, opts)  # warm the graphs
     c.close()
+    # the plain forward: Solver::solve's loop on the device (cf_steps), the
+    # fastest forward this build has, so the ratio is against it
     c = fresh()
     barrier_sync(dist)
     c.timer_start()
-    its = 0
-    for _ in range(w.steps):
-        its += c.step(w.dt, w.order, opts, raise_on_maxit=True)["iterations"]
+    last = c.steps(w.steps, w.dt, w.order, opts, raise_on_maxit=True)
     t_fwd = c.timer_stop()
     qT = c.download("q")
+    c.close()
+    c = fresh()
+    its = sum(c.step(w.dt, w.order, opts)["iterations"] for _ in range(min(w.steps, 20)))
+    its_steps = min(w.steps, 20)
     c.close()
     c = fresh()
     c.timer_start()
@@ -577,7 +581,7 @@ def bench_adjoint(args, device, dist):
                        f"checkpoint every {every}, FP64, PCG + {args.precon}, tol {w.tol:g}",
            "forward_ms": t_fwd, "forward_checkpointed_ms": t_fc, "backward_ms": t_bwd,
            "forward_plus_adjoint_over_forward": (t_fc + t_bwd) / t_fwd,
-           "cg_iters_per_forward_step": its / w.steps,
+           "cg_iters_per_forward_step": its / its_steps, "forward_unconverged": last["unconverged"],
            "loss": 0.5 * float(np.sum((qT - target) ** 2))}
     # central differences of the FP64 forward on seeded directions
     rng = np.random.default_rng(16)

@@ -297,6 +297,14 @@ __global__ void k_adj_box_rows(Phys p, Grid<double> aq, double* rows) {
 }
 
 // --------------------------------------------------------------------------
+// sum of the box rows in row order, times dt, added to the rate adjoint
+// (one thread: the same order as a host loop over the rows)
+__global__ void k_adj_rate_acc(const double* rows, int ny, double dt, double* rbar) {
+    double s = 0.0;
+    for (int r = 0; r < ny; ++r) s += rows[r];
+    *rbar += dt * s;
+}
+
 // host side
 
 static void* grid_base(const Grid<double>& g) { return (void*)(g.o - (32 - CF_HALO)); }
@@ -315,6 +323,7 @@ struct AdjState {
     RecKind F[3], Su[3][3], Sv[3][3];
     int* d_err = nullptr;
     double* d_rows = nullptr;
+    double* d_rbar = nullptr;  // dL/d(rate), accumulated on the device
     std::vector<void*> allocs;
 };
 
@@ -413,34 +422,36 @@ int setup_records(cf_ctx* c, AdjState* A) {
     }
     if (!rc) rc = dalloc(c, A, (void**)&A->d_err, sizeof(int));
     if (!rc) rc = dalloc(c, A, (void**)&A->d_rows, sizeof(double) * (c->ph.ny + 1));
+    if (!rc) rc = dalloc(c, A, (void**)&A->d_rbar, sizeof(double));
     return rc;
 }
 
-int adjoint_step(cf_ctx* c, AdjState* A, const SolveOpts& so, double* rbar) {
+// One reverse step, enqueued without a synchronisation: the transposed
+// projection (deferred through its resident graph when that serves it;
+// non-convergence and failures are tallied on the device), the inputs'
+// transpose with dL/d(rate) accumulated on the device, and the advection's
+// transpose (a trace that moved too far sets the device error flag).
+int adjoint_step(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_ready) {
     const Phys& p = c->ph;
     dim3 blk(32, 8);
     int rc;
     // P^T: mask, then the projection pipeline without the final mask
     k_adj_mask<<<dim3((p.nx + 2 + 31) / 32, (p.ny + 2 + 7) / 8, 2), blk, 0, c->stream>>>(p, A->ag[1], A->ag[2]);
     SolveResult res{};
-    if ((rc = project_grids(c, A->dt, so, &res, A->ag[1], A->ag[2], 1))) return rc;
-    if (res.status != ST_CONVERGED && res.status != ST_MAXIT)
+    bool deferred = false;
+    if ((rc = project_adjoint_async(c, A->dt, so, &res, &deferred, params_ready, A->ag[1], A->ag[2]))) return rc;
+    if (!deferred && res.status != ST_CONVERGED && res.status != ST_MAXIT)
         return fail(c, CF_ERR_NUMERIC, "adjoint projection failed (status %d)", res.status);
     // I^T: wall masks of the inputs; dL/dQ from the rate source
     k_adj_mask<<<dim3((p.nx + 2 + 31) / 32, (p.ny + 2 + 7) / 8, 2), blk, 0, c->stream>>>(p, A->ag[1], A->ag[2]);
     bool src_active = p.bbox[2] > p.bbox[0] && p.bbox[3] > p.bbox[1];
     if (src_active && p.src_mode == 1) {
         k_adj_box_rows<<<(p.ny + 127) / 128, 128, 0, c->stream>>>(p, A->ag[0], A->d_rows);
-        std::vector<double> rows(p.ny);
-        cudaMemcpyAsync(rows.data(), A->d_rows, sizeof(double) * p.ny, cudaMemcpyDeviceToHost, c->stream);
-        if ((rc = cuda_check(c, cudaStreamSynchronize(c->stream), "adjoint source"))) return rc;
-        double s = 0.0;
-        for (double r : rows) s += r;
-        *rbar += A->dt * s;
+        k_adj_rate_acc<<<1, 1, 0, c->stream>>>(A->d_rows, p.ny, A->dt, A->d_rbar);
+        c->launches += 2;
     }
     // A^T at the forward state of this step (already loaded)
     if ((rc = cuda_check(c, launch_fill_ghosts(c), "fill ghosts"))) return rc;
-    cudaMemsetAsync(A->d_err, 0, sizeof(int), c->stream);
     for (int e = 0; e < 3; ++e) A->F[e].n = A->order == 1 ? 2 : 4;
     AdjRec ar;
     ar.p = p;
@@ -483,12 +494,16 @@ int adjoint_step(cf_ctx* c, AdjState* A, const SolveOpts& so, double* rbar) {
         std::swap(A->ag[gsel], A->bg[gsel]);
     }
     c->launches += 6 + (p.per_x || p.per_y ? 3 : 0);
-    int herr = 0;
-    cudaMemcpyAsync(&herr, A->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
-    if ((rc = cuda_check(c, cudaStreamSynchronize(c->stream), "adjoint advection"))) return rc;
-    if (herr)
-        return fail(c, CF_ERR_UNSUPPORTED, "adjoint: a trace moved more than one cell in a step (reduce dt)");
-    return CF_OK;
+    return cuda_check(c, cudaGetLastError(), "adjoint advection");
+}
+
+// The device tally of a run of enqueued projections: a solve that broke
+// down, produced NaN or timed out fails the call (one that stopped at
+// max_iter is tolerated, as cf_step's callers here tolerate it).
+int check_tally(cf_ctx* c, const int* tally, const char* what) {
+    if (tally[0] == 0 || tally[1] == ST_MAXIT) return CF_OK;
+    return fail(c, tally[1] == ST_TIMEOUT ? CF_ERR_TIMEOUT : CF_ERR_NUMERIC, "%s: a pressure solve failed (status %d)",
+                what, tally[1]);
 }
 
 // owned region of an adjoint grid <-> contiguous host array
@@ -553,16 +568,40 @@ int cf_forward_checkpointed(cf_ctx* ctx, int nsteps, int ckpt_every, double dt, 
     A->opts.solver = A->solver.c_str();
     A->opts.precon = A->precon.c_str();
     A->ready = false;
-    cf_solve_stats st{};
-    for (int k = 0; k < nsteps; ++k) {
-        if (k % ckpt_every == 0 && (rc = save_state(ctx, A->ckpt[k / ckpt_every]))) return rc;
-        rc = cf_step(ctx, dt, value_order, &A->opts, &st);
-        if (rc && rc != CF_ERR_NOT_CONVERGED) return rc;
+    SolveOpts so{};
+    if ((rc = parse_solver_opts(ctx, &A->opts, &so))) return rc;
+    // the steps go back to back on the stream (checkpoint copies between
+    // them), one synchronisation at the end
+    rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_tally, 0, 3 * sizeof(int), ctx->stream), "tally");
+    SolveResult r{};
+    bool deferred = false;
+    for (int k = 0; k < nsteps && !rc; ++k) {
+        if (k % ckpt_every == 0) rc = save_state(ctx, A->ckpt[k / ckpt_every]);
+        if (!rc) rc = enqueue_step(ctx, dt, value_order, so, &r, &deferred, k > 0);
+        if (!rc && !deferred && r.status != ST_CONVERGED && r.status != ST_MAXIT)
+            rc = fail(ctx, CF_ERR_NUMERIC, "pressure solve failed (status %d)", r.status);
     }
-    if ((rc = save_state(ctx, A->final_state))) return rc;
-    if ((rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "forward"))) return rc;
+    if (!rc) rc = save_state(ctx, A->final_state);
+    int tally[3] = {0, 0, 0};
+    if (!rc)
+        rc = cuda_check(ctx, cudaMemcpyAsync(tally, ctx->d_tally, sizeof(tally), cudaMemcpyDeviceToHost, ctx->stream),
+                        "tally");
+    const int rc1 = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "forward");
+    if (rc) return rc;
+    if (rc1) return rc1;
+    if (deferred) project_collect(ctx, &r, nsteps, tally[2]);
+    if ((rc = check_tally(ctx, tally, "forward"))) return rc;
     A->ready = true;
-    if (last) *last = st;
+    if (last) {
+        *last = cf_solve_stats{};
+        last->iterations = r.iterations;
+        last->outer_iterations = r.outer;
+        last->status = r.status;
+        last->b_norm = sqrt(r.bb);
+        last->r_norm = sqrt(r.rr);
+        last->div_l2 = r.div_l2;
+        last->div_linf = r.div_linf;
+    }
     return CF_OK;
 }
 
@@ -591,26 +630,49 @@ int cf_backward(cf_ctx* ctx, const double* dL_dq_T, const double* dL_du_T, const
     for (int k = 0; k < 3 && !rc; ++k)
         if (seeds[k]) rc = adj_io(ctx, A->ag[k], fields[k], const_cast<double*>(seeds[k]), false);
     if (rc) return rc;
-    double rbar = 0.0;
+    // the forward recomputation, the checkpoint copies and the reverse steps
+    // are all enqueued; one synchronisation at the end reads the tally of
+    // the pressure solves, the trace check and dL/d(rate)
+    SolveOpts fo{};
+    if ((rc = parse_solver_opts(ctx, &A->opts, &fo))) return rc;
+    cudaMemsetAsync(ctx->d_tally, 0, 3 * sizeof(int), ctx->stream);
+    cudaMemsetAsync(A->d_err, 0, sizeof(int), ctx->stream);
+    cudaMemsetAsync(A->d_rbar, 0, sizeof(double), ctx->stream);
     const int C = A->every, T = A->nsteps;
     const int nseg = (T + C - 1) / C;
-    cf_solve_stats st{};
+    SolveResult r{};
+    bool deferred = false, fwd_params = false, adj_params = false;
     for (int sg = nseg - 1; sg >= 0 && !rc; --sg) {
         const int k0 = sg * C, k1 = (k0 + C < T) ? k0 + C : T;
         rc = load_state(ctx, A->ckpt[sg]);
         for (int k = k0; k < k1 && !rc; ++k) {
             rc = save_state(ctx, A->seg[k - k0]);
             if (!rc && k < k1 - 1) {
-                rc = cf_step(ctx, A->dt, A->order, &A->opts, &st);
-                if (rc == CF_ERR_NOT_CONVERGED) rc = CF_OK;
+                rc = enqueue_step(ctx, A->dt, A->order, fo, &r, &deferred, fwd_params);
+                fwd_params = true;
+                if (!rc && !deferred && r.status != ST_CONVERGED && r.status != ST_MAXIT)
+                    rc = fail(ctx, CF_ERR_NUMERIC, "pressure solve failed (status %d)", r.status);
             }
         }
         for (int k = k1 - 1; k >= k0 && !rc; --k) {
             rc = load_state(ctx, A->seg[k - k0]);
-            if (!rc) rc = adjoint_step(ctx, A, so, &rbar);
+            if (!rc) rc = adjoint_step(ctx, A, so, adj_params);
+            adj_params = true;
         }
     }
+    int tally[3] = {0, 0, 0}, herr = 0;
+    double rbar = 0.0;
+    if (!rc) {
+        cudaMemcpyAsync(tally, ctx->d_tally, sizeof(tally), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(&herr, A->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(&rbar, A->d_rbar, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+    }
+    const int rc1 = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "backward");
     if (rc) return rc;
+    if (rc1) return rc1;
+    if ((rc = check_tally(ctx, tally, "backward"))) return rc;
+    if (herr)
+        return fail(ctx, CF_ERR_UNSUPPORTED, "adjoint: a trace moved more than one cell in a step (reduce dt)");
     if (dL_dq0) rc = adj_io(ctx, A->ag[0], CF_FIELD_QUANTITY, dL_dq0, true);
     if (!rc && dL_du0) rc = adj_io(ctx, A->ag[1], CF_FIELD_U, dL_du0, true);
     if (!rc && dL_dv0) rc = adj_io(ctx, A->ag[2], CF_FIELD_V, dL_dv0, true);

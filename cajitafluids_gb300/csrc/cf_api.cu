@@ -209,6 +209,26 @@ int record_advect(cf_ctx* c) {
 
 }  // namespace
 
+namespace cf {
+// One Solver::step (src/Solver.hpp:135-147) enqueued on the context's stream:
+// ghost fills, advection (inputs fused unless the force is density-scaled),
+// then the projection, deferred when the resident graph serves it (the
+// caller synchronises and collects; a resident projection adds to the
+// device tally when it does not converge).  params_ready: the projection's
+// parameters were written by an earlier enqueued step with the same options.
+int enqueue_step(cf_ctx* ctx, double dt, int value_order, const SolveOpts& so, SolveResult* r, bool* deferred,
+                 bool params_ready) {
+    const bool fuse = !ctx->ph.force_density;
+    int rc = cuda_check(ctx, launch_fill_ghosts(ctx), "fill ghosts");
+    if (!rc) rc = cuda_check(ctx, launch_advect(ctx, dt, value_order, fuse ? 1 : 0), "advect");
+    if (!rc && !fuse) rc = cuda_check(ctx, launch_add_inputs(ctx, dt), "add inputs");
+    if (!rc) rc = project_async(ctx, dt, so, r, deferred, params_ready);
+    return rc;
+}
+
+int parse_solver_opts(cf_ctx* ctx, const cf_solver_opts* opts, SolveOpts* so) { return parse_opts(ctx, opts, so); }
+}  // namespace cf
+
 extern "C" {
 
 int cf_abi_version(void) { return CF_ABI_VERSION; }
@@ -302,6 +322,7 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
     if (!rc) rc = alloc_dev(c, c->staging, c->staging_elems);
     if (!rc) rc = cuda_check(c, cudaMallocHost(&c->hS, sizeof(SolverState)), "cudaMallocHost");
     if (!rc) rc = cuda_check(c, cudaMallocHost(&c->hP, sizeof(SolverState)), "cudaMallocHost");
+    if (!rc) rc = cuda_check(c, cudaMallocHost(&c->hPa, sizeof(SolverState)), "cudaMallocHost");
     if (!rc) rc = alloc_dev(c, c->d_tally, 4);
     if (!rc) rc = cuda_check(c, cudaMallocHost(&c->h_out, 4 * sizeof(double)), "cudaMallocHost");
     if (!rc && c->precision == CF_PREC_MIXED) rc = cg32_setup(c);
@@ -332,6 +353,7 @@ int cf_ctx_destroy(cf_ctx* ctx) {
     for (void* p : ctx->allocs) cudaFree(p);
     if (ctx->hS) cudaFreeHost(ctx->hS);
     if (ctx->hP) cudaFreeHost(ctx->hP);
+    if (ctx->hPa) cudaFreeHost(ctx->hPa);
     if (ctx->h_out) cudaFreeHost(ctx->h_out);
     if (ctx->stream2) {
         cudaStreamSynchronize(ctx->stream2);
@@ -643,7 +665,7 @@ int cf_steps(cf_ctx* ctx, int nsteps, double dt, int value_order, const cf_solve
     SolveOpts so{};
     int rc = parse_opts(ctx, opts, &so);
     if (rc) return rc;
-    if (ctx->prof || !resident_projection()) {
+    if (ctx->prof || ctx->direct || !resident_projection()) {
         // host-polled projections: one step at a time
         int bad = 0, worst = CF_OK;
         for (int k = 0; k < nsteps; ++k) {
@@ -658,16 +680,10 @@ int cf_steps(cf_ctx* ctx, int nsteps, double dt, int value_order, const cf_solve
         if (unconverged) *unconverged = bad;
         return worst;
     }
-    const bool fuse = !ctx->ph.force_density;
     rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_tally, 0, 3 * sizeof(int), ctx->stream), "tally");
     SolveResult r{};
     bool deferred = false;
-    for (int k = 0; k < nsteps && !rc; ++k) {
-        rc = cuda_check(ctx, launch_fill_ghosts(ctx), "fill ghosts");
-        if (!rc) rc = cuda_check(ctx, launch_advect(ctx, dt, value_order, fuse ? 1 : 0), "advect");
-        if (!rc && !fuse) rc = cuda_check(ctx, launch_add_inputs(ctx, dt), "add inputs");
-        if (!rc) rc = project_async(ctx, dt, so, &r, &deferred, k > 0);
-    }
+    for (int k = 0; k < nsteps && !rc; ++k) rc = enqueue_step(ctx, dt, value_order, so, &r, &deferred, k > 0);
     int tally[3] = {0, 0, 0};
     if (!rc)
         rc = cuda_check(ctx, cudaMemcpyAsync(tally, ctx->d_tally, sizeof(tally), cudaMemcpyDeviceToHost, ctx->stream),

@@ -44,6 +44,7 @@ struct cf_ctx {
     cf::SolverState* S = nullptr;   // device
     cf::SolverState* hS = nullptr;  // pinned host mirror (solver state copied back)
     cf::SolverState* hP = nullptr;  // pinned solver parameters copied in (not overwritten by a projection)
+    cf::SolverState* hPa = nullptr; // the same for the adjoint's projections
     int* d_tally = nullptr;         // resident projections: [0] unconverged solves, [1] worst status, [2] trips
     double* d_out = nullptr;        // small device output slots
     double* h_out = nullptr;        // pinned host mirror
@@ -69,13 +70,15 @@ struct cf_ctx {
     cudaGraphExec_t gmg_pre = nullptr;  // V-cycle + r.z after the residual is (re)formed
     cf::Stencil gmg_st{};
     int gmg_per_iter = 0, gmg_pre_launches = 0;
-    // device-resident projection graphs, one per current buffer (cf_project.cu)
-    cudaGraphExec_t rgx[2] = {nullptr, nullptr};
-    cf::Stencil rg_st[2]{};
-    cf::Phys rg_ph[2]{};
-    int rg_flags[2] = {-1, -1};
-    int rg_head[2] = {0, 0}, rg_trip[2] = {0, 0}, rg_tail[2] = {0, 0};
-    int rg_pending = 0;  // buffer of the last resident projection launched
+    // device-resident projection graphs (cf_project.cu): slots 0, 1 for the
+    // two state buffers, 2, 3 for the adjoint's two pairs of face arrays
+    cudaGraphExec_t rgx[4] = {nullptr, nullptr, nullptr, nullptr};
+    cf::Stencil rg_st[4]{};
+    cf::Phys rg_ph[4]{};
+    int rg_flags[4] = {-1, -1, -1, -1};
+    const double* rg_u[4] = {nullptr, nullptr, nullptr, nullptr};  // the u array each slot projects
+    int rg_head[4] = {0, 0, 0, 0}, rg_trip[4] = {0, 0, 0, 0}, rg_tail[4] = {0, 0, 0, 0};
+    int rg_pending = 0;  // slot of the last resident projection launched
     // FP32 z = M^-1 r of the mixed MG-PCG, ghost ring as the other FP32 vectors
     cf::Vec32 z32{};
     float* z32b = nullptr;
@@ -141,6 +144,14 @@ int project_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, bo
 void project_collect(cf_ctx* c, SolveResult* res, int nproj = 0, long long trips = 0);
 int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Grid<double> gu, Grid<double> gv,
                   int adjoint);
+// the adjoint's projection of gu, gv, deferred like project_async when the
+// resident graph serves it
+int project_adjoint_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, bool* deferred,
+                          bool params_ready, Grid<double> gu, Grid<double> gv);
+// one step enqueued without a synchronisation (cf_api.cu)
+int enqueue_step(cf_ctx* ctx, double dt, int value_order, const SolveOpts& so, SolveResult* r, bool* deferred,
+                 bool params_ready);
+int parse_solver_opts(cf_ctx* ctx, const cf_solver_opts* opts, SolveOpts* so);
 // FP32 TMA inner CG (cf_cg32.cu)
 int cg32_setup(cf_ctx* c);
 void cg32_launch_iteration(cf_ctx* c, const Stencil& st);

@@ -324,16 +324,23 @@ __device__ __forceinline__ float cub32(const Grid<T>& g, int bi, int bj, float f
     float wx[4], wy[4];
     cubic_w32(tx, wx);
     cubic_w32(ty, wy);
+    // Difference form: c + sum w (f - c) with c = the tap at (ix, iy).  The
+    // FP32 weights do not sum to exactly 1 (2/3 and 1/6 both round up, so
+    // the sum is about 1 + 2.5e-8 per axis); summing w * f directly would
+    // scale the field by that much every step, a drift that grows linearly
+    // over a run.  Against differences the weight error only touches the
+    // local variation of the field, and a constant is reproduced exactly.
+    const float c = (float)__ldg(g.o + (size_t)iy * g.pitch + ix);
     float val = 0.f;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
         const T* row = g.o + (size_t)(iy - 1 + b) * g.pitch + (ix - 1);
-        float rs = wx[0] * (float)__ldg(row);
+        float rs = wx[0] * ((float)__ldg(row) - c);
 #pragma unroll
-        for (int k = 1; k < 4; ++k) rs = fmaf(wx[k], (float)__ldg(row + k), rs);
+        for (int k = 1; k < 4; ++k) rs = fmaf(wx[k], (float)__ldg(row + k) - c, rs);
         val = b == 0 ? wy[0] * rs : fmaf(wy[b], rs, val);
     }
-    return val;
+    return c + val;
 }
 
 template <int ORDER>

@@ -1246,14 +1246,19 @@ static int capture_graph(cf_ctx* c, cudaGraph_t* g, const std::function<void()>&
     return cuda_check(c, cudaStreamEndCapture(c->stream, g), "capture end");
 }
 
-static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, bool mg, int cur) {
+// slot: the cache entry (0, 1: the two state buffers; 2, 3: the adjoint's
+// two pairs of adjoint face arrays); adjoint = 1 builds the transpose of the
+// projection on gu, gv (no wall mask after the gradient subtraction, no
+// warm start, no event for cf_step_host).
+static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, bool mg, int slot, Grid<double> gu,
+                          Grid<double> gv, int adjoint) {
     if (!c->ev_press) {
         int rc0 = cuda_check(c, cudaEventCreateWithFlags(&c->ev_press, cudaEventDisableTiming), "event create");
         if (rc0) return rc0;
     }
     const int nb = red_blocks(c);
     const double scale = -st.ms;
-    Grid<double> gu = c->u[cur], gv = c->v[cur];
+    const int warm = adjoint ? 0 : c->warm;
     cudaGraph_t g = nullptr, head = nullptr, tail = nullptr;
     int nhead = 0, ntrip = 0, ntail = 0;
     int rc = cuda_check(c, cudaGraphCreate(&g, 0), "graph create");
@@ -1262,13 +1267,13 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
             DivArgs da = div_args(c, st);
             da.u = gu;
             da.v = gv;
-            da.warm = c->warm;
+            da.warm = warm;
             if (mixed)
                 k_div_init_mixed<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
             else
                 k_div_init64<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
             nhead = 1;
-            if (c->warm) nhead += launch_warm_init(c, st, mixed);
+            if (warm) nhead += launch_warm_init(c, st, mixed);
             if (mg) {
                 if (mixed) {
                     nhead += cg32_mg_precondition(c, scale);
@@ -1311,12 +1316,12 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
                 k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, c->ph.nx, c->ph.ny, c->vpitch);
                 ntail += 1;
             }
-            Press pa{c->ph, gu, gv, c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx)), 0, c->u32, c->v32,
-                     mixed ? 1 : 0};
+            Press pa{c->ph, gu, gv, c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx)), adjoint, c->u32, c->v32,
+                     (mixed && !adjoint) ? 1 : 0};
             dim3 grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
             k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
             // u, v are final here: a caller may copy them out beside the norms
-            cudaEventRecordWithFlags(c->ev_press, c->stream, cudaEventRecordExternal);
+            if (!adjoint) cudaEventRecordWithFlags(c->ev_press, c->stream, cudaEventRecordExternal);
             DivArgs da = div_args(c, st);
             da.u = gu;
             da.v = gv;
@@ -1327,18 +1332,18 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
             cudaMemcpyAsync(c->h_out, c->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
         });
     if (!rc) rc = cuda_check(c, cudaGraphAddChildGraphNode(&nt, g, &nc, 1, tail), "graph tail");
-    if (c->rgx[cur]) {
-        cudaGraphExecDestroy(c->rgx[cur]);
-        c->rgx[cur] = nullptr;
+    if (c->rgx[slot]) {
+        cudaGraphExecDestroy(c->rgx[slot]);
+        c->rgx[slot] = nullptr;
     }
-    if (!rc) rc = cuda_check(c, cudaGraphInstantiate(&c->rgx[cur], g, 0), "graph instantiate");
+    if (!rc) rc = cuda_check(c, cudaGraphInstantiate(&c->rgx[slot], g, 0), "graph instantiate");
     if (head) cudaGraphDestroy(head);
     if (tail) cudaGraphDestroy(tail);
     if (g) cudaGraphDestroy(g);
     if (rc) return rc;
-    c->rg_head[cur] = nhead;
-    c->rg_trip[cur] = ntrip;
-    c->rg_tail[cur] = ntail;
+    c->rg_head[slot] = nhead;
+    c->rg_trip[slot] = ntrip;
+    c->rg_tail[slot] = ntail;
     return CF_OK;
 }
 
@@ -1353,27 +1358,39 @@ static bool resident_enabled() {
 
 bool resident_projection() { return resident_enabled(); }
 
-// the projection of the current buffers through the resident graph; with
-// defer, returns after the launch (project_collect reads the results)
+// the projection of gu, gv (the current buffers, or with adjoint = 1 the
+// adjoint's face arrays) through a resident graph; with defer, returns after
+// the launch (project_collect reads the results)
 static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, const Stencil& st,
-                            bool mixed, bool mg, bool defer = false, bool params_ready = false) {
-    const int cur = c->cur;
+                            bool mixed, bool mg, bool defer, bool params_ready, Grid<double> gu, Grid<double> gv,
+                            int adjoint) {
+    int slot = c->cur;
+    if (adjoint) {
+        // the adjoint's arrays alternate between two buffers: one slot each
+        slot = c->rg_u[2] == gu.o ? 2 : (c->rg_u[3] == gu.o ? 3 : (c->rg_u[2] ? 3 : 2));
+        if (c->rg_u[slot] != gu.o && c->rg_u[2] && c->rg_u[3]) slot = 2;
+    }
     c->x_only = (mixed && mg && o.inner_tol >= 0.5) ? 1 : 0;
-    const int flags = (mixed ? 1 : 0) | (mg ? 2 : 0) | (c->warm ? 4 : 0) | (c->x_only ? 8 : 0);
+    const int flags = (mixed ? 1 : 0) | (mg ? 2 : 0) | ((c->warm && !adjoint) ? 4 : 0) | (c->x_only ? 8 : 0) |
+                      (adjoint ? 16 : 0);
     int rc = CF_OK;
-    if (!c->rgx[cur] || c->rg_flags[cur] != flags || std::memcmp(&c->rg_st[cur], &st, sizeof(Stencil)) != 0 ||
-        std::memcmp(&c->rg_ph[cur], &c->ph, sizeof(Phys)) != 0) {
-        rc = build_resident(c, st, dt, mixed, mg, cur);
+    if (!c->rgx[slot] || c->rg_flags[slot] != flags || c->rg_u[slot] != gu.o ||
+        std::memcmp(&c->rg_st[slot], &st, sizeof(Stencil)) != 0 ||
+        std::memcmp(&c->rg_ph[slot], &c->ph, sizeof(Phys)) != 0) {
+        rc = build_resident(c, st, dt, mixed, mg, slot, gu, gv, adjoint);
         if (rc) return rc;
-        c->rg_flags[cur] = flags;
-        c->rg_st[cur] = st;
-        c->rg_ph[cur] = c->ph;
+        c->rg_flags[slot] = flags;
+        c->rg_st[slot] = st;
+        c->rg_ph[slot] = c->ph;
+        c->rg_u[slot] = gu.o;
     }
     // The parameters go in from their own pinned buffer: the tail copies the
     // final state back into hS, and a caller that enqueues several steps
     // without synchronising (params_ready: the same parameters, written once)
-    // must not have a later step read an earlier step's final state.
-    SolverState* h = c->hP;
+    // must not have a later step read an earlier step's final state.  The
+    // adjoint's projections have a buffer of their own, so that forward and
+    // adjoint projections can be enqueued in turn.
+    SolverState* h = adjoint ? c->hPa : c->hP;
     if (!params_ready) {
         memset(h, 0, sizeof(SolverState));
         h->tol2 = o.tol * o.tol;
@@ -1389,9 +1406,9 @@ static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResul
         h->test_stall = c->test_stall;
     }
     cudaMemcpyAsync(c->S, h, sizeof(SolverState), cudaMemcpyHostToDevice, c->stream);
-    if ((rc = cuda_check(c, cudaGraphLaunch(c->rgx[cur], c->stream), "graph launch"))) return rc;
-    if (mixed) c->uv32 = 1;  // the graph's gradient subtraction wrote the FP32 velocity copies
-    c->rg_pending = cur;
+    if ((rc = cuda_check(c, cudaGraphLaunch(c->rgx[slot], c->stream), "graph launch"))) return rc;
+    if (mixed && !adjoint) c->uv32 = 1;  // the graph's gradient subtraction wrote the FP32 velocity copies
+    c->rg_pending = slot;
     if (defer) return CF_OK;
     if ((rc = cuda_check(c, cudaStreamSynchronize(c->stream), "projection"))) return rc;
     project_collect(c, res);
@@ -1424,7 +1441,20 @@ int project_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, bo
     int rc = mg ? mg_setup(c) : CF_OK;
     if (rc) return rc;
     *deferred = true;
-    return project_resident(c, dt, o, res, st, mixed, mg, true, params_ready);
+    return project_resident(c, dt, o, res, st, mixed, mg, true, params_ready, c->u[c->cur], c->v[c->cur], 0);
+}
+
+int project_adjoint_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, bool* deferred,
+                          bool params_ready, Grid<double> gu, Grid<double> gv) {
+    *deferred = false;
+    if (c->prof || c->direct || !resident_enabled()) return project_grids(c, dt, o, res, gu, gv, 1);
+    Stencil st{};
+    build_stencil(c, dt, o.precon_none, &st);
+    const bool mg = o.precon_mg != 0;
+    int rc = mg ? mg_setup(c) : CF_OK;
+    if (rc) return rc;
+    *deferred = true;
+    return project_resident(c, dt, o, res, st, c->precision == CF_PREC_MIXED, mg, true, params_ready, gu, gv, 1);
 }
 
 int div_norms(cf_ctx* c, double* l2, double* linf) {
@@ -1459,8 +1489,8 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     // the resident graph serves plain projections; the adjoint's projection
     // (other arrays) and profiled runs (events between batches) take the
     // host-polled batches below
-    if (!adjoint && !c->prof && !c->direct && resident_enabled())
-        return project_resident(c, dt, o, res, st, mixed, mg);
+    if (!c->prof && !c->direct && resident_enabled())
+        return project_resident(c, dt, o, res, st, mixed, mg, false, false, gu, gv, adjoint);
     rc = mg ? ensure_graph_mg(c, st) : ensure_graph(c, st, mixed);
     if (rc) return rc;
 
