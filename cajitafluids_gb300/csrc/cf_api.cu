@@ -9,6 +9,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 
 #include <cstring>
 #include <new>
@@ -254,6 +255,10 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
     }
     cf_ctx* c = ctx;
     c->device = d->device;
+    // CF_GRAPHS=0 in the environment: contexts start with every kernel of the
+    // solve launched on its own (as cf_set_graphs(ctx, 0)), for profilers
+    // that list kernel launches one by one
+    if (const char* e = getenv("CF_GRAPHS")) c->direct = atoi(e) == 0 ? 1 : 0;
     int rc = cuda_check(c, cudaSetDevice(d->device), "cudaSetDevice");
     if (!rc) rc = cuda_check(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream create");
     if (rc) {

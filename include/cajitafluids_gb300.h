@@ -163,7 +163,8 @@ int cf_set_quirks(cf_ctx* ctx, unsigned flags);
  * CUDA graphs (one device-resident graph per projection, or host-polled
  * graph batches).  on = 0: every kernel of the solve is launched on its own
  * and the host polls the solver state between batches, for tools that list
- * kernel launches one by one.  The results are the same bits either way. */
+ * kernel launches one by one.  The results are the same bits either way.
+ * The environment variable CF_GRAPHS=0 sets every new context to on = 0. */
 int cf_set_graphs(cf_ctx* ctx, int on);
 
 /* ---- state (ProblemManager::get / initialize / advance) ---- */
