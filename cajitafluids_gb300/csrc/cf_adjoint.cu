@@ -282,27 +282,26 @@ __global__ void k_adj_mask(Phys p, Grid<double> u, Grid<double> v) {
     }
 }
 
-// per-row sums of the quantity adjoint inside the inflow box
-__global__ void k_adj_box_rows(Phys p, Grid<double> aq, double* rows) {
-    const int gj = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gj >= p.ny) return;
-    double y = p.gl[1] + ((double)(gj + CF_HALO) + 0.5) * p.dx;
+// dL/d(rate) += dt * (sum of the quantity adjoint over the inflow box's
+// cells).  One block: the box's cells (local index ranges the host found
+// with the forward's coordinate test) in row-major order, thread t taking
+// cells t, t + 256, ...; then a fixed-order block sum, so the result is
+// deterministic.
+constexpr int kBoxThreads = 256;
+__global__ void __launch_bounds__(kBoxThreads) k_adj_rate(Phys p, Grid<double> aq, double dt, double* rbar) {
+    const int i0 = p.box[E_CELL][0], i1 = p.box[E_CELL][1], j0 = p.box[E_CELL][2], j1 = p.box[E_CELL][3];
+    const int w = i1 - i0, n = w > 0 && j1 > j0 ? w * (j1 - j0) : 0;
     double s = 0.0;
-    if (y >= p.bbox[1] && y < p.bbox[3])
-        for (int gi = 0; gi < p.nx; ++gi) {
-            double x = p.gl[0] + ((double)(gi + CF_HALO) + 0.5) * p.dx;
-            if (x >= p.bbox[0] && x < p.bbox[2]) s = s + aq.at(gi + CF_HALO, gj + CF_HALO);
-        }
-    rows[gj] = s;
-}
-
-// --------------------------------------------------------------------------
-// sum of the box rows in row order, times dt, added to the rate adjoint
-// (one thread: the same order as a host loop over the rows)
-__global__ void k_adj_rate_acc(const double* rows, int ny, double dt, double* rbar) {
-    double s = 0.0;
-    for (int r = 0; r < ny; ++r) s += rows[r];
-    *rbar += dt * s;
+    for (int k = threadIdx.x; k < n; k += kBoxThreads) s = s + aq.at(i0 + k % w, j0 + k / w);
+    __shared__ double ws[kBoxThreads / 32];
+    s = warp_fold(s);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = ws[0];
+        for (int k = 1; k < kBoxThreads / 32; ++k) t = t + ws[k];
+        *rbar += dt * t;
+    }
 }
 
 // host side
@@ -324,6 +323,10 @@ struct AdjState {
     int* d_err = nullptr;
     double* d_rows = nullptr;
     double* d_rbar = nullptr;  // dL/d(rate), accumulated on the device
+    double* xa = nullptr;      // the adjoint pressure between reverse steps (the warm start)
+    // the forward pass left the last segment's states in seg: the backward's
+    // first segment needs no recomputation (cleared once seg is reused)
+    bool last_seg_valid = false;
     std::vector<void*> allocs;
 };
 
@@ -423,6 +426,7 @@ int setup_records(cf_ctx* c, AdjState* A) {
     if (!rc) rc = dalloc(c, A, (void**)&A->d_err, sizeof(int));
     if (!rc) rc = dalloc(c, A, (void**)&A->d_rows, sizeof(double) * (c->ph.ny + 1));
     if (!rc) rc = dalloc(c, A, (void**)&A->d_rbar, sizeof(double));
+    if (!rc) rc = dalloc(c, A, (void**)&A->xa, sizeof(double) * (size_t)c->vpitch * c->ph.ny);
     return rc;
 }
 
@@ -437,18 +441,25 @@ int adjoint_step(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_ready)
     int rc;
     // P^T: mask, then the projection pipeline without the final mask
     k_adj_mask<<<dim3((p.nx + 2 + 31) / 32, (p.ny + 2 + 7) / 8, 2), blk, 0, c->stream>>>(p, A->ag[1], A->ag[2]);
+    // the solve starts from the previous reverse step's adjoint pressure
+    // (zero for the first), kept in A->xa between steps because the
+    // forward recomputation reuses the solver's solution vector
+    const size_t xbytes = sizeof(double) * (size_t)c->vpitch * p.ny;
+    if ((rc = cuda_check(c, cudaMemcpyAsync(c->x.a, A->xa, xbytes, cudaMemcpyDeviceToDevice, c->stream), "adjoint x")))
+        return rc;
     SolveResult res{};
     bool deferred = false;
     if ((rc = project_adjoint_async(c, A->dt, so, &res, &deferred, params_ready, A->ag[1], A->ag[2]))) return rc;
     if (!deferred && res.status != ST_CONVERGED && res.status != ST_MAXIT)
         return fail(c, CF_ERR_NUMERIC, "adjoint projection failed (status %d)", res.status);
+    if ((rc = cuda_check(c, cudaMemcpyAsync(A->xa, c->x.a, xbytes, cudaMemcpyDeviceToDevice, c->stream), "adjoint x")))
+        return rc;
     // I^T: wall masks of the inputs; dL/dQ from the rate source
     k_adj_mask<<<dim3((p.nx + 2 + 31) / 32, (p.ny + 2 + 7) / 8, 2), blk, 0, c->stream>>>(p, A->ag[1], A->ag[2]);
     bool src_active = p.bbox[2] > p.bbox[0] && p.bbox[3] > p.bbox[1];
     if (src_active && p.src_mode == 1) {
-        k_adj_box_rows<<<(p.ny + 127) / 128, 128, 0, c->stream>>>(p, A->ag[0], A->d_rows);
-        k_adj_rate_acc<<<1, 1, 0, c->stream>>>(A->d_rows, p.ny, A->dt, A->d_rbar);
-        c->launches += 2;
+        k_adj_rate<<<1, kBoxThreads, 0, c->stream>>>(p, A->ag[0], A->dt, A->d_rbar);
+        c->launches += 1;
     }
     // A^T at the forward state of this step (already loaded)
     if ((rc = cuda_check(c, launch_fill_ghosts(c), "fill ghosts"))) return rc;
@@ -575,8 +586,12 @@ int cf_forward_checkpointed(cf_ctx* ctx, int nsteps, int ckpt_every, double dt, 
     rc = cuda_check(ctx, cudaMemsetAsync(ctx->d_tally, 0, 3 * sizeof(int), ctx->stream), "tally");
     SolveResult r{};
     bool deferred = false;
+    // the last segment's states also go to the segment buffers, so the
+    // backward starts its reverse sweep without recomputing them
+    const int k_last = (nck - 1) * ckpt_every;
     for (int k = 0; k < nsteps && !rc; ++k) {
         if (k % ckpt_every == 0) rc = save_state(ctx, A->ckpt[k / ckpt_every]);
+        if (!rc && k >= k_last) rc = save_state(ctx, A->seg[k - k_last]);
         if (!rc) rc = enqueue_step(ctx, dt, value_order, so, &r, &deferred, k > 0);
         if (!rc && !deferred && r.status != ST_CONVERGED && r.status != ST_MAXIT)
             rc = fail(ctx, CF_ERR_NUMERIC, "pressure solve failed (status %d)", r.status);
@@ -592,6 +607,7 @@ int cf_forward_checkpointed(cf_ctx* ctx, int nsteps, int ckpt_every, double dt, 
     if (deferred) project_collect(ctx, &r, nsteps, tally[2]);
     if ((rc = check_tally(ctx, tally, "forward"))) return rc;
     A->ready = true;
+    A->last_seg_valid = true;
     if (last) {
         *last = cf_solve_stats{};
         last->iterations = r.iterations;
@@ -638,14 +654,18 @@ int cf_backward(cf_ctx* ctx, const double* dL_dq_T, const double* dL_du_T, const
     cudaMemsetAsync(ctx->d_tally, 0, 3 * sizeof(int), ctx->stream);
     cudaMemsetAsync(A->d_err, 0, sizeof(int), ctx->stream);
     cudaMemsetAsync(A->d_rbar, 0, sizeof(double), ctx->stream);
+    cudaMemsetAsync(A->xa, 0, sizeof(double) * (size_t)ctx->vpitch * ctx->ph.ny, ctx->stream);
+    ctx->adj_warm = 1;
     const int C = A->every, T = A->nsteps;
     const int nseg = (T + C - 1) / C;
     SolveResult r{};
     bool deferred = false, fwd_params = false, adj_params = false;
     for (int sg = nseg - 1; sg >= 0 && !rc; --sg) {
         const int k0 = sg * C, k1 = (k0 + C < T) ? k0 + C : T;
-        rc = load_state(ctx, A->ckpt[sg]);
-        for (int k = k0; k < k1 && !rc; ++k) {
+        const bool stored = sg == nseg - 1 && A->last_seg_valid;
+        A->last_seg_valid = false;  // seg is about to be reused
+        if (!stored) rc = load_state(ctx, A->ckpt[sg]);
+        for (int k = k0; k < k1 && !rc && !stored; ++k) {
             rc = save_state(ctx, A->seg[k - k0]);
             if (!rc && k < k1 - 1) {
                 rc = enqueue_step(ctx, A->dt, A->order, fo, &r, &deferred, fwd_params);
@@ -668,6 +688,7 @@ int cf_backward(cf_ctx* ctx, const double* dL_dq_T, const double* dL_du_T, const
         cudaMemcpyAsync(&rbar, A->d_rbar, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
     }
     const int rc1 = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "backward");
+    ctx->adj_warm = 0;
     if (rc) return rc;
     if (rc1) return rc1;
     if ((rc = check_tally(ctx, tally, "backward"))) return rc;

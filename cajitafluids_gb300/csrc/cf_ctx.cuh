@@ -15,6 +15,10 @@ struct cf_ctx {
     int precision = 0;
     double density = 1.0;
     int warm = 0;  // start each projection from the previous pressure (cf_set_warm_start)
+    // the adjoint's transposed projections start from the previous reverse
+    // step's adjoint pressure (set by cf_backward, which keeps that pressure
+    // in a vector of its own between steps)
+    int adj_warm = 0;
     // mixed MG-PCG with a reliable update after every iteration (threshold >=
     // 0.5): the inner step only advances x (set per projection from its options)
     int x_only = 0;

@@ -1304,7 +1304,7 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
     }
     const int nb = red_blocks(c);
     const double scale = -st.ms;
-    const int warm = adjoint ? 0 : c->warm;
+    const int warm = adjoint ? c->adj_warm : c->warm;
     cudaGraph_t g = nullptr, head = nullptr, tail = nullptr;
     int nhead = 0, ntrip = 0, ntail = 0;
     int rc = cuda_check(c, cudaGraphCreate(&g, 0), "graph create");
@@ -1412,7 +1412,7 @@ static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResul
         if (c->rg_u[slot] != gu.o && c->rg_u[2] && c->rg_u[3]) slot = 2;
     }
     c->x_only = (mixed && mg && o.inner_tol >= 0.5) ? 1 : 0;
-    const int flags = (mixed ? 1 : 0) | (mg ? 2 : 0) | ((c->warm && !adjoint) ? 4 : 0) | (c->x_only ? 8 : 0) |
+    const int flags = (mixed ? 1 : 0) | (mg ? 2 : 0) | ((adjoint ? c->adj_warm : c->warm) ? 4 : 0) | (c->x_only ? 8 : 0) |
                       (adjoint ? 16 : 0);
     int rc = CF_OK;
     if (!c->rgx[slot] || c->rg_flags[slot] != flags || c->rg_u[slot] != gu.o ||
@@ -1559,7 +1559,7 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     DivArgs da = div_args(c, st);
     da.u = gu;
     da.v = gv;
-    const bool warm = c->warm && !adjoint;
+    const bool warm = adjoint ? c->adj_warm != 0 : c->warm != 0;
     da.warm = warm;
     if (c->prof) cudaEventRecord(c->ev[4], c->stream);
     if (!mixed) {
