@@ -139,7 +139,6 @@ SIGNATURES = {
     "cf_test_stall_wait": (ctypes.c_int, [_vp, ctypes.c_int]),
     "cf_set_graphs": (ctypes.c_int, [_vp, ctypes.c_int]),
     "cf_test_conversions": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_float), _dp]),
-    "cf_test_split": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_float)]),
     "cf_test_strip_geometry": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                               ctypes.c_int, _ip, _ip, ctypes.c_int]),
     "cf_interp_points": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]),

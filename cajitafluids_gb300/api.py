@@ -271,14 +271,6 @@ class Context:
                                                  w.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return f, w
 
-    def test_split(self, d: np.ndarray):
-        """The device's double-float split of d: (hi, lo) FP32 arrays."""
-        d = np.ascontiguousarray(d, dtype=np.float64).ravel()
-        out = np.empty(2 * d.size, dtype=np.float32)
-        self._check(self.lib.cf_test_split(self.h, d.size, d.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
-                                           out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
-        return out[0::2].copy(), out[1::2].copy()
-
     def max_velocity(self) -> float:
         a = ctypes.c_double()
         self._check(self.lib.cf_max_velocity(self.h, ctypes.byref(a)))

@@ -523,11 +523,7 @@ int cf_download(cf_ctx* ctx, int field, double* host, ptrdiff_t si, ptrdiff_t sj
     const double* src;
     size_t spitch;
     int rc = CF_OK;
-    if (field == CF_FIELD_PRESSURE && ctx->precision == CF_PREC_MIXED) {
-        rc = pressure_to_f64(ctx, ctx->staging);
-        src = ctx->staging;
-        spitch = ox;
-    } else if (field == CF_FIELD_PRESSURE) {
+    if (field == CF_FIELD_PRESSURE) {
         src = ctx->x.a;
         spitch = ctx->vpitch;
     } else if (field == CF_FIELD_QUANTITY && ctx->precision == CF_PREC_MIXED) {
@@ -868,26 +864,6 @@ int cf_div_norms(cf_ctx* ctx, double* l2, double* linf) {
     if (!ctx || !l2 || !linf) return CF_ERR_INVALID;
     cudaSetDevice(ctx->device);
     return div_norms(ctx, l2, linf);
-}
-
-int cf_test_split(cf_ctx* ctx, int n, const double* d, float* hilo) {
-    if (!ctx || n < 0 || (n > 0 && (!d || !hilo))) return CF_ERR_INVALID;
-    if (n == 0) return CF_OK;
-    CF_GUARD_BEGIN
-    cudaSetDevice(ctx->device);
-    double* dd = nullptr;
-    float2* dp = nullptr;
-    int rc = cuda_check(ctx, cudaMalloc(&dd, sizeof(double) * n), "alloc");
-    if (!rc) rc = cuda_check(ctx, cudaMalloc(&dp, sizeof(float2) * n), "alloc");
-    if (!rc) rc = cuda_check(ctx, cudaMemcpyAsync(dd, d, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream), "copy");
-    if (!rc) rc = cuda_check(ctx, launch_test_split(ctx, n, dd, dp), "split");
-    if (!rc)
-        rc = cuda_check(ctx, cudaMemcpyAsync(hilo, dp, sizeof(float2) * n, cudaMemcpyDeviceToHost, ctx->stream), "copy");
-    if (!rc) rc = sync(ctx, "split");
-    cudaFree(dd);
-    cudaFree(dp);
-    return rc;
-    CF_GUARD_END
 }
 
 int cf_test_conversions(cf_ctx* ctx, int n, const double* d, float* f, double* w) {

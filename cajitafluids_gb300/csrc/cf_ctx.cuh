@@ -122,7 +122,6 @@ cudaError_t launch_trace_points(cf_ctx* c, int n, const double* d_xy, double dt,
 cudaError_t launch_cell_velocity(cf_ctx* c, double* d_uc, double* d_vc);
 cudaError_t launch_max_velocity(cf_ctx* c, double* d_out);
 cudaError_t launch_test_convert(cf_ctx* c, int n, const double* d, float* f, double* w);
-cudaError_t launch_test_split(cf_ctx* c, int n, const double* d, float2* out);
 cudaError_t launch_convert_q(cf_ctx* c, int to_device, int version, cudaStream_t stream = nullptr);
 cudaError_t launch_q_to_f64(cf_ctx* c, int version, double* dst, cudaStream_t stream);
 
@@ -164,8 +163,6 @@ int cg32_mg_setup(cf_ctx* c);
 int cg32_mg_precondition(cf_ctx* c, double scale);  // returns kernels launched
 void cg32_launch_pair_mg(cf_ctx* c, const Stencil& st);
 int div_norms(cf_ctx* c, double* l2, double* linf);
-// mixed: the double-float solution as an FP64 pressure (owned, row pitch nx)
-int pressure_to_f64(cf_ctx* c, double* out);
 // multigrid preconditioner (cf_mg.cu)
 int mg_setup(cf_ctx* c);
 void mg_free(cf_ctx* c);

@@ -689,19 +689,6 @@ cudaError_t launch_test_convert(cf_ctx* c, int n, const double* d, float* f, dou
     return cudaGetLastError();
 }
 
-__global__ void k_test_split(int n, const double* d, float2* out) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    out[k] = df_split_bits(d[k]);
-}
-
-cudaError_t launch_test_split(cf_ctx* c, int n, const double* d, float2* out) {
-    if (n <= 0) return cudaSuccess;
-    k_test_split<<<(n + 255) / 256, 256, 0, c->stream>>>(n, d, out);
-    c->launches += 1;
-    return cudaGetLastError();
-}
-
 cudaError_t launch_max_velocity(cf_ctx* c, double* d_out) {
     const Phys& p = c->ph;
     int s = c->cur;

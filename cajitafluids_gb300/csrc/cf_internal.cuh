@@ -287,34 +287,6 @@ __device__ __forceinline__ float2 df_quick(float a, float b) {  // |a| >= |b|
     float s = a + b;
     return make_float2(s, b - (s - a));
 }
-// An FP64 value as a double-float pair without FP64 arithmetic: hi = v
-// rounded to FP32 (d2f_rn's integer rounding), lo = the rest v - hi, formed
-// exactly as an integer (the low 29 significand bits, less 2^29 when hi
-// rounded up) and converted with one int-to-float rounding, so lo keeps the
-// next 24 bits: about 48 significant bits in all.  Values whose hi or lo
-// would leave FP32's normal range (and zeros' signs aside, nothing else
-// here) take the FP64 path.
-__device__ __forceinline__ float2 df_split_bits(double v) {
-    const unsigned hi = (unsigned)__double2hiint(v), lo = (unsigned)__double2loint(v);
-    const unsigned e = (hi >> 20) & 0x7ffu;
-    const bool zero = (hi & 0x7fffffffu) == 0u && lo == 0u;
-    const bool fast = zero || (e >= 949u && e <= 1150u);
-    if (__all_sync(__activemask(), fast)) {
-        if (zero) return make_float2(0.f, 0.f);
-        const unsigned m23 = ((hi & 0xfffffu) << 3) | (lo >> 29);
-        const unsigned rest = lo & 0x1fffffffu, half = 0x10000000u;
-        const unsigned up = (rest > half || (rest == half && (m23 & 1u))) ? 1u : 0u;
-        const unsigned sign = hi & 0x80000000u;
-        const float fhi = __uint_as_float(sign | ((((e - 896u) << 23) | m23) + up));
-        const int r = up ? (int)rest - (int)0x20000000u : (int)rest;  // v - hi in units of 2^(e - 1075)
-        const float scale = __uint_as_float((e - 1075u + 127u) << 23);  // 2^(e - 1075), normal for e >= 949
-        const float flo = __fmul_rn(__int2float_rn(sign ? -r : r), scale);
-        return make_float2(fhi, flo);
-    }
-    const float fh = __double2float_rn(v);
-    return make_float2(fh, __double2float_rn(v - (double)fh));
-}
-
 // double-float + FP32
 __device__ __forceinline__ float2 df_add_f(float2 x, float e) {
     float2 s = df_two_sum(x.x, e);

@@ -412,7 +412,10 @@ __device__ __forceinline__ float2 df_mul(float2 x, float2 y) {
     e = fmaf(x.y, y.x, e);
     return df_quick(p, e);
 }
-__device__ __forceinline__ float2 df_neg(float2 x) { return make_float2(-x.x, -x.y); }
+__device__ __forceinline__ float2 df_split(double v) {
+    const float hi = d2f_rn(v);
+    return make_float2(hi, d2f_rn(v - f2d_exact(hi)));
+}
 
 // FP64 init: b, r = b, x = 0, partial r.z and r.r
 __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init64(DivArgs a) {
@@ -485,27 +488,20 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
             for (int s = 0; s < 2; ++s) {
                 int c = c0 + s;
                 if (c >= a.nx) continue;
-                // the divergence ((u_E - u_W) + v_N) - v_S and its scale
-                // -1/dx in double-float on the FP32 pipe: the FP64 face
-                // values split into pairs on the integer pipe (48 bits kept,
-                // far more than the 1e-8 divergence target needs), no FP64
-                // arithmetic
+                // the divergence sum in FP64 (it cancels), its scale -1/dx as
+                // a double-float product on the FP32 pipe
                 int ie = c + 1, jn = j + 1;
                 if (a.per_x && ie == a.nx) ie = 0;
                 if (a.per_y && jn == a.ny) jn = 0;
-                const float2 ue = df_split_bits(a.u.at(ie + CF_HALO, j + CF_HALO));
-                const float2 uw = df_split_bits(a.u.at(c + CF_HALO, j + CF_HALO));
-                const float2 vn = df_split_bits(a.v.at(c + CF_HALO, jn + CF_HALO));
-                const float2 vs = df_split_bits(a.v.at(c + CF_HALO, j + CF_HALO));
-                float2 t = df_add(ue, df_neg(uw));
-                t = df_add(t, vn);
-                t = df_add(t, df_neg(vs));
+                double t = a.u.at(ie + CF_HALO, j + CF_HALO) - a.u.at(c + CF_HALO, j + CF_HALO);
+                t = t + a.v.at(c + CF_HALO, jn + CF_HALO);
+                t = t - a.v.at(c + CF_HALO, j + CF_HALO);
                 const size_t k = (size_t)j * a.pitch + c;
-                const float2 bs = df_mul(a.mscale2, t);
+                const float2 bs = df_mul(a.mscale2, df_split(t));
                 reinterpret_cast<float2*>(a.b)[k] = bs;
                 // x as a double-float pair: 0, or (warm start) the previous
-                // solution, which a mixed context keeps as pairs
-                if (!a.warm) reinterpret_cast<float2*>(a.x)[k] = make_float2(0.f, 0.f);
+                // FP64 solution split in place (same 8 bytes per cell)
+                reinterpret_cast<float2*>(a.x)[k] = a.warm ? df_split(a.x[k]) : make_float2(0.f, 0.f);
                 const float r = bs.x;
                 put_r32(a.r32, a.pitch32, a.nx, a.ny, a.per_x, a.per_y, c, j, r);
                 float z = a.st.minv32[edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y)] * r;
@@ -794,14 +790,14 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
     }
 }
 
-// mixed: the double-float solution to an FP64 pressure (owned cells, row
-// pitch nx) for a download
-__global__ void k_df_to_f64(const double* x, int nx, int ny, int pitch, double* out) {
+// mixed: the double-float solution, in place, to FP64 for the gradient
+__global__ void k_df_to_f64(double* x, int nx, int ny, int pitch) {
     int gi = blockIdx.x * blockDim.x + threadIdx.x;
     int gj = blockIdx.y * blockDim.y + threadIdx.y;
     if (gi >= nx || gj >= ny) return;
-    const float2 v = reinterpret_cast<const float2*>(x)[(size_t)gj * pitch + gi];
-    out[(size_t)gj * nx + gi] = f2d_exact(v.x) + f2d_exact(v.y);
+    const size_t k = (size_t)gj * pitch + gi;
+    const float2 v = reinterpret_cast<const float2*>(x)[k];
+    x[k] = f2d_exact(v.x) + f2d_exact(v.y);
 }
 
 // --------------------------------------------------------------------------
@@ -819,35 +815,12 @@ struct Press {
     // copies (the next FP32 advection's velocity arrays)
     Grid<float> u32, v32;
     int w32;
-    // mixed: x holds the double-float solution (hi, lo pairs): the pressure
-    // difference and its product with ms2 (= ms as a pair) run on the FP32
-    // pipe, and one exact assembly plus one FP64 addition apply it
-    int xdf;
-    float2 ms2;
 };
 
 __device__ __forceinline__ double pval(const Press& a, int gi, int gj) {
     int ci = wrap_index(gi, a.p.nx, a.p.per_x), cj = wrap_index(gj, a.p.ny, a.p.per_y);
     if (ci < 0 || cj < 0) return 0.0;
     return a.x[(size_t)cj * a.pitch + ci];
-}
-
-__device__ __forceinline__ float2 pval_df(const Press& a, int gi, int gj) {
-    int ci = wrap_index(gi, a.p.nx, a.p.per_x), cj = wrap_index(gj, a.p.ny, a.p.per_y);
-    if (ci < 0 || cj < 0) return make_float2(0.f, 0.f);
-    return reinterpret_cast<const float2*>(a.x)[(size_t)cj * a.pitch + ci];
-}
-
-// w + ms (p(c) - p(n)): FP64 as the reference writes it, or from the
-// double-float solution (two FP64 additions instead of three FP64
-// operations and a separate conversion of the solution)
-__device__ __forceinline__ double press_update(const Press& a, double w, int ci, int cj, int ni, int nj) {
-    if (a.xdf) {
-        const float2 c = df_mul(a.ms2, df_add(pval_df(a, ci, cj), df_neg(pval_df(a, ni, nj))));
-        return w + (f2d_exact(c.x) + f2d_exact(c.y));
-    }
-    const double d = pval(a, ci, cj) - pval(a, ni, nj);
-    return __dadd_rn(w, __dmul_rn(a.ms, d));
 }
 
 __global__ void k_apply_pressure(Press a) {
@@ -863,7 +836,8 @@ __global__ void k_apply_pressure(Press a) {
         double& u = a.u.at(gi + CF_HALO, gj + CF_HALO);
         // u -= scale * (p(i) - p(i-1)) (src/VelocityCorrector.hpp:245), one
         // rounding per operation; ms = -scale, so u + ms*d gives those bits
-        double w = press_update(a, u, gi, gj, gi - 1, gj);
+        double d = pval(a, gi, gj) - pval(a, gi - 1, gj);
+        double w = __dadd_rn(u, __dmul_rn(a.ms, d));
         if (!a.adjoint) {
             if (!p.per_x) {
                 if (gi <= 0 && p.bc[0] == 0) w = 0.0;
@@ -875,7 +849,8 @@ __global__ void k_apply_pressure(Press a) {
         if (a.w32) a.u32.at(gi + CF_HALO, gj + CF_HALO) = d2f_rn(w);
     } else {
         double& v = a.v.at(gi + CF_HALO, gj + CF_HALO);
-        double w = press_update(a, v, gi, gj, gi, gj - 1);  // :256
+        double d = pval(a, gi, gj) - pval(a, gi, gj - 1);
+        double w = __dadd_rn(v, __dmul_rn(a.ms, d));  // :256
         if (!p.per_y && !a.adjoint) {
             if (fix_q1) {
                 if (gj <= 0 && p.bc[1] == 0) w = 0.0;
@@ -975,27 +950,6 @@ static DivArgs div_args(cf_ctx* c, const Stencil& st) {
     a.out = c->d_out;
     a.S = c->S;
     return a;
-}
-
-// the gradient subtraction's arguments; a mixed context's solution x is a
-// double-float pair per cell (it stays one: the FP64 pressure is made only
-// when it is downloaded)
-static Press press_args(cf_ctx* c, double dt, Grid<double> gu, Grid<double> gv, int adjoint, bool w32) {
-    Press pa{};
-    pa.p = c->ph;
-    pa.u = gu;
-    pa.v = gv;
-    pa.x = c->x.a;
-    pa.pitch = c->vpitch;
-    pa.ms = -(dt / (c->density * c->ph.dx));
-    pa.adjoint = adjoint;
-    pa.u32 = c->u32;
-    pa.v32 = c->v32;
-    pa.w32 = w32 ? 1 : 0;
-    pa.xdf = c->precision == CF_PREC_MIXED ? 1 : 0;
-    const float hi = (float)pa.ms;
-    pa.ms2 = make_float2(hi, (float)(pa.ms - (double)hi));
-    return pa;
 }
 
 static Cg64 cg64_args(cf_ctx* c, const Stencil& st) {
@@ -1357,8 +1311,13 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
     if (!rc)
         rc = capture_graph(c, &tail, [&] {
             dim3 blk(32, 8);
-            // mixed: the gradient reads the double-float solution itself
-            Press pa = press_args(c, dt, gu, gv, adjoint, mixed && !adjoint);
+            if (mixed) {
+                dim3 grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
+                k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, c->ph.nx, c->ph.ny, c->vpitch);
+                ntail += 1;
+            }
+            Press pa{c->ph, gu, gv, c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx)), adjoint, c->u32, c->v32,
+                     (mixed && !adjoint) ? 1 : 0};
             dim3 grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
             k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
             // u, v are final here: a caller may copy them out beside the norms
@@ -1498,13 +1457,6 @@ int project_adjoint_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult*
     return project_resident(c, dt, o, res, st, c->precision == CF_PREC_MIXED, mg, true, params_ready, gu, gv, 1);
 }
 
-int pressure_to_f64(cf_ctx* c, double* out) {
-    dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
-    k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, c->ph.nx, c->ph.ny, c->vpitch, out);
-    c->launches += 1;
-    return cuda_check(c, cudaGetLastError(), "pressure conversion");
-}
-
 int div_norms(cf_ctx* c, double* l2, double* linf) {
     Stencil st{};
     DivArgs a = div_args(c, st);
@@ -1635,6 +1587,11 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
             }
         }
     }
+    if (mixed) {
+        dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
+        k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, c->ph.nx, c->ph.ny, c->vpitch);
+        c->launches += 1;
+    }
     const SolverState* hs = c->hS;
     res->iterations = hs->iter;
     res->outer = hs->outer_iter;
@@ -1644,7 +1601,8 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
 
     // gradient subtraction
     const bool w32 = mixed && !adjoint && gu.o == c->u[c->cur].o && gv.o == c->v[c->cur].o;
-    Press pa = press_args(c, dt, gu, gv, adjoint, w32);
+    Press pa{c->ph, gu, gv, c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx)), adjoint, c->u32, c->v32,
+             w32 ? 1 : 0};
     dim3 blk(32, 8), grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
     k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
     c->launches += 1;

@@ -243,10 +243,6 @@ int cf_trace_points(cf_ctx* ctx, int n, const double* xy, double dt, double* out
  * conversions of the mixed-precision kernels, applied to d[n]: f = narrowed,
  * w = f widened (no counterpart in the reference) */
 int cf_test_conversions(cf_ctx* ctx, int n, const double* d, float* f, double* w);
-/* Test export: the double-float split the mixed divergence uses, on the
- * device: hilo[2k] = d[k] rounded to FP32, hilo[2k+1] = d[k] - hilo[2k]
- * rounded to FP32. */
-int cf_test_split(cf_ctx* ctx, int n, const double* d, float* hilo);
 
 /* launch geometry of the fused multigrid pre-smoothing (pre != 0) or
  * post-smoothing kernel on an nx x ny level with tile_w x tile_h tiles
