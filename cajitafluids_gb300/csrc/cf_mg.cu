@@ -1035,195 +1035,139 @@ __device__ __forceinline__ T gs_cell(const MgBc& p, const T* x, int nx, int ny, 
     return t * invd[mg_bits(p, nx, ny, gi, gj)];
 }
 
-// Threads that work on a level of n cells: one per cell of a colour, in
-// whole warps, at most the block.  A level's phases end at a barrier of just
-// those threads (one warp: __syncwarp; the block: __syncthreads; otherwise
-// the named barrier 1 for the first `a` threads), and every level change at
-// a full __syncthreads, so the small levels near the coarsest do not pay for
-// a 1024-thread barrier in each of their many half sweeps.
-__device__ __forceinline__ int bottom_threads(int n) {
-    int a = ((n + 1) / 2 + 31) / 32 * 32;
-    if (a < 32) a = 32;
-    return a < MG_BOTTOM_THREADS ? a : MG_BOTTOM_THREADS;
-}
-
-__device__ __forceinline__ void bottom_bar(int a) {
-    if (a >= MG_BOTTOM_THREADS)
-        __syncthreads();
-    else if (a == 32)
-        __syncwarp();
-    else
-        asm volatile("bar.sync 1, %0;" ::"r"(a) : "memory");
-}
-
 template <typename T>
 __global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(MgBottom<T> P, MgBc p, SolverState* S, int inner) {
     if (!block_live(S, inner)) return;
     extern __shared__ __align__(16) unsigned char mg_smem[];
     T* sm = reinterpret_cast<T*>(mg_smem);
-    // the level tables and extents in shared memory: the parameter block is
-    // indexed by level at run time below, which would otherwise copy it to
-    // every thread's local memory
-    __shared__ T s_scale[MG_BOTTOM_LEVELS], s_ms[MG_BOTTOM_LEVELS];
-    __shared__ T s_diag[MG_BOTTOM_LEVELS][16], s_invd[MG_BOTTOM_LEVELS][16];
-    __shared__ int s_nx[MG_BOTTOM_LEVELS], s_ny[MG_BOTTOM_LEVELS], s_off[MG_BOTTOM_LEVELS];
-    const int tid = threadIdx.x;
-    if (tid == 0) {
-#pragma unroll
-        for (int l = 0; l < MG_BOTTOM_LEVELS; ++l) {
-            s_scale[l] = P.lev[l].scale;
-            s_ms[l] = P.lev[l].ms;
-            s_nx[l] = P.lev[l].nx;
-            s_ny[l] = P.lev[l].ny;
-            s_off[l] = P.off[l];
-#pragma unroll
-            for (int b = 0; b < 16; ++b) {
-                s_diag[l][b] = P.lev[l].diag[b];
-                s_invd[l][b] = P.lev[l].invd[b];
-            }
-        }
-    }
+    // 32 x 32 threads: tx walks columns (or column pairs), ty rows
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    auto X = [&](int l) { return sm + P.off[l]; };
+    auto B = [&](int l) { return sm + P.off[l] + P.lev[l].nx * P.lev[l].ny; };
+    auto R = [&](int l) { return sm + P.off[l] + 2 * P.lev[l].nx * P.lev[l].ny; };
     {
         const MgLev<T>& G = P.lev[0];
-        T* b = sm + P.off[0] + G.nx * G.ny;
-        for (int k = tid; k < G.nx * G.ny; k += MG_BOTTOM_THREADS) {
-            const int gj = k / G.nx, gi = k - gj * G.nx;
-            b[k] = G.b[(size_t)gj * G.pitch + gi];
-        }
+        T* b = B(0);
+        for (int gj = ty; gj < G.ny; gj += 32)
+            for (int gi = tx; gi < G.nx; gi += 32) b[gj * G.nx + gi] = G.b[(size_t)gj * G.pitch + gi];
     }
     __syncthreads();
-    auto X = [&](int l) { return sm + s_off[l]; };
-    auto B = [&](int l) { return sm + s_off[l] + s_nx[l] * s_ny[l]; };
-    auto R = [&](int l) { return sm + s_off[l] + 2 * s_nx[l] * s_ny[l]; };
-    // the per-cell arithmetic below is that of the grid kernels (same
-    // formulas and order); only the threads and barriers differ
-    auto half = [&](int l, int color, bool first, int a) {
-        const int nx = s_nx[l], ny = s_ny[l];
+    auto half = [&](int l, int color, bool first) {
+        const MgLev<T>& L = P.lev[l];
         T* x = X(l);
         const T* b = B(l);
-        const int pairs = (nx + 1) / 2;
-        for (int k = tid; k < ny * pairs; k += a) {
-            const int gj = k / pairs, pr = k - gj * pairs;
+        const int pairs = (L.nx + 1) / 2;
+        for (int gj = ty; gj < L.ny; gj += 32) {
             const int par = (gj + color) & 1;
-            const int gi = 2 * pr + par, go = 2 * pr + 1 - par;
-            if (gi < nx) x[gj * nx + gi] = gs_cell(p, x, nx, ny, gi, gj, b[gj * nx + gi], s_scale[l], s_invd[l], first);
-            if (first && go < nx) x[gj * nx + go] = T(0);
+            for (int pr = tx; pr < pairs; pr += 32) {
+                const int gi = 2 * pr + par, go = 2 * pr + 1 - par;
+                if (gi < L.nx)
+                    x[gj * L.nx + gi] = gs_cell(p, x, L.nx, L.ny, gi, gj, b[gj * L.nx + gi], L.scale, L.invd, first);
+                if (first && go < L.nx) x[gj * L.nx + go] = T(0);
+            }
         }
-        bottom_bar(a);
+        __syncthreads();
     };
-    auto residual = [&](int l, int a) {
-        const int nx = s_nx[l], ny = s_ny[l];
+    auto residual = [&](int l) {
+        const MgLev<T>& L = P.lev[l];
         const T* x = X(l);
         const T* b = B(l);
         T* r = R(l);
-        const T ms = s_ms[l];
-        for (int k = tid; k < nx * ny; k += a) {
-            const int gj = k / nx, gi = k - gj * nx;
-            T ax = s_diag[l][mg_bits(p, nx, ny, gi, gj)] * x[k];
-            ax = mg_fma(ms, mg_at(p, x, nx, nx, ny, gi - 1, gj), ax);
-            ax = mg_fma(ms, mg_at(p, x, nx, nx, ny, gi + 1, gj), ax);
-            ax = mg_fma(ms, mg_at(p, x, nx, nx, ny, gi, gj - 1), ax);
-            ax = mg_fma(ms, mg_at(p, x, nx, nx, ny, gi, gj + 1), ax);
-            r[k] = b[k] - ax;
-        }
-        bottom_bar(a);
+        for (int gj = ty; gj < L.ny; gj += 32)
+            for (int gi = tx; gi < L.nx; gi += 32) {
+                const int k = gj * L.nx + gi;
+                T ax = L.diag[mg_bits(p, L.nx, L.ny, gi, gj)] * x[k];
+                ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi - 1, gj), ax);
+                ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi + 1, gj), ax);
+                ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi, gj - 1), ax);
+                ax = mg_fma(L.ms, mg_at(p, x, L.nx, L.nx, L.ny, gi, gj + 1), ax);
+                r[k] = b[k] - ax;
+            }
+        __syncthreads();
     };
-    auto restrict_to = [&](int l, int a) {
-        const int fnx = s_nx[l], fny = s_ny[l], cnx = s_nx[l + 1], cny = s_ny[l + 1];
+    auto restrict_to = [&](int l) {
+        const MgLev<T>& F = P.lev[l];
+        const MgLev<T>& C = P.lev[l + 1];
         const T* fr = R(l);
         T* cb = B(l + 1);
-        for (int k = tid; k < cnx * cny; k += a) {
-            const int J = k / cnx, I = k - J * cnx;
-            T acc = T(0);
-            for (int fy0 = 2 * J - 1; fy0 <= 2 * J + 2; ++fy0) {
-                int fy = fy0;
-                if (fy < 0 || fy >= fny) {
-                    if (!p.per_y) continue;
-                    fy = fy < 0 ? fy + fny : fy - fny;
-                }
-                const T wy = (T)mg_pwq(fy, J, cny, p.per_y, p.bc[1], p.bc[3]) * T(0.25);
-                T rs = T(0);
-                for (int fx0 = 2 * I - 1; fx0 <= 2 * I + 2; ++fx0) {
-                    int fx = fx0;
-                    if (fx < 0 || fx >= fnx) {
-                        if (!p.per_x) continue;
-                        fx = fx < 0 ? fx + fnx : fx - fnx;
+        for (int J = ty; J < C.ny; J += 32)
+            for (int I = tx; I < C.nx; I += 32) {
+                T acc = T(0);
+                for (int fy0 = 2 * J - 1; fy0 <= 2 * J + 2; ++fy0) {
+                    int fy = fy0;
+                    if (fy < 0 || fy >= F.ny) {
+                        if (!p.per_y) continue;
+                        fy = fy < 0 ? fy + F.ny : fy - F.ny;
                     }
-                    const T wx = (T)mg_pwq(fx, I, cnx, p.per_x, p.bc[0], p.bc[2]) * T(0.25);
-                    rs = mg_fma(wx, fr[fy * fnx + fx], rs);
+                    const T wy = (T)mg_pwq(fy, J, C.ny, p.per_y, p.bc[1], p.bc[3]) * T(0.25);
+                    T rs = T(0);
+                    for (int fx0 = 2 * I - 1; fx0 <= 2 * I + 2; ++fx0) {
+                        int fx = fx0;
+                        if (fx < 0 || fx >= F.nx) {
+                            if (!p.per_x) continue;
+                            fx = fx < 0 ? fx + F.nx : fx - F.nx;
+                        }
+                        const T wx = (T)mg_pwq(fx, I, C.nx, p.per_x, p.bc[0], p.bc[2]) * T(0.25);
+                        rs = mg_fma(wx, fr[fy * F.nx + fx], rs);
+                    }
+                    acc = mg_fma(wy, rs, acc);
                 }
-                acc = mg_fma(wy, rs, acc);
+                cb[J * C.nx + I] = T(0.25) * acc;
             }
-            cb[k] = T(0.25) * acc;
-        }
+        __syncthreads();
     };
-    auto prolong_from = [&](int l, int a) {  // x_l += P x_{l+1}
-        const int fnx = s_nx[l], fny = s_ny[l], cnx = s_nx[l + 1], cny = s_ny[l + 1];
+    auto prolong_from = [&](int l) {  // x_l += P x_{l+1}
+        const MgLev<T>& F = P.lev[l];
+        const MgLev<T>& C = P.lev[l + 1];
         const T* cx = X(l + 1);
         T* fxs = X(l);
-        for (int k = tid; k < fnx * fny; k += a) {
-            const int fy = k / fnx, fx = k - fy * fnx;
-            int I, NI, J, NJ;
-            T wxI, wxN, wyJ, wyN;
-            mg_axis<T>(fx, cnx, p.per_x, p.bc[0], p.bc[2], I, NI, wxI, wxN);
-            mg_axis<T>(fy, cny, p.per_y, p.bc[1], p.bc[3], J, NJ, wyJ, wyN);
-            T row0 = wxI * cx[J * cnx + I];
-            if (NI >= 0) row0 = mg_fma(wxN, cx[J * cnx + NI], row0);
-            T v = wyJ * row0;
-            if (NJ >= 0) {
-                T row1 = wxI * cx[NJ * cnx + I];
-                if (NI >= 0) row1 = mg_fma(wxN, cx[NJ * cnx + NI], row1);
-                v = mg_fma(wyN, row1, v);
+        for (int fy = ty; fy < F.ny; fy += 32)
+            for (int fx = tx; fx < F.nx; fx += 32) {
+                int I, NI, J, NJ;
+                T wxI, wxN, wyJ, wyN;
+                mg_axis<T>(fx, C.nx, p.per_x, p.bc[0], p.bc[2], I, NI, wxI, wxN);
+                mg_axis<T>(fy, C.ny, p.per_y, p.bc[1], p.bc[3], J, NJ, wyJ, wyN);
+                T row0 = wxI * cx[J * C.nx + I];
+                if (NI >= 0) row0 = mg_fma(wxN, cx[J * C.nx + NI], row0);
+                T v = wyJ * row0;
+                if (NJ >= 0) {
+                    T row1 = wxI * cx[NJ * C.nx + I];
+                    if (NI >= 0) row1 = mg_fma(wxN, cx[NJ * C.nx + NI], row1);
+                    v = mg_fma(wyN, row1, v);
+                }
+                fxs[fy * F.nx + fx] = fxs[fy * F.nx + fx] + v;
             }
-            fxs[k] = fxs[k] + v;
-        }
-        bottom_bar(a);
+        __syncthreads();
     };
     const int nb = P.nlev;
     for (int l = 0; l < nb - 1; ++l) {
-        const int a = bottom_threads(s_nx[l] * s_ny[l]);
-        if (tid < a) {
-            for (int k = 0; k < MG_NU; ++k) {
-                half(l, 0, k == 0, a);
-                half(l, 1, false, a);
-            }
-            residual(l, a);
-            restrict_to(l, a);
+        for (int k = 0; k < MG_NU; ++k) {
+            half(l, 0, k == 0);
+            half(l, 1, false);
         }
-        __syncthreads();
+        residual(l);
+        restrict_to(l);
     }
-    {
-        const int l = nb - 1, a = bottom_threads(s_nx[l] * s_ny[l]);
-        if (tid < a) {
-            for (int k = 0; k < MG_NC; ++k) {
-                half(l, 0, k == 0, a);
-                half(l, 1, false, a);
-            }
-            for (int k = 0; k < MG_NC; ++k) {
-                half(l, 1, false, a);
-                half(l, 0, false, a);
-            }
-        }
-        __syncthreads();
+    for (int k = 0; k < MG_NC; ++k) {
+        half(nb - 1, 0, k == 0);
+        half(nb - 1, 1, false);
+    }
+    for (int k = 0; k < MG_NC; ++k) {
+        half(nb - 1, 1, false);
+        half(nb - 1, 0, false);
     }
     for (int l = nb - 2; l >= 0; --l) {
-        const int a = bottom_threads(s_nx[l] * s_ny[l]);
-        if (tid < a) {
-            prolong_from(l, a);
-            for (int k = 0; k < MG_NU; ++k) {
-                half(l, 1, false, a);
-                half(l, 0, false, a);
-            }
+        prolong_from(l);
+        for (int k = 0; k < MG_NU; ++k) {
+            half(l, 1, false);
+            half(l, 0, false);
         }
-        __syncthreads();
     }
     {
         const MgLev<T>& G = P.lev[0];
-        const T* x = sm + P.off[0];
-        for (int k = tid; k < G.nx * G.ny; k += MG_BOTTOM_THREADS) {
-            const int gj = k / G.nx, gi = k - gj * G.nx;
-            G.x[(size_t)gj * G.pitch + gi] = x[k];
-        }
+        const T* x = X(0);
+        for (int gj = ty; gj < G.ny; gj += 32)
+            for (int gi = tx; gi < G.nx; gi += 32) G.x[(size_t)gj * G.pitch + gi] = x[gj * G.nx + gi];
     }
 }
 
