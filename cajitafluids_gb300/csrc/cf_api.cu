@@ -68,7 +68,7 @@ size_t round_up(size_t v, size_t m) { return (v + m - 1) / m * m; }
 
 template <typename T>
 int alloc_grid(cf_ctx* c, Grid<T>& g, int ex, int ey) {
-    const int col0 = 32 - CF_HALO;  // local column 3 lands on a 32-element boundary
+    const int col0 = CF_COL0;  // local column 3 lands on a 32-element boundary
     int pitch = (int)round_up((size_t)col0 + ex, 32);
     void* base = nullptr;
     size_t bytes = (size_t)pitch * ey * sizeof(T);
@@ -451,6 +451,12 @@ int cf_set_graphs(cf_ctx* ctx, int on) {
 int cf_test_stall_wait(cf_ctx* ctx, int on) {
     if (!ctx) return CF_ERR_INVALID;
     ctx->test_stall = on ? 1 : 0;
+    return CF_OK;
+}
+
+int cf_test_advect_unstaged(cf_ctx* ctx, int on) {
+    if (!ctx) return CF_ERR_INVALID;
+    ctx->test_unstaged = on ? 1 : 0;
     return CF_OK;
 }
 

@@ -94,6 +94,9 @@ struct cf_ctx {
     // cf_test_stall_wait: the inner FP32 CG's first tile wait of block 0
     // waits on an mbarrier nothing arrives on (timeout-path test)
     int test_stall = 0;
+    // cf_test_advect_unstaged: every FP32 advection tile reads its taps from
+    // global memory instead of its shared-memory window (same bits)
+    int test_unstaged = 0;
     // profiling (cf_profile_enable)
     int prof = 0;
     cf_profile pd{};

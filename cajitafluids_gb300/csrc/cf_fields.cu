@@ -275,6 +275,7 @@ struct Adv32 {
     double dt;
     int fuse;
     int ent0;     // entity of blockIdx.z == 0 (a launch may cover a subset)
+    int unstaged; // tests: every tile reads global memory (same bits)
 };
 
 // FP32 copy of a ghosted FP64 array (ghosts included)
@@ -286,19 +287,61 @@ __global__ void k_to32(Grid<double> src, Grid<float> dst) {
 }
 
 
-template <typename T>
-__device__ __forceinline__ float lin32(const Grid<T>& g, int bi, int bj, float fx, float fy) {
+// Tap access for the FP32 samplers.  GlobalTaps reads a ghosted FP32 array
+// and clamps the stencil to it, as the FP64 samplers do; WindowTaps reads a
+// CTA's staged copy of part of the array in shared memory and does not
+// clamp.  The advection uses a window only where no position of a trace
+// moves a full cell from its entity; the taps then lie within two cells of
+// the entity, inside the window and at least one cell inside the ghosted
+// array, where the clamps cannot fire, so both give the same bits.
+struct GlobalTaps {
+    const float* o;
+    int pitch, ex, ey;
+    static constexpr bool kClamp = true;
+    __device__ __forceinline__ const float* at(int ix, int iy) const { return o + (size_t)iy * pitch + ix; }
+    __device__ __forceinline__ int stride() const { return pitch; }
+    __device__ __forceinline__ static float ld(const float* p) { return __ldg(p); }
+};
+
+// Advection tiles: 32 x 32 entities per CTA of 256 threads (lane = column,
+// four rows per thread).  An entity of the tile at ghosted (li, lj) has
+// li in [gi0 + 3, gi0 + 35), lj in [gj0 + 3, gj0 + 35); with every RK
+// position less than a cell from it, its taps lie in [li - 2, li + 2] x
+// [lj - 2, lj + 2].  The window, ghosted columns [gi0 - 1, gi0 + 39) and rows
+// [gj0 + 1, gj0 + 38), holds that with a cell to spare; its first column
+// sits on a 16-byte boundary (ghosted column 3 of every row is on a
+// 128-byte one), so rows are copied as float4.
+constexpr int AT_X = 32;
+constexpr int AT_Y = 32;
+constexpr int AW_X = 40;
+constexpr int AW_Y = AT_Y + 5;
+constexpr int AW_N = AW_X * AW_Y;
+
+struct WindowTaps {
+    const float* s;  // ghosted (x0, y0)
+    int x0, y0;
+    int ex = 0, ey = 0;  // unused: a window does not clamp
+    static constexpr bool kClamp = false;
+    __device__ __forceinline__ const float* at(int ix, int iy) const { return s + ((iy - y0) * AW_X + (ix - x0)); }
+    __device__ __forceinline__ int stride() const { return AW_X; }
+    __device__ __forceinline__ static float ld(const float* p) { return *p; }
+};
+
+template <typename A>
+__device__ __forceinline__ float lin32(const A& g, int bi, int bj, float fx, float fy) {
     float flx = floorf(fx), fly = floorf(fy);
     int ix = bi + (int)flx, iy = bj + (int)fly;
     float tx = fx - flx, ty = fy - fly;
-    if (ix < 0) { ix = 0; tx = 0.f; }
-    if (ix > g.ex - 2) { ix = g.ex - 2; tx = 1.f; }
-    if (iy < 0) { iy = 0; ty = 0.f; }
-    if (iy > g.ey - 2) { iy = g.ey - 2; ty = 1.f; }
-    const T* r0 = g.o + (size_t)iy * g.pitch + ix;
-    const T* r1 = r0 + g.pitch;
-    float a0 = (float)__ldg(r0), a1 = (float)__ldg(r0 + 1);
-    float b0 = (float)__ldg(r1), b1 = (float)__ldg(r1 + 1);
+    if constexpr (A::kClamp) {
+        if (ix < 0) { ix = 0; tx = 0.f; }
+        if (ix > g.ex - 2) { ix = g.ex - 2; tx = 1.f; }
+        if (iy < 0) { iy = 0; ty = 0.f; }
+        if (iy > g.ey - 2) { iy = g.ey - 2; ty = 1.f; }
+    }
+    const float* r0 = g.at(ix, iy);
+    const float* r1 = r0 + g.stride();
+    float a0 = A::ld(r0), a1 = A::ld(r0 + 1);
+    float b0 = A::ld(r1), b1 = A::ld(r1 + 1);
     float s0 = fmaf(tx, a1 - a0, a0);
     float s1 = fmaf(tx, b1 - b0, b0);
     return fmaf(ty, s1 - s0, s0);
@@ -312,15 +355,17 @@ __device__ __forceinline__ void cubic_w32(float t, float* w) {
     w[3] = t3 * (1.f / 6.f);
 }
 
-template <typename T>
-__device__ __forceinline__ float cub32(const Grid<T>& g, int bi, int bj, float fx, float fy) {
+template <typename A>
+__device__ __forceinline__ float cub32(const A& g, int bi, int bj, float fx, float fy) {
     float flx = floorf(fx), fly = floorf(fy);
     int ix = bi + (int)flx, iy = bj + (int)fly;
     float tx = fx - flx, ty = fy - fly;
-    if (ix < 1) { ix = 1; tx = 0.f; }
-    if (ix > g.ex - 3) { ix = g.ex - 3; tx = 1.f; }
-    if (iy < 1) { iy = 1; ty = 0.f; }
-    if (iy > g.ey - 3) { iy = g.ey - 3; ty = 1.f; }
+    if constexpr (A::kClamp) {
+        if (ix < 1) { ix = 1; tx = 0.f; }
+        if (ix > g.ex - 3) { ix = g.ex - 3; tx = 1.f; }
+        if (iy < 1) { iy = 1; ty = 0.f; }
+        if (iy > g.ey - 3) { iy = g.ey - 3; ty = 1.f; }
+    }
     float wx[4], wy[4];
     cubic_w32(tx, wx);
     cubic_w32(ty, wy);
@@ -330,106 +375,172 @@ __device__ __forceinline__ float cub32(const Grid<T>& g, int bi, int bj, float f
     // scale the field by that much every step, a drift that grows linearly
     // over a run.  Against differences the weight error only touches the
     // local variation of the field, and a constant is reproduced exactly.
-    const float c = (float)__ldg(g.o + (size_t)iy * g.pitch + ix);
+    const float* base = g.at(ix - 1, iy - 1);
+    const int st = g.stride();
+    const float c = A::ld(base + st + 1);
     float val = 0.f;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-        const T* row = g.o + (size_t)(iy - 1 + b) * g.pitch + (ix - 1);
-        float rs = wx[0] * ((float)__ldg(row) - c);
+        const float* row = base + b * st;
+        float rs = wx[0] * (A::ld(row) - c);
 #pragma unroll
-        for (int k = 1; k < 4; ++k) rs = fmaf(wx[k], (float)__ldg(row + k) - c, rs);
+        for (int k = 1; k < 4; ++k) rs = fmaf(wx[k], A::ld(row + k) - c, rs);
         val = b == 0 ? wy[0] * rs : fmaf(wy[b], rs, val);
     }
     return c + val;
 }
 
-template <int ORDER>
-__global__ void __launch_bounds__(256) k_advect32(Adv32 a) {
-    const Phys& p = a.p;
-    int ent = blockIdx.z + a.ent0;
-    int gi = blockIdx.x * blockDim.x + threadIdx.x;
-    int gj = blockIdx.y * blockDim.y + threadIdx.y;
-    int ox = p.nx + ((ent == E_FACEI && !p.per_x) ? 1 : 0);
-    int oy = p.ny + ((ent == E_FACEJ && !p.per_y) ? 1 : 0);
-    if (gi >= ox || gj >= oy) return;
-    int li = gi + CF_HALO, lj = gj + CF_HALO;
+// The RK3 trace of one entity at ghosted (li, lj) and the value sampled at
+// its foot, U and V the velocity taps, F the advected field's.
+template <int ORDER, typename A>
+__device__ __forceinline__ float advect_value(const Adv32& a, int ent, int li, int lj, const A& U, const A& V,
+                                              const A& F) {
     // entity offset minus the velocity grids' offsets (u: (0, .5), v: (.5, 0))
-    float ox_e = ent == E_FACEI ? 0.f : 0.5f;
-    float oy_e = ent == E_FACEJ ? 0.f : 0.5f;
-    float uox = ox_e, uoy = oy_e - 0.5f, vox = ox_e - 0.5f, voy = oy_e;
+    const float ox_e = ent == E_FACEI ? 0.f : 0.5f;
+    const float oy_e = ent == E_FACEJ ? 0.f : 0.5f;
+    const float uox = ox_e, uoy = oy_e - 0.5f, vox = ox_e - 0.5f, voy = oy_e;
     // first RK stage at the entity itself: the linear samples' integer cells
     // and fractions (0 or 1/2) are known, so the taps are read directly with
     // the same arithmetic (a zero-weight row is dropped: it only could turn a
     // -0 into +0, which no later step can tell apart)
     float v0x, v0y;
     {
-        const float* u0 = &a.u.at(li, lj);
-        const float* w0 = &a.v.at(li, lj);
-        const int pu = a.u.pitch, pv = a.v.pitch;
+        const float* u0 = U.at(li, lj);
+        const float* w0 = V.at(li, lj);
+        const int pu = U.stride(), pv = V.stride();
         if (ent == E_CELL) {
-            v0x = fmaf(0.5f, __ldg(u0 + 1) - __ldg(u0), __ldg(u0));
-            v0y = fmaf(0.5f, __ldg(w0 + pv) - __ldg(w0), __ldg(w0));
+            v0x = fmaf(0.5f, A::ld(u0 + 1) - A::ld(u0), A::ld(u0));
+            v0y = fmaf(0.5f, A::ld(w0 + pv) - A::ld(w0), A::ld(w0));
         } else if (ent == E_FACEI) {
-            v0x = __ldg(u0);
+            v0x = A::ld(u0);
             const float* r0 = w0 - 1;
-            const float s0 = fmaf(0.5f, __ldg(r0 + 1) - __ldg(r0), __ldg(r0));
-            const float s1 = fmaf(0.5f, __ldg(r0 + pv + 1) - __ldg(r0 + pv), __ldg(r0 + pv));
+            const float s0 = fmaf(0.5f, A::ld(r0 + 1) - A::ld(r0), A::ld(r0));
+            const float s1 = fmaf(0.5f, A::ld(r0 + pv + 1) - A::ld(r0 + pv), A::ld(r0 + pv));
             v0y = fmaf(0.5f, s1 - s0, s0);
         } else {
             const float* r0 = u0 - pu;
-            const float s0 = fmaf(0.5f, __ldg(r0 + 1) - __ldg(r0), __ldg(r0));
-            const float s1 = fmaf(0.5f, __ldg(r0 + pu + 1) - __ldg(r0 + pu), __ldg(r0 + pu));
+            const float s0 = fmaf(0.5f, A::ld(r0 + 1) - A::ld(r0), A::ld(r0));
+            const float s1 = fmaf(0.5f, A::ld(r0 + pu + 1) - A::ld(r0 + pu), A::ld(r0 + pu));
             v0x = fmaf(0.5f, s1 - s0, s0);
-            v0y = __ldg(w0);
+            v0y = A::ld(w0);
         }
     }
-    float h1 = -0.5f * a.c, h2 = -0.75f * a.c;
-    float d1x = h1 * v0x, d1y = h1 * v0y;
-    float v1x = lin32(a.u, li, lj, uox + d1x, uoy + d1y);
-    float v1y = lin32(a.v, li, lj, vox + d1x, voy + d1y);
-    bool ralston = (p.quirks & 2u) != 0;
-    float d2x = h2 * (ralston ? v1x : v0x), d2y = h2 * (ralston ? v1y : v0y);
-    float v2x = lin32(a.u, li, lj, uox + d2x, uoy + d2y);
-    float v2y = lin32(a.v, li, lj, vox + d2x, voy + d2y);
-    float ax = fmaf(4.f / 9.f, v2x, fmaf(3.f / 9.f, v1x, (2.f / 9.f) * v0x));
-    float ay = fmaf(4.f / 9.f, v2y, fmaf(3.f / 9.f, v1y, (2.f / 9.f) * v0y));
-    float dx = -a.c * ax, dy = -a.c * ay;
-    float val;
-    if (ent == E_CELL)
-        val = ORDER == 1 ? lin32(a.q, li, lj, dx, dy) : cub32(a.q, li, lj, dx, dy);
-    else if (ent == E_FACEI)
-        val = ORDER == 1 ? lin32(a.u, li, lj, dx, dy) : cub32(a.u, li, lj, dx, dy);
-    else
-        val = ORDER == 1 ? lin32(a.v, li, lj, dx, dy) : cub32(a.v, li, lj, dx, dy);
-    if (ent == E_CELL) {
-        // cell inputs (src/Solver.hpp:181-263): the clamp max(q, Q) rounds to
-        // the same FP32 value when taken in FP32; the rate form in FP64
-        if (a.fuse && in_box_idx(p, E_CELL, li, lj)) {
-            if (p.src_mode == 0) {
-                const float qf = (float)p.src_q;
-                if (val < qf) val = qf;
-            } else {
-                val = (float)__dadd_rn((double)val, __dmul_rn(p.src_q, a.dt));
+    const float h1 = -0.5f * a.c, h2 = -0.75f * a.c;
+    const float d1x = h1 * v0x, d1y = h1 * v0y;
+    const float v1x = lin32(U, li, lj, uox + d1x, uoy + d1y);
+    const float v1y = lin32(V, li, lj, vox + d1x, voy + d1y);
+    const bool ralston = (a.p.quirks & 2u) != 0;
+    const float d2x = h2 * (ralston ? v1x : v0x), d2y = h2 * (ralston ? v1y : v0y);
+    const float v2x = lin32(U, li, lj, uox + d2x, uoy + d2y);
+    const float v2y = lin32(V, li, lj, vox + d2x, voy + d2y);
+    const float ax = fmaf(4.f / 9.f, v2x, fmaf(3.f / 9.f, v1x, (2.f / 9.f) * v0x));
+    const float ay = fmaf(4.f / 9.f, v2y, fmaf(3.f / 9.f, v1y, (2.f / 9.f) * v0y));
+    const float dx = -a.c * ax, dy = -a.c * ay;
+    return ORDER == 1 ? lin32(F, li, lj, dx, dy) : cub32(F, li, lj, dx, dy);
+}
+
+// max that keeps a NaN (so a NaN in a window sends its tile to the clamped path)
+__device__ __forceinline__ float max_nan(float x, float y) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(x), "f"(y));
+    return r;
+}
+
+// One CTA per 32 x 32 tile and entity kind (blockIdx.x, fastest, so that the
+// kinds of one tile run together and share its windows through L2; tiles
+// along blockIdx.y, blockIdx.z).  The CTA copies the windows of u, v and
+// (cells) q into shared memory, 16-byte rows, and takes the largest |u|, |v|
+// in them, M.  Every RK velocity is a convex combination of window values,
+// so while (dt / dx) M <= 0.99 no position moves a full cell and the traces
+// read only the window; otherwise (or with a NaN, or when a test asks for
+// it) the tile reads global memory with the clamped stencil.  Either way
+// each entity gets the same bits.
+template <int ORDER>
+__global__ void __launch_bounds__(256) k_advect32(Adv32 a) {
+    __shared__ __align__(16) float sw[3 * AW_N];  // u, v, q windows
+    __shared__ float red[8];
+    const Phys& p = a.p;
+    const int ent = blockIdx.x + a.ent0;
+    const int gi0 = blockIdx.y * AT_X, gj0 = blockIdx.z * AT_Y;
+    const int lane = threadIdx.x & 31, wrow = threadIdx.x >> 5;
+    const int narr = ent == E_CELL ? 3 : 2;
+    constexpr int kRowChunks = AW_X / 4, kChunks = AW_Y * kRowChunks;
+    float m = 0.f;
+    for (int arr = 0; arr < narr; ++arr) {
+        const float* go = arr == 0 ? a.u.o : (arr == 1 ? a.v.o : a.q.o);
+        const int gp = arr == 0 ? a.u.pitch : (arr == 1 ? a.v.pitch : a.q.pitch);
+        const int gey = arr == 0 ? a.u.ey : (arr == 1 ? a.v.ey : a.q.ey);
+        // the window's origin, ghosted (gi0 - 1, gj0 + 1); rows past the array
+        // and chunks past its padded row (chunk c4 ends at element CF_COL0 +
+        // gi0 - 1 + 4 c4 + 4 of the row) read as zeros
+        const float* src = go + (size_t)(gj0 + 1) * gp + (gi0 - 1);
+        const int nrow = gey - (gj0 + 1), nc4 = (gp - CF_COL0 - gi0 + 1) >> 2;
+        float* dst = sw + arr * AW_N;
+        for (int k = threadIdx.x; k < kChunks; k += 256) {
+            const int r = k / kRowChunks, c4 = k - r * kRowChunks;
+            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r < nrow && c4 < nc4) w = __ldg(reinterpret_cast<const float4*>(src + (size_t)r * gp + 4 * c4));
+            *reinterpret_cast<float4*>(dst + 4 * k) = w;  // r AW_X + 4 c4 = 4 k
+            if (arr < 2) m = max_nan(m, max_nan(max_nan(fabsf(w.x), fabsf(w.y)), max_nan(fabsf(w.z), fabsf(w.w))));
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max_nan(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) red[wrow] = m;
+    __syncthreads();
+    float big = red[0];
+#pragma unroll
+    for (int w = 1; w < 8; ++w) big = max_nan(big, red[w]);
+    const bool staged = !a.unstaged && a.c * big <= 0.99f;
+
+    const int ox = p.nx + ((ent == E_FACEI && !p.per_x) ? 1 : 0);
+    const int oy = p.ny + ((ent == E_FACEJ && !p.per_y) ? 1 : 0);
+    const int fa = ent == E_CELL ? 2 : (ent == E_FACEI ? 0 : 1);
+    const GlobalTaps gu{a.u.o, a.u.pitch, a.u.ex, a.u.ey}, gv{a.v.o, a.v.pitch, a.v.ex, a.v.ey};
+    const GlobalTaps gf = ent == E_CELL ? GlobalTaps{a.q.o, a.q.pitch, a.q.ex, a.q.ey} : (ent == E_FACEI ? gu : gv);
+#pragma unroll 1
+    for (int k = 0; k < AT_Y / 8; ++k) {
+        const int gi = gi0 + lane, gj = gj0 + wrow + 8 * k;
+        if (gi >= ox || gj >= oy) continue;
+        const int li = gi + CF_HALO, lj = gj + CF_HALO;
+        float val;
+        if (staged) {
+            const WindowTaps U{sw, gi0 - 1, gj0 + 1}, V{sw + AW_N, gi0 - 1, gj0 + 1},
+                F{sw + fa * AW_N, gi0 - 1, gj0 + 1};
+            val = advect_value<ORDER>(a, ent, li, lj, U, V, F);
+        } else {
+            val = advect_value<ORDER>(a, ent, li, lj, gu, gv, gf);
+        }
+        if (ent == E_CELL) {
+            // cell inputs (src/Solver.hpp:181-263): the clamp max(q, Q) rounds to
+            // the same FP32 value when taken in FP32; the rate form in FP64
+            if (a.fuse && in_box_idx(p, E_CELL, li, lj)) {
+                if (p.src_mode == 0) {
+                    const float qf = (float)p.src_q;
+                    if (val < qf) val = qf;
+                } else {
+                    val = (float)__dadd_rn((double)val, __dmul_rn(p.src_q, a.dt));
+                }
+            }
+            a.qn.at(li, lj) = val;
+            continue;
+        }
+        const int axis = ent == E_FACEI ? 0 : 1;
+        double w = (double)val;
+        if (a.fuse) {
+            if (in_box_idx(p, ent, li, lj) && fabs(w) < fabs(p.src_vel[axis])) w = p.src_vel[axis];
+            if (p.force[axis] != 0.0) w = __dadd_rn(w, __dmul_rn(p.force[axis], a.dt));
+            const int per = axis == 0 ? p.per_x : p.per_y, n = axis == 0 ? p.nx : p.ny, gg = axis == 0 ? gi : gj;
+            if (!per) {
+                if (gg <= 0 && p.bc[axis] == 0) w = 0.0;
+                if (gg > n - 1 && p.bc[axis + 2] == 0) w = 0.0;
             }
         }
-        a.qn.at(li, lj) = val;
-        return;
+        if (axis == 0)
+            a.un.at(li, lj) = w;
+        else
+            a.vn.at(li, lj) = w;
     }
-    const int axis = ent == E_FACEI ? 0 : 1;
-    double w = (double)val;
-    if (a.fuse) {
-        if (in_box_idx(p, ent, li, lj) && fabs(w) < fabs(p.src_vel[axis])) w = p.src_vel[axis];
-        if (p.force[axis] != 0.0) w = __dadd_rn(w, __dmul_rn(p.force[axis], a.dt));
-        const int per = axis == 0 ? p.per_x : p.per_y, n = axis == 0 ? p.nx : p.ny, g = axis == 0 ? gi : gj;
-        if (!per) {
-            if (g <= 0 && p.bc[axis] == 0) w = 0.0;
-            if (g > n - 1 && p.bc[axis + 2] == 0) w = 0.0;
-        }
-    }
-    if (axis == 0)
-        a.un.at(li, lj) = w;
-    else
-        a.vn.at(li, lj) = w;
 }
 
 // --------------------------------------------------------------------------
@@ -596,7 +707,8 @@ cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs, int 
     } else {
         // fused inputs with a density-scaled force are applied by the
         // standalone inputs kernels after the advection
-        Adv32 a{p, c->q32[s], c->q32[n], c->u32, c->v32, c->u[n], c->v[n], (float)(dt / p.dx), dt, fuse_inputs, ent0};
+        Adv32 a{p,   c->q32[s], c->q32[n], c->u32, c->v32, c->u[n], c->v[n], (float)(dt / p.dx), dt, fuse_inputs,
+                ent0, c->test_unstaged};
         if (!prep) {
             // the FP32 velocity copies were prepared by an earlier part of this advection
         } else if (c->uv32) {
@@ -617,10 +729,11 @@ cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs, int 
             k_to32<<<grid2(c->v[s].ex, c->v[s].ey, blk), blk, 0, c->stream>>>(c->v[s], c->v32);
             c->launches += 2;
         }
+        const dim3 tiles(nent, (p.nx + 1 + AT_X - 1) / AT_X, (p.ny + 1 + AT_Y - 1) / AT_Y);
         if (order == 1)
-            k_advect32<1><<<grd, blk, 0, c->stream>>>(a);
+            k_advect32<1><<<tiles, 256, 0, c->stream>>>(a);
         else
-            k_advect32<3><<<grd, blk, 0, c->stream>>>(a);
+            k_advect32<3><<<tiles, 256, 0, c->stream>>>(a);
     }
     c->launches += 1;
     if (advance) {

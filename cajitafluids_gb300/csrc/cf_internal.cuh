@@ -15,6 +15,9 @@
 #include <stdint.h>
 
 #define CF_HALO 3
+// element offset of a ghosted array's local (0, 0) from its allocation: local
+// column CF_HALO (owned column 0) of every row lands on a 128-byte boundary
+#define CF_COL0 (32 - CF_HALO)
 #define CF_UNIT_COLS 64   // columns per reduction unit (32 lanes x 2)
 #define CF_BAND_ROWS 16   // rows per reduction unit
 #define CF_RED_THREADS 256

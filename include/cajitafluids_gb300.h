@@ -268,6 +268,11 @@ int cf_test_fail_alloc(int nth);
  * its own bulk copies in flight and returns, and the projection returns
  * CF_ERR_TIMEOUT.  The context stays usable; 0 switches the hook off. */
 int cf_test_stall_wait(cf_ctx* ctx, int on);
+/* Test hook: with on != 0, every tile of the mixed-precision advection reads
+ * its stencil taps from global memory (the path a tile takes when a trace
+ * could leave its shared-memory window) instead of the staged window.  The
+ * results are the same bits either way; 0 switches the hook off. */
+int cf_test_advect_unstaged(cf_ctx* ctx, int on);
 
 /* ---- output (replaces the device half of SiloWriter::writeFile) ----
  * SiloWriter interpolates the face velocities to cell centres for its
