@@ -1000,14 +1000,11 @@ struct FtRows<double> {
 // coarsest and back, in shared memory.  The per-cell arithmetic is the same as
 // in the grid kernels above (same formulas and order), so the result is the
 // same as that of the level-by-level launches; each phase ends at a barrier.
-// FP32: levels up to 64^2 in the one CTA.  FP64: up to 32^2, because one SM's
-// FP64 pipe would make a 64^2 level slower than a few grid launches.
+// Levels up to 32^2 go to the one CTA: a 64^2 level's eleven phases there
+// (2048 cells per half sweep on one SM) took longer than its two tile
+// launches (8 CTAs each), in FP32 as in FP64.
 template <typename T>
 struct MgBottomMax {
-    static constexpr int value = 4096;
-};
-template <>
-struct MgBottomMax<double> {
     static constexpr int value = 1024;
 };
 constexpr int MG_BOTTOM_LEVELS = 6;
