@@ -77,16 +77,17 @@ def alg_bytes_per_iter(nx, ny, periodic, precon, word, outer_frac=0.0, mixed=Fal
     is a double-float pair (8 bytes) in the update, and the reliable update
     (R x, b at 8 bytes, W r at 4 = 20 B per cell) runs on the fraction
     outer_frac of the iterations; when that is every iteration, the update
-    replaces r, so the inner step needs only R p and R/W x."""
+    replaces r, and the x update and the reliable update are one pass
+    (R p, x, b, W x, r: 32 B per cell)."""
     n = nx * ny
     if precon not in MG_NAMES:
         return 11 * word * n + outer_frac * 20.0 * n
     xw = 8 if mixed else word
     b = 3 * word * n
     if mixed and outer_frac >= 1.0:
-        # an update after every iteration replaces r: the inner step only
-        # advances x (R p, R/W x)
-        b += (word + 2 * xw) * n
+        # x update fused with the reliable update that replaces r
+        b += (2 * word + 3 * xw) * n
+        outer_frac = 0.0
     else:
         b += (3 * word + 2 * xw) * n
     if not mixed:
@@ -335,9 +336,9 @@ def bench_gb300(args, rank, world, dist, device):
                                       mixed=True)
         achieved = it_bytes / (it_ms / 1e3) / 1e9
         if mg:
-            kname = ("MG-PCG inner iteration: k_tma_dir_matvec32 + k_x_update32 (k_tma_update32 below an update "
-                     "threshold of 0.5) + gated k_outer_resid + V-cycle (k_mg_pre/k_mg_post per level with r.z in "
-                     "the finest post-smoothing, k_mg_bottom)")
+            kname = ("MG-PCG inner iteration: k_tma_dir_matvec32 + k_outer_resid<true> (x update fused with the "
+                     "reliable update; at an update threshold below 0.5, k_tma_update32 + gated k_outer_resid) + "
+                     "V-cycle (k_mg_pre/k_mg_post per level with r.z in the finest post-smoothing, k_mg_bottom)")
             kern_extra = {}
         else:
             kname = "inner CG iteration (k_tma_dir_matvec32 + k_tma_update32)"

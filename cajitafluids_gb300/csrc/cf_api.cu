@@ -306,6 +306,7 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
         if (!rc) rc = alloc_dev(c, c->qv.a, vn);
     } else {
         if (!rc) rc = alloc_dev(c, c->b.a, vn);
+        if (!rc) rc = alloc_dev(c, c->xb.a, vn);
         // FP32 vectors with a one-cell ghost ring, owned column 0 on 16 bytes
         c->p32 = (int)round_up((size_t)nx + 8, 32);
         size_t n32 = (size_t)c->p32 * (ny + 2);
@@ -317,6 +318,8 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
             vecs[k]->pitch = c->p32;
         }
     }
+    if (cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || c->sms < 1)
+        c->sms = 1;
     c->G = (nx + CF_UNIT_COLS - 1) / CF_UNIT_COLS;
     c->B = (ny + CF_BAND_ROWS - 1) / CF_BAND_ROWS;
     c->n_units = c->G * c->B;

@@ -659,73 +659,17 @@ int cg32_mg_precondition(cf_ctx* c, double scale) {
     return n + 1;
 }
 
-// MG-PCG with a reliable update after every iteration (reliable-update
-// threshold >= 0.5): the update replaces the FP32 residual each time, so the
-// inner step only advances x += alpha p (double-float, the same arithmetic as
-// K2) and hands over to the update; the CG scalars move as K2 moves them in
-// MG mode (rho_prev = rho, iteration counts).  x and p are read as float4 by
-// lanes of consecutive columns; one thread block per row band.
-__global__ void __launch_bounds__(256) k_x_update32(Cg32T a) {
-    SolverState* S = a.S;
-    if (!running(S)) return;
-    const int it = S->inner_iter;
-    const float* p = (it & 1) ? a.pa : a.pb;
-    const float alpha = (float)S->alpha_in;
-    const int nq = (a.nx + 3) / 4;  // column quads per row
-    // grid-stride walk over (row j, quad q) without a division per element:
-    // the stride splits once into whole rows dj and a remainder dq < nq
-    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    const int dj = (int)(stride / nq), dq = (int)(stride % nq);
-    int j = (int)(t0 / nq), q = (int)(t0 % nq);
-    while (j < a.ny) {
-        const int i = 4 * q;
-        const float* pr = p + (ptrdiff_t)j * a.pitch + i;
-        float2* xr = a.x + (size_t)j * a.xpitch + i;
-        if (i + 3 < a.nx) {
-            const float4 pv = *reinterpret_cast<const float4*>(pr);
-            float4 x0 = reinterpret_cast<const float4*>(xr)[0], x1 = reinterpret_cast<const float4*>(xr)[1];
-            const float2 r0 = df_add_f(make_float2(x0.x, x0.y), alpha * pv.x);
-            const float2 r1 = df_add_f(make_float2(x0.z, x0.w), alpha * pv.y);
-            const float2 r2 = df_add_f(make_float2(x1.x, x1.y), alpha * pv.z);
-            const float2 r3 = df_add_f(make_float2(x1.z, x1.w), alpha * pv.w);
-            reinterpret_cast<float4*>(xr)[0] = make_float4(r0.x, r0.y, r1.x, r1.y);
-            reinterpret_cast<float4*>(xr)[1] = make_float4(r2.x, r2.y, r3.x, r3.y);
-        } else {
-            for (int k = 0; i + k < a.nx; ++k) xr[k] = df_add_f(xr[k], alpha * pr[k]);
-        }
-        q += dq;
-        j += dj;
-        if (q >= nq) {
-            q -= nq;
-            ++j;
-        }
-    }
-    if (last_block_arrive(&S->ticket[6])) {
-        if (threadIdx.x == 0) {
-            S->ticket[6] = 0;
-            S->rho_prev = S->rho_in;
-            S->inner_iter = it + 1;
-            S->iter = S->iter + 1;
-            S->inner_status = ST_CONVERGED;  // the reliable update follows
-        }
-    }
-}
-
-// K1 on z (M^-1 = 1) and K2 of one MG-PCG inner iteration (K2 reduced to the
-// x update when every iteration ends with a reliable update, c->x_only)
+// K1 on z (M^-1 = 1) and K2 of one MG-PCG inner iteration.  When every
+// iteration ends with a reliable update (c->x_only), K2 reduces to the x
+// update, which the fused reliable update does (k_outer_resid<true>), so K1
+// runs alone.
 void cg32_launch_pair_mg(cf_ctx* c, const Stencil& st) {
     Stencil stz = st;
     for (int b = 0; b < 16; ++b) stz.minv32[b] = 1.0f;
     Cg32T a = cg32_args(c, stz);
     a.mg = 1;
     k_tma_dir_matvec32<<<c->cta32, kThreads, kStages * 2 * kSlot + 128, c->stream>>>(c->map_z, c->map_pa, c->map_pb, a);
-    if (c->x_only) {
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        k_x_update32<<<sms * 8, 256, 0, c->stream>>>(a);
-    } else {
+    if (!c->x_only) {
         k_tma_update32<<<c->cta32b, kThreads, kStages * 2 * kSlot + 128, c->stream>>>(c->map_r, c->map_pa, c->map_pb,
                                                                                 a);
     }

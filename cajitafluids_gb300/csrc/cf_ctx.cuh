@@ -36,6 +36,9 @@ struct cf_ctx {
     // solver vectors (owned cells)
     int vpitch = 0;
     cf::Vec64 x{}, r{}, pa{}, pb{}, qv{}, b{};
+    // mixed: the second buffer of the double-float solution (the MG-PCG's
+    // fused x update writes the updated x there; SolverState::xsel)
+    cf::Vec64 xb{};
     // FP32 vectors with a one-cell ghost ring: element (i, j) at a[j * p32 + i],
     // storage base = a - p32 - 4 (see cf_cg32.cu)
     cf::Vec32 r32{}, pa32{}, pb32{};
@@ -45,6 +48,7 @@ struct cf_ctx {
     int tiles_x = 0, tiles = 0, cta32 = 0, cta32b = 0;
     double* partials = nullptr;  // 4 * n_units
     int G = 0, B = 0, n_units = 0;
+    int sms = 1;  // multiprocessors of the device (launch sizing)
     cf::SolverState* S = nullptr;   // device
     cf::SolverState* hS = nullptr;  // pinned host mirror (solver state copied back)
     cf::SolverState* hP = nullptr;  // pinned solver parameters copied in (not overwritten by a projection)

@@ -81,6 +81,7 @@ struct SolverState {
     int inner_iter, inner_status;
     int outer_iter, max_outer;
     int test_stall;  // test knob (cf_test_stall_wait): see k_tma_dir_matvec32
+    int xsel;        // mixed MG-PCG, fused x update: the x buffer holding the solution
     unsigned int ticket[8];
 };
 

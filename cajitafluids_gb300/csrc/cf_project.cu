@@ -551,45 +551,70 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
     }
 }
 
-// true while the outer refinement is due: the solve runs and the inner
-// iteration has stopped (read once per block)
-__device__ __forceinline__ bool outer_due(const SolverState* S) {
-    __shared__ int due;
-    if (threadIdx.x == 0 && threadIdx.y == 0)
-        due = *(volatile const int*)&S->status == ST_RUNNING &&
-              *(volatile const int*)&S->inner_status != ST_RUNNING;
-    __syncthreads();
-    return due != 0;
-}
-
 // Outer refinement (reliable update): r = b - A x in double-float, x as the
-// inner iterations left it; inner r = hi part.
+// inner iterations left it; inner r = hi part.  The mixed MG-PCG with an
+// update after every iteration (x_only) fuses the iteration's x += alpha p
+// into it: x is read from one of two buffers and the updated x written to the
+// other (SolverState::xsel names the current one), since a unit reads its
+// neighbours' boundary rows while they write theirs.
 struct Outer {
     int nx, ny, per_x, per_y, G, U, pitch, pitch32;
     float dfac[16];  // diagonal / scale by wall-adjacency bits
     float minv32[16];
     float2 scale;    // dt / (rho dx^2) as hi + lo
-    const float2 *x, *b;
+    float2* xbuf[2]; // the solution as double-float pairs: two buffers
+    const float2* b;
+    const float *pa, *pb;  // search directions (fused update: p of iteration it is pa when it is odd)
     float* r32;
     double *part0, *part1, *part2;
     SolverState* S;
     int gated;  // inside the MG-PCG graph: run only while the refinement is due
 };
 
-__device__ __forceinline__ float2 xval(const Outer& a, int c, int j) {
+// The solution values the residual is taken of: x itself, or (fused, upd)
+// x + alpha p, one df_add_f of fl32(alpha p) per cell (the x update of the
+// mixed CG's K2).
+struct XSrc {
+    const float2* x;
+    const float* p;
+    float alpha;
+    bool upd;
+};
+
+__device__ __forceinline__ float2 xval(const Outer& a, const XSrc& xs, int c, int j) {
     int cc = wrap_index(c, a.nx, a.per_x), jj = wrap_index(j, a.ny, a.per_y);
     if (cc < 0 || jj < 0) return make_float2(0.f, 0.f);
-    return a.x[(size_t)jj * a.pitch + cc];
+    const float2 v = xs.x[(size_t)jj * a.pitch + cc];
+    return xs.upd ? df_add_f(v, xs.alpha * xs.p[(ptrdiff_t)jj * a.pitch32 + cc]) : v;
 }
 
 // x at columns c0, c0 + 1 of row j (wrapped row; 0 beyond a wall or past nx)
-__device__ __forceinline__ float4 xrow2(const Outer& a, const float2* v, int c0, int j) {
+__device__ __forceinline__ float4 xrow2(const Outer& a, const XSrc& xs, int c0, int j) {
     int jj = wrap_index(j, a.ny, a.per_y);
     if (jj < 0 || c0 >= a.nx) return make_float4(0.f, 0.f, 0.f, 0.f);
-    const float2* row = v + (size_t)jj * a.pitch + c0;
-    if (c0 + 1 < a.nx) return *reinterpret_cast<const float4*>(row);
-    const float2 x0 = row[0];
+    const float2* row = xs.x + (size_t)jj * a.pitch + c0;
+    const float* prow = xs.p + (ptrdiff_t)jj * a.pitch32 + c0;
+    if (c0 + 1 < a.nx) {
+        float4 v = *reinterpret_cast<const float4*>(row);
+        if (xs.upd) {
+            const float2 n0 = df_add_f(make_float2(v.x, v.y), xs.alpha * prow[0]);
+            const float2 n1 = df_add_f(make_float2(v.z, v.w), xs.alpha * prow[1]);
+            v = make_float4(n0.x, n0.y, n1.x, n1.y);
+        }
+        return v;
+    }
+    float2 x0 = row[0];
+    if (xs.upd) x0 = df_add_f(x0, xs.alpha * prow[0]);
     return make_float4(x0.x, x0.y, 0.f, 0.f);
+}
+
+// b at columns c0, c0 + 1 of row j (owned row)
+__device__ __forceinline__ float4 brow2(const Outer& a, int c0, int j) {
+    if (c0 >= a.nx) return make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2* row = a.b + (size_t)j * a.pitch + c0;
+    if (c0 + 1 < a.nx) return *reinterpret_cast<const float4*>(row);
+    const float2 b0 = row[0];
+    return make_float4(b0.x, b0.y, 0.f, 0.f);
 }
 
 // a + b for double-float pairs of like magnitude, error ~2^-44 (|a| + |b|)
@@ -625,37 +650,62 @@ __device__ __forceinline__ float2 df_resid_int(const Outer& a, float2 b, float2 
 
 // Interior unit (every cell and neighbour inside the domain, no wrap, no
 // wall): the same arithmetic without the boundary logic.  The rows arrive
-// through a per-warp cp.async ring OR_RING - 1 rows ahead (group k: x of
-// row j0 - 1 + k, and for the unit's own rows b and the outer columns'
-// neighbours of lanes 0 and 31); each lane reads back only what it copied.
+// through a per-warp cp.async ring OR_RING - 1 rows ahead (group k: x (and,
+// fused, p) of row j0 - 1 + k, and for the unit's own rows b; the outer
+// columns' neighbours of lanes 0 and 31); each lane reads back only what it
+// copied.  Slot layout (floats): x row [0, 128), b row [128, 256), the edge
+// x pairs of lanes 0 / 31 at 256 / 258, p row [264, 328), edge p at 328 / 329.
 constexpr int OR_RING = 4;
-constexpr int OR_SLOT = 64 * 2 + 64 * 2 + 8;  // floats: x row, b row, two edge pairs (16-byte multiple)
-__device__ __forceinline__ void outer_unit_interior(const Outer& a, float* ring, int lane, int c0, int j0, int j1,
-                                                    float& arz, float& arr) {
+template <bool FUSED>
+struct OrSlot {
+    static constexpr int value = FUSED ? 332 : 264;  // 16-byte multiples
+};
+template <bool FUSED>
+__device__ __forceinline__ void outer_unit_interior(const Outer& a, const XSrc& xs, float2* xo, float* ring, int lane,
+                                                    int c0, int j0, int j1, float& arz, float& arr) {
+    constexpr int SLOT = OrSlot<FUSED>::value;
+    const bool upd = FUSED && xs.upd;
     const float m0 = a.minv32[0];
     const bool edge = lane == 0 || lane == 31;
     const int ec = lane == 0 ? c0 - 1 : c0 + 2;  // outer neighbour column of lanes 0 and 31
     const int eo = 256 + (lane == 31 ? 2 : 0);
+    const int eop = 328 + (lane == 31 ? 1 : 0);
     const int last = j1;                         // groups cover rows j0 - 1 .. j1
     auto issue = [&](int k) {
         const int row = j0 - 1 + k;
-        float* sl = ring + (k % OR_RING) * OR_SLOT;
+        float* sl = ring + (k % OR_RING) * SLOT;
         if (row <= last) {
             const size_t o = (size_t)row * a.pitch;
-            cpa16(sl + 4 * lane, a.x + o + c0);
-            if (row >= j0 && row < j1) {
-                cpa16(sl + 128 + 4 * lane, a.b + o + c0);
-                if (edge) cpa8(sl + eo, a.x + o + ec);
+            cpa16(sl + 4 * lane, xs.x + o + c0);
+            if (upd) cpa8(sl + 264 + 2 * lane, xs.p + (ptrdiff_t)row * a.pitch32 + c0);
+            if (row >= j0 && row < j1) cpa16(sl + 128 + 4 * lane, a.b + o + c0);
+            if (edge) {
+                cpa8(sl + eo, xs.x + o + ec);
+                if (upd) cpa4(sl + eop, xs.p + (ptrdiff_t)row * a.pitch32 + ec);
             }
         }
         cpa_commit();
     };
-    auto xrow = [&](int k) { return *reinterpret_cast<const float4*>(ring + (k % OR_RING) * OR_SLOT + 4 * lane); };
+    auto xrow = [&](int k) {
+        const float* sl = ring + (k % OR_RING) * SLOT;
+        float4 v = *reinterpret_cast<const float4*>(sl + 4 * lane);
+        if (upd) {
+            const float2 pv = *reinterpret_cast<const float2*>(sl + 264 + 2 * lane);
+            const float2 n0 = df_add_f(make_float2(v.x, v.y), xs.alpha * pv.x);
+            const float2 n1 = df_add_f(make_float2(v.z, v.w), xs.alpha * pv.y);
+            v = make_float4(n0.x, n0.y, n1.x, n1.y);
+        }
+        return v;
+    };
     auto brow = [&](int k) {
-        return *reinterpret_cast<const float4*>(ring + (k % OR_RING) * OR_SLOT + 128 + 4 * lane);
+        return *reinterpret_cast<const float4*>(ring + (k % OR_RING) * SLOT + 128 + 4 * lane);
     };
     auto erow = [&](int k) {
-        return edge ? *reinterpret_cast<const float2*>(ring + (k % OR_RING) * OR_SLOT + eo) : make_float2(0.f, 0.f);
+        if (!edge) return make_float2(0.f, 0.f);
+        const float* sl = ring + (k % OR_RING) * SLOT;
+        float2 v = *reinterpret_cast<const float2*>(sl + eo);
+        if (upd) v = df_add_f(v, xs.alpha * sl[eop]);
+        return v;
     };
 #pragma unroll
     for (int k = 0; k < OR_RING - 1; ++k) issue(k);
@@ -668,6 +718,7 @@ __device__ __forceinline__ void outer_unit_interior(const Outer& a, float* ring,
     float2 ev = erow(1);
     for (int j = j0; j < j1; ++j) {
         const int k = j - j0 + 2;  // group of row j + 1
+        if (upd) *reinterpret_cast<float4*>(xo + (size_t)j * a.pitch + c0) = xc;
         issue(k + OR_RING - 1);
         cpa_wait<OR_RING - 1>();
         const float4 xp = xrow(k), bn = brow(k);
@@ -693,11 +744,33 @@ __device__ __forceinline__ void outer_unit_interior(const Outer& a, float* ring,
     cpa_wait<0>();
 }
 
-// one warp per unit of 64 columns x 16 rows, lane l on columns 2l, 2l + 1;
-// rows slide through registers, W/E neighbours come by shuffle
+// One warp per unit of 64 columns x 16 rows, lane l on columns 2l, 2l + 1;
+// rows slide through registers, W/E neighbours come by shuffle.  FUSED: the
+// x update of the iteration first (when the inner step did not break down),
+// the updated x written to the other buffer.
+template <bool FUSED>
 __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
     SolverState* S = a.S;
-    if (a.gated && !outer_due(S)) return;
+    __shared__ int mode_s, sel_s, it_s;
+    __shared__ float alpha_s;
+    if (threadIdx.x == 0) {
+        const int st = *(volatile const int*)&S->status, ist = *(volatile const int*)&S->inner_status;
+        int mode;  // 0: nothing to do, 1: residual of x, 2: x update and residual
+        if (FUSED)
+            mode = st != ST_RUNNING ? 0 : (ist == ST_RUNNING ? 2 : 1);
+        else
+            mode = (!a.gated || (st == ST_RUNNING && ist != ST_RUNNING)) ? 1 : 0;
+        mode_s = mode;
+        sel_s = S->xsel;
+        it_s = S->inner_iter;
+        alpha_s = (float)S->alpha_in;
+    }
+    __syncthreads();
+    const int mode = mode_s;
+    if (mode == 0) return;
+    const int sel = sel_s, it = it_s;
+    const XSrc xs{a.xbuf[sel], (it & 1) ? a.pa : a.pb, alpha_s, FUSED && mode == 2};
+    float2* xo = a.xbuf[sel ^ 1];
     const int lane = threadIdx.x & 31;
     const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
     float arz = 0.f, arr = 0.f;
@@ -706,29 +779,30 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
     // rows j0u - 1 .. j1u + 1 and columns g * 64 - 1 .. g * 64 + 64 are read
     const bool interior = unit < a.U && g * CF_UNIT_COLS >= 1 && (g + 1) * CF_UNIT_COLS + 1 <= a.nx &&
                           j0u >= 1 && j1u + 2 <= a.ny;
-    __shared__ __align__(16) float ring[CF_RED_WARPS * OR_RING * OR_SLOT];
+    __shared__ __align__(16) float ring[CF_RED_WARPS * OR_RING * OrSlot<FUSED>::value];
     if (interior) {
-        outer_unit_interior(a, ring + (threadIdx.x >> 5) * OR_RING * OR_SLOT, lane, g * CF_UNIT_COLS + 2 * lane, j0u,
-                            j1u, arz, arr);
+        outer_unit_interior<FUSED>(a, xs, xo, ring + (threadIdx.x >> 5) * OR_RING * OrSlot<FUSED>::value, lane,
+                                   g * CF_UNIT_COLS + 2 * lane, j0u, j1u, arz, arr);
     } else if (unit < a.U) {
         const int c0 = g * CF_UNIT_COLS + 2 * lane;
         const int j0 = j0u;
         const int j1 = j1u;
         // rows j - 1, j, j + 1 in registers; row j + 2 and b of row j + 1 are
         // fetched one row ahead, so the loads overlap the arithmetic
-        float4 xm = xrow2(a, a.x, c0, j0 - 1), xc = xrow2(a, a.x, c0, j0), xp = xrow2(a, a.x, c0, j0 + 1);
-        float4 bnext = xrow2(a, a.b, c0, j0);
+        float4 xm = xrow2(a, xs, c0, j0 - 1), xc = xrow2(a, xs, c0, j0), xp = xrow2(a, xs, c0, j0 + 1);
+        float4 bnext = brow2(a, c0, j0);
         for (int j = j0; j < j1; ++j) {
-            const float4 xpp = xrow2(a, a.x, c0, j + 2);
+            const float4 xpp = xrow2(a, xs, c0, j + 2);
             const float4 bv = bnext;
-            if (j + 1 < j1) bnext = xrow2(a, a.b, c0, j + 1);
+            if (j + 1 < j1) bnext = brow2(a, c0, j + 1);
             float2 left = make_float2(__shfl_up_sync(FULLMASK, xc.z, 1), __shfl_up_sync(FULLMASK, xc.w, 1));
             float2 right = make_float2(__shfl_down_sync(FULLMASK, xc.x, 1), __shfl_down_sync(FULLMASK, xc.y, 1));
-            if (lane == 0) left = xval(a, c0 - 1, j);
-            if (lane == 31 || c0 + 2 >= a.nx) right = xval(a, c0 + 2, j);
+            if (lane == 0) left = xval(a, xs, c0 - 1, j);
+            if (lane == 31 || c0 + 2 >= a.nx) right = xval(a, xs, c0 + 2, j);
             float2 mid1 = make_float2(xc.z, xc.w);
-            if (c0 + 1 >= a.nx) mid1 = xval(a, c0 + 1, j);  // E neighbour of the last column
+            if (c0 + 1 >= a.nx) mid1 = xval(a, xs, c0 + 1, j);  // E neighbour of the last column
             if (c0 < a.nx) {
+                if (xs.upd) xo[(size_t)j * a.pitch + c0] = make_float2(xc.x, xc.y);
                 const int eb = edge_bits(c0, j, a.nx, a.ny, a.per_x, a.per_y);
                 const float2 r = df_resid(a, eb, make_float2(bv.x, bv.y), make_float2(xc.x, xc.y), left, mid1,
                                           make_float2(xm.x, xm.y), make_float2(xp.x, xp.y));
@@ -737,6 +811,7 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
                 arr = fmaf(r.x, r.x, arr);
             }
             if (c0 + 1 < a.nx) {
+                if (xs.upd) xo[(size_t)j * a.pitch + c0 + 1] = make_float2(xc.z, xc.w);
                 const int eb = edge_bits(c0 + 1, j, a.nx, a.ny, a.per_x, a.per_y);
                 const float2 r = df_resid(a, eb, make_float2(bv.z, bv.w), make_float2(xc.z, xc.w),
                                           make_float2(xc.x, xc.y), right, make_float2(xm.z, xm.w),
@@ -762,6 +837,14 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
         double rr = final_tree(a.part2, a.U);
         if (threadIdx.x == 0) {
             S->ticket[4] = 0;
+            if (FUSED && mode == 2) {
+                // the end of the inner step (as K2 ends it)
+                S->rho_prev = S->rho_in;
+                S->inner_iter = it + 1;
+                S->iter = S->iter + 1;
+                S->inner_status = ST_CONVERGED;
+                S->xsel = sel ^ 1;
+            }
             S->outer_iter += 1;
             S->rr = rr64;
             S->rr_out = rr64;
@@ -790,13 +873,15 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
     }
 }
 
-// mixed: the double-float solution, in place, to FP64 for the gradient
-__global__ void k_df_to_f64(double* x, int nx, int ny, int pitch) {
+// mixed: the double-float solution (in the buffer SolverState::xsel names)
+// to FP64 in the first buffer, for the gradient
+__global__ void k_df_to_f64(double* x, const float2* xb, const SolverState* S, int nx, int ny, int pitch) {
     int gi = blockIdx.x * blockDim.x + threadIdx.x;
     int gj = blockIdx.y * blockDim.y + threadIdx.y;
     if (gi >= nx || gj >= ny) return;
+    const float2* src = S->xsel ? xb : reinterpret_cast<const float2*>(x);
     const size_t k = (size_t)gj * pitch + gi;
-    const float2 v = reinterpret_cast<const float2*>(x)[k];
+    const float2 v = src[k];
     x[k] = f2d_exact(v.x) + f2d_exact(v.y);
 }
 
@@ -997,8 +1082,11 @@ static Outer outer_args(cf_ctx* c, const Stencil& st, int gated) {
     }
     const float hi = (float)scale;
     oa.scale = make_float2(hi, (float)(scale - (double)hi));
-    oa.x = reinterpret_cast<const float2*>(c->x.a);
+    oa.xbuf[0] = reinterpret_cast<float2*>(c->x.a);
+    oa.xbuf[1] = reinterpret_cast<float2*>(c->xb.a);
     oa.b = reinterpret_cast<const float2*>(c->b.a);
+    oa.pa = c->pa32.a;
+    oa.pb = c->pb32.a;
     oa.r32 = c->r32.a;
     oa.part0 = c->partials;
     oa.part1 = c->partials + c->n_units;
@@ -1013,7 +1101,7 @@ static Outer outer_args(cf_ctx* c, const Stencil& st, int gated) {
 static int launch_warm_init(cf_ctx* c, const Stencil& st, bool mixed) {
     if (mixed) {
         Outer oa = outer_args(c, st, 0);
-        k_outer_resid<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(oa);
+        k_outer_resid<false><<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(oa);
     } else {
         Cg64 a = cg64_args(c, st);
         k_warm_resid64<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(a);
@@ -1024,7 +1112,21 @@ static int launch_warm_init(cf_ctx* c, const Stencil& st, bool mixed) {
 // the outer refinement; gated = 1 inside the MG-PCG graph
 static void launch_outer(cf_ctx* c, const Stencil& st, int gated) {
     Outer oa = outer_args(c, st, gated);
-    k_outer_resid<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(oa);
+    k_outer_resid<false><<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(oa);
+}
+
+// one mixed MG-PCG inner iteration before its V-cycle: K1, then the x update
+// and the reliable update (fused when every iteration ends with one,
+// c->x_only; else K2 and the gated update); returns kernels launched
+static int launch_mixed_mg_step(cf_ctx* c, const Stencil& st) {
+    cg32_launch_pair_mg(c, st);
+    if (c->x_only) {
+        Outer oa = outer_args(c, st, 1);
+        k_outer_resid<true><<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(oa);
+        return 2;
+    }
+    launch_outer(c, st, 1);
+    return 3;
 }
 
 static const int kBatch = CF_CG_BATCH;  // CG iterations per graph launch
@@ -1056,9 +1158,8 @@ static int batch_mg(cf_ctx* c, const Stencil& st) {
     int per = 0;
     for (int i = 0; i < kBatchMG; ++i) {
         if (mixed) {
-            cg32_launch_pair_mg(c, st);
-            launch_outer(c, st, 1);
-            per = 3 + cg32_mg_precondition(c, scale);
+            per = launch_mixed_mg_step(c, st);
+            per += cg32_mg_precondition(c, scale);
         } else {
             k_cg_dir_matvec64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
             k_cg_update64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
@@ -1216,16 +1317,17 @@ static int launch_iterations(cf_ctx* c, const Stencil& st, bool mixed, bool mg, 
         if (mixed) {
             // MG: a reliable update follows almost every iteration, so the
             // gated outer kernels sit in every iteration; Jacobi: once a trip
-            if (mg)
-                cg32_launch_pair_mg(c, st);
-            else
+            if (mg) {
+                k += launch_mixed_mg_step(c, st);
+                k += cg32_mg_precondition(c, scale);
+            } else {
                 cg32_launch_iteration(c, st);
-            k += 2;
-            if (mg || i == n - 1) {
-                launch_outer(c, st, 1);
-                k += 1;
+                k += 2;
+                if (i == n - 1) {
+                    launch_outer(c, st, 1);
+                    k += 1;
+                }
             }
-            if (mg) k += cg32_mg_precondition(c, scale);
         } else {
             k_cg_dir_matvec64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
             k_cg_update64<<<nb, CF_RED_THREADS, 0, c->stream>>>(a);
@@ -1313,7 +1415,8 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
             dim3 blk(32, 8);
             if (mixed) {
                 dim3 grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
-                k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, c->ph.nx, c->ph.ny, c->vpitch);
+                k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, reinterpret_cast<const float2*>(c->xb.a), c->S,
+                                                        c->ph.nx, c->ph.ny, c->vpitch);
                 ntail += 1;
             }
             Press pa{c->ph, gu, gv, c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx)), adjoint, c->u32, c->v32,
@@ -1589,7 +1692,8 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     }
     if (mixed) {
         dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
-        k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, c->ph.nx, c->ph.ny, c->vpitch);
+        k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, reinterpret_cast<const float2*>(c->xb.a), c->S, c->ph.nx,
+                                                c->ph.ny, c->vpitch);
         c->launches += 1;
     }
     const SolverState* hs = c->hS;
