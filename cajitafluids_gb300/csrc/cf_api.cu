@@ -532,7 +532,12 @@ int cf_download(cf_ctx* ctx, int field, double* host, ptrdiff_t si, ptrdiff_t sj
     const double* src;
     size_t spitch;
     int rc = CF_OK;
-    if (field == CF_FIELD_PRESSURE) {
+    if (field == CF_FIELD_PRESSURE && ctx->p_df) {
+        // the last mixed projection left its solution as double-float pairs
+        rc = cuda_check(ctx, pressure_to_f64(ctx, ctx->staging), "convert");
+        src = ctx->staging;
+        spitch = ox;
+    } else if (field == CF_FIELD_PRESSURE) {
         src = ctx->x.a;
         spitch = ctx->vpitch;
     } else if (field == CF_FIELD_QUANTITY && ctx->precision == CF_PREC_MIXED) {

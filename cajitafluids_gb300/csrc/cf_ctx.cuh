@@ -39,6 +39,9 @@ struct cf_ctx {
     // mixed: the second buffer of the double-float solution (the MG-PCG's
     // fused x update writes the updated x there; SolverState::xsel)
     cf::Vec64 xb{};
+    // the last mixed projection left the pressure as double-float pairs (in
+    // the buffer SolverState::xsel names); a download converts it
+    int p_df = 0;
     // FP32 vectors with a one-cell ghost ring: element (i, j) at a[j * p32 + i],
     // storage base = a - p32 - 4 (see cf_cg32.cu)
     cf::Vec32 r32{}, pa32{}, pb32{};
@@ -170,6 +173,9 @@ int cg32_mg_setup(cf_ctx* c);
 int cg32_mg_precondition(cf_ctx* c, double scale);  // returns kernels launched
 void cg32_launch_pair_mg(cf_ctx* c, const Stencil& st);
 int div_norms(cf_ctx* c, double* l2, double* linf);
+// mixed: the double-float solution as an FP64 pressure (owned cells, row
+// pitch nx) in out
+cudaError_t pressure_to_f64(cf_ctx* c, double* out);
 // multigrid preconditioner (cf_mg.cu)
 int mg_setup(cf_ctx* c);
 void mg_free(cf_ctx* c);

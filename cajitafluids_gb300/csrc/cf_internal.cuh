@@ -129,10 +129,22 @@ __device__ __forceinline__ bool last_block_arrive(unsigned int* ticket) {
 
 // Canonical final sum over n partials; blockDim.x must be 256.  All threads
 // return the same value.
+// Each thread adds partial[t], partial[t + 256], ... in that order; the
+// loads go out eight at a time ahead of the additions (one block does this
+// at the end of a launch, so a chain of dependent loads would be its tail).
+constexpr int CF_FOLD_BATCH = 8;
 __device__ __forceinline__ double final_tree(const double* partial, int n) {
     __shared__ double ws[CF_RED_WARPS];
     double s = 0.0;
-    for (int u = threadIdx.x; u < n; u += CF_RED_THREADS) s = s + __ldcg(partial + u);
+    int u = threadIdx.x;
+    for (; u + (CF_FOLD_BATCH - 1) * CF_RED_THREADS < n; u += CF_FOLD_BATCH * CF_RED_THREADS) {
+        double v[CF_FOLD_BATCH];
+#pragma unroll
+        for (int k = 0; k < CF_FOLD_BATCH; ++k) v[k] = __ldcg(partial + u + k * CF_RED_THREADS);
+#pragma unroll
+        for (int k = 0; k < CF_FOLD_BATCH; ++k) s = s + v[k];
+    }
+    for (; u < n; u += CF_RED_THREADS) s = s + __ldcg(partial + u);
     s = warp_fold(s);
     __syncthreads();
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
@@ -147,7 +159,15 @@ __device__ __forceinline__ double final_tree(const double* partial, int n) {
 __device__ __forceinline__ double final_max(const double* partial, int n) {
     __shared__ double ws[CF_RED_WARPS];
     double s = 0.0;
-    for (int u = threadIdx.x; u < n; u += CF_RED_THREADS) s = fmax(s, __ldcg(partial + u));
+    int u = threadIdx.x;
+    for (; u + (CF_FOLD_BATCH - 1) * CF_RED_THREADS < n; u += CF_FOLD_BATCH * CF_RED_THREADS) {
+        double v[CF_FOLD_BATCH];
+#pragma unroll
+        for (int k = 0; k < CF_FOLD_BATCH; ++k) v[k] = __ldcg(partial + u + k * CF_RED_THREADS);
+#pragma unroll
+        for (int k = 0; k < CF_FOLD_BATCH; ++k) s = fmax(s, v[k]);
+    }
+    for (; u < n; u += CF_RED_THREADS) s = fmax(s, __ldcg(partial + u));
     s = warp_max(s);
     __syncthreads();
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;

@@ -354,7 +354,7 @@ struct DivArgs {
     Stencil st;
     double *x, *r, *b;
     float* r32;
-    double *part0, *part1, *part2;
+    double *part0, *part1;
     double* out;
     SolverState* S;
     int warm;  // keep x from the previous solve (warm start) instead of x = 0
@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
     SolverState* S = a.S;
     const int lane = threadIdx.x & 31;
     const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
-    float abb = 0.f, arz = 0.f, arr = 0.f;
+    float abb = 0.f, arz = 0.f;
     if (unit < a.U) {
         const int g = unit % a.G, band = unit / a.G;
         const int c0 = g * CF_UNIT_COLS + 2 * lane;
@@ -507,20 +507,19 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
                 float z = a.st.minv32[edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y)] * r;
                 abb = fmaf(r, r, abb);
                 arz = fmaf(r, z, arz);
-                arr = fmaf(r, r, arr);
             }
     }
+    // inner r.r equals b.b here (the same squares in the same order)
     const double dbb = warp_fold((double)abb);
-    double drz = warp_fold((double)arz), drr = warp_fold((double)arr);
+    const double drz = warp_fold((double)arz);
     if (unit < a.U && lane == 0) {
         a.part0[unit] = dbb;
         a.part1[unit] = drz;
-        a.part2[unit] = drr;
     }
     if (last_block_arrive(&S->ticket[2])) {
-        double bb = final_tree(a.part0, a.U);
-        double rz = final_tree(a.part1, a.U);
-        double rr = final_tree(a.part2, a.U);
+        const double bb = final_tree(a.part0, a.U);
+        const double rz = final_tree(a.part1, a.U);
+        const double rr = bb;
         if (threadIdx.x == 0) {
             S->ticket[2] = 0;
             S->bb = bb;
@@ -566,7 +565,7 @@ struct Outer {
     const float2* b;
     const float *pa, *pb;  // search directions (fused update: p of iteration it is pa when it is odd)
     float* r32;
-    double *part0, *part1, *part2;
+    double *part0, *part1;
     SolverState* S;
     int gated;  // inside the MG-PCG graph: run only while the refinement is due
 };
@@ -829,12 +828,11 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
     if (unit < a.U && lane == 0) {
         a.part0[unit] = drr;
         a.part1[unit] = drz;
-        a.part2[unit] = drr;
     }
     if (last_block_arrive(&S->ticket[4])) {
-        double rr64 = final_tree(a.part0, a.U);
-        double rz = final_tree(a.part1, a.U);
-        double rr = final_tree(a.part2, a.U);
+        const double rr64 = final_tree(a.part0, a.U);
+        const double rz = final_tree(a.part1, a.U);
+        const double rr = rr64;
         if (threadIdx.x == 0) {
             S->ticket[4] = 0;
             if (FUSED && mode == 2) {
@@ -885,6 +883,16 @@ __global__ void k_df_to_f64(double* x, const float2* xb, const SolverState* S, i
     x[k] = f2d_exact(v.x) + f2d_exact(v.y);
 }
 
+// the same into out (owned cells, row pitch nx), for a download
+__global__ void k_df_to_f64_out(const float2* x, const float2* xb, const SolverState* S, int nx, int ny, int pitch,
+                                double* out) {
+    int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    if (gi >= nx || gj >= ny) return;
+    const float2 v = (S->xsel ? xb : x)[(size_t)gj * pitch + gi];
+    out[(size_t)gj * nx + gi] = f2d_exact(v.x) + f2d_exact(v.y);
+}
+
 // --------------------------------------------------------------------------
 // _applyPressure (:214-264).  z = 0: I-faces, z = 1: J-faces.  Quirk Q1 (the
 // J-face wall condition lands on u, :260) zeroes u in row 0 (done in the
@@ -900,12 +908,40 @@ struct Press {
     // copies (the next FP32 advection's velocity arrays)
     Grid<float> u32, v32;
     int w32;
+    // mixed (xdf = 1): the solution is read as double-float pairs from the
+    // buffer SolverState::xsel names (x or xb); the pressure difference and
+    // its product with ms (ms2 = ms as a pair) run on the FP32 pipe and two
+    // FP64 additions apply it, instead of three FP64 operations on an FP64
+    // solution made by a conversion pass
+    int xdf;
+    float2 ms2;
+    const float2* xb;
+    const SolverState* S;
 };
 
 __device__ __forceinline__ double pval(const Press& a, int gi, int gj) {
     int ci = wrap_index(gi, a.p.nx, a.p.per_x), cj = wrap_index(gj, a.p.ny, a.p.per_y);
     if (ci < 0 || cj < 0) return 0.0;
     return a.x[(size_t)cj * a.pitch + ci];
+}
+
+__device__ __forceinline__ float2 pval_df(const Press& a, const float2* x, int gi, int gj) {
+    int ci = wrap_index(gi, a.p.nx, a.p.per_x), cj = wrap_index(gj, a.p.ny, a.p.per_y);
+    if (ci < 0 || cj < 0) return make_float2(0.f, 0.f);
+    return x[(size_t)cj * a.pitch + ci];
+}
+
+// w + ms (p(c) - p(n)): FP64 as the reference writes it (one rounding per
+// operation; ms = -scale), or (xdf) from the double-float solution
+__device__ __forceinline__ double press_update(const Press& a, const float2* xdf, double w, int ci, int cj, int ni,
+                                               int nj) {
+    if (a.xdf) {
+        const float2 pc = pval_df(a, xdf, ci, cj), pn = pval_df(a, xdf, ni, nj);
+        const float2 m = df_mul(a.ms2, df_add_s(pc, make_float2(-pn.x, -pn.y)));
+        return __dadd_rn(__dadd_rn(w, f2d_exact(m.x)), f2d_exact(m.y));
+    }
+    const double d = pval(a, ci, cj) - pval(a, ni, nj);
+    return __dadd_rn(w, __dmul_rn(a.ms, d));
 }
 
 __global__ void k_apply_pressure(Press a) {
@@ -917,12 +953,11 @@ __global__ void k_apply_pressure(Press a) {
     int oy = p.ny + ((axis == 1 && !p.per_y) ? 1 : 0);
     if (gi >= ox || gj >= oy) return;
     const bool fix_q1 = (p.quirks & 1u) != 0;
+    const float2* xdf = a.xdf ? (a.S->xsel ? a.xb : reinterpret_cast<const float2*>(a.x)) : nullptr;
     if (axis == 0) {
         double& u = a.u.at(gi + CF_HALO, gj + CF_HALO);
-        // u -= scale * (p(i) - p(i-1)) (src/VelocityCorrector.hpp:245), one
-        // rounding per operation; ms = -scale, so u + ms*d gives those bits
-        double d = pval(a, gi, gj) - pval(a, gi - 1, gj);
-        double w = __dadd_rn(u, __dmul_rn(a.ms, d));
+        // u -= scale * (p(i) - p(i-1)) (src/VelocityCorrector.hpp:245)
+        double w = press_update(a, xdf, u, gi, gj, gi - 1, gj);
         if (!a.adjoint) {
             if (!p.per_x) {
                 if (gi <= 0 && p.bc[0] == 0) w = 0.0;
@@ -934,8 +969,7 @@ __global__ void k_apply_pressure(Press a) {
         if (a.w32) a.u32.at(gi + CF_HALO, gj + CF_HALO) = d2f_rn(w);
     } else {
         double& v = a.v.at(gi + CF_HALO, gj + CF_HALO);
-        double d = pval(a, gi, gj) - pval(a, gi, gj - 1);
-        double w = __dadd_rn(v, __dmul_rn(a.ms, d));  // :256
+        double w = press_update(a, xdf, v, gi, gj, gi, gj - 1);  // :256
         if (!p.per_y && !a.adjoint) {
             if (fix_q1) {
                 if (gj <= 0 && p.bc[1] == 0) w = 0.0;
@@ -1031,10 +1065,32 @@ static DivArgs div_args(cf_ctx* c, const Stencil& st) {
     a.r32 = c->r32.a;
     a.part0 = c->partials;
     a.part1 = c->partials + c->n_units;
-    a.part2 = c->partials + 2 * c->n_units;
     a.out = c->d_out;
     a.S = c->S;
     return a;
+}
+
+// the gradient subtraction's arguments; a mixed projection without a warm
+// start reads the double-float solution directly (xdf): its FP64 pressure is
+// made only when it is downloaded (c->p_df)
+static Press press_args(cf_ctx* c, double dt, Grid<double> gu, Grid<double> gv, int adjoint, bool w32, bool xdf) {
+    Press pa{};
+    pa.p = c->ph;
+    pa.u = gu;
+    pa.v = gv;
+    pa.x = c->x.a;
+    pa.pitch = c->vpitch;
+    pa.ms = -(dt / (c->density * c->ph.dx));
+    pa.adjoint = adjoint;
+    pa.u32 = c->u32;
+    pa.v32 = c->v32;
+    pa.w32 = w32 ? 1 : 0;
+    pa.xdf = xdf ? 1 : 0;
+    const float hi = (float)pa.ms;
+    pa.ms2 = make_float2(hi, (float)(pa.ms - (double)hi));
+    pa.xb = reinterpret_cast<const float2*>(c->xb.a);
+    pa.S = c->S;
+    return pa;
 }
 
 static Cg64 cg64_args(cf_ctx* c, const Stencil& st) {
@@ -1090,7 +1146,6 @@ static Outer outer_args(cf_ctx* c, const Stencil& st, int gated) {
     oa.r32 = c->r32.a;
     oa.part0 = c->partials;
     oa.part1 = c->partials + c->n_units;
-    oa.part2 = c->partials + 2 * c->n_units;
     oa.S = c->S;
     oa.gated = gated;
     return oa;
@@ -1413,14 +1468,16 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
     if (!rc)
         rc = capture_graph(c, &tail, [&] {
             dim3 blk(32, 8);
-            if (mixed) {
+            // mixed: the gradient reads the double-float solution, unless a
+            // warm start wants the FP64 pressure kept for the next solve
+            const bool xdf = mixed && !adjoint && !warm;
+            if (mixed && !xdf) {
                 dim3 grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
                 k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, reinterpret_cast<const float2*>(c->xb.a), c->S,
                                                         c->ph.nx, c->ph.ny, c->vpitch);
                 ntail += 1;
             }
-            Press pa{c->ph, gu, gv, c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx)), adjoint, c->u32, c->v32,
-                     (mixed && !adjoint) ? 1 : 0};
+            Press pa = press_args(c, dt, gu, gv, adjoint, mixed && !adjoint, xdf);
             dim3 grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
             k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
             // u, v are final here: a caller may copy them out beside the norms
@@ -1461,6 +1518,18 @@ static bool resident_enabled() {
 
 bool resident_projection() { return resident_enabled(); }
 
+// A warm start reads the previous solution as an FP64 pressure: convert it in
+// place when the last mixed projection left it as double-float pairs (before
+// the solver state is replaced: the conversion reads SolverState::xsel).
+static void settle_pressure(cf_ctx* c) {
+    if (!c->p_df) return;
+    dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
+    k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, reinterpret_cast<const float2*>(c->xb.a), c->S, c->ph.nx, c->ph.ny,
+                                            c->vpitch);
+    c->launches += 1;
+    c->p_df = 0;
+}
+
 // the projection of gu, gv (the current buffers, or with adjoint = 1 the
 // adjoint's face arrays) through a resident graph; with defer, returns after
 // the launch (project_collect reads the results)
@@ -1493,6 +1562,7 @@ static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResul
     // must not have a later step read an earlier step's final state.  The
     // adjoint's projections have a buffer of their own, so that forward and
     // adjoint projections can be enqueued in turn.
+    if (flags & 4) settle_pressure(c);
     SolverState* h = adjoint ? c->hPa : c->hP;
     if (!params_ready) {
         memset(h, 0, sizeof(SolverState));
@@ -1511,6 +1581,7 @@ static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResul
     cudaMemcpyAsync(c->S, h, sizeof(SolverState), cudaMemcpyHostToDevice, c->stream);
     if ((rc = cuda_check(c, cudaGraphLaunch(c->rgx[slot], c->stream), "graph launch"))) return rc;
     if (mixed && !adjoint) c->uv32 = 1;  // the graph's gradient subtraction wrote the FP32 velocity copies
+    c->p_df = (mixed && !adjoint && !(flags & 4)) ? 1 : 0;
     c->rg_pending = slot;
     if (defer) return CF_OK;
     if ((rc = cuda_check(c, cudaStreamSynchronize(c->stream), "projection"))) return rc;
@@ -1560,6 +1631,15 @@ int project_adjoint_async(cf_ctx* c, double dt, const SolveOpts& o, SolveResult*
     return project_resident(c, dt, o, res, st, c->precision == CF_PREC_MIXED, mg, true, params_ready, gu, gv, 1);
 }
 
+cudaError_t pressure_to_f64(cf_ctx* c, double* out) {
+    dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
+    k_df_to_f64_out<<<grd, blk, 0, c->stream>>>(reinterpret_cast<const float2*>(c->x.a),
+                                                reinterpret_cast<const float2*>(c->xb.a), c->S, c->ph.nx, c->ph.ny,
+                                                c->vpitch, out);
+    c->launches += 1;
+    return cudaGetLastError();
+}
+
 int div_norms(cf_ctx* c, double* l2, double* linf) {
     Stencil st{};
     DivArgs a = div_args(c, st);
@@ -1597,6 +1677,7 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     rc = mg ? ensure_graph_mg(c, st) : ensure_graph(c, st, mixed);
     if (rc) return rc;
 
+    if (adjoint ? c->adj_warm : c->warm) settle_pressure(c);
     // solver parameters
     SolverState* h = c->hS;
     memset(h, 0, sizeof(SolverState));
@@ -1690,7 +1771,9 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
             }
         }
     }
-    if (mixed) {
+    if (mixed && (adjoint || warm)) {
+        // the FP64 pressure now (a warm start reads it); otherwise the
+        // gradient reads the double-float solution and a download converts it
         dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
         k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, reinterpret_cast<const float2*>(c->xb.a), c->S, c->ph.nx,
                                                 c->ph.ny, c->vpitch);
@@ -1705,8 +1788,8 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
 
     // gradient subtraction
     const bool w32 = mixed && !adjoint && gu.o == c->u[c->cur].o && gv.o == c->v[c->cur].o;
-    Press pa{c->ph, gu, gv, c->x.a, c->vpitch, -(dt / (c->density * c->ph.dx)), adjoint, c->u32, c->v32,
-             w32 ? 1 : 0};
+    Press pa = press_args(c, dt, gu, gv, adjoint, w32, mixed && !adjoint && !warm);
+    c->p_df = pa.xdf;
     dim3 blk(32, 8), grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
     k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
     c->launches += 1;

@@ -35,11 +35,12 @@ def test_bytes_per_cell_4096_periodic():
     above, last = _geometric(lv)
     n = nx * ny
     per = lambda **k: bench.alg_bytes_per_iter(nx, ny, (True, True), **k) / n
-    # mixed, an update after every iteration: K1 3 words, x step R p + R/W x (4 + 16),
-    # V-cycle 5.5 words per level cell, coarsest 2 words, reliable update 20
+    # mixed, an update after every iteration: K1 3 words, the x step fused with
+    # the reliable update (R p 4, R x 8, R b 8, W x 8, W r 4 = 32), V-cycle 5.5
+    # words per level cell, coarsest 2 words
     assert per(precon="PFMG", word=4, outer_frac=1.0, mixed=True) == pytest.approx(
-        12 + 20 + 22 * above + 8 * last + 20, rel=1e-12)
-    assert per(precon="PFMG", word=4, outer_frac=1.0, mixed=True) == pytest.approx(81.333, abs=1e-3)
+        12 + 32 + 22 * above + 8 * last, rel=1e-12)
+    assert per(precon="PFMG", word=4, outer_frac=1.0, mixed=True) == pytest.approx(73.333, abs=1e-3)
     # mixed, updates on half the iterations: the inner step also moves r (3 words + x pair)
     assert per(precon="PFMG", word=4, outer_frac=0.5, mixed=True) == pytest.approx(
         12 + 28 + 22 * above + 8 * last + 10, rel=1e-12)

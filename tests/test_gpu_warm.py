@@ -81,3 +81,34 @@ def test_warm_start_rejected_by_adjoint(built):
     with pytest.raises(CfError) as e:
         c.forward_checkpointed(2, 1, 0.001, 3)
     assert e.value.code == L.CF_ERR_UNSUPPORTED
+
+
+def test_mixed_pressure_kept_as_pairs_then_warm(built):
+    """A mixed projection without a warm start leaves its solution as
+    double-float pairs (the gradient reads them; a download converts them).
+    Switching the warm start on afterwards converts them first, so the next
+    projection starts from the same FP64 pressure as in a context that kept
+    the warm start on throughout: same pressure downloads, same second
+    projection, bit for bit."""
+    n = 96
+    rng = np.random.default_rng(21)
+    so = opts(tol=1e-9, max_iter=500, precon="PFMG")
+    a = make_pair(n, n, periodic=(True, False), precision="mixed", precon_mg=True)
+    b = make_pair(n, n, periodic=(True, False), precision="mixed", precon_mg=True, warm_start=True)
+    st = random_state(a[0], rng, scale=0.1)
+    for _, c in (a, b):
+        load_state(a[0], c, st)
+    ca, cb = a[1], b[1]
+    ra = ca.project(0.002, so, raise_on_maxit=True)
+    rb = cb.project(0.002, so, raise_on_maxit=True)
+    assert ra["iterations"] == rb["iterations"]
+    assert np.array_equal(ca.download("p"), cb.download("p"))
+    ca.set_warm_start(True)
+    for c in (ca, cb):
+        for f in ("u", "v"):
+            c.upload(f, st[f])
+    ra = ca.project(0.002, so, raise_on_maxit=True)
+    rb = cb.project(0.002, so, raise_on_maxit=True)
+    assert ra["iterations"] == rb["iterations"]
+    for f in ("u", "v", "p"):
+        assert np.array_equal(ca.download(f), cb.download(f)), f
