@@ -228,6 +228,8 @@ int enqueue_step(cf_ctx* ctx, double dt, int value_order, const SolveOpts& so, S
 }
 
 int parse_solver_opts(cf_ctx* ctx, const cf_solver_opts* opts, SolveOpts* so) { return parse_opts(ctx, opts, so); }
+
+int alloc_grid64(cf_ctx* c, Grid<double>& g, int ex, int ey) { return alloc_grid(c, g, ex, ey); }
 }  // namespace cf
 
 extern "C" {
@@ -291,10 +293,6 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
             rc = alloc_grid(c, c->q32[s], nx + 2 * CF_HALO, ny + 2 * CF_HALO);
         if (!rc) rc = alloc_grid(c, c->u[s], nx + 2 * CF_HALO + 1, ny + 2 * CF_HALO);
         if (!rc) rc = alloc_grid(c, c->v[s], nx + 2 * CF_HALO, ny + 2 * CF_HALO + 1);
-    }
-    if (!rc && c->precision == CF_PREC_MIXED) {
-        rc = alloc_grid(c, c->u32, nx + 2 * CF_HALO + 1, ny + 2 * CF_HALO);
-        if (!rc) rc = alloc_grid(c, c->v32, nx + 2 * CF_HALO, ny + 2 * CF_HALO + 1);
     }
     c->vpitch = (int)round_up(nx, 32);
     size_t vn = (size_t)c->vpitch * ny;
@@ -487,12 +485,15 @@ int cf_upload(cf_ctx* ctx, int field, const double* host, ptrdiff_t si, ptrdiff_
     if (si <= 0 || sj <= 0) return fail(ctx, CF_ERR_INVALID, "strides must be positive");
     int s = ctx->cur;
     bool q32 = field == CF_FIELD_QUANTITY && ctx->precision == CF_PREC_MIXED;
-    if (field != CF_FIELD_QUANTITY) ctx->uv32 = 0;
+    // a mixed context's u, v are stored as double-float pairs: the FP64
+    // values land in place and are split there
+    const bool pairs = field != CF_FIELD_QUANTITY && ctx->precision == CF_PREC_MIXED;
     Grid<double> g = field == CF_FIELD_QUANTITY ? ctx->q64[s] : (field == CF_FIELD_U ? ctx->u[s] : ctx->v[s]);
     int rc;
     if (si == 1 && !q32) {
         rc = cuda_check(ctx, cudaMemcpy2DAsync(&g.at(CF_HALO, CF_HALO), g.pitch * sizeof(double), host, sj * sizeof(double),
                                                ox * sizeof(double), oy, cudaMemcpyDefault, ctx->stream), "upload");
+        if (!rc && pairs) rc = cuda_check(ctx, launch_to_pairs(ctx, field, s), "split");
         if (rc) return rc;
         return sync(ctx, "upload");
     }
@@ -515,6 +516,7 @@ int cf_upload(cf_ctx* ctx, int field, const double* host, ptrdiff_t si, ptrdiff_
         rc = cuda_check(ctx, cudaMemcpy2DAsync(&g.at(CF_HALO, CF_HALO), g.pitch * sizeof(double), ctx->staging,
                                                ox * sizeof(double), ox * sizeof(double), oy, cudaMemcpyDeviceToDevice,
                                                ctx->stream), "upload");
+        if (!rc && pairs) rc = cuda_check(ctx, launch_to_pairs(ctx, field, s), "split");
     }
     if (rc) return rc;
     return sync(ctx, "upload");
@@ -542,6 +544,11 @@ int cf_download(cf_ctx* ctx, int field, double* host, ptrdiff_t si, ptrdiff_t sj
         spitch = ctx->vpitch;
     } else if (field == CF_FIELD_QUANTITY && ctx->precision == CF_PREC_MIXED) {
         rc = cuda_check(ctx, launch_convert_q(ctx, 0, s), "convert");
+        src = ctx->staging;
+        spitch = ox;
+    } else if (ctx->precision == CF_PREC_MIXED) {
+        // u, v pairs to FP64
+        rc = cuda_check(ctx, launch_from_pairs(ctx, field, s, ctx->staging), "convert");
         src = ctx->staging;
         spitch = ox;
     } else {
@@ -589,6 +596,12 @@ int cf_download_ghosted(cf_ctx* ctx, int field, double* host, int* ex, int* ey) 
     if (field != CF_FIELD_QUANTITY && field != CF_FIELD_U && field != CF_FIELD_V)
         return fail(ctx, CF_ERR_INVALID, "field %d has no ghosted array", field);
     Grid<double> g = field == CF_FIELD_QUANTITY ? ctx->q64[s] : (field == CF_FIELD_U ? ctx->u[s] : ctx->v[s]);
+    if (field != CF_FIELD_QUANTITY && ctx->precision == CF_PREC_MIXED && host) {
+        // u, v pairs: FP64 copies of the ghosted arrays
+        Grid<double> gu, gv;
+        if ((rc = velocity_f64(ctx, &gu, &gv))) return rc;
+        g = field == CF_FIELD_U ? gu : gv;
+    }
     *ex = g.ex;
     *ey = g.ey;
     if (!host) return CF_OK;
@@ -744,6 +757,12 @@ static int step_host_resources(cf_ctx* ctx, bool mixed) {
         if (rc) return rc;
         ctx->staging2 = p;
     }
+    if (mixed && !ctx->staging_uv) {
+        double* p = nullptr;
+        int rc = alloc_dev(ctx, p, 2 * (size_t)(ctx->ph.nx + 1) * (ctx->ph.ny + 1));
+        if (rc) return rc;
+        ctx->staging_uv = p;
+    }
     return CF_OK;
 }
 
@@ -785,7 +804,6 @@ int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* 
     // quantity once they are in (they share the link), on the second stream,
     // while the velocities' own advection runs on the main one.
     const int s0 = ctx->cur;
-    ctx->uv32 = 0;
     for (int f = CF_FIELD_U; f <= CF_FIELD_V && !rc; ++f) {
         int ox, oy;
         owned(ctx, f, &ox, &oy);
@@ -794,6 +812,8 @@ int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* 
                                                f == CF_FIELD_U ? u_in : v_in, ox * sizeof(double), ox * sizeof(double),
                                                oy, cudaMemcpyDefault, ctx->stream),
                         "upload");
+        // mixed: the FP64 values to the pairs the context keeps, in place
+        if (!rc && mixed) rc = cuda_check(ctx, launch_to_pairs(ctx, f, s0), "split");
     }
     if (!rc) rc = cuda_check(ctx, cudaEventRecord(ctx->ev_uv, ctx->stream), "event");
     if (!rc) rc = cuda_check(ctx, cudaStreamWaitEvent(ctx->stream2, ctx->ev_uv, 0), "event wait");
@@ -852,6 +872,16 @@ int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* 
         if (!outs[f]) continue;
         int ox, oy;
         owned(ctx, f, &ox, &oy);
+        if (mixed) {
+            // the pairs to FP64 in the staging buffer, then one copy out
+            double* st = ctx->staging_uv + (f - 1) * (size_t)(ctx->ph.nx + 1) * (ctx->ph.ny + 1);
+            rc = cuda_check(ctx, launch_from_pairs(ctx, f, s1, st, out_stream), "convert");
+            if (!rc)
+                rc = cuda_check(ctx, cudaMemcpyAsync(outs[f], st, sizeof(double) * (size_t)ox * oy, cudaMemcpyDefault,
+                                                     out_stream),
+                                "download");
+            continue;
+        }
         const Grid<double>& g = f == CF_FIELD_U ? ctx->u[s1] : ctx->v[s1];
         rc = cuda_check(ctx, cudaMemcpy2DAsync(outs[f], ox * sizeof(double), &g.at(CF_HALO, CF_HALO),
                                                g.pitch * sizeof(double), ox * sizeof(double), oy, cudaMemcpyDefault,

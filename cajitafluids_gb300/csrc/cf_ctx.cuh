@@ -23,14 +23,13 @@ struct cf_ctx {
     // 0.5): the inner step only advances x (set per projection from its options)
     int x_only = 0;
     int gmg_xonly = -1;  // x_only of the cached host-polled MG graphs
-    // mixed: u32/v32 hold the FP32 copies of the owned u, v of the current
-    // state (written by the last gradient subtraction; ghosts not yet filled)
-    int uv32 = 0;
-
-    // fields, two versions each (src/ProblemManager.hpp:143-165); index cur is Current
+    // fields, two versions each (src/ProblemManager.hpp:143-165); index cur is
+    // Current.  A mixed context keeps q in FP32 (q32) and u, v as double-float
+    // pairs: each 8-byte element of u, v holds (hi, lo) = (fl32(w), fl32(w -
+    // hi)) of the face velocity w.
     cf::Grid<double> q64[2]{}, u[2]{}, v[2]{};
     cf::Grid<float> q32[2]{};
-    cf::Grid<float> u32{}, v32{};  // mixed: FP32 copies of the current u, v (ghosts included) for advection
+    cf::Grid<double> vel64[2]{};  // mixed: FP64 copies of u, v for the sampling exports, made on first use
     int cur = 0;
 
     // solver vectors (owned cells)
@@ -77,6 +76,7 @@ struct cf_ctx {
     cudaEvent_t ev_uv = nullptr, ev_q = nullptr;  // cf_step_host: velocities in, quantity in
     cudaEvent_t ev_press = nullptr;  // recorded by the resident projection right after the gradient subtraction
     double* staging2 = nullptr;
+    double* staging_uv = nullptr;  // cf_step_host (mixed): u, v as FP64 for their download
     cudaGraphExec_t gmg = nullptr;      // batch of MG-PCG iterations
     cudaGraphExec_t gmg_pre = nullptr;  // V-cycle + r.z after the residual is (re)formed
     cf::Stencil gmg_st{};
@@ -133,6 +133,14 @@ cudaError_t launch_cell_velocity(cf_ctx* c, double* d_uc, double* d_vc);
 cudaError_t launch_max_velocity(cf_ctx* c, double* d_out);
 cudaError_t launch_test_convert(cf_ctx* c, int n, const double* d, float* f, double* w);
 cudaError_t launch_convert_q(cf_ctx* c, int to_device, int version, cudaStream_t stream = nullptr);
+// mixed u, v (field CF_FIELD_U / CF_FIELD_V of state version): the owned FP64
+// values in place to pairs, or the owned pairs to FP64 in dst (row pitch =
+// the owned width)
+cudaError_t launch_to_pairs(cf_ctx* c, int field, int version, cudaStream_t stream = nullptr);
+cudaError_t launch_from_pairs(cf_ctx* c, int field, int version, double* dst, cudaStream_t stream = nullptr);
+// the current u, v as FP64 ghosted arrays (mixed: converted copies)
+int velocity_f64(cf_ctx* c, Grid<double>* gu, Grid<double>* gv);
+int alloc_grid64(cf_ctx* c, Grid<double>& g, int ex, int ey);
 cudaError_t launch_q_to_f64(cf_ctx* c, int version, double* dst, cudaStream_t stream);
 
 // projection (cf_project.cu)

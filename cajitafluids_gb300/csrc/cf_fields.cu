@@ -258,34 +258,27 @@ __global__ void __launch_bounds__(256) k_advect64(Adv64 a) {
 // --------------------------------------------------------------------------
 // FP32 advection (mixed precision).  Positions are kept as an integer base
 // (the entity's local index) plus a small FP32 displacement in cell units,
-// so FP32 keeps full relative precision at any grid size.  u and v are
-// stored in FP64 (the projection works on them in FP64) and read here from
-// FP32 copies, so no sample converts: the gradient subtraction writes them,
-// or (after an upload or inputs) k_to32 makes them from the FP64 arrays;
-// q is FP32.
+// so FP32 keeps full relative precision at any grid size.  A mixed context
+// stores u and v as double-float pairs (each 8-byte element holds hi =
+// fl32(w), lo = fl32(w - hi) of the face velocity w, about 48 significant
+// bits): the projection works on the pairs on the FP32 pipe, and the
+// advection samples the hi parts; q is FP32.
 // The inputs epilogue tests the inflow box on integer index ranges that the
-// host evaluated with the FP64 coordinate test, and works in FP64 only where
-// the FP64 result needs it (inside the box, a non-zero body force).
+// host evaluated with the FP64 coordinate test; a body force is added to the
+// advected value as a pair (fdt2 = the pair of force * dt), and only a face
+// inside the box takes FP64 arithmetic.
 struct Adv32 {
     Phys p;
     Grid<float> q, qn;
-    Grid<float> u, v;  // FP32 copies of the current velocities
-    Grid<double> un, vn;
+    Grid<double> u, v;    // current velocities, double-float pairs
+    Grid<double> un, vn;  // next velocities, written as pairs
     float c;      // dt / dx
     double dt;
     int fuse;
-    int ent0;     // entity of blockIdx.z == 0 (a launch may cover a subset)
+    int ent0;     // entity of blockIdx.x == 0 (a launch may cover a subset)
     int unstaged; // tests: every tile reads global memory (same bits)
+    float2 fdt2[2];  // force[axis] * dt as pairs (zero without a force)
 };
-
-// FP32 copy of a ghosted FP64 array (ghosts included)
-__global__ void k_to32(Grid<double> src, Grid<float> dst) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= src.ex || j >= src.ey) return;
-    dst.at(i, j) = d2f_rn(src.at(i, j));
-}
-
 
 // Tap access for the FP32 samplers.  GlobalTaps reads a ghosted FP32 array
 // and clamps the stencil to it, as the FP64 samplers do; WindowTaps reads a
@@ -294,12 +287,17 @@ __global__ void k_to32(Grid<double> src, Grid<float> dst) {
 // moves a full cell from its entity; the taps then lie within two cells of
 // the entity, inside the window and at least one cell inside the ghosted
 // array, where the clamps cannot fire, so both give the same bits.
+// A pair array is read as floats two apart (es = 2, the hi parts).
 struct GlobalTaps {
     const float* o;
     int pitch, ex, ey;
+    int es;  // floats per element: 1 (FP32 array), 2 (pair array)
     static constexpr bool kClamp = true;
-    __device__ __forceinline__ const float* at(int ix, int iy) const { return o + (size_t)iy * pitch + ix; }
-    __device__ __forceinline__ int stride() const { return pitch; }
+    __device__ __forceinline__ const float* at(int ix, int iy) const {
+        return o + ((size_t)iy * pitch + ix) * es;
+    }
+    __device__ __forceinline__ int stride() const { return pitch * es; }
+    __device__ __forceinline__ int step() const { return es; }
     __device__ __forceinline__ static float ld(const float* p) { return __ldg(p); }
 };
 
@@ -324,6 +322,7 @@ struct WindowTaps {
     static constexpr bool kClamp = false;
     __device__ __forceinline__ const float* at(int ix, int iy) const { return s + ((iy - y0) * AW_X + (ix - x0)); }
     __device__ __forceinline__ int stride() const { return AW_X; }
+    __device__ __forceinline__ static constexpr int step() { return 1; }
     __device__ __forceinline__ static float ld(const float* p) { return *p; }
 };
 
@@ -340,8 +339,9 @@ __device__ __forceinline__ float lin32(const A& g, int bi, int bj, float fx, flo
     }
     const float* r0 = g.at(ix, iy);
     const float* r1 = r0 + g.stride();
-    float a0 = A::ld(r0), a1 = A::ld(r0 + 1);
-    float b0 = A::ld(r1), b1 = A::ld(r1 + 1);
+    const int e = g.step();
+    float a0 = A::ld(r0), a1 = A::ld(r0 + e);
+    float b0 = A::ld(r1), b1 = A::ld(r1 + e);
     float s0 = fmaf(tx, a1 - a0, a0);
     float s1 = fmaf(tx, b1 - b0, b0);
     return fmaf(ty, s1 - s0, s0);
@@ -376,15 +376,15 @@ __device__ __forceinline__ float cub32(const A& g, int bi, int bj, float fx, flo
     // over a run.  Against differences the weight error only touches the
     // local variation of the field, and a constant is reproduced exactly.
     const float* base = g.at(ix - 1, iy - 1);
-    const int st = g.stride();
-    const float c = A::ld(base + st + 1);
+    const int st = g.stride(), e = g.step();
+    const float c = A::ld(base + st + e);
     float val = 0.f;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
         const float* row = base + b * st;
         float rs = wx[0] * (A::ld(row) - c);
 #pragma unroll
-        for (int k = 1; k < 4; ++k) rs = fmaf(wx[k], A::ld(row + k) - c, rs);
+        for (int k = 1; k < 4; ++k) rs = fmaf(wx[k], A::ld(row + k * e) - c, rs);
         val = b == 0 ? wy[0] * rs : fmaf(wy[b], rs, val);
     }
     return c + val;
@@ -407,20 +407,20 @@ __device__ __forceinline__ float advect_value(const Adv32& a, int ent, int li, i
     {
         const float* u0 = U.at(li, lj);
         const float* w0 = V.at(li, lj);
-        const int pu = U.stride(), pv = V.stride();
+        const int pu = U.stride(), pv = V.stride(), eu = U.step(), ev = V.step();
         if (ent == E_CELL) {
-            v0x = fmaf(0.5f, A::ld(u0 + 1) - A::ld(u0), A::ld(u0));
+            v0x = fmaf(0.5f, A::ld(u0 + eu) - A::ld(u0), A::ld(u0));
             v0y = fmaf(0.5f, A::ld(w0 + pv) - A::ld(w0), A::ld(w0));
         } else if (ent == E_FACEI) {
             v0x = A::ld(u0);
-            const float* r0 = w0 - 1;
-            const float s0 = fmaf(0.5f, A::ld(r0 + 1) - A::ld(r0), A::ld(r0));
-            const float s1 = fmaf(0.5f, A::ld(r0 + pv + 1) - A::ld(r0 + pv), A::ld(r0 + pv));
+            const float* r0 = w0 - ev;
+            const float s0 = fmaf(0.5f, A::ld(r0 + ev) - A::ld(r0), A::ld(r0));
+            const float s1 = fmaf(0.5f, A::ld(r0 + pv + ev) - A::ld(r0 + pv), A::ld(r0 + pv));
             v0y = fmaf(0.5f, s1 - s0, s0);
         } else {
             const float* r0 = u0 - pu;
-            const float s0 = fmaf(0.5f, A::ld(r0 + 1) - A::ld(r0), A::ld(r0));
-            const float s1 = fmaf(0.5f, A::ld(r0 + pu + 1) - A::ld(r0 + pu), A::ld(r0 + pu));
+            const float s0 = fmaf(0.5f, A::ld(r0 + eu) - A::ld(r0), A::ld(r0));
+            const float s1 = fmaf(0.5f, A::ld(r0 + pu + eu) - A::ld(r0 + pu), A::ld(r0 + pu));
             v0x = fmaf(0.5f, s1 - s0, s0);
             v0y = A::ld(w0);
         }
@@ -456,32 +456,45 @@ __device__ __forceinline__ float max_nan(float x, float y) {
 // it) the tile reads global memory with the clamped stencil.  Either way
 // each entity gets the same bits.
 template <int ORDER>
-__global__ void __launch_bounds__(256) k_advect32(Adv32 a) {
+__global__ void __launch_bounds__(256, 8) k_advect32(Adv32 a) {
     __shared__ __align__(16) float sw[3 * AW_N];  // u, v, q windows
     __shared__ float red[8];
     const Phys& p = a.p;
     const int ent = blockIdx.x + a.ent0;
     const int gi0 = blockIdx.y * AT_X, gj0 = blockIdx.z * AT_Y;
     const int lane = threadIdx.x & 31, wrow = threadIdx.x >> 5;
-    const int narr = ent == E_CELL ? 3 : 2;
-    constexpr int kRowChunks = AW_X / 4, kChunks = AW_Y * kRowChunks;
+    // The window's origin is ghosted (gi0 - 1, gj0 + 1); rows past an array
+    // and chunks past its padded row read as zeros.  u, v: 16-byte chunks of
+    // two pairs, their hi parts kept (chunk c2 ends at element CF_COL0 + gi0
+    // - 1 + 2 c2 + 2 of the row); q: chunks of four floats (ending at element
+    // CF_COL0 + gi0 - 1 + 4 c4 + 4).
     float m = 0.f;
-    for (int arr = 0; arr < narr; ++arr) {
-        const float* go = arr == 0 ? a.u.o : (arr == 1 ? a.v.o : a.q.o);
-        const int gp = arr == 0 ? a.u.pitch : (arr == 1 ? a.v.pitch : a.q.pitch);
-        const int gey = arr == 0 ? a.u.ey : (arr == 1 ? a.v.ey : a.q.ey);
-        // the window's origin, ghosted (gi0 - 1, gj0 + 1); rows past the array
-        // and chunks past its padded row (chunk c4 ends at element CF_COL0 +
-        // gi0 - 1 + 4 c4 + 4 of the row) read as zeros
-        const float* src = go + (size_t)(gj0 + 1) * gp + (gi0 - 1);
-        const int nrow = gey - (gj0 + 1), nc4 = (gp - CF_COL0 - gi0 + 1) >> 2;
+    for (int arr = 0; arr < 2; ++arr) {
+        const double* go = arr == 0 ? a.u.o : a.v.o;
+        const int gp = arr == 0 ? a.u.pitch : a.v.pitch, gey = arr == 0 ? a.u.ey : a.v.ey;
+        constexpr int kRowChunks = AW_X / 2, kChunks = AW_Y * kRowChunks;
+        const float* src = reinterpret_cast<const float*>(go + (size_t)(gj0 + 1) * gp + (gi0 - 1));
+        const int nrow = gey - (gj0 + 1), nc2 = (gp - CF_COL0 - gi0 + 1) >> 1;
         float* dst = sw + arr * AW_N;
+        for (int k = threadIdx.x; k < kChunks; k += 256) {
+            const int r = k / kRowChunks, c2 = k - r * kRowChunks;
+            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r < nrow && c2 < nc2)
+                w = __ldg(reinterpret_cast<const float4*>(src + 2 * ((size_t)r * gp + 2 * c2)));
+            *reinterpret_cast<float2*>(dst + 2 * k) = make_float2(w.x, w.z);  // r AW_X + 2 c2 = 2 k
+            m = max_nan(m, max_nan(fabsf(w.x), fabsf(w.z)));
+        }
+    }
+    if (ent == E_CELL) {
+        constexpr int kRowChunks = AW_X / 4, kChunks = AW_Y * kRowChunks;
+        const float* src = a.q.o + (size_t)(gj0 + 1) * a.q.pitch + (gi0 - 1);
+        const int nrow = a.q.ey - (gj0 + 1), nc4 = (a.q.pitch - CF_COL0 - gi0 + 1) >> 2;
+        float* dst = sw + 2 * AW_N;
         for (int k = threadIdx.x; k < kChunks; k += 256) {
             const int r = k / kRowChunks, c4 = k - r * kRowChunks;
             float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (r < nrow && c4 < nc4) w = __ldg(reinterpret_cast<const float4*>(src + (size_t)r * gp + 4 * c4));
+            if (r < nrow && c4 < nc4) w = __ldg(reinterpret_cast<const float4*>(src + (size_t)r * a.q.pitch + 4 * c4));
             *reinterpret_cast<float4*>(dst + 4 * k) = w;  // r AW_X + 4 c4 = 4 k
-            if (arr < 2) m = max_nan(m, max_nan(max_nan(fabsf(w.x), fabsf(w.y)), max_nan(fabsf(w.z), fabsf(w.w))));
         }
     }
 #pragma unroll
@@ -496,8 +509,10 @@ __global__ void __launch_bounds__(256) k_advect32(Adv32 a) {
     const int ox = p.nx + ((ent == E_FACEI && !p.per_x) ? 1 : 0);
     const int oy = p.ny + ((ent == E_FACEJ && !p.per_y) ? 1 : 0);
     const int fa = ent == E_CELL ? 2 : (ent == E_FACEI ? 0 : 1);
-    const GlobalTaps gu{a.u.o, a.u.pitch, a.u.ex, a.u.ey}, gv{a.v.o, a.v.pitch, a.v.ex, a.v.ey};
-    const GlobalTaps gf = ent == E_CELL ? GlobalTaps{a.q.o, a.q.pitch, a.q.ex, a.q.ey} : (ent == E_FACEI ? gu : gv);
+    const GlobalTaps gu{reinterpret_cast<const float*>(a.u.o), a.u.pitch, a.u.ex, a.u.ey, 2},
+        gv{reinterpret_cast<const float*>(a.v.o), a.v.pitch, a.v.ex, a.v.ey, 2};
+    const GlobalTaps gf =
+        ent == E_CELL ? GlobalTaps{a.q.o, a.q.pitch, a.q.ex, a.q.ey, 1} : (ent == E_FACEI ? gu : gv);
 #pragma unroll 1
     for (int k = 0; k < AT_Y / 8; ++k) {
         const int gi = gi0 + lane, gj = gj0 + wrow + 8 * k;
@@ -525,27 +540,29 @@ __global__ void __launch_bounds__(256) k_advect32(Adv32 a) {
             a.qn.at(li, lj) = val;
             continue;
         }
+        // face inputs (src/Solver.hpp:181-263) on the pair (val, 0): the inflow
+        // velocity where it is larger, then the body force, then the walls
         const int axis = ent == E_FACEI ? 0 : 1;
-        double w = (double)val;
+        float2 w = make_float2(val, 0.f);
         if (a.fuse) {
-            if (in_box_idx(p, ent, li, lj) && fabs(w) < fabs(p.src_vel[axis])) w = p.src_vel[axis];
-            if (p.force[axis] != 0.0) w = __dadd_rn(w, __dmul_rn(p.force[axis], a.dt));
+            if (in_box_idx(p, ent, li, lj) && fabs((double)val) < fabs(p.src_vel[axis])) w = df_split(p.src_vel[axis]);
+            if (p.force[axis] != 0.0) w = df_add(w, a.fdt2[axis]);
             const int per = axis == 0 ? p.per_x : p.per_y, n = axis == 0 ? p.nx : p.ny, gg = axis == 0 ? gi : gj;
             if (!per) {
-                if (gg <= 0 && p.bc[axis] == 0) w = 0.0;
-                if (gg > n - 1 && p.bc[axis + 2] == 0) w = 0.0;
+                if (gg <= 0 && p.bc[axis] == 0) w = make_float2(0.f, 0.f);
+                if (gg > n - 1 && p.bc[axis + 2] == 0) w = make_float2(0.f, 0.f);
             }
         }
-        if (axis == 0)
-            a.un.at(li, lj) = w;
-        else
-            a.vn.at(li, lj) = w;
+        double& dst = axis == 0 ? a.un.at(li, lj) : a.vn.at(li, lj);
+        reinterpret_cast<float2&>(dst) = w;
     }
 }
 
 // --------------------------------------------------------------------------
 // Standalone inputs (Solver::setup and density-scaled body forces): pass 0
-// updates cells, pass 1 updates faces reading the updated cells.
+// updates cells, pass 1 updates faces reading the updated cells.  A mixed
+// context (TQ = float) keeps u, v as double-float pairs: a face value is
+// taken to FP64, the inputs applied in FP64 and the result split again.
 template <typename TQ>
 struct Inp {
     Phys p;
@@ -587,7 +604,12 @@ __global__ void k_inputs_faces(Inp<TQ> a) {
         rho = axis == 0 ? (cell_q(a, gi - 1, gj) + cell_q(a, gi, gj)) * 0.5
                         : (cell_q(a, gi, gj - 1) + cell_q(a, gi, gj)) * 0.5;
     double& w = axis == 0 ? a.u.at(gi + CF_HALO, gj + CF_HALO) : a.v.at(gi + CF_HALO, gj + CF_HALO);
-    w = inputs_face(p, axis, w, x, y, a.dt, axis == 0 ? gi : gj, rho);
+    if constexpr (sizeof(TQ) == sizeof(float)) {
+        float2& wp = reinterpret_cast<float2&>(w);
+        wp = df_split(inputs_face(p, axis, df_value(wp), x, y, a.dt, axis == 0 ? gi : gj, rho));
+    } else {
+        w = inputs_face(p, axis, w, x, y, a.dt, axis == 0 ? gi : gj, rho);
+    }
 }
 
 // --------------------------------------------------------------------------
@@ -707,28 +729,14 @@ cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs, int 
     } else {
         // fused inputs with a density-scaled force are applied by the
         // standalone inputs kernels after the advection
-        Adv32 a{p,   c->q32[s], c->q32[n], c->u32, c->v32, c->u[n], c->v[n], (float)(dt / p.dx), dt, fuse_inputs,
-                ent0, c->test_unstaged};
-        if (!prep) {
-            // the FP32 velocity copies were prepared by an earlier part of this advection
-        } else if (c->uv32) {
-            // the last gradient subtraction left the owned FP32 copies: only their ghosts
-            const int nux = p.per_x ? p.nx : p.nx + 1, nvy = p.per_y ? p.ny : p.ny + 1;
-            if (p.per_x || p.per_y) {
-                auto frame = [&](const Grid<float>& g, int nox, int noy) {
-                    return (CF_HALO * g.ex + noy * (g.ex - nox) + (g.ey - CF_HALO - noy) * g.ex + 255) / 256;
-                };
-                k_fill_ghosts<float><<<frame(c->u32, nux, p.ny), 256, 0, c->stream>>>(c->u32, nux, p.ny, p.per_x,
-                                                                                     p.per_y);
-                k_fill_ghosts<float><<<frame(c->v32, p.nx, nvy), 256, 0, c->stream>>>(c->v32, p.nx, nvy, p.per_x,
-                                                                                     p.per_y);
-                c->launches += 2;
-            }
-        } else {
-            k_to32<<<grid2(c->u[s].ex, c->u[s].ey, blk), blk, 0, c->stream>>>(c->u[s], c->u32);
-            k_to32<<<grid2(c->v[s].ex, c->v[s].ey, blk), blk, 0, c->stream>>>(c->v[s], c->v32);
-            c->launches += 2;
+        Adv32 a{p,   c->q32[s], c->q32[n], c->u[s], c->v[s], c->u[n], c->v[n], (float)(dt / p.dx), dt, fuse_inputs,
+                ent0, c->test_unstaged, {}};
+        for (int k = 0; k < 2; ++k) {
+            const double f = p.force[k] * dt;
+            const float hi = (float)f;
+            a.fdt2[k] = make_float2(hi, (float)(f - (double)hi));
         }
+        (void)prep;
         const dim3 tiles(nent, (p.nx + 1 + AT_X - 1) / AT_X, (p.ny + 1 + AT_Y - 1) / AT_Y);
         if (order == 1)
             k_advect32<1><<<tiles, 256, 0, c->stream>>>(a);
@@ -737,8 +745,7 @@ cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs, int 
     }
     c->launches += 1;
     if (advance) {
-        c->uv32 = 0;  // the advection wrote the next u, v
-        c->cur = n;   // ProblemManager::advance for q, u, v
+        c->cur = n;  // ProblemManager::advance for q, u, v
     }
     return cudaGetLastError();
 }
@@ -746,7 +753,6 @@ cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs, int 
 cudaError_t launch_add_inputs(cf_ctx* c, double dt) {
     const Phys& p = c->ph;
     int s = c->cur;
-    c->uv32 = 0;  // writes u, v
     dim3 blk(32, 8);
     if (c->precision == CF_PREC_FP64) {
         Inp<double> a{p, c->q64[s], c->u[s], c->v[s], dt};
@@ -761,10 +767,81 @@ cudaError_t launch_add_inputs(cf_ctx* c, double dt) {
     return cudaGetLastError();
 }
 
+// Mixed storage of u, v: double-float pairs.  k_to_pairs turns the FP64
+// values of the owned region in place into pairs; k_from_pairs writes the
+// FP64 values of a region [i0, i0 + nx) x [j0, j0 + ny) of the ghosted array
+// to dst (row pitch dp elements).
+__global__ void k_to_pairs(Grid<double> g, int nx, int ny) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= nx || j >= ny) return;
+    double& e = g.at(i + CF_HALO, j + CF_HALO);
+    reinterpret_cast<float2&>(e) = df_split(e);
+}
+
+__global__ void k_from_pairs(Grid<double> g, int i0, int j0, int nx, int ny, double* dst, int dp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= nx || j >= ny) return;
+    dst[(size_t)j * dp + i] = df_value(reinterpret_cast<const float2&>(g.at(i0 + i, j0 + j)));
+}
+
+static Grid<double> vel_grid(cf_ctx* c, int field, int version) {
+    return field == CF_FIELD_U ? c->u[version] : c->v[version];
+}
+
+cudaError_t launch_to_pairs(cf_ctx* c, int field, int version, cudaStream_t stream) {
+    const Phys& p = c->ph;
+    const int ox = p.nx + ((field == CF_FIELD_U && !p.per_x) ? 1 : 0);
+    const int oy = p.ny + ((field == CF_FIELD_V && !p.per_y) ? 1 : 0);
+    dim3 blk(32, 8);
+    k_to_pairs<<<grid2(ox, oy, blk), blk, 0, stream ? stream : c->stream>>>(vel_grid(c, field, version), ox, oy);
+    c->launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_from_pairs(cf_ctx* c, int field, int version, double* dst, cudaStream_t stream) {
+    const Phys& p = c->ph;
+    const int ox = p.nx + ((field == CF_FIELD_U && !p.per_x) ? 1 : 0);
+    const int oy = p.ny + ((field == CF_FIELD_V && !p.per_y) ? 1 : 0);
+    dim3 blk(32, 8);
+    k_from_pairs<<<grid2(ox, oy, blk), blk, 0, stream ? stream : c->stream>>>(vel_grid(c, field, version), CF_HALO,
+                                                                            CF_HALO, ox, oy, dst, ox);
+    c->launches += 1;
+    return cudaGetLastError();
+}
+
+// The current u, v as FP64 ghosted arrays: the state itself (FP64 context),
+// or (mixed) FP64 copies of the pairs in arrays made on first use.
+int velocity_f64(cf_ctx* c, Grid<double>* gu, Grid<double>* gv) {
+    const int s = c->cur;
+    if (c->precision != CF_PREC_MIXED) {
+        *gu = c->u[s];
+        *gv = c->v[s];
+        return CF_OK;
+    }
+    for (int f = 0; f < 2; ++f) {
+        const Grid<double>& g = f == 0 ? c->u[s] : c->v[s];
+        if (!c->vel64[f].o) {
+            const int rc = alloc_grid64(c, c->vel64[f], g.ex, g.ey);
+            if (rc) return rc;
+        }
+        Grid<double>& d = c->vel64[f];
+        dim3 blk(32, 8);
+        k_from_pairs<<<grid2(g.ex, g.ey, blk), blk, 0, c->stream>>>(g, 0, 0, g.ex, g.ey, &d.at(0, 0), d.pitch);
+        c->launches += 1;
+    }
+    *gu = c->vel64[0];
+    *gv = c->vel64[1];
+    return cuda_check(c, cudaGetLastError(), "velocity conversion");
+}
+
 cudaError_t launch_interp_points(cf_ctx* c, int field, int order, int n, const double* d_xy, double* d_out) {
     int s = c->cur;
-    Grid<double> f = field == CF_FIELD_QUANTITY ? c->q64[s] : (field == CF_FIELD_U ? c->u[s] : c->v[s]);
-    Pts a{c->ph, f, c->u[s], c->v[s], field, order, n, d_xy, d_out, 0.0};
+    Grid<double> gu, gv;
+    if (velocity_f64(c, &gu, &gv)) return cudaErrorMemoryAllocation;
+    Grid<double> f = field == CF_FIELD_QUANTITY ? c->q64[s] : (field == CF_FIELD_U ? gu : gv);
+    Pts a{c->ph, f, gu, gv, field, order, n, d_xy, d_out, 0.0};
     k_interp_points<<<(n + 127) / 128, 128, 0, c->stream>>>(a);
     c->launches += 1;
     return cudaGetLastError();
@@ -773,14 +850,17 @@ cudaError_t launch_interp_points(cf_ctx* c, int field, int order, int n, const d
 cudaError_t launch_cell_velocity(cf_ctx* c, double* d_uc, double* d_vc) {
     const Phys& p = c->ph;
     dim3 blk(32, 8);
-    k_cell_velocity<<<grid2(p.nx, p.ny, blk), blk, 0, c->stream>>>(p, c->u[c->cur], c->v[c->cur], d_uc, d_vc);
+    Grid<double> gu, gv;
+    if (velocity_f64(c, &gu, &gv)) return cudaErrorMemoryAllocation;
+    k_cell_velocity<<<grid2(p.nx, p.ny, blk), blk, 0, c->stream>>>(p, gu, gv, d_uc, d_vc);
     c->launches += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_trace_points(cf_ctx* c, int n, const double* d_xy, double dt, double* d_out) {
-    int s = c->cur;
-    Pts a{c->ph, c->u[s], c->u[s], c->v[s], 0, 1, n, d_xy, d_out, dt};
+    Grid<double> gu, gv;
+    if (velocity_f64(c, &gu, &gv)) return cudaErrorMemoryAllocation;
+    Pts a{c->ph, gu, gu, gv, 0, 1, n, d_xy, d_out, dt};
     k_trace_points<<<(n + 127) / 128, 128, 0, c->stream>>>(a);
     c->launches += 1;
     return cudaGetLastError();
@@ -804,12 +884,13 @@ cudaError_t launch_test_convert(cf_ctx* c, int n, const double* d, float* f, dou
 
 cudaError_t launch_max_velocity(cf_ctx* c, double* d_out) {
     const Phys& p = c->ph;
-    int s = c->cur;
+    Grid<double> gu, gv;
+    if (velocity_f64(c, &gu, &gv)) return cudaErrorMemoryAllocation;
     cudaMemsetAsync(d_out, 0, sizeof(double), c->stream);
     dim3 blk(32, 8);
     int nux = p.per_x ? p.nx : p.nx + 1, nvy = p.per_y ? p.ny : p.ny + 1;
-    k_max_abs<<<grid2(nux, p.ny, blk), blk, 0, c->stream>>>(c->u[s], nux, p.ny, (unsigned long long*)d_out);
-    k_max_abs<<<grid2(p.nx, nvy, blk), blk, 0, c->stream>>>(c->v[s], p.nx, nvy, (unsigned long long*)d_out);
+    k_max_abs<<<grid2(nux, p.ny, blk), blk, 0, c->stream>>>(gu, nux, p.ny, (unsigned long long*)d_out);
+    k_max_abs<<<grid2(p.nx, nvy, blk), blk, 0, c->stream>>>(gv, p.nx, nvy, (unsigned long long*)d_out);
     c->launches += 2;
     return cudaGetLastError();
 }

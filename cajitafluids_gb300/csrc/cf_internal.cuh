@@ -317,6 +317,29 @@ __device__ __forceinline__ float2 df_add_f(float2 x, float e) {
     s.y = s.y + x.y;
     return df_quick(s.x, s.y);
 }
+__device__ __forceinline__ float2 df_add(float2 x, float2 y) {
+    float2 s = df_two_sum(x.x, y.x);
+    float2 t = df_two_sum(x.y, y.y);
+    s.y = s.y + t.x;
+    s = df_quick(s.x, s.y);
+    s.y = s.y + t.y;
+    return df_quick(s.x, s.y);
+}
+__device__ __forceinline__ float2 df_mul(float2 x, float2 y) {
+    float p = x.x * y.x;
+    float e = fmaf(x.x, y.x, -p);
+    e = fmaf(x.x, y.y, e);
+    e = fmaf(x.y, y.x, e);
+    return df_quick(p, e);
+}
+// An FP64 value as a pair: hi = the value rounded to FP32, lo = the rest
+// rounded to FP32 (about 48 significant bits; one FP64 subtraction), and
+// back (one FP64 addition, exact for pairs made this way).
+__device__ __forceinline__ float2 df_split(double v) {
+    const float hi = d2f_rn(v);
+    return make_float2(hi, d2f_rn(v - f2d_exact(hi)));
+}
+__device__ __forceinline__ double df_value(float2 p) { return f2d_exact(p.x) + f2d_exact(p.y); }
 
 }  // namespace cf
 

@@ -397,25 +397,7 @@ __device__ __forceinline__ void put_r32(float* o, int pitch, int nx, int ny, int
 // narrow FP64 pipe, with an error (~1e-14 relative to |b| + |A x|) far below
 // what the 1e-8 divergence target needs.  nvcc --fmad=false keeps the
 // error-free transformations exact.
-__device__ __forceinline__ float2 df_add(float2 x, float2 y) {
-    float2 s = df_two_sum(x.x, y.x);
-    float2 t = df_two_sum(x.y, y.y);
-    s.y = s.y + t.x;
-    s = df_quick(s.x, s.y);
-    s.y = s.y + t.y;
-    return df_quick(s.x, s.y);
-}
-__device__ __forceinline__ float2 df_mul(float2 x, float2 y) {
-    float p = x.x * y.x;
-    float e = fmaf(x.x, y.x, -p);
-    e = fmaf(x.x, y.y, e);
-    e = fmaf(x.y, y.x, e);
-    return df_quick(p, e);
-}
-__device__ __forceinline__ float2 df_split(double v) {
-    const float hi = d2f_rn(v);
-    return make_float2(hi, d2f_rn(v - f2d_exact(hi)));
-}
+// (df_add, df_mul, df_split and df_value: cf_internal.cuh)
 
 // FP64 init: b, r = b, x = 0, partial r.z and r.r
 __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init64(DivArgs a) {
@@ -470,6 +452,22 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init64(DivArgs a) {
     }
 }
 
+// A mixed context's u, v element as its double-float pair
+__device__ __forceinline__ float2 pair_at(const Grid<double>& g, int i, int j) {
+    return reinterpret_cast<const float2&>(g.at(i, j));
+}
+__device__ __forceinline__ float2 df_neg(float2 x) { return make_float2(-x.x, -x.y); }
+
+// ((u_E - u_W) + v_N) - v_S of cell (c, j) from the pairs (FP32 pipe)
+__device__ __forceinline__ float2 div_pairs(const DivArgs& a, int c, int j) {
+    int ie = c + 1, jn = j + 1;
+    if (a.per_x && ie == a.nx) ie = 0;
+    if (a.per_y && jn == a.ny) jn = 0;
+    float2 t = df_add(pair_at(a.u, ie + CF_HALO, j + CF_HALO), df_neg(pair_at(a.u, c + CF_HALO, j + CF_HALO)));
+    t = df_add(t, pair_at(a.v, c + CF_HALO, jn + CF_HALO));
+    return df_add(t, df_neg(pair_at(a.v, c + CF_HALO, j + CF_HALO)));
+}
+
 // Mixed init: b (double-float, kept for the outer residual), x = 0, inner
 // r = hi part of b; partial b.b (the tolerance base), inner r.z and r.r
 // (FP32 per lane, FP64 beyond).
@@ -488,16 +486,10 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
             for (int s = 0; s < 2; ++s) {
                 int c = c0 + s;
                 if (c >= a.nx) continue;
-                // the divergence sum in FP64 (it cancels), its scale -1/dx as
-                // a double-float product on the FP32 pipe
-                int ie = c + 1, jn = j + 1;
-                if (a.per_x && ie == a.nx) ie = 0;
-                if (a.per_y && jn == a.ny) jn = 0;
-                double t = a.u.at(ie + CF_HALO, j + CF_HALO) - a.u.at(c + CF_HALO, j + CF_HALO);
-                t = t + a.v.at(c + CF_HALO, jn + CF_HALO);
-                t = t - a.v.at(c + CF_HALO, j + CF_HALO);
+                // the divergence of the velocity pairs and its scale -1/dx, in
+                // double-float on the FP32 pipe
                 const size_t k = (size_t)j * a.pitch + c;
-                const float2 bs = df_mul(a.mscale2, df_split(t));
+                const float2 bs = df_mul(a.mscale2, div_pairs(a, c, j));
                 reinterpret_cast<float2*>(a.b)[k] = bs;
                 // x as a double-float pair: 0, or (warm start) the previous
                 // FP64 solution split in place (same 8 bytes per cell)
@@ -904,16 +896,11 @@ struct Press {
     int pitch;
     double ms;    // -(dt / (density dx))
     int adjoint;  // 1: transpose of the projection (masks applied by the caller, none here)
-    // mixed: every value written to u, v also goes, rounded to FP32, to these
-    // copies (the next FP32 advection's velocity arrays)
-    Grid<float> u32, v32;
-    int w32;
-    // mixed (xdf = 1): the solution is read as double-float pairs from the
-    // buffer SolverState::xsel names (x or xb); the pressure difference and
-    // its product with ms (ms2 = ms as a pair) run on the FP32 pipe and two
-    // FP64 additions apply it, instead of three FP64 operations on an FP64
-    // solution made by a conversion pass
-    int xdf;
+    // mixed (pairs = 1): u, v hold double-float pairs and the solution is read
+    // as pairs from the buffer SolverState::xsel names (x or xb); the update
+    // u + ms (p(c) - p(n)) runs in double-float on the FP32 pipe (ms2 = ms as
+    // a pair)
+    int pairs;
     float2 ms2;
     const float2* xb;
     const SolverState* S;
@@ -932,18 +919,20 @@ __device__ __forceinline__ float2 pval_df(const Press& a, const float2* x, int g
 }
 
 // w + ms (p(c) - p(n)): FP64 as the reference writes it (one rounding per
-// operation; ms = -scale), or (xdf) from the double-float solution
+// operation; ms = -scale), or (pairs) on the pair stored in w's 8 bytes
 __device__ __forceinline__ double press_update(const Press& a, const float2* xdf, double w, int ci, int cj, int ni,
                                                int nj) {
-    if (a.xdf) {
+    if (a.pairs) {
         const float2 pc = pval_df(a, xdf, ci, cj), pn = pval_df(a, xdf, ni, nj);
         const float2 m = df_mul(a.ms2, df_add_s(pc, make_float2(-pn.x, -pn.y)));
-        return __dadd_rn(__dadd_rn(w, f2d_exact(m.x)), f2d_exact(m.y));
+        const float2 r = df_add(reinterpret_cast<const float2&>(w), m);
+        return __hiloint2double(__float_as_int(r.y), __float_as_int(r.x));  // the pair's 8 bytes
     }
     const double d = pval(a, ci, cj) - pval(a, ni, nj);
     return __dadd_rn(w, __dmul_rn(a.ms, d));
 }
 
+// (a zero written to u or v is the pair (0, 0) as well)
 __global__ void k_apply_pressure(Press a) {
     const Phys& p = a.p;
     int axis = blockIdx.z;
@@ -953,7 +942,7 @@ __global__ void k_apply_pressure(Press a) {
     int oy = p.ny + ((axis == 1 && !p.per_y) ? 1 : 0);
     if (gi >= ox || gj >= oy) return;
     const bool fix_q1 = (p.quirks & 1u) != 0;
-    const float2* xdf = a.xdf ? (a.S->xsel ? a.xb : reinterpret_cast<const float2*>(a.x)) : nullptr;
+    const float2* xdf = a.pairs ? (a.S->xsel ? a.xb : reinterpret_cast<const float2*>(a.x)) : nullptr;
     if (axis == 0) {
         double& u = a.u.at(gi + CF_HALO, gj + CF_HALO);
         // u -= scale * (p(i) - p(i-1)) (src/VelocityCorrector.hpp:245)
@@ -966,7 +955,6 @@ __global__ void k_apply_pressure(Press a) {
             if (!fix_q1 && !p.per_y && gj == 0 && gi < p.nx && p.bc[1] == 0) w = 0.0;
         }
         u = w;
-        if (a.w32) a.u32.at(gi + CF_HALO, gj + CF_HALO) = d2f_rn(w);
     } else {
         double& v = a.v.at(gi + CF_HALO, gj + CF_HALO);
         double w = press_update(a, xdf, v, gi, gj, gi, gj - 1);  // :256
@@ -976,11 +964,9 @@ __global__ void k_apply_pressure(Press a) {
                 if (gj > p.ny - 1 && p.bc[3] == 0) w = 0.0;
             } else if (gj > p.ny - 1 && p.bc[3] == 0) {
                 a.u.at(gi + CF_HALO, gj + CF_HALO) = 0.0;  // u ghost row ny
-                if (a.w32) a.u32.at(gi + CF_HALO, gj + CF_HALO) = 0.f;
             }
         }
         v = w;
-        if (a.w32) a.v32.at(gi + CF_HALO, gj + CF_HALO) = d2f_rn(w);
     }
 }
 
@@ -1002,14 +988,9 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_norms(DivArgs a) {
                 int c = c0 + s;
                 if (c >= a.nx) continue;
                 if (a.mixed) {
-                    // the FP64 divergence sum, then its square and magnitude in FP32
-                    int ie = c + 1, jn = j + 1;
-                    if (a.per_x && ie == a.nx) ie = 0;
-                    if (a.per_y && jn == a.ny) jn = 0;
-                    double t = a.u.at(ie + CF_HALO, j + CF_HALO) - a.u.at(c + CF_HALO, j + CF_HALO);
-                    t = t + a.v.at(c + CF_HALO, jn + CF_HALO);
-                    t = t - a.v.at(c + CF_HALO, j + CF_HALO);
-                    const float bf = d2f_rn(t) * a.mscale32;
+                    // the divergence of the pairs, then its square and
+                    // magnitude in FP32
+                    const float bf = div_pairs(a, c, j).x * a.mscale32;
                     fss = fmaf(bf, bf, fss);
                     fmx = fmaxf(fmx, fabsf(bf));
                 } else {
@@ -1070,10 +1051,9 @@ static DivArgs div_args(cf_ctx* c, const Stencil& st) {
     return a;
 }
 
-// the gradient subtraction's arguments; a mixed projection without a warm
-// start reads the double-float solution directly (xdf): its FP64 pressure is
-// made only when it is downloaded (c->p_df)
-static Press press_args(cf_ctx* c, double dt, Grid<double> gu, Grid<double> gv, int adjoint, bool w32, bool xdf) {
+// the gradient subtraction's arguments (mixed: on pairs, from the
+// double-float solution)
+static Press press_args(cf_ctx* c, double dt, Grid<double> gu, Grid<double> gv, int adjoint) {
     Press pa{};
     pa.p = c->ph;
     pa.u = gu;
@@ -1082,10 +1062,7 @@ static Press press_args(cf_ctx* c, double dt, Grid<double> gu, Grid<double> gv, 
     pa.pitch = c->vpitch;
     pa.ms = -(dt / (c->density * c->ph.dx));
     pa.adjoint = adjoint;
-    pa.u32 = c->u32;
-    pa.v32 = c->v32;
-    pa.w32 = w32 ? 1 : 0;
-    pa.xdf = xdf ? 1 : 0;
+    pa.pairs = c->precision == CF_PREC_MIXED ? 1 : 0;
     const float hi = (float)pa.ms;
     pa.ms2 = make_float2(hi, (float)(pa.ms - (double)hi));
     pa.xb = reinterpret_cast<const float2*>(c->xb.a);
@@ -1468,20 +1445,19 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
     if (!rc)
         rc = capture_graph(c, &tail, [&] {
             dim3 blk(32, 8);
-            // mixed: the gradient reads the double-float solution, unless a
-            // warm start wants the FP64 pressure kept for the next solve
-            const bool xdf = mixed && !adjoint && !warm;
-            if (mixed && !xdf) {
-                dim3 grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
-                k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, reinterpret_cast<const float2*>(c->xb.a), c->S,
-                                                        c->ph.nx, c->ph.ny, c->vpitch);
-                ntail += 1;
-            }
-            Press pa = press_args(c, dt, gu, gv, adjoint, mixed && !adjoint, xdf);
+            // mixed: the gradient reads the double-float solution; a warm
+            // start then has it converted to the FP64 pressure it starts from
+            Press pa = press_args(c, dt, gu, gv, adjoint);
             dim3 grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
             k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
             // u, v are final here: a caller may copy them out beside the norms
             if (!adjoint) cudaEventRecordWithFlags(c->ev_press, c->stream, cudaEventRecordExternal);
+            if (mixed && warm) {
+                dim3 grdc((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
+                k_df_to_f64<<<grdc, blk, 0, c->stream>>>(c->x.a, reinterpret_cast<const float2*>(c->xb.a), c->S,
+                                                         c->ph.nx, c->ph.ny, c->vpitch);
+                ntail += 1;
+            }
             DivArgs da = div_args(c, st);
             da.u = gu;
             da.v = gv;
@@ -1580,8 +1556,7 @@ static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResul
     }
     cudaMemcpyAsync(c->S, h, sizeof(SolverState), cudaMemcpyHostToDevice, c->stream);
     if ((rc = cuda_check(c, cudaGraphLaunch(c->rgx[slot], c->stream), "graph launch"))) return rc;
-    if (mixed && !adjoint) c->uv32 = 1;  // the graph's gradient subtraction wrote the FP32 velocity copies
-    c->p_df = (mixed && !adjoint && !(flags & 4)) ? 1 : 0;
+    c->p_df = (mixed && !(flags & 4)) ? 1 : 0;
     c->rg_pending = slot;
     if (defer) return CF_OK;
     if ((rc = cuda_check(c, cudaStreamSynchronize(c->stream), "projection"))) return rc;
@@ -1771,14 +1746,6 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
             }
         }
     }
-    if (mixed && (adjoint || warm)) {
-        // the FP64 pressure now (a warm start reads it); otherwise the
-        // gradient reads the double-float solution and a download converts it
-        dim3 blk(32, 8), grd((c->ph.nx + 31) / 32, (c->ph.ny + 7) / 8);
-        k_df_to_f64<<<grd, blk, 0, c->stream>>>(c->x.a, reinterpret_cast<const float2*>(c->xb.a), c->S, c->ph.nx,
-                                                c->ph.ny, c->vpitch);
-        c->launches += 1;
-    }
     const SolverState* hs = c->hS;
     res->iterations = hs->iter;
     res->outer = hs->outer_iter;
@@ -1786,14 +1753,14 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     res->bb = hs->bb;
     res->rr = hs->rr;
 
-    // gradient subtraction
-    const bool w32 = mixed && !adjoint && gu.o == c->u[c->cur].o && gv.o == c->v[c->cur].o;
-    Press pa = press_args(c, dt, gu, gv, adjoint, w32, mixed && !adjoint && !warm);
-    c->p_df = pa.xdf;
+    // gradient subtraction (mixed: from the double-float solution; the FP64
+    // pressure is made afterwards for a warm start, or when it is downloaded)
+    Press pa = press_args(c, dt, gu, gv, adjoint);
     dim3 blk(32, 8), grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
     k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
     c->launches += 1;
-    c->uv32 = w32 ? 1 : 0;
+    c->p_df = mixed ? 1 : 0;
+    if (mixed && warm) settle_pressure(c);
     if ((rc = cuda_check(c, cudaGetLastError(), "apply pressure"))) return rc;
     if (c->prof) cudaEventRecord(c->ev[5], c->stream);
     if (adjoint) return cuda_check(c, cudaStreamSynchronize(c->stream), "adjoint projection");

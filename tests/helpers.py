@@ -80,3 +80,13 @@ def assert_fields_equal(o, c, fields=FIELDS, tag=""):
 
 def opts(tol=1e-8, max_iter=20000, abs_tol=0.0, **kw):
     return SolverOptions(tol=tol, abs_tol=abs_tol, max_iter=max_iter, **kw)
+
+
+def pair_round(a):
+    """FP64 values as a mixed context stores velocities: the double-float pair
+    hi = fl32(a), lo = fl32(a - hi), read back as hi + lo (about 48 bits)."""
+    a = np.asarray(a, dtype=np.float64)
+    hi = a.astype(np.float32).astype(np.float64)
+    lo = (a - hi).astype(np.float32).astype(np.float64)
+    return hi + lo
+

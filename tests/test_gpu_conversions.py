@@ -1,6 +1,6 @@
 """The integer-pipe FP64 <-> FP32 conversions used by the mixed-precision
-kernels (FP32 copies of u and v, the double-float split of b, the
-double-float pressure to FP64) give the hardware's results bit for bit:
+kernels (the double-float pairs of u, v and b, the double-float pressure to
+FP64) give the hardware's results bit for bit:
 round to nearest even, exact widening, zeros, subnormals, infinities, NaN,
 the overflow threshold and exact ties."""
 import numpy as np

@@ -69,7 +69,8 @@ def test_step_host_failed_setup_is_retried(built):
     so = opts(tol=1e-9, precon="PFMG")
     outs_a = [np.empty(a.owned_shape(f)) for f in ("q", "u", "v")]
     outs_b = [np.empty(b.owned_shape(f)) for f in ("q", "u", "v")]
-    # the mixed context's first cf_step_host allocates one staging buffer
+    # the mixed context's first cf_step_host allocates its staging buffers;
+    # the first of them fails
     lib.cf_test_fail_alloc(1)
     try:
         with pytest.raises(CfError) as e:
