@@ -932,41 +932,45 @@ __device__ __forceinline__ double press_update(const Press& a, const float2* xdf
     return __dadd_rn(w, __dmul_rn(a.ms, d));
 }
 
-// (a zero written to u or v is the pair (0, 0) as well)
+// One thread per (I-face, J-face) of index (gi, gj), both axes in the same
+// block so that a tile's pressure is read from memory once.  (A zero written
+// to u or v is the pair (0, 0) as well.)
 __global__ void k_apply_pressure(Press a) {
     const Phys& p = a.p;
-    int axis = blockIdx.z;
-    int gi = blockIdx.x * blockDim.x + threadIdx.x;
-    int gj = blockIdx.y * blockDim.y + threadIdx.y;
-    int ox = p.nx + ((axis == 0 && !p.per_x) ? 1 : 0);
-    int oy = p.ny + ((axis == 1 && !p.per_y) ? 1 : 0);
-    if (gi >= ox || gj >= oy) return;
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gj = blockIdx.y * blockDim.y + threadIdx.y;
     const bool fix_q1 = (p.quirks & 1u) != 0;
     const float2* xdf = a.pairs ? (a.S->xsel ? a.xb : reinterpret_cast<const float2*>(a.x)) : nullptr;
-    if (axis == 0) {
-        double& u = a.u.at(gi + CF_HALO, gj + CF_HALO);
-        // u -= scale * (p(i) - p(i-1)) (src/VelocityCorrector.hpp:245)
-        double w = press_update(a, xdf, u, gi, gj, gi - 1, gj);
-        if (!a.adjoint) {
-            if (!p.per_x) {
-                if (gi <= 0 && p.bc[0] == 0) w = 0.0;
-                if (gi > p.nx - 1 && p.bc[2] == 0) w = 0.0;
+#pragma unroll 1
+    for (int axis = 0; axis < 2; ++axis) {
+        const int ox = p.nx + ((axis == 0 && !p.per_x) ? 1 : 0);
+        const int oy = p.ny + ((axis == 1 && !p.per_y) ? 1 : 0);
+        if (gi >= ox || gj >= oy) continue;
+        if (axis == 0) {
+            double& u = a.u.at(gi + CF_HALO, gj + CF_HALO);
+            // u -= scale * (p(i) - p(i-1)) (src/VelocityCorrector.hpp:245)
+            double w = press_update(a, xdf, u, gi, gj, gi - 1, gj);
+            if (!a.adjoint) {
+                if (!p.per_x) {
+                    if (gi <= 0 && p.bc[0] == 0) w = 0.0;
+                    if (gi > p.nx - 1 && p.bc[2] == 0) w = 0.0;
+                }
+                if (!fix_q1 && !p.per_y && gj == 0 && gi < p.nx && p.bc[1] == 0) w = 0.0;
             }
-            if (!fix_q1 && !p.per_y && gj == 0 && gi < p.nx && p.bc[1] == 0) w = 0.0;
-        }
-        u = w;
-    } else {
-        double& v = a.v.at(gi + CF_HALO, gj + CF_HALO);
-        double w = press_update(a, xdf, v, gi, gj, gi, gj - 1);  // :256
-        if (!p.per_y && !a.adjoint) {
-            if (fix_q1) {
-                if (gj <= 0 && p.bc[1] == 0) w = 0.0;
-                if (gj > p.ny - 1 && p.bc[3] == 0) w = 0.0;
-            } else if (gj > p.ny - 1 && p.bc[3] == 0) {
-                a.u.at(gi + CF_HALO, gj + CF_HALO) = 0.0;  // u ghost row ny
+            u = w;
+        } else {
+            double& v = a.v.at(gi + CF_HALO, gj + CF_HALO);
+            double w = press_update(a, xdf, v, gi, gj, gi, gj - 1);  // :256
+            if (!p.per_y && !a.adjoint) {
+                if (fix_q1) {
+                    if (gj <= 0 && p.bc[1] == 0) w = 0.0;
+                    if (gj > p.ny - 1 && p.bc[3] == 0) w = 0.0;
+                } else if (gj > p.ny - 1 && p.bc[3] == 0) {
+                    a.u.at(gi + CF_HALO, gj + CF_HALO) = 0.0;  // u ghost row ny
+                }
             }
+            v = w;
         }
-        v = w;
     }
 }
 
@@ -1448,7 +1452,7 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
             // mixed: the gradient reads the double-float solution; a warm
             // start then has it converted to the FP64 pressure it starts from
             Press pa = press_args(c, dt, gu, gv, adjoint);
-            dim3 grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
+            dim3 grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8);
             k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
             // u, v are final here: a caller may copy them out beside the norms
             if (!adjoint) cudaEventRecordWithFlags(c->ev_press, c->stream, cudaEventRecordExternal);
@@ -1756,7 +1760,7 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     // gradient subtraction (mixed: from the double-float solution; the FP64
     // pressure is made afterwards for a warm start, or when it is downloaded)
     Press pa = press_args(c, dt, gu, gv, adjoint);
-    dim3 blk(32, 8), grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8, 2);
+    dim3 blk(32, 8), grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8);
     k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
     c->launches += 1;
     c->p_df = mixed ? 1 : 0;
