@@ -259,6 +259,13 @@ __global__ void __launch_bounds__(MG_BX* MG_BY) k_mg_prolong(MgLev<T> C, MgLev<T
 // k_mg_post reads it from there and writes x: a CTA of k_mg_post reads its
 // halo from other tiles, which must not be written by the same launch.
 constexpr int FT_THREADS = 256;
+// Resident blocks per SM the level kernels are compiled for: the FP32
+// 32x16 tiles fit 4 (64 registers, measured faster: 21.5 vs 24.5 us at 1024^2
+// post), the register strips and FP64 tiles keep 3 (the strips spill at 64).
+template <typename T, int TW>
+struct FtBlocks {
+    static constexpr int value = (sizeof(T) == 4 && TW == 32) ? 4 : 3;
+};
 
 // index along an axis after the periodic wrap; -1 beyond a wall
 __device__ __forceinline__ int mg_dom(int g, int n, int per) {
@@ -737,7 +744,8 @@ __device__ __forceinline__ float strip_post(const MgLev<float>& C, const MgLev<f
 }
 
 template <typename T, int TW, int TH>
-__global__ void __launch_bounds__(FT_THREADS, 3) k_mg_pre(MgLev<T> F, MgLev<T> C, MgBc p, SolverState* S, int inner,
+__global__ void __launch_bounds__(FT_THREADS, FtBlocks<T, TW>::value) k_mg_pre(MgLev<T> F, MgLev<T> C, MgBc p,
+                                                                        SolverState* S, int inner,
                                                        StripMap m) {
     if (!block_live(S, inner)) return;
     constexpr int H = 5, W = TW + 2 * H, HT = TH + 2 * H;
@@ -853,7 +861,8 @@ __global__ void __launch_bounds__(FT_THREADS, 3) k_mg_pre(MgLev<T> F, MgLev<T> C
 }
 
 template <typename T, int TW, int TH>
-__global__ void __launch_bounds__(FT_THREADS, 3) k_mg_post(MgLev<T> C, MgLev<T> F, MgBc p, SolverState* S, int inner,
+__global__ void __launch_bounds__(FT_THREADS, FtBlocks<T, TW>::value) k_mg_post(MgLev<T> C, MgLev<T> F, MgBc p,
+                                                                         SolverState* S, int inner,
                                                            StripMap m, RzEpi E) {
     if (!block_live(S, inner)) return;
     constexpr int H = 4, W = TW + 2 * H, HT = TH + 2 * H;
