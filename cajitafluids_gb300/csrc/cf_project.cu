@@ -458,14 +458,59 @@ __device__ __forceinline__ float2 pair_at(const Grid<double>& g, int i, int j) {
 }
 __device__ __forceinline__ float2 df_neg(float2 x) { return make_float2(-x.x, -x.y); }
 
-// ((u_E - u_W) + v_N) - v_S of cell (c, j) from the pairs (FP32 pipe)
-__device__ __forceinline__ float2 div_pairs(const DivArgs& a, int c, int j) {
-    int ie = c + 1, jn = j + 1;
-    if (a.per_x && ie == a.nx) ie = 0;
-    if (a.per_y && jn == a.ny) jn = 0;
-    float2 t = df_add(pair_at(a.u, ie + CF_HALO, j + CF_HALO), df_neg(pair_at(a.u, c + CF_HALO, j + CF_HALO)));
-    t = df_add(t, pair_at(a.v, c + CF_HALO, jn + CF_HALO));
-    return df_add(t, df_neg(pair_at(a.v, c + CF_HALO, j + CF_HALO)));
+// The divergences of one unit's cells (64 columns x up to 16 rows, lane l
+// on columns c0 = 64 g + 2 l and c0 + 1), row by row: each row loads the
+// lane's two u pairs and two v pairs of row j + 1 as 16-byte vectors (row j's
+// v pairs come from the previous row), the E face of column c0 + 1 from the
+// next lane, and reads directly only what a wrap, the domain's last column
+// or the warp's last lane needs.  Calls f(c, j, div) for every owned cell,
+// div = ((u_E - u_W) + v_N) - v_S of its face pairs in double-float (E across
+// a periodic wrap is column 0, N row 0).
+template <typename F>
+__device__ __forceinline__ void div_pairs_unit(const DivArgs& a, int g, int band, int lane, F&& f) {
+    const int c0 = g * CF_UNIT_COLS + 2 * lane;
+    const int j0 = band * CF_BAND_ROWS, j1 = min(j0 + CF_BAND_ROWS, a.ny);
+    // the two pairs at columns c0, c0 + 1 of a row of u or v (in the ghosted
+    // arrays: a column past the owned range is a ghost or a boundary face,
+    // read but unused)
+    auto pair2 = [&](const Grid<double>& g2, int jj) {
+        return *reinterpret_cast<const float4*>(&g2.at(c0 + CF_HALO, jj + CF_HALO));
+    };
+    const bool live = c0 < a.nx;
+    float4 v0 = live ? pair2(a.v, j0) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int j = j0; j < j1; ++j) {
+        int jn = j + 1;
+        if (a.per_y && jn == a.ny) jn = 0;
+        float4 uu = make_float4(0.f, 0.f, 0.f, 0.f), v1 = uu;
+        if (live) {
+            uu = pair2(a.u, j);
+            v1 = pair2(a.v, jn);
+        }
+        // u at column c0 + 2 (the E face of column c0 + 1): the next lane's first
+        // pair, or read (the warp's last lane; the domain's last column: the
+        // boundary face, or column 0 across a periodic wrap)
+        float2 ue2 = make_float2(__shfl_down_sync(FULLMASK, uu.x, 1), __shfl_down_sync(FULLMASK, uu.y, 1));
+        if (live && c0 + 1 < a.nx && (lane == 31 || c0 + 2 >= a.nx)) {
+            const int ie2 = (a.per_x && c0 + 2 == a.nx) ? 0 : c0 + 2;
+            ue2 = pair_at(a.u, ie2 + CF_HALO, j + CF_HALO);
+        }
+        if (live) {
+            // column c0: E face c0 + 1 (or column 0 across a periodic wrap)
+            float2 ue1 = make_float2(uu.z, uu.w);
+            if (a.per_x && c0 + 1 == a.nx) ue1 = pair_at(a.u, CF_HALO, j + CF_HALO);
+            float2 t = df_add(ue1, df_neg(make_float2(uu.x, uu.y)));
+            t = df_add(t, make_float2(v1.x, v1.y));
+            t = df_add(t, df_neg(make_float2(v0.x, v0.y)));
+            f(c0, j, t);
+            if (c0 + 1 < a.nx) {
+                float2 t1 = df_add(ue2, df_neg(make_float2(uu.z, uu.w)));
+                t1 = df_add(t1, make_float2(v1.z, v1.w));
+                t1 = df_add(t1, df_neg(make_float2(v0.z, v0.w)));
+                f(c0 + 1, j, t1);
+            }
+        }
+        v0 = v1;
+    }
 }
 
 // Mixed init: b (double-float, kept for the outer residual), x = 0, inner
@@ -477,29 +522,21 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
     const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
     float abb = 0.f, arz = 0.f;
     if (unit < a.U) {
-        const int g = unit % a.G, band = unit / a.G;
-        const int c0 = g * CF_UNIT_COLS + 2 * lane;
-        const int j0 = band * CF_BAND_ROWS;
-        const int j1 = min(j0 + CF_BAND_ROWS, a.ny);
-        for (int j = j0; j < j1; ++j)
-#pragma unroll
-            for (int s = 0; s < 2; ++s) {
-                int c = c0 + s;
-                if (c >= a.nx) continue;
-                // the divergence of the velocity pairs and its scale -1/dx, in
-                // double-float on the FP32 pipe
-                const size_t k = (size_t)j * a.pitch + c;
-                const float2 bs = df_mul(a.mscale2, div_pairs(a, c, j));
-                reinterpret_cast<float2*>(a.b)[k] = bs;
-                // x as a double-float pair: 0, or (warm start) the previous
-                // FP64 solution split in place (same 8 bytes per cell)
-                reinterpret_cast<float2*>(a.x)[k] = a.warm ? df_split(a.x[k]) : make_float2(0.f, 0.f);
-                const float r = bs.x;
-                put_r32(a.r32, a.pitch32, a.nx, a.ny, a.per_x, a.per_y, c, j, r);
-                float z = a.st.minv32[edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y)] * r;
-                abb = fmaf(r, r, abb);
-                arz = fmaf(r, z, arz);
-            }
+        // the divergence of the velocity pairs and its scale -1/dx, in
+        // double-float on the FP32 pipe
+        div_pairs_unit(a, unit % a.G, unit / a.G, lane, [&](int c, int j, float2 t) {
+            const size_t k = (size_t)j * a.pitch + c;
+            const float2 bs = df_mul(a.mscale2, t);
+            reinterpret_cast<float2*>(a.b)[k] = bs;
+            // x as a double-float pair: 0, or (warm start) the previous
+            // FP64 solution split in place (same 8 bytes per cell)
+            reinterpret_cast<float2*>(a.x)[k] = a.warm ? df_split(a.x[k]) : make_float2(0.f, 0.f);
+            const float r = bs.x;
+            put_r32(a.r32, a.pitch32, a.nx, a.ny, a.per_x, a.per_y, c, j, r);
+            float z = a.st.minv32[edge_bits(c, j, a.nx, a.ny, a.per_x, a.per_y)] * r;
+            abb = fmaf(r, r, abb);
+            arz = fmaf(r, z, arz);
+        });
     }
     // inner r.r equals b.b here (the same squares in the same order)
     const double dbb = warp_fold((double)abb);
@@ -981,7 +1018,14 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_norms(DivArgs a) {
     const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
     double ass = 0.0, amx = 0.0;
     float fss = 0.f, fmx = 0.f;
-    if (unit < a.U) {
+    if (unit < a.U && a.mixed) {
+        // the divergence of the pairs, then its square and magnitude in FP32
+        div_pairs_unit(a, unit % a.G, unit / a.G, lane, [&](int, int, float2 t) {
+            const float bf = t.x * a.mscale32;
+            fss = fmaf(bf, bf, fss);
+            fmx = fmaxf(fmx, fabsf(bf));
+        });
+    } else if (unit < a.U) {
         const int g = unit % a.G, band = unit / a.G;
         const int c0 = g * CF_UNIT_COLS + 2 * lane;
         const int j0 = band * CF_BAND_ROWS;
@@ -991,17 +1035,9 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_norms(DivArgs a) {
             for (int s = 0; s < 2; ++s) {
                 int c = c0 + s;
                 if (c >= a.nx) continue;
-                if (a.mixed) {
-                    // the divergence of the pairs, then its square and
-                    // magnitude in FP32
-                    const float bf = div_pairs(a, c, j).x * a.mscale32;
-                    fss = fmaf(bf, bf, fss);
-                    fmx = fmaxf(fmx, fabsf(bf));
-                } else {
-                    double b = div_b(a, c, j);
-                    ass = fma(b, b, ass);
-                    amx = fmax(amx, fabs(b));
-                }
+                double b = div_b(a, c, j);
+                ass = fma(b, b, ass);
+                amx = fmax(amx, fabs(b));
             }
     }
     if (a.mixed) {
