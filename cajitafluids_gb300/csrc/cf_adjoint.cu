@@ -26,7 +26,13 @@
 //           Along periodic axes the adjoint that lands on ghosts is folded
 //           back onto the owned entity each ghost copies; wall ghosts are
 //           constants and drop out.
-// Supported: FP64 contexts; the rate-form quantity source with zero inflow
+// Mixed contexts (FP32 bulk): the checkpoints hold the mixed state (FP32 q,
+// velocity pairs), the recomputation repeats the mixed forward bit for bit,
+// the transposed projection runs the mixed PCG on the adjoint face arrays
+// held as pairs, and the advection's transpose runs in FP32 without records
+// (k_adj_advect32: the forward's FP32 trace recomputed, contributions
+// gathered through a register window per warp, deterministic).
+// Supported: FP64 and mixed contexts; the rate-form quantity source with zero inflow
 // velocity; constant body forces; the projection with CF_FIX_Q1 whenever a
 // y-wall is SOLID (the quirk's projection has an inconsistent adjoint
 // right-hand side).  Other settings return CF_ERR_UNSUPPORTED.
@@ -37,6 +43,7 @@
 #include <string>
 #include <vector>
 
+#include "cf_adv32.cuh"
 #include "cf_ctx.cuh"
 
 namespace cf {
@@ -249,12 +256,294 @@ __global__ void k_adj_gather(AdjGather a) {
     a.out.at(di, dj) = acc;
 }
 
-// periodic axes: add the adjoint that landed on ghost copies to the owned entity
-__global__ void k_adj_fold(Grid<double> g, int nox, int noy, int per_x, int per_y) {
+// --------------------------------------------------------------------------
+// Mixed precision (FP32 bulk): the transpose of the FP32 advection without
+// records.  One warp per strip of 28 destination columns x 32 destination
+// rows (ghosted index space, from (1, 1)); lane l takes target column
+// X0 - 2 + l, and lanes 2 .. 29 own destination column X0 - 2 + l.  While
+// every RK position stays within a cell of its entity (checked; the call
+// fails otherwise), each tap of a target lies within two columns and two
+// rows of it, for every entity kind, stage and sample.  So a lane gathers
+// the contributions of one target row (cell, I-face and J-face targets at
+// its column) into three 5 x 5 register tiles P[dy][dx] (destination
+// fields q, u, v at offsets dx, dy in [-2, 2]); five shuffles per tile row
+// then hand each destination lane the contributions of the five target
+// columns that reach it, in a fixed order, into a window of five
+// destination rows per field.  The warp walks the target rows from Y0 - 2
+// to Y0 + 33; after target row t, destination row t - 2 is complete and is
+// written.  No atomics, no scatter records: deterministic, and the
+// forward's traces are recomputed with the forward's own FP32 arithmetic
+// (cf_adv32.cuh), so every stencil is the forward's.
+constexpr int AJ_COLS = 28;
+constexpr int AJ_ROWS = 32;
+constexpr int AJ_WARPS = 4;
+
+struct AdjAdv32 {
+    Phys p;
+    Grid<float> q;            // forward quantity of the step (ghosts filled)
+    Grid<double> u, v;        // forward velocities, pairs (hi parts read)
+    Grid<float> aq;           // adjoint of the advected quantity
+    Grid<double> au, av;      // adjoint of the advected velocities, pairs (hi parts read)
+    Grid<float> oq, ou, ov;   // adjoint of the step's initial fields (ghosted)
+    float c;                  // dt / dx, as the forward's
+    int nsx, nsy;             // strips along x, y
+    int* err;
+};
+
+__device__ __forceinline__ int aj_at(int dx, int dy) { return (dy + 2) * 5 + (dx + 2); }
+
+// weights of a linear sample whose stencil starts o in [-2, 1] from the
+// target, on offsets -2 .. 2
+__device__ __forceinline__ void aj_spread_lin(int o, float t, float* W) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) W[k] = (k - 2 == o) ? 1.f - t : ((k - 3 == o) ? t : 0.f);
+}
+// a cubic sample's weights, stencil start o in {-2, -1}
+__device__ __forceinline__ void aj_spread_cub(int o, const float* w, float* W) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) W[k] = o == -2 ? (k < 4 ? w[k] : 0.f) : (k > 0 ? w[k - 1] : 0.f);
+}
+__device__ __forceinline__ void aj_outer(float* P, float s, const float* WX, const float* WY) {
+    float x[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) x[k] = s * WX[k];
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+        for (int k = 0; k < 5; ++k) P[r * 5 + k] = fmaf(WY[r], x[k], P[r * 5 + k]);
+}
+__device__ __forceinline__ void aj_lin(float* P, float s, const Lin32& l) {
+    float WX[5], WY[5];
+    aj_spread_lin(l.ox, l.tx, WX);
+    aj_spread_lin(l.oy, l.ty, WY);
+    aj_outer(P, s, WX, WY);
+}
+
+// A trace displacement (index units) that reaches a full cell, or is NaN,
+// fails the call; it is replaced by 0 so that every tap stays inside the
+// arrays (a valid trace keeps its bits).
+__device__ __forceinline__ float aj_safe(float d, bool& bad) {
+    if (fabsf(d) < 1.f) return d;
+    bad = true;
+    return 0.f;
+}
+
+// One target: the forward trace (advect_value in cf_fields.cu, same
+// operations), then its transpose with fbar the adjoint of the advected
+// value.  Position derivatives are in index units (the trace moves by
+// d = -c a, c = dt / dx).
+template <int ORDER, int ENT>
+__device__ __forceinline__ void aj_target(const AdjAdv32& a, int li, int lj, float fbar, float* Pq, float* Pu,
+                                          float* Pv, bool& bad) {
+    const GlobalTaps U{reinterpret_cast<const float*>(a.u.o), a.u.pitch, a.u.ex, a.u.ey, 2};
+    const GlobalTaps V{reinterpret_cast<const float*>(a.v.o), a.v.pitch, a.v.ex, a.v.ey, 2};
+    const float ox_e = ENT == E_FACEI ? 0.f : 0.5f;
+    const float oy_e = ENT == E_FACEJ ? 0.f : 0.5f;
+    const float uox = ox_e, uoy = oy_e - 0.5f, vox = ox_e - 0.5f, voy = oy_e;
+    float v0x, v0y;
+    stage0_32(ENT, U, V, li, lj, v0x, v0y);
+    const float c = a.c;
+    const float h1 = -0.5f * c, h2 = -0.75f * c;
+    const float d1x = aj_safe(h1 * v0x, bad), d1y = aj_safe(h1 * v0y, bad);
+    const Lin32 s1u = lin32g(U, li, lj, uox + d1x, uoy + d1y);
+    const Lin32 s1v = lin32g(V, li, lj, vox + d1x, voy + d1y);
+    const bool ralston = (a.p.quirks & 2u) != 0;
+    const float d2x = aj_safe(h2 * (ralston ? s1u.val : v0x), bad);
+    const float d2y = aj_safe(h2 * (ralston ? s1v.val : v0y), bad);
+    const Lin32 s2u = lin32g(U, li, lj, uox + d2x, uoy + d2y);
+    const Lin32 s2v = lin32g(V, li, lj, vox + d2x, voy + d2y);
+    const float ax = fmaf(4.f / 9.f, s2u.val, fmaf(3.f / 9.f, s1u.val, (2.f / 9.f) * v0x));
+    const float ay = fmaf(4.f / 9.f, s2v.val, fmaf(3.f / 9.f, s1v.val, (2.f / 9.f) * v0y));
+    const float dx = aj_safe(-c * ax, bad), dy = aj_safe(-c * ay, bad);
+    // the advected field's sample at the foot
+    float* PF = ENT == E_CELL ? Pq : (ENT == E_FACEI ? Pu : Pv);
+    const GlobalTaps F = ENT == E_CELL ? GlobalTaps{a.q.o, a.q.pitch, a.q.ex, a.q.ey, 1} : (ENT == E_FACEI ? U : V);
+    float gx, gy;
+    if (ORDER == 1) {
+        const Lin32 sf = lin32g(F, li, lj, dx, dy);
+        gx = sf.gx;
+        gy = sf.gy;
+        aj_lin(PF, fbar, sf);
+    } else {
+        const float flx = floorf(dx), fly = floorf(dy);
+        const int ox = (int)flx, oy = (int)fly;
+        const float tx = dx - flx, ty = dy - fly;
+        float wx[4], wy[4], dwx[4], dwy[4];
+        cubic_w32(tx, wx);
+        cubic_w32(ty, wy);
+        cubic_dw32(tx, dwx);
+        cubic_dw32(ty, dwy);
+        // derivatives against differences from the centre tap, as the
+        // forward samples (a constant field has zero gradient exactly)
+        const float* base = F.at(li + ox - 1, lj + oy - 1);
+        const int st = F.stride(), e = F.step();
+        const float cc = GlobalTaps::ld(base + st + e);
+        gx = 0.f;
+        gy = 0.f;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const float* row = base + b * st;
+            float rs = 0.f, rd = 0.f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float f = GlobalTaps::ld(row + k * e) - cc;
+                rs = fmaf(wx[k], f, rs);
+                rd = fmaf(dwx[k], f, rd);
+            }
+            gx = fmaf(wy[b], rd, gx);
+            gy = fmaf(dwy[b], rs, gy);
+        }
+        float WX[5], WY[5];
+        aj_spread_cub(ox - 1, wx, WX);
+        aj_spread_cub(oy - 1, wy, WY);
+        aj_outer(PF, fbar, WX, WY);
+    }
+    // reverse of a = 2/9 v0 + 3/9 v1 + 4/9 v2, d = -c a
+    const float abx = -c * (fbar * gx), aby = -c * (fbar * gy);
+    float v0bx = (2.f / 9.f) * abx, v0by = (2.f / 9.f) * aby;
+    float v1bx = (3.f / 9.f) * abx, v1by = (3.f / 9.f) * aby;
+    const float v2bx = (4.f / 9.f) * abx, v2by = (4.f / 9.f) * aby;
+    // stage 2 at d2 = h2 (v1 or v0)
+    aj_lin(Pu, v2bx, s2u);
+    aj_lin(Pv, v2by, s2v);
+    const float d2bx = fmaf(v2bx, s2u.gx, v2by * s2v.gx), d2by = fmaf(v2bx, s2u.gy, v2by * s2v.gy);
+    if (ralston) {
+        v1bx = fmaf(h2, d2bx, v1bx);
+        v1by = fmaf(h2, d2by, v1by);
+    } else {
+        v0bx = fmaf(h2, d2bx, v0bx);
+        v0by = fmaf(h2, d2by, v0by);
+    }
+    // stage 1 at d1 = h1 v0
+    aj_lin(Pu, v1bx, s1u);
+    aj_lin(Pv, v1by, s1v);
+    const float d1bx = fmaf(v1bx, s1u.gx, v1by * s1v.gx), d1by = fmaf(v1bx, s1u.gy, v1by * s1v.gy);
+    v0bx = fmaf(h1, d1bx, v0bx);
+    v0by = fmaf(h1, d1by, v0by);
+    // stage 0 at the entity (the taps and weights of stage0_32)
+    if (ENT == E_CELL) {
+        const float hx = 0.5f * v0bx, hy = 0.5f * v0by;
+        Pu[aj_at(0, 0)] += hx;
+        Pu[aj_at(1, 0)] += hx;
+        Pv[aj_at(0, 0)] += hy;
+        Pv[aj_at(0, 1)] += hy;
+    } else if (ENT == E_FACEI) {
+        const float qy = 0.25f * v0by;
+        Pu[aj_at(0, 0)] += v0bx;
+        Pv[aj_at(-1, 0)] += qy;
+        Pv[aj_at(0, 0)] += qy;
+        Pv[aj_at(-1, 1)] += qy;
+        Pv[aj_at(0, 1)] += qy;
+    } else {
+        const float qx = 0.25f * v0bx;
+        Pu[aj_at(0, -1)] += qx;
+        Pu[aj_at(1, -1)] += qx;
+        Pu[aj_at(0, 0)] += qx;
+        Pu[aj_at(1, 0)] += qx;
+        Pv[aj_at(0, 0)] += v0by;
+    }
+}
+
+// destination lane c takes P[dy][dx] of the lane at column c - dx, dx from
+// +2 down to -2, into the window row of destination row t + dy
+__device__ __forceinline__ void aj_exchange(const float* P, float* A) {
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+        float s = A[r];
+        s += __shfl_up_sync(0xffffffffu, P[r * 5 + 4], 2);
+        s += __shfl_up_sync(0xffffffffu, P[r * 5 + 3], 1);
+        s += P[r * 5 + 2];
+        s += __shfl_down_sync(0xffffffffu, P[r * 5 + 1], 1);
+        s += __shfl_down_sync(0xffffffffu, P[r * 5 + 0], 2);
+        A[r] = s;
+    }
+}
+
+template <int ORDER>
+__global__ void __launch_bounds__(AJ_WARPS * 32) k_adj_advect32(AdjAdv32 a) {
+    const int lane = threadIdx.x & 31;
+    const int strip = blockIdx.x * AJ_WARPS + (threadIdx.x >> 5);
+    if (strip >= a.nsx * a.nsy) return;  // whole warps
+    const int X0 = 1 + (strip % a.nsx) * AJ_COLS, Y0 = 1 + (strip / a.nsx) * AJ_ROWS;
+    const int tc = X0 - 2 + lane;
+    const bool owner = lane >= 2 && lane < 2 + AJ_COLS;
+    const Phys& p = a.p;
+    const int gi = tc - CF_HALO;
+    const int oxu = p.nx + (p.per_x ? 0 : 1), oyv = p.ny + (p.per_y ? 0 : 1);
+    float Aq[5], Au[5], Av[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) Aq[k] = Au[k] = Av[k] = 0.f;
+    bool bad = false;
+#pragma unroll 1
+    for (int tr = Y0 - 2; tr < Y0 + AJ_ROWS + 2; ++tr) {
+        float Pq[25], Pu[25], Pv[25];
+#pragma unroll
+        for (int k = 0; k < 25; ++k) Pq[k] = Pu[k] = Pv[k] = 0.f;
+        const int gj = tr - CF_HALO;
+        if (gi >= 0 && gj >= 0) {
+            if (gi < p.nx && gj < p.ny) aj_target<ORDER, E_CELL>(a, tc, tr, a.aq.at(tc, tr), Pq, Pu, Pv, bad);
+            if (gi < oxu && gj < p.ny)
+                aj_target<ORDER, E_FACEI>(a, tc, tr, reinterpret_cast<const float2&>(a.au.at(tc, tr)).x, Pq, Pu,
+                                          Pv, bad);
+            if (gi < p.nx && gj < oyv)
+                aj_target<ORDER, E_FACEJ>(a, tc, tr, reinterpret_cast<const float2&>(a.av.at(tc, tr)).x, Pq, Pu,
+                                          Pv, bad);
+        }
+        aj_exchange(Pq, Aq);
+        aj_exchange(Pu, Au);
+        aj_exchange(Pv, Av);
+        const int r = tr - 2;  // complete
+        if (owner && r >= Y0 && r < Y0 + AJ_ROWS) {
+            if (tc < a.oq.ex && r < a.oq.ey) a.oq.at(tc, r) = Aq[0];
+            if (tc < a.ou.ex && r < a.ou.ey) a.ou.at(tc, r) = Au[0];
+            if (tc < a.ov.ex && r < a.ov.ey) a.ov.at(tc, r) = Av[0];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            Aq[k] = Aq[k + 1];
+            Au[k] = Au[k + 1];
+            Av[k] = Av[k + 1];
+        }
+        Aq[4] = Au[4] = Av[4] = 0.f;
+    }
+    if (bad) atomicOr(a.err, 1);
+}
+
+// owned entries of an FP32 grid as pairs (value, 0) of a pair grid
+__global__ void k_adj_to_pairs(Grid<float> s, Grid<double> d, int nox, int noy) {
     const int gi = blockIdx.x * blockDim.x + threadIdx.x;
     const int gj = blockIdx.y * blockDim.y + threadIdx.y;
     if (gi >= nox || gj >= noy) return;
-    double acc = g.at(gi + CF_HALO, gj + CF_HALO);
+    reinterpret_cast<float2&>(d.at(gi + CF_HALO, gj + CF_HALO)) = make_float2(s.at(gi + CF_HALO, gj + CF_HALO), 0.f);
+}
+
+// host arrays (row pitch nox, FP64) <-> owned entries of an FP32 grid
+// (pairs = 0) or of a pair grid (pairs = 1)
+__global__ void k_adj_import(Grid<double> d, Grid<float> f, int pairs, const double* src, int nox, int noy) {
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    if (gi >= nox || gj >= noy) return;
+    const double w = src[(size_t)gj * nox + gi];
+    if (pairs)
+        reinterpret_cast<float2&>(d.at(gi + CF_HALO, gj + CF_HALO)) = df_split(w);
+    else
+        f.at(gi + CF_HALO, gj + CF_HALO) = __double2float_rn(w);
+}
+__global__ void k_adj_export(Grid<double> d, Grid<float> f, int pairs, double* dst, int nox, int noy) {
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    if (gi >= nox || gj >= noy) return;
+    dst[(size_t)gj * nox + gi] = pairs ? df_value(reinterpret_cast<const float2&>(d.at(gi + CF_HALO, gj + CF_HALO)))
+                                       : (double)f.at(gi + CF_HALO, gj + CF_HALO);
+}
+
+// periodic axes: add the adjoint that landed on ghost copies to the owned entity
+template <typename T>
+__global__ void k_adj_fold(Grid<T> g, int nox, int noy, int per_x, int per_y) {
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    if (gi >= nox || gj >= noy) return;
+    T acc = g.at(gi + CF_HALO, gj + CF_HALO);
     for (int ky = -1; ky <= 1; ++ky)
         for (int kx = -1; kx <= 1; ++kx) {
             if (kx == 0 && ky == 0) continue;
@@ -288,11 +577,12 @@ __global__ void k_adj_mask(Phys p, Grid<double> u, Grid<double> v) {
 // cells t, t + 256, ...; then a fixed-order block sum, so the result is
 // deterministic.
 constexpr int kBoxThreads = 256;
-__global__ void __launch_bounds__(kBoxThreads) k_adj_rate(Phys p, Grid<double> aq, double dt, double* rbar) {
+template <typename T>
+__global__ void __launch_bounds__(kBoxThreads) k_adj_rate(Phys p, Grid<T> aq, double dt, double* rbar) {
     const int i0 = p.box[E_CELL][0], i1 = p.box[E_CELL][1], j0 = p.box[E_CELL][2], j1 = p.box[E_CELL][3];
     const int w = i1 - i0, n = w > 0 && j1 > j0 ? w * (j1 - j0) : 0;
     double s = 0.0;
-    for (int k = threadIdx.x; k < n; k += kBoxThreads) s = s + aq.at(i0 + k % w, j0 + k / w);
+    for (int k = threadIdx.x; k < n; k += kBoxThreads) s = s + (double)aq.at(i0 + k % w, j0 + k / w);
     __shared__ double ws[kBoxThreads / 32];
     s = warp_fold(s);
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
@@ -306,8 +596,14 @@ __global__ void __launch_bounds__(kBoxThreads) k_adj_rate(Phys p, Grid<double> a
 
 // host side
 
-static void* grid_base(const Grid<double>& g) { return (void*)(g.o - (32 - CF_HALO)); }
-static size_t grid_bytes(const Grid<double>& g) { return (size_t)g.pitch * g.ey * sizeof(double); }
+template <typename T>
+static void* grid_base(const Grid<T>& g) {
+    return (void*)(g.o - CF_COL0);
+}
+template <typename T>
+static size_t grid_bytes(const Grid<T>& g) {
+    return (size_t)g.pitch * g.ey * sizeof(T);
+}
 
 struct AdjState {
     bool ready = false;
@@ -319,9 +615,13 @@ struct AdjState {
     std::vector<double*> seg;
     double* final_state = nullptr;
     Grid<double> ag[3]{}, bg[3]{};  // adjoint grids (current and gather output)
+    // mixed contexts: the adjoint of q in FP32 (aq32; ag[1], ag[2] hold the
+    // velocity adjoints as pairs, bg is unused) and the FP32 outputs of the
+    // reverse advection (o32: q, u, v shapes)
+    bool mixed = false;
+    Grid<float> aq32{}, o32[3]{};
     RecKind F[3], Su[3][3], Sv[3][3];
     int* d_err = nullptr;
-    double* d_rows = nullptr;
     double* d_rbar = nullptr;  // dL/d(rate), accumulated on the device
     double* xa = nullptr;      // the adjoint pressure between reverse steps (the warm start)
     // the forward pass left the last segment's states in seg: the backward's
@@ -336,7 +636,14 @@ using namespace cf;
 
 namespace {
 
-size_t state_bytes(cf_ctx* c) { return grid_bytes(c->q64[0]) + grid_bytes(c->u[0]) + grid_bytes(c->v[0]); }
+bool is_mixed(const cf_ctx* c) { return c->precision == CF_PREC_MIXED; }
+
+// a checkpoint holds the state as the context stores it: q (FP64, or FP32 in
+// a mixed context) and u, v (FP64, or pairs), ghosted, back to back
+size_t state_bytes(cf_ctx* c) {
+    const size_t qb = is_mixed(c) ? grid_bytes(c->q32[0]) : grid_bytes(c->q64[0]);
+    return qb + grid_bytes(c->u[0]) + grid_bytes(c->v[0]);
+}
 
 int dalloc(cf_ctx* c, AdjState* A, void** p, size_t bytes) {
     cudaError_t e = cudaMalloc(p, bytes);
@@ -345,24 +652,44 @@ int dalloc(cf_ctx* c, AdjState* A, void** p, size_t bytes) {
     return CF_OK;
 }
 
+// the current state's three arrays as (base, bytes)
+void state_parts(cf_ctx* c, void** base, size_t* bytes) {
+    const int k = c->cur;
+    if (is_mixed(c)) {
+        base[0] = grid_base(c->q32[k]);
+        bytes[0] = grid_bytes(c->q32[k]);
+    } else {
+        base[0] = grid_base(c->q64[k]);
+        bytes[0] = grid_bytes(c->q64[k]);
+    }
+    base[1] = grid_base(c->u[k]);
+    bytes[1] = grid_bytes(c->u[k]);
+    base[2] = grid_base(c->v[k]);
+    bytes[2] = grid_bytes(c->v[k]);
+}
+
 int save_state(cf_ctx* c, double* dst) {
     char* d = (char*)dst;
-    const Grid<double>* gs[3] = {&c->q64[c->cur], &c->u[c->cur], &c->v[c->cur]};
-    for (auto* g : gs) {
-        cudaError_t e = cudaMemcpyAsync(d, grid_base(*g), grid_bytes(*g), cudaMemcpyDeviceToDevice, c->stream);
+    void* base[3];
+    size_t bytes[3];
+    state_parts(c, base, bytes);
+    for (int k = 0; k < 3; ++k) {
+        cudaError_t e = cudaMemcpyAsync(d, base[k], bytes[k], cudaMemcpyDeviceToDevice, c->stream);
         if (e != cudaSuccess) return cuda_check(c, e, "checkpoint save");
-        d += grid_bytes(*g);
+        d += bytes[k];
     }
     return CF_OK;
 }
 
 int load_state(cf_ctx* c, const double* src) {
     const char* s = (const char*)src;
-    const Grid<double>* gs[3] = {&c->q64[c->cur], &c->u[c->cur], &c->v[c->cur]};
-    for (auto* g : gs) {
-        cudaError_t e = cudaMemcpyAsync(grid_base(*g), s, grid_bytes(*g), cudaMemcpyDeviceToDevice, c->stream);
+    void* base[3];
+    size_t bytes[3];
+    state_parts(c, base, bytes);
+    for (int k = 0; k < 3; ++k) {
+        cudaError_t e = cudaMemcpyAsync(base[k], s, bytes[k], cudaMemcpyDeviceToDevice, c->stream);
         if (e != cudaSuccess) return cuda_check(c, e, "checkpoint load");
-        s += grid_bytes(*g);
+        s += bytes[k];
     }
     return CF_OK;
 }
@@ -374,7 +701,6 @@ int check_supported(cf_ctx* c) {
     // would depend on a pressure the checkpoints do not hold
     if (c->warm) return fail(c, CF_ERR_UNSUPPORTED, "the adjoint needs cold-started projections (warm start is on)");
     const Phys& p = c->ph;
-    if (c->precision != CF_PREC_FP64) return fail(c, CF_ERR_UNSUPPORTED, "the adjoint runs on FP64 contexts");
     bool src_active = p.bbox[2] > p.bbox[0] && p.bbox[3] > p.bbox[1];
     if (src_active && p.src_mode == 0 && p.src_q != 0.0)
         return fail(c, CF_ERR_UNSUPPORTED, "adjoint of the clamp-form quantity source (use the rate form)");
@@ -424,18 +750,48 @@ int setup_records(cf_ctx* c, AdjState* A) {
         }
     }
     if (!rc) rc = dalloc(c, A, (void**)&A->d_err, sizeof(int));
-    if (!rc) rc = dalloc(c, A, (void**)&A->d_rows, sizeof(double) * (c->ph.ny + 1));
     if (!rc) rc = dalloc(c, A, (void**)&A->d_rbar, sizeof(double));
     if (!rc) rc = dalloc(c, A, (void**)&A->xa, sizeof(double) * (size_t)c->vpitch * c->ph.ny);
     return rc;
 }
 
-// One reverse step, enqueued without a synchronisation: the transposed
-// projection (deferred through its resident graph when that serves it;
-// non-convergence and failures are tallied on the device), the inputs'
-// transpose with dL/d(rate) accumulated on the device, and the advection's
-// transpose (a trace that moved too far sets the device error flag).
-int adjoint_step(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_ready) {
+// a zeroed ghosted grid laid out as the context's grids (cf_api.cu alloc_grid)
+template <typename T>
+int adj_grid(cf_ctx* c, AdjState* A, Grid<T>& g, int ex, int ey) {
+    const int pitch = (int)(((size_t)CF_COL0 + ex + 31) / 32 * 32);
+    void* base = nullptr;
+    const size_t bytes = (size_t)pitch * ey * sizeof(T);
+    int rc = dalloc(c, A, &base, bytes);
+    if (rc) return rc;
+    cudaMemsetAsync(base, 0, bytes, c->stream);
+    g.o = (T*)base + CF_COL0;
+    g.pitch = pitch;
+    g.ex = ex;
+    g.ey = ey;
+    return CF_OK;
+}
+
+// mixed contexts: adjoint grids only (the reverse advection keeps no records)
+int setup_mixed(cf_ctx* c, AdjState* A) {
+    if (A->aq32.o) return CF_OK;
+    const Grid<double>& gu = c->u[0];
+    const Grid<double>& gv = c->v[0];
+    const Grid<float>& gq = c->q32[0];
+    int rc = adj_grid(c, A, A->aq32, gq.ex, gq.ey);
+    if (!rc) rc = adj_grid(c, A, A->o32[0], gq.ex, gq.ey);
+    if (!rc) rc = adj_grid(c, A, A->o32[1], gu.ex, gu.ey);
+    if (!rc) rc = adj_grid(c, A, A->o32[2], gv.ex, gv.ey);
+    if (!rc) rc = adj_grid(c, A, A->ag[1], gu.ex, gu.ey);
+    if (!rc) rc = adj_grid(c, A, A->ag[2], gv.ex, gv.ey);
+    if (!rc) rc = dalloc(c, A, (void**)&A->d_err, sizeof(int));
+    if (!rc) rc = dalloc(c, A, (void**)&A->d_rbar, sizeof(double));
+    if (!rc) rc = dalloc(c, A, (void**)&A->xa, sizeof(double) * (size_t)c->vpitch * c->ph.ny);
+    return rc;
+}
+
+// The transposed projection on the adjoint face arrays (pairs in a mixed
+// context), starting from the previous reverse step's adjoint pressure.
+int adjoint_projection(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_ready) {
     const Phys& p = c->ph;
     dim3 blk(32, 8);
     int rc;
@@ -443,7 +799,9 @@ int adjoint_step(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_ready)
     k_adj_mask<<<dim3((p.nx + 2 + 31) / 32, (p.ny + 2 + 7) / 8, 2), blk, 0, c->stream>>>(p, A->ag[1], A->ag[2]);
     // the solve starts from the previous reverse step's adjoint pressure
     // (zero for the first), kept in A->xa between steps because the
-    // forward recomputation reuses the solver's solution vector
+    // forward recomputation reuses the solver's solution vector (which is
+    // replaced here: a mixed forward's pressure pairs need no conversion)
+    c->p_df = 0;
     const size_t xbytes = sizeof(double) * (size_t)c->vpitch * p.ny;
     if ((rc = cuda_check(c, cudaMemcpyAsync(c->x.a, A->xa, xbytes, cudaMemcpyDeviceToDevice, c->stream), "adjoint x")))
         return rc;
@@ -452,10 +810,84 @@ int adjoint_step(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_ready)
     if ((rc = project_adjoint_async(c, A->dt, so, &res, &deferred, params_ready, A->ag[1], A->ag[2]))) return rc;
     if (!deferred && res.status != ST_CONVERGED && res.status != ST_MAXIT)
         return fail(c, CF_ERR_NUMERIC, "adjoint projection failed (status %d)", res.status);
+    // (a warm-started mixed projection leaves its solution as FP64)
     if ((rc = cuda_check(c, cudaMemcpyAsync(A->xa, c->x.a, xbytes, cudaMemcpyDeviceToDevice, c->stream), "adjoint x")))
         return rc;
-    // I^T: wall masks of the inputs; dL/dQ from the rate source
+    // I^T: wall masks of the inputs
     k_adj_mask<<<dim3((p.nx + 2 + 31) / 32, (p.ny + 2 + 7) / 8, 2), blk, 0, c->stream>>>(p, A->ag[1], A->ag[2]);
+    c->launches += 2;
+    return CF_OK;
+}
+
+// One reverse step of a mixed context: the transposed projection (mixed
+// MG/Jacobi PCG on the pair arrays), the inputs' transpose, then the FP32
+// reverse advection at the forward state of this step (already loaded), the
+// periodic fold, and the velocity adjoints back to pairs.
+int adjoint_step_mixed(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_ready) {
+    const Phys& p = c->ph;
+    dim3 blk(32, 8);
+    int rc = adjoint_projection(c, A, so, params_ready);
+    if (rc) return rc;
+    bool src_active = p.bbox[2] > p.bbox[0] && p.bbox[3] > p.bbox[1];
+    if (src_active && p.src_mode == 1) {
+        k_adj_rate<<<1, kBoxThreads, 0, c->stream>>>(p, A->aq32, A->dt, A->d_rbar);
+        c->launches += 1;
+    }
+    if ((rc = cuda_check(c, launch_fill_ghosts(c), "fill ghosts"))) return rc;
+    AdjAdv32 a;
+    a.p = p;
+    a.q = c->q32[c->cur];
+    a.u = c->u[c->cur];
+    a.v = c->v[c->cur];
+    a.aq = A->aq32;
+    a.au = A->ag[1];
+    a.av = A->ag[2];
+    a.oq = A->o32[0];
+    a.ou = A->o32[1];
+    a.ov = A->o32[2];
+    a.c = (float)(A->dt / p.dx);
+    // destinations reach two entities past the owned targets: ghosted
+    // [1, 3 + n(+1) + 2) on each axis
+    const int wx = p.nx + (p.per_x ? 0 : 1) + 4, wy = p.ny + (p.per_y ? 0 : 1) + 4;
+    a.nsx = (wx + AJ_COLS - 1) / AJ_COLS;
+    a.nsy = (wy + AJ_ROWS - 1) / AJ_ROWS;
+    a.err = A->d_err;
+    const int blocks = (a.nsx * a.nsy + AJ_WARPS - 1) / AJ_WARPS;
+    if (A->order == 1)
+        k_adj_advect32<1><<<blocks, AJ_WARPS * 32, 0, c->stream>>>(a);
+    else
+        k_adj_advect32<3><<<blocks, AJ_WARPS * 32, 0, c->stream>>>(a);
+    c->launches += 1;
+    for (int f = 0; f < 3; ++f) {
+        const int nox = p.nx + ((f == 1 && !p.per_x) ? 1 : 0);
+        const int noy = p.ny + ((f == 2 && !p.per_y) ? 1 : 0);
+        const dim3 g((nox + 31) / 32, (noy + 7) / 8);
+        if (p.per_x || p.per_y) {
+            k_adj_fold<<<g, blk, 0, c->stream>>>(A->o32[f], nox, noy, p.per_x, p.per_y);
+            c->launches += 1;
+        }
+        if (f == 0) {
+            std::swap(A->aq32, A->o32[0]);
+        } else {
+            k_adj_to_pairs<<<g, blk, 0, c->stream>>>(A->o32[f], A->ag[f], nox, noy);
+            c->launches += 1;
+        }
+    }
+    return cuda_check(c, cudaGetLastError(), "adjoint advection");
+}
+
+// One reverse step, enqueued without a synchronisation: the transposed
+// projection (deferred through its resident graph when that serves it;
+// non-convergence and failures are tallied on the device), the inputs'
+// transpose with dL/d(rate) accumulated on the device, and the advection's
+// transpose (a trace that moved too far sets the device error flag).
+int adjoint_step(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_ready) {
+    if (A->mixed) return adjoint_step_mixed(c, A, so, params_ready);
+    const Phys& p = c->ph;
+    dim3 blk(32, 8);
+    int rc = adjoint_projection(c, A, so, params_ready);
+    if (rc) return rc;
+    // dL/dQ from the rate source
     bool src_active = p.bbox[2] > p.bbox[0] && p.bbox[3] > p.bbox[1];
     if (src_active && p.src_mode == 1) {
         k_adj_rate<<<1, kBoxThreads, 0, c->stream>>>(p, A->ag[0], A->dt, A->d_rbar);
@@ -504,7 +936,7 @@ int adjoint_step(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_ready)
                                                                                      p.per_y);
         std::swap(A->ag[gsel], A->bg[gsel]);
     }
-    c->launches += 6 + (p.per_x || p.per_y ? 3 : 0);
+    c->launches += 4 + (p.per_x || p.per_y ? 3 : 0);
     return cuda_check(c, cudaGetLastError(), "adjoint advection");
 }
 
@@ -531,6 +963,29 @@ int adj_io(cf_ctx* c, Grid<double>& g, int field, double* host, bool to_host) {
     return cuda_check(c, e, "adjoint copy");
 }
 
+// mixed contexts: owned region of an adjoint array (0: q in FP32, 1, 2: u, v
+// as pairs) <-> contiguous FP64 host array, through the FP64 staging buffer
+int adj_io_mixed(cf_ctx* c, AdjState* A, int k, double* host, bool to_host) {
+    int ox = c->ph.nx, oy = c->ph.ny;
+    if (k == 1 && !c->ph.per_x) ox += 1;
+    if (k == 2 && !c->ph.per_y) oy += 1;
+    const size_t bytes = sizeof(double) * (size_t)ox * oy;
+    const Grid<double> d = k == 0 ? Grid<double>{} : A->ag[k];
+    const dim3 blk(32, 8), g((ox + 31) / 32, (oy + 7) / 8);
+    if (to_host) {
+        k_adj_export<<<g, blk, 0, c->stream>>>(d, A->aq32, k != 0, c->staging, ox, oy);
+        int rc = cuda_check(c, cudaGetLastError(), "adjoint export");
+        if (!rc)
+            rc = cuda_check(c, cudaMemcpyAsync(host, c->staging, bytes, cudaMemcpyDeviceToHost, c->stream),
+                            "adjoint copy");
+        return rc;
+    }
+    int rc = cuda_check(c, cudaMemcpyAsync(c->staging, host, bytes, cudaMemcpyHostToDevice, c->stream), "adjoint copy");
+    if (rc) return rc;
+    k_adj_import<<<g, blk, 0, c->stream>>>(d, A->aq32, k != 0, c->staging, ox, oy);
+    return cuda_check(c, cudaGetLastError(), "adjoint import");
+}
+
 }  // namespace
 
 extern "C" {
@@ -540,12 +995,12 @@ int cf_forward_checkpointed(cf_ctx* ctx, int nsteps, int ckpt_every, double dt, 
     if (!ctx) return CF_ERR_INVALID;
     if (nsteps <= 0 || ckpt_every <= 0 || !(dt > 0.0) || (value_order != 1 && value_order != 3))
         return fail(ctx, CF_ERR_INVALID, "bad forward_checkpointed arguments");
-    if (ctx->precision != CF_PREC_FP64) return fail(ctx, CF_ERR_UNSUPPORTED, "the adjoint runs on FP64 contexts");
     if (ctx->warm)
         return fail(ctx, CF_ERR_UNSUPPORTED, "the adjoint needs cold-started projections (warm start is on)");
     cudaSetDevice(ctx->device);
     if (!ctx->adjoint) ctx->adjoint = new AdjState();
     AdjState* A = adj(ctx);
+    A->mixed = is_mixed(ctx);
     int nck = (nsteps + ckpt_every - 1) / ckpt_every;
     size_t sb = state_bytes(ctx);
     int rc = CF_OK;
@@ -628,29 +1083,39 @@ int cf_backward(cf_ctx* ctx, const double* dL_dq_T, const double* dL_du_T, const
     if (!A || !A->ready) return fail(ctx, CF_ERR_INVALID, "cf_backward needs a preceding cf_forward_checkpointed");
     cudaSetDevice(ctx->device);
     int rc = check_supported(ctx);
-    if (!rc) rc = setup_records(ctx, A);
+    if (!rc) rc = A->mixed ? setup_mixed(ctx, A) : setup_records(ctx, A);
     if (rc) return rc;
+    SolveOpts fo{};
+    if ((rc = parse_solver_opts(ctx, &A->opts, &fo))) return rc;
     SolveOpts so{};
     so.tol = A->opts.tol;
     so.abs_tol = 0.0;  // the adjoint right-hand side has its own scale
     so.max_iter = A->opts.max_iter;
-    so.inner_tol = 0.1;
-    so.max_outer = 200;
+    // mixed: the forward's reliable-update threshold and outer limit
+    so.inner_tol = A->mixed ? fo.inner_tol : 0.1;
+    so.max_outer = A->mixed ? fo.max_outer : 200;
     so.precon_none = (!strcmp(A->precon.c_str(), "None") || !strcmp(A->precon.c_str(), "none")) ? 1 : 0;
     so.precon_mg = (A->precon == "PFMG" || A->precon == "SMG" || A->precon == "MG") ? 1 : 0;
-    if (!(so.tol > 0.0)) so.tol = 1e-12;
+    // default relative tolerance of the transposed solves: near the FP64
+    // floor, or (mixed) well above the double-float refinement's floor
+    if (!(so.tol > 0.0)) so.tol = A->mixed ? 1e-10 : 1e-12;
     // lambda_T
-    for (int k = 0; k < 3; ++k) cudaMemsetAsync(grid_base(A->ag[k]), 0, grid_bytes(A->ag[k]), ctx->stream);
     const double* seeds[3] = {dL_dq_T, dL_du_T, dL_dv_T};
     const int fields[3] = {CF_FIELD_QUANTITY, CF_FIELD_U, CF_FIELD_V};
-    for (int k = 0; k < 3 && !rc; ++k)
-        if (seeds[k]) rc = adj_io(ctx, A->ag[k], fields[k], const_cast<double*>(seeds[k]), false);
+    if (A->mixed) {
+        cudaMemsetAsync(grid_base(A->aq32), 0, grid_bytes(A->aq32), ctx->stream);
+        for (int k = 1; k < 3; ++k) cudaMemsetAsync(grid_base(A->ag[k]), 0, grid_bytes(A->ag[k]), ctx->stream);
+        for (int k = 0; k < 3 && !rc; ++k)
+            if (seeds[k]) rc = adj_io_mixed(ctx, A, k, const_cast<double*>(seeds[k]), false);
+    } else {
+        for (int k = 0; k < 3; ++k) cudaMemsetAsync(grid_base(A->ag[k]), 0, grid_bytes(A->ag[k]), ctx->stream);
+        for (int k = 0; k < 3 && !rc; ++k)
+            if (seeds[k]) rc = adj_io(ctx, A->ag[k], fields[k], const_cast<double*>(seeds[k]), false);
+    }
     if (rc) return rc;
     // the forward recomputation, the checkpoint copies and the reverse steps
     // are all enqueued; one synchronisation at the end reads the tally of
     // the pressure solves, the trace check and dL/d(rate)
-    SolveOpts fo{};
-    if ((rc = parse_solver_opts(ctx, &A->opts, &fo))) return rc;
     cudaMemsetAsync(ctx->d_tally, 0, 3 * sizeof(int), ctx->stream);
     cudaMemsetAsync(A->d_err, 0, sizeof(int), ctx->stream);
     cudaMemsetAsync(A->d_rbar, 0, sizeof(double), ctx->stream);
@@ -694,9 +1159,10 @@ int cf_backward(cf_ctx* ctx, const double* dL_dq_T, const double* dL_du_T, const
     if ((rc = check_tally(ctx, tally, "backward"))) return rc;
     if (herr)
         return fail(ctx, CF_ERR_UNSUPPORTED, "adjoint: a trace moved more than one cell in a step (reduce dt)");
-    if (dL_dq0) rc = adj_io(ctx, A->ag[0], CF_FIELD_QUANTITY, dL_dq0, true);
-    if (!rc && dL_du0) rc = adj_io(ctx, A->ag[1], CF_FIELD_U, dL_du0, true);
-    if (!rc && dL_dv0) rc = adj_io(ctx, A->ag[2], CF_FIELD_V, dL_dv0, true);
+    double* outs[3] = {dL_dq0, dL_du0, dL_dv0};
+    for (int k = 0; k < 3 && !rc; ++k)
+        if (outs[k])
+            rc = A->mixed ? adj_io_mixed(ctx, A, k, outs[k], true) : adj_io(ctx, A->ag[k], fields[k], outs[k], true);
     if (!rc) rc = load_state(ctx, A->final_state);
     if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "backward");
     if (!rc && dL_drate) *dL_drate = rbar;

@@ -163,3 +163,18 @@ def config3(n: int = 512, steps: int = 200, seed: int = 3) -> Workload:
                  q0=q, u0=u, v0=v)
     w.extra["target"] = gaussian_blobs(n, seed + 2)
     return w
+
+
+def config4(n: int = 8192, steps: int = 100, seed: int = 4) -> Workload:
+    """Large mixed forward + adjoint: walls, cubic values, seeded spectral
+    velocity (no normal flow at the walls) and scalar as in config 2,
+    projection to ||div u||_L2 <= 1e-8; loss 1/2 |q(T) - target|^2 with a
+    second seeded spectral scalar as the target."""
+    u, v = spectral_velocity(n, seed, periodic=False)
+    q = spectral_scalar(n, seed + 1000)
+    dx = 1.0 / n
+    umax = max(np.abs(u).max(), np.abs(v).max())
+    w = Workload("config4-walls-spectral-mixed-adjoint", n, n, dt=0.5 * dx / umax, order=3, tol=0.0,
+                 abs_tol=1e-8, steps=steps, q0=q, u0=u, v0=v)
+    w.extra["target"] = spectral_scalar(n, seed + 2000)
+    return w

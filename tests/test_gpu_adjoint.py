@@ -146,7 +146,8 @@ def test_unsupported_and_invalid_settings():
     with pytest.raises(CfError) as e:
         c2.backward(q0)
     assert e.value.code == L.CF_ERR_INVALID
-    c3 = Context(N, N, precision="mixed")
+    c3 = Context(N, N)
+    c3.set_warm_start(True)
     with pytest.raises(CfError) as e:
         c3.forward_checkpointed(2, 1, dt)
     assert e.value.code == L.CF_ERR_UNSUPPORTED
