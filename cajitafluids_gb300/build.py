@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcfgpu.so")
 SOURCES = ["cf_api.cu", "cf_fields.cu", "cf_project.cu", "cf_cg32.cu", "cf_adjoint.cu", "cf_noalloc.cu", "cf_mg.cu"]
-HEADERS = ["cf_internal.cuh", "cf_ctx.cuh"]
+HEADERS = ["cf_internal.cuh", "cf_ctx.cuh", "cf_adv32.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "--fmad=false", "-std=c++17",

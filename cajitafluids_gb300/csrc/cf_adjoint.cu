@@ -292,12 +292,6 @@ struct AdjAdv32 {
 
 __device__ __forceinline__ int aj_at(int dx, int dy) { return (dy + 2) * 5 + (dx + 2); }
 
-// weights of a linear sample whose stencil starts o in [-2, 1] from the
-// target, on offsets -2 .. 2
-__device__ __forceinline__ void aj_spread_lin(int o, float t, float* W) {
-#pragma unroll
-    for (int k = 0; k < 5; ++k) W[k] = (k - 2 == o) ? 1.f - t : ((k - 3 == o) ? t : 0.f);
-}
 // a cubic sample's weights, stencil start o in {-2, -1}
 __device__ __forceinline__ void aj_spread_cub(int o, const float* w, float* W) {
 #pragma unroll
@@ -312,11 +306,29 @@ __device__ __forceinline__ void aj_outer(float* P, float s, const float* WX, con
 #pragma unroll
         for (int k = 0; k < 5; ++k) P[r * 5 + k] = fmaf(WY[r], x[k], P[r * 5 + k]);
 }
+// A linear sample at a position p = o + d of the target (o in {-1/2, 0,
+// 1/2} per axis, |d| < 1) has its stencil cell in [floor(o - 1) + 1 ..
+// floor(o + 1)] and its taps in columns [XLO, XLO + XN): o = 0: [-1, 2),
+// o = 1/2: [-1, 3), o = -1/2: [-2, 2).  Only that block of the tile is
+// touched (the same products as the full tile, without the zero terms).
+template <int TWO_O>
+struct AjSpan {
+    static constexpr int lo = TWO_O < 0 ? -2 : -1;
+    static constexpr int n = TWO_O == 0 ? 3 : 4;
+};
+template <int TWO_OX, int TWO_OY>
 __device__ __forceinline__ void aj_lin(float* P, float s, const Lin32& l) {
-    float WX[5], WY[5];
-    aj_spread_lin(l.ox, l.tx, WX);
-    aj_spread_lin(l.oy, l.ty, WY);
-    aj_outer(P, s, WX, WY);
+    constexpr int XL = AjSpan<TWO_OX>::lo, XN = AjSpan<TWO_OX>::n;
+    constexpr int YL = AjSpan<TWO_OY>::lo, YN = AjSpan<TWO_OY>::n;
+    float x[XN];
+#pragma unroll
+    for (int k = 0; k < XN; ++k) x[k] = s * ((XL + k == l.ox) ? 1.f - l.tx : ((XL + k == l.ox + 1) ? l.tx : 0.f));
+#pragma unroll
+    for (int r = 0; r < YN; ++r) {
+        const float wy = (YL + r == l.oy) ? 1.f - l.ty : ((YL + r == l.oy + 1) ? l.ty : 0.f);
+#pragma unroll
+        for (int k = 0; k < XN; ++k) P[aj_at(XL + k, YL + r)] = fmaf(wy, x[k], P[aj_at(XL + k, YL + r)]);
+    }
 }
 
 // A trace displacement (index units) that reaches a full cell, or is NaN,
@@ -332,11 +344,9 @@ __device__ __forceinline__ float aj_safe(float d, bool& bad) {
 // operations), then its transpose with fbar the adjoint of the advected
 // value.  Position derivatives are in index units (the trace moves by
 // d = -c a, c = dt / dx).
-template <int ORDER, int ENT>
-__device__ __forceinline__ void aj_target(const AdjAdv32& a, int li, int lj, float fbar, float* Pq, float* Pu,
-                                          float* Pv, bool& bad) {
-    const GlobalTaps U{reinterpret_cast<const float*>(a.u.o), a.u.pitch, a.u.ex, a.u.ey, 2};
-    const GlobalTaps V{reinterpret_cast<const float*>(a.v.o), a.v.pitch, a.v.ex, a.v.ey, 2};
+template <int ORDER, int ENT, typename T>
+__device__ __forceinline__ void aj_target(const AdjAdv32& a, const T& U, const T& V, const T& Q, int li, int lj,
+                                          float fbar, float* Pq, float* Pu, float* Pv, bool& bad) {
     const float ox_e = ENT == E_FACEI ? 0.f : 0.5f;
     const float oy_e = ENT == E_FACEJ ? 0.f : 0.5f;
     const float uox = ox_e, uoy = oy_e - 0.5f, vox = ox_e - 0.5f, voy = oy_e;
@@ -357,13 +367,13 @@ __device__ __forceinline__ void aj_target(const AdjAdv32& a, int li, int lj, flo
     const float dx = aj_safe(-c * ax, bad), dy = aj_safe(-c * ay, bad);
     // the advected field's sample at the foot
     float* PF = ENT == E_CELL ? Pq : (ENT == E_FACEI ? Pu : Pv);
-    const GlobalTaps F = ENT == E_CELL ? GlobalTaps{a.q.o, a.q.pitch, a.q.ex, a.q.ey, 1} : (ENT == E_FACEI ? U : V);
+    const T& F = ENT == E_CELL ? Q : (ENT == E_FACEI ? U : V);
     float gx, gy;
     if (ORDER == 1) {
         const Lin32 sf = lin32g(F, li, lj, dx, dy);
         gx = sf.gx;
         gy = sf.gy;
-        aj_lin(PF, fbar, sf);
+        aj_lin<0, 0>(PF, fbar, sf);
     } else {
         const float flx = floorf(dx), fly = floorf(dy);
         const int ox = (int)flx, oy = (int)fly;
@@ -377,7 +387,7 @@ __device__ __forceinline__ void aj_target(const AdjAdv32& a, int li, int lj, flo
         // forward samples (a constant field has zero gradient exactly)
         const float* base = F.at(li + ox - 1, lj + oy - 1);
         const int st = F.stride(), e = F.step();
-        const float cc = GlobalTaps::ld(base + st + e);
+        const float cc = T::ld(base + st + e);
         gx = 0.f;
         gy = 0.f;
 #pragma unroll
@@ -386,7 +396,7 @@ __device__ __forceinline__ void aj_target(const AdjAdv32& a, int li, int lj, flo
             float rs = 0.f, rd = 0.f;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const float f = GlobalTaps::ld(row + k * e) - cc;
+                const float f = T::ld(row + k * e) - cc;
                 rs = fmaf(wx[k], f, rs);
                 rd = fmaf(dwx[k], f, rd);
             }
@@ -404,8 +414,11 @@ __device__ __forceinline__ void aj_target(const AdjAdv32& a, int li, int lj, flo
     float v1bx = (3.f / 9.f) * abx, v1by = (3.f / 9.f) * aby;
     const float v2bx = (4.f / 9.f) * abx, v2by = (4.f / 9.f) * aby;
     // stage 2 at d2 = h2 (v1 or v0)
-    aj_lin(Pu, v2bx, s2u);
-    aj_lin(Pv, v2by, s2v);
+    // doubled sample offsets of the velocity grids from the entity
+    constexpr int UX = ENT == E_FACEI ? 0 : 1, UY = ENT == E_FACEJ ? -1 : 0;
+    constexpr int VX = ENT == E_FACEI ? -1 : 0, VY = ENT == E_FACEJ ? 0 : 1;
+    aj_lin<UX, UY>(Pu, v2bx, s2u);
+    aj_lin<VX, VY>(Pv, v2by, s2v);
     const float d2bx = fmaf(v2bx, s2u.gx, v2by * s2v.gx), d2by = fmaf(v2bx, s2u.gy, v2by * s2v.gy);
     if (ralston) {
         v1bx = fmaf(h2, d2bx, v1bx);
@@ -415,8 +428,8 @@ __device__ __forceinline__ void aj_target(const AdjAdv32& a, int li, int lj, flo
         v0by = fmaf(h2, d2by, v0by);
     }
     // stage 1 at d1 = h1 v0
-    aj_lin(Pu, v1bx, s1u);
-    aj_lin(Pv, v1by, s1v);
+    aj_lin<UX, UY>(Pu, v1bx, s1u);
+    aj_lin<VX, VY>(Pv, v1by, s1v);
     const float d1bx = fmaf(v1bx, s1u.gx, v1by * s1v.gx), d1by = fmaf(v1bx, s1u.gy, v1by * s1v.gy);
     v0bx = fmaf(h1, d1bx, v0bx);
     v0by = fmaf(h1, d1by, v0by);
@@ -459,12 +472,53 @@ __device__ __forceinline__ void aj_exchange(const float* P, float* A) {
     }
 }
 
+// A block's AJ_WARPS warps take horizontally adjacent strips and share one
+// window per field (the hi parts of u, v; q) in shared memory: ghosted
+// columns [28 s0 - 3, 28 s0 + 117) for strips s0 .. s0 + 3 and rows
+// [Y0 - 4, Y0 + 36), every tap of the strips' targets (two entities around
+// targets [X0 - 2, X0 + 30) x [Y0 - 2, Y0 + 34)); entries outside an
+// array read as zero and are never tapped.
+constexpr int AJW_X = AJ_WARPS * AJ_COLS + 8;
+constexpr int AJW_Y = AJ_ROWS + 8;
+constexpr int AJW_N = AJW_X * AJW_Y;
+constexpr size_t AJ_SMEM = 3 * AJW_N * sizeof(float);
+
+struct AjWin {
+    const float* s;  // ghosted (x0, y0)
+    int x0, y0;
+    static constexpr bool kClamp = false;
+    __device__ __forceinline__ const float* at(int ix, int iy) const { return s + ((iy - y0) * AJW_X + (ix - x0)); }
+    __device__ __forceinline__ static constexpr int stride() { return AJW_X; }
+    __device__ __forceinline__ static constexpr int step() { return 1; }
+    __device__ __forceinline__ static float ld(const float* p) { return *p; }
+};
+
 template <int ORDER>
 __global__ void __launch_bounds__(AJ_WARPS * 32) k_adj_advect32(AdjAdv32 a) {
-    const int lane = threadIdx.x & 31;
-    const int strip = blockIdx.x * AJ_WARPS + (threadIdx.x >> 5);
-    if (strip >= a.nsx * a.nsy) return;  // whole warps
-    const int X0 = 1 + (strip % a.nsx) * AJ_COLS, Y0 = 1 + (strip / a.nsx) * AJ_ROWS;
+    extern __shared__ __align__(16) float aw[];  // u, v, q windows
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nbx = (a.nsx + AJ_WARPS - 1) / AJ_WARPS;
+    const int s0 = (blockIdx.x % nbx) * AJ_WARPS, sy = blockIdx.x / nbx;
+    const int Y0 = 1 + sy * AJ_ROWS;
+    const int wx0 = 1 + s0 * AJ_COLS - 4, wy0 = Y0 - 4;
+    for (int k = threadIdx.x; k < AJW_N; k += AJ_WARPS * 32) {
+        const int r = k / AJW_X, cx = k - r * AJW_X;
+        const int gx = wx0 + cx, gy = wy0 + r;
+        float uu = 0.f, vv = 0.f, qq = 0.f;
+        if (gx >= 0 && gy >= 0) {
+            if (gx < a.u.ex && gy < a.u.ey) uu = reinterpret_cast<const float2&>(a.u.at(gx, gy)).x;
+            if (gx < a.v.ex && gy < a.v.ey) vv = reinterpret_cast<const float2&>(a.v.at(gx, gy)).x;
+            if (gx < a.q.ex && gy < a.q.ey) qq = a.q.at(gx, gy);
+        }
+        aw[k] = uu;
+        aw[AJW_N + k] = vv;
+        aw[2 * AJW_N + k] = qq;
+    }
+    __syncthreads();
+    const int sx = s0 + warp;
+    if (sx >= a.nsx) return;  // whole warps, after the block's last barrier
+    const AjWin U{aw, wx0, wy0}, V{aw + AJW_N, wx0, wy0}, Q{aw + 2 * AJW_N, wx0, wy0};
+    const int X0 = 1 + sx * AJ_COLS;
     const int tc = X0 - 2 + lane;
     const bool owner = lane >= 2 && lane < 2 + AJ_COLS;
     const Phys& p = a.p;
@@ -481,13 +535,14 @@ __global__ void __launch_bounds__(AJ_WARPS * 32) k_adj_advect32(AdjAdv32 a) {
         for (int k = 0; k < 25; ++k) Pq[k] = Pu[k] = Pv[k] = 0.f;
         const int gj = tr - CF_HALO;
         if (gi >= 0 && gj >= 0) {
-            if (gi < p.nx && gj < p.ny) aj_target<ORDER, E_CELL>(a, tc, tr, a.aq.at(tc, tr), Pq, Pu, Pv, bad);
+            if (gi < p.nx && gj < p.ny)
+                aj_target<ORDER, E_CELL>(a, U, V, Q, tc, tr, a.aq.at(tc, tr), Pq, Pu, Pv, bad);
             if (gi < oxu && gj < p.ny)
-                aj_target<ORDER, E_FACEI>(a, tc, tr, reinterpret_cast<const float2&>(a.au.at(tc, tr)).x, Pq, Pu,
-                                          Pv, bad);
+                aj_target<ORDER, E_FACEI>(a, U, V, Q, tc, tr, reinterpret_cast<const float2&>(a.au.at(tc, tr)).x,
+                                          Pq, Pu, Pv, bad);
             if (gi < p.nx && gj < oyv)
-                aj_target<ORDER, E_FACEJ>(a, tc, tr, reinterpret_cast<const float2&>(a.av.at(tc, tr)).x, Pq, Pu,
-                                          Pv, bad);
+                aj_target<ORDER, E_FACEJ>(a, U, V, Q, tc, tr, reinterpret_cast<const float2&>(a.av.at(tc, tr)).x,
+                                          Pq, Pu, Pv, bad);
         }
         aj_exchange(Pq, Aq);
         aj_exchange(Pu, Au);
@@ -619,6 +674,7 @@ struct AdjState {
     // velocity adjoints as pairs, bg is unused) and the FP32 outputs of the
     // reverse advection (o32: q, u, v shapes)
     bool mixed = false;
+    bool smem_set = false;  // the reverse advection's shared-memory limit raised
     Grid<float> aq32{}, o32[3]{};
     RecKind F[3], Su[3][3], Sv[3][3];
     int* d_err = nullptr;
@@ -852,11 +908,18 @@ int adjoint_step_mixed(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_
     a.nsx = (wx + AJ_COLS - 1) / AJ_COLS;
     a.nsy = (wy + AJ_ROWS - 1) / AJ_ROWS;
     a.err = A->d_err;
-    const int blocks = (a.nsx * a.nsy + AJ_WARPS - 1) / AJ_WARPS;
+    const int blocks = (a.nsx + AJ_WARPS - 1) / AJ_WARPS * a.nsy;
+    if (!A->smem_set) {
+        for (auto fn : {k_adj_advect32<1>, k_adj_advect32<3>})
+            if ((rc = cuda_check(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AJ_SMEM),
+                                 "adjoint smem")))
+                return rc;
+        A->smem_set = true;
+    }
     if (A->order == 1)
-        k_adj_advect32<1><<<blocks, AJ_WARPS * 32, 0, c->stream>>>(a);
+        k_adj_advect32<1><<<blocks, AJ_WARPS * 32, AJ_SMEM, c->stream>>>(a);
     else
-        k_adj_advect32<3><<<blocks, AJ_WARPS * 32, 0, c->stream>>>(a);
+        k_adj_advect32<3><<<blocks, AJ_WARPS * 32, AJ_SMEM, c->stream>>>(a);
     c->launches += 1;
     for (int f = 0; f < 3; ++f) {
         const int nox = p.nx + ((f == 1 && !p.per_x) ? 1 : 0);
