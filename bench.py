@@ -458,6 +458,9 @@ def bench_gb300(args, rank, world, dist, device):
         line["adjoint"] = bench_adjoint(args, device, dist)
         line["adjoint_forward_ratio"] = line["adjoint"]["forward_plus_adjoint_over_forward"]
 
+    if "adjoint4" in legs:
+        line["adjoint_mixed"] = bench_adjoint4(args, device, dist, peak)
+
     # ---- CPU baseline (rank 0, N = 1) ----
     if rank == 0 and world == 1 and "cpu" in legs and not args.skip_cpu:
         k_ref = k64 if k64 else (line.get("mixed", {}).get("cg_inner_iters_per_step") or args.ref_iters)
@@ -618,6 +621,129 @@ def bench_adjoint(args, device, dist):
     return out
 
 
+def mixed_state_bytes(n):
+    """Bytes of one checkpointed mixed state at n^2 with walls: the ghosted
+    FP32 q and the u, v pair arrays as the library lays them out (rows padded
+    so that owned column 0 sits on a 128-byte boundary)."""
+    def pitch(ex):
+        return (29 + ex + 31) // 32 * 32
+    return pitch(n + 6) * (n + 6) * 4 + pitch(n + 7) * (n + 6) * 8 + pitch(n + 6) * (n + 7) * 8
+
+
+def bench_adjoint4(args, device, dist, peak):
+    """Config 4: mixed-precision forward + adjoint at 8192^2 with walls,
+    cubic values, seeded spectral velocity and scalar, ||div u||_L2 <= 1e-8,
+    T steps with a checkpoint every sqrt(T).  Timed after one warm-up
+    forward/backward on the same context (graphs built), from the initial
+    state re-uploaded.  Per-kernel rates come from a short profiled run of
+    the same context (events around each stage)."""
+    from cajitafluids_gb300 import Context, SolverOptions
+    from cajitafluids_gb300 import _lib as L
+    from cajitafluids_gb300.workloads import config4
+    t0 = time.perf_counter()
+    n, T = args.adjoint4_size, args.adjoint4_steps
+    w = config4(n, steps=T)
+    t_gen = time.perf_counter() - t0
+    sq = max(1, int(round(math.sqrt(T))))
+    sb = mixed_state_bytes(n)
+
+    def fits(C):
+        return ((T + C - 1) // C + C + 1) * sb <= 150e9
+
+    # checkpoints sized to the 150 GB budget with recomputation between them:
+    # the smallest spacing >= 2 that fits; the sqrt(T) spacing is timed too
+    every = args.adjoint4_every or next((C for C in range(2, T + 1) if fits(C)), sq)
+    mg = args.precon in MG_NAMES
+    opts = SolverOptions(tol=0.0, abs_tol=w.abs_tol, max_iter=2000 if mg else 200000, precon=args.precon,
+                         inner_tol=0.5 if mg else 0.0)
+    target = w.extra["target"]
+
+    def load(c):
+        for f, a in (("q", w.q0), ("u", w.u0), ("v", w.v0)):
+            c.upload(f, a)
+
+    def fresh():
+        c = Context(n, n, precision="mixed", device=device)
+        c.set_density(w.density)
+        c.set_quirks(L.CF_FIX_Q1)
+        load(c)
+        return c
+
+    # plain forward (cf_steps), after one warm-up step
+    c = fresh()
+    c.step(w.dt, w.order, opts)
+    load(c)
+    barrier_sync(dist)
+    c.timer_start()
+    last = c.steps(T, w.dt, w.order, opts, raise_on_maxit=True)
+    t_fwd = c.timer_stop()
+    qT = c.download("q")
+    c.close()
+    # checkpointed forward + backward, after a 2-step warm-up of both
+    c = fresh()
+    c.forward_checkpointed(2, 1, w.dt, w.order, opts)
+    c.backward(np.zeros_like(w.q0))
+    runs = {}
+    for C in dict.fromkeys((every, sq)):
+        load(c)
+        c.timer_start()
+        st = c.forward_checkpointed(T, C, w.dt, w.order, opts)
+        t_fc = c.timer_stop()
+        q_fc = c.download("q")
+        c.timer_start()
+        g = c.backward(q_fc - target)
+        t_bwd = c.timer_stop()
+        runs[C] = {"every": C, "checkpoint_gb": ((T + C - 1) // C + C + 1) * sb / 1e9,
+                   "forward_checkpointed_ms": t_fc, "backward_ms": t_bwd,
+                   "forward_plus_adjoint_over_forward": (t_fc + t_bwd) / t_fwd,
+                   "checkpointed_forward_equals_plain": bool(np.array_equal(q_fc, qT))}
+        if C == every:
+            g_main, st_main, q_main = g, st, q_fc
+    g, st, q_fc = g_main, st_main, q_main
+    # per-kernel rates (profiled run: host-polled projections, events around
+    # each stage; 4 steps, checkpoint every 2)
+    load(c)
+    c.profile_enable(True)
+    c.forward_checkpointed(4, 2, w.dt, w.order, opts)
+    c.backward(c.download("q") - target)
+    prof = c.profile_read()
+    c.profile_enable(False)
+    c.close()
+    ncell = n * n
+    adv_ms = prof["advect_ms"] / max(prof["advect_calls"], 1)
+    radv_ms = prof["adj_advect_ms"] / max(prof["adj_advect_calls"], 1)
+    it_ms = prof["solve_ms"] / prof["solve_iters"] if prof["solve_iters"] else float("nan")
+    it_bytes = alg_bytes_per_iter(n, n, (False, False), args.precon, 4, 1.0, mixed=True)
+    # bytes per cell: advection R q 4 + u, v pairs 16, W the same (40); reverse
+    # advection R forward q 4 + u, v pairs 16, R adjoint q 4 + u, v pairs 16,
+    # W the three FP32 outputs 12 (52)
+    kern = {"advect32": {"ms": adv_ms, "bytes_per_cell": 40,
+                         "gbs": 40 * ncell / (adv_ms / 1e3) / 1e9 if adv_ms else None},
+            "adj_advect32": {"ms": radv_ms, "bytes_per_cell": 52,
+                             "gbs": 52 * ncell / (radv_ms / 1e3) / 1e9 if radv_ms else None},
+            "mg_pcg_iteration": {"ms": it_ms, "bytes": it_bytes,
+                                 "gbs": it_bytes / (it_ms / 1e3) / 1e9 if it_ms == it_ms else None}}
+    for k in kern.values():
+        if k.get("gbs"):
+            k["hbm_frac"] = k["gbs"] / peak
+    main = runs[every]
+    return {"workload": f"{n}^2 walls, cubic, seeded spectral velocity + scalar, T={T}, checkpoint every {every} "
+                        f"(the smallest spacing whose checkpoints fit 150 GB), mixed precision (FP32 bulk, "
+                        f"double-float refinement), PCG + {args.precon}, ||div u||_L2 <= {w.abs_tol:g}; adjoint: "
+                        f"FP32 reverse advection, transposed projection to relative 1e-8 (warm-started)",
+            "forward_ms": t_fwd, "forward_steps_per_s": T / (t_fwd / 1e3),
+            **main,
+            "sqrt_spacing": runs[sq],
+            "adjoint_cg_iters_per_projection": prof["adj_iters"] / max(prof["adj_projects"], 1),
+            "forward_last_step": {"iterations": st["iterations"], "outer_iterations": st["outer_iterations"],
+                                  "div_l2": st["div_l2"]},
+            "forward_unconverged": last["unconverged"],
+            "loss": 0.5 * float(np.sum((q_fc - target) ** 2)),
+            "gradient_norms": {f: float(np.linalg.norm(g[f])) for f in ("q", "u", "v")},
+            "gradient_finite": bool(all(np.isfinite(g[f]).all() for f in ("q", "u", "v"))),
+            "kernels": kern, "workload_gen_s": t_gen}
+
+
 def bench_reference(args, rank, world, dist):
     """The reference algorithm's CPU implementation (oracle port) on the same
     workload and metric; rank 0 only."""
@@ -670,15 +796,18 @@ def main():
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--legs", default="mixed,e2e,warm,fp64,accuracy,configs,adjoint,cpu",
+    ap.add_argument("--legs", default="mixed,e2e,warm,fp64,accuracy,configs,adjoint,adjoint4,cpu",
                     help="comma list of legs to run: mixed (headline), e2e, warm, fp64, accuracy, configs, "
-                         "adjoint, cpu")
+                         "adjoint (config 3, FP64), adjoint4 (config 4, mixed), cpu")
     ap.add_argument("--accuracy-steps", type=int, default=200,
                     help="steps of the mixed-vs-FP64 accuracy run (the workload's full run length)")
     ap.add_argument("--adjoint-size", type=int, default=512)
     ap.add_argument("--adjoint-steps", type=int, default=200)
     ap.add_argument("--adjoint-every", type=int, default=14)
     ap.add_argument("--adjoint-fd", type=int, default=2, help="central-difference checks of the gradient")
+    ap.add_argument("--adjoint4-size", type=int, default=8192)
+    ap.add_argument("--adjoint4-steps", type=int, default=100)
+    ap.add_argument("--adjoint4-every", type=int, default=0, help="checkpoint spacing (0: sqrt of the steps)")
     ap.add_argument("--ref-iters", type=int, default=12000)
     ap.add_argument("--precon", default="PFMG",
                     help="PCG preconditioner: PFMG/SMG/MG (geometric multigrid, the reference CLI default), "

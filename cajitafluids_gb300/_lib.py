@@ -93,6 +93,8 @@ class Profile(ctypes.Structure):
         ("solve_ms", ctypes.c_double), ("solve_iters", ctypes.c_longlong), ("solve_batches", ctypes.c_longlong),
         ("advect_ms", ctypes.c_double), ("advect_calls", ctypes.c_longlong),
         ("project_ms", ctypes.c_double), ("projects", ctypes.c_longlong),
+        ("adj_advect_ms", ctypes.c_double), ("adj_advect_calls", ctypes.c_longlong),
+        ("adj_projects", ctypes.c_longlong), ("adj_iters", ctypes.c_longlong),
     ]
 
     def as_dict(self):

@@ -221,7 +221,12 @@ int enqueue_step(cf_ctx* ctx, double dt, int value_order, const SolveOpts& so, S
                  bool params_ready) {
     const bool fuse = !ctx->ph.force_density;
     int rc = cuda_check(ctx, launch_fill_ghosts(ctx), "fill ghosts");
+    if (ctx->prof) cudaEventRecord(ctx->ev[2], ctx->stream);
     if (!rc) rc = cuda_check(ctx, launch_advect(ctx, dt, value_order, fuse ? 1 : 0), "advect");
+    if (ctx->prof) {
+        cudaEventRecord(ctx->ev[3], ctx->stream);
+        rc = rc ? rc : record_advect(ctx);
+    }
     if (!rc && !fuse) rc = cuda_check(ctx, launch_add_inputs(ctx, dt), "add inputs");
     if (!rc) rc = project_async(ctx, dt, so, r, deferred, params_ready);
     return rc;

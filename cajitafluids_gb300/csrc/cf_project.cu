@@ -1498,12 +1498,16 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
                                                          c->ph.nx, c->ph.ny, c->vpitch);
                 ntail += 1;
             }
-            DivArgs da = div_args(c, st);
-            da.u = gu;
-            da.v = gv;
-            k_div_norms<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
+            // (the adjoint's projections report no divergence norms)
+            if (!adjoint) {
+                DivArgs da = div_args(c, st);
+                da.u = gu;
+                da.v = gv;
+                k_div_norms<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
+                ntail += 1;
+            }
             k_step_tally<<<1, 1, 0, c->stream>>>(c->S, c->d_tally);
-            ntail += 3;
+            ntail += 2;
             cudaMemcpyAsync(c->hS, c->S, sizeof(SolverState), cudaMemcpyDeviceToHost, c->stream);
             cudaMemcpyAsync(c->h_out, c->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
         });

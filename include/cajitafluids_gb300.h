@@ -226,12 +226,12 @@ int cf_max_velocity(cf_ctx* ctx, double* umax);
  * (NULL = 0), recomputes each segment from its checkpoint, runs the reverse
  * steps, and writes dL/dq(0), dL/du(0), dL/dv(0) and dL/dQ for the quantity
  * rate of a rate-form source (any output may be NULL); the context is left
- * in s_T.  Host arrays are contiguous owned regions (x fastest).  An FP64
+ * in s_T with the pressure at zero.  Host arrays are contiguous owned regions (x fastest).  An FP64
  * context runs the FP64 adjoint; a mixed context checkpoints its own state
  * (FP32 q, velocity pairs), recomputes the mixed forward, and runs the
  * reverse advection in FP32 and the transposed projection with the mixed
- * PCG (FP32 inner iterations, double-float refinement; default relative
- * tolerance 1e-10).  See cf_adjoint.cu for the supported inputs. */
+ * PCG (FP32 inner iterations, double-float refinement; relative tolerance
+ * opts->tol, default 1e-8).  See cf_adjoint.cu for the supported inputs. */
 int cf_forward_checkpointed(cf_ctx* ctx, int nsteps, int ckpt_every, double dt, int value_order,
                             const cf_solver_opts* opts, cf_solve_stats* last);
 int cf_backward(cf_ctx* ctx, const double* dL_dq_T, const double* dL_du_T, const double* dL_dv_T, double* dL_dq0,
@@ -316,6 +316,10 @@ typedef struct {
     long long advect_calls;
     double project_ms;
     long long projects;
+    double adj_advect_ms;        /* mixed adjoint: the FP32 reverse advection (k_adj_advect32) */
+    long long adj_advect_calls;
+    long long adj_projects;      /* the adjoint's transposed projections and their PCG iterations */
+    long long adj_iters;
 } cf_profile;
 /* on != 0 resets the counters and starts recording; 0 stops recording */
 int cf_profile_enable(cf_ctx* ctx, int on);
