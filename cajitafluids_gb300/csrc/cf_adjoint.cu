@@ -3,14 +3,18 @@
 //
 // Forward step (src/Solver.hpp:135-147): s_k = (q, u, v) ->
 //   A  advection   (q_a, u_a, v_a) = Adv(q, u, v)         src/TimeIntegrator.hpp:36-177
-//   I  inputs      rate source q += Q dt in the box, wall masks on faces
+//   I  inputs      quantity source (rate q += Q dt, or clamp q = max(q, Q)) in
+//                  the box, velocity inflow, body force, wall masks on faces
 //                                                          src/Solver.hpp:181-263
 //   P  projection  u_p = M u_i + (s'/dx) M G A^-1 D u_i   src/VelocityCorrector.hpp:182-264
 // Reverse step, given the adjoint lambda_{k+1}:
 //   P^T w = M w + (s'/dx) G A^-1 D (M w)   (G = -D^T exactly and A is
 //           symmetric, so the transpose is the same pipeline with the mask
 //           applied first and none at the end; one more PCG solve)
-//   I^T     wall masks; dL/dQ += dt * sum over the box of the quantity adjoint
+//   I^T     wall masks; the density-scaled force's coupling into the quantity
+//           adjoint; dL/dQ += dt * sum over the box of the quantity adjoint
+//           (rate form); the replacing inputs (clamp, velocity inflow) are
+//           transposed inside A^T, which recomputes the advected value
 //   A^T     transpose of the spline samples and of the RK3 trace:
 //           pass 1 (one thread per target entity) recomputes the trace and
 //           writes scatter records -- stencil start plus weights already
@@ -32,10 +36,16 @@
 // held as pairs, and the advection's transpose runs in FP32 without records
 // (k_adj_advect32: the forward's FP32 trace recomputed, contributions
 // gathered through a register window per warp, deterministic).
-// Supported: FP64 and mixed contexts; the rate-form quantity source with zero inflow
-// velocity; constant body forces; the projection with CF_FIX_Q1 whenever a
-// y-wall is SOLID (the quirk's projection has an inconsistent adjoint
-// right-hand side).  Other settings return CF_ERR_UNSUPPORTED.
+// Supported: FP64 and mixed contexts; the quantity source in either form
+// (rate: dL/dQ from the box's adjoint; clamp q = max(q, Q): no adjoint flows
+// through the cells where the clamp fired, dL/dQ collects it there); the
+// velocity inflow (the faces it overwrote pass no adjoint back; the inflow
+// velocity itself gets no gradient); constant and density-scaled body forces
+// (the latter couples the face adjoints into the quantity's); the projection
+// with CF_FIX_Q1 whenever a y-wall is SOLID.  With the quirk the projected
+// wall-normal v keeps a value that depends on the constant mode of the
+// pressure, which the PCG leaves to its iteration, so the forward map has no
+// well-defined derivative there (CF_ERR_UNSUPPORTED).
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -140,6 +150,7 @@ struct AdjRec {
     int order;
     RecKind F[3], Su[3][3], Sv[3][3];
     int* err;
+    double* qclamp;  // clamp-form source: per box cell, the adjoint where the clamp fired, else 0
 };
 
 __device__ __forceinline__ void put_rec(const RecKind& R, int t, int kx, int ky, double val, const double* wx,
@@ -149,6 +160,28 @@ __device__ __forceinline__ void put_rec(const RecKind& R, int t, int kx, int ky,
         R.cx[a * R.nt + t] = val * wx[a];
         R.wy[a * R.nt + t] = wy[a];
     }
+}
+
+// The adjoint of an advected value through the inputs that replace it:
+// the clamp-form quantity source (q < Q in the box: q becomes Q; the
+// adjoint is recorded per box cell for dL/dQ and none flows back) and the
+// velocity inflow (|w| < |V| in the box: w becomes V).  val is the advected
+// value as the forward compared it.
+template <typename TV>
+__device__ __forceinline__ double inputs_adjoint_gate(const Phys& p, int ent, int li, int lj, TV val, double fbar,
+                                                      double* qclamp) {
+    if (!in_box_idx(p, ent, li, lj)) return fbar;
+    if (ent == E_CELL) {
+        if (p.src_mode != 0) return fbar;
+        // FP64 and the unfused FP32 inputs compare in FP64; the fused FP32
+        // epilogue compares with Q rounded to FP32
+        const bool clamped =
+            (sizeof(TV) == 8 || p.force_density) ? (double)val < p.src_q : (float)val < (float)p.src_q;
+        qclamp[(lj - p.box[E_CELL][2]) * (p.box[E_CELL][1] - p.box[E_CELL][0]) + (li - p.box[E_CELL][0])] =
+            clamped ? fbar : 0.0;
+        return clamped ? 0.0 : fbar;
+    }
+    return fabs((double)val) < fabs(p.src_vel[ent - 1]) ? 0.0 : fbar;
 }
 
 // pass 1: one thread per owned target entity (blockIdx.z = entity type)
@@ -199,8 +232,12 @@ __global__ void k_adj_records(AdjRec a) {
         fabs(x2 - x0) > lim || fabs(y2 - y0) > lim)
         atomicOr(a.err, 1);
     // reverse
-    put_rec(a.F[ent], t, sf.kx, sf.ky, fbar, sf.wx, sf.wy, a.order == 1 ? 2 : 4);
-    double tbx = fbar * sf.gx, tby = fbar * sf.gy;
+    // inputs that replace the advected value where they fire carry no
+    // sensitivity to it there: the clamp q = max(q, Q) (the adjoint goes to
+    // dL/dQ instead) and the velocity inflow (src/InflowSource.hpp:39-77)
+    const double fb = inputs_adjoint_gate(p, ent, li, lj, sf.val, fbar, a.qclamp);
+    put_rec(a.F[ent], t, sf.kx, sf.ky, fb, sf.wx, sf.wy, a.order == 1 ? 2 : 4);
+    double tbx = fb * sf.gx, tby = fb * sf.gy;
     double abx = -dt * tbx, aby = -dt * tby;
     double v0x = (2.0 / 9.0) * abx, v0y = (2.0 / 9.0) * aby;
     double v1x = (3.0 / 9.0) * abx, v1y = (3.0 / 9.0) * aby;
@@ -289,6 +326,7 @@ struct AdjAdv32 {
     float c;                  // dt / dx, as the forward's
     int nsx, nsy;             // strips along x, y
     int* err;
+    double* qclamp;           // clamp-form source (inputs_adjoint_gate)
 };
 
 __device__ __forceinline__ int aj_at(int dx, int dy) { return (dy + 2) * 5 + (dx + 2); }
@@ -366,15 +404,18 @@ __device__ __forceinline__ void aj_target(const AdjAdv32& a, const T& U, const T
     const float ax = fmaf(4.f / 9.f, s2u.val, fmaf(3.f / 9.f, s1u.val, (2.f / 9.f) * v0x));
     const float ay = fmaf(4.f / 9.f, s2v.val, fmaf(3.f / 9.f, s1v.val, (2.f / 9.f) * v0y));
     const float dx = aj_safe(-c * ax, bad), dy = aj_safe(-c * ay, bad);
-    // the advected field's sample at the foot
+    // the advected field's sample at the foot: its value (the forward's
+    // bits: the inputs that replace it compare it), derivatives, weights
     float* PF = ENT == E_CELL ? Pq : (ENT == E_FACEI ? Pu : Pv);
     const T& F = ENT == E_CELL ? Q : (ENT == E_FACEI ? U : V);
-    float gx, gy;
+    float gx, gy, val;
+    Lin32 sf;
+    float WX[5], WY[5];
     if (ORDER == 1) {
-        const Lin32 sf = lin32g(F, li, lj, dx, dy);
+        sf = lin32g(F, li, lj, dx, dy);
         gx = sf.gx;
         gy = sf.gy;
-        aj_lin<0, 0>(PF, fbar, sf);
+        val = sf.val;
     } else {
         const float flx = floorf(dx), fly = floorf(dy);
         const int ox = (int)flx, oy = (int)fly;
@@ -384,13 +425,14 @@ __device__ __forceinline__ void aj_target(const AdjAdv32& a, const T& U, const T
         cubic_w32(ty, wy);
         cubic_dw32(tx, dwx);
         cubic_dw32(ty, dwy);
-        // derivatives against differences from the centre tap, as the
-        // forward samples (a constant field has zero gradient exactly)
+        // the value and the derivatives against differences from the centre
+        // tap, as the forward samples (a constant field has zero gradient)
         const float* base = F.at(li + ox - 1, lj + oy - 1);
         const int st = F.stride(), e = F.step();
         const float cc = T::ld(base + st + e);
         gx = 0.f;
         gy = 0.f;
+        float vs = 0.f;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             const float* row = base + b * st;
@@ -401,14 +443,19 @@ __device__ __forceinline__ void aj_target(const AdjAdv32& a, const T& U, const T
                 rs = fmaf(wx[k], f, rs);
                 rd = fmaf(dwx[k], f, rd);
             }
+            vs = fmaf(wy[b], rs, vs);
             gx = fmaf(wy[b], rd, gx);
             gy = fmaf(dwy[b], rs, gy);
         }
-        float WX[5], WY[5];
+        val = cc + vs;
         aj_spread_cub(ox - 1, wx, WX);
         aj_spread_cub(oy - 1, wy, WY);
-        aj_outer(PF, fbar, WX, WY);
     }
+    fbar = (float)inputs_adjoint_gate(a.p, ENT, li, lj, val, (double)fbar, a.qclamp);
+    if (ORDER == 1)
+        aj_lin<0, 0>(PF, fbar, sf);
+    else
+        aj_outer(PF, fbar, WX, WY);
     // reverse of a = 2/9 v0 + 3/9 v1 + 4/9 v2, d = -c a
     const float abx = -c * (fbar * gx), aby = -c * (fbar * gy);
     float v0bx = (2.f / 9.f) * abx, v0by = (2.f / 9.f) * aby;
@@ -675,6 +722,46 @@ __global__ void __launch_bounds__(kBoxThreads) k_adj_rate(Phys p, Grid<T> aq, do
     }
 }
 
+// Density-scaled body force (u += dt f rho, rho the mean of the face's two
+// cells after the cell inputs; Q5): each owned cell's quantity adjoint gains
+// dt f / 2 times the adjoint of its two faces per axis (wall faces are
+// masked already; periodic faces wrap as the forward's cell reads do).
+// Pair arrays (mixed) contribute their value.
+template <typename TQ>
+__global__ void k_adj_density(Phys p, Grid<TQ> aq, Grid<double> au, Grid<double> av, double dt, int pairs) {
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gj = blockIdx.y * blockDim.y + threadIdx.y;
+    if (gi >= p.nx || gj >= p.ny) return;
+    auto face = [&](const Grid<double>& g, int i, int j) {
+        const double w = g.at(i + CF_HALO, j + CF_HALO);
+        return pairs ? df_value(reinterpret_cast<const float2&>(w)) : w;
+    };
+    const int ir = (p.per_x && gi + 1 == p.nx) ? 0 : gi + 1;
+    const int jt = (p.per_y && gj + 1 == p.ny) ? 0 : gj + 1;
+    const double cx = 0.5 * p.force[0] * dt, cy = 0.5 * p.force[1] * dt;
+    double s = 0.0;
+    if (cx != 0.0) s = cx * (face(au, gi, gj) + face(au, ir, gj));
+    if (cy != 0.0) s = s + cy * (face(av, gi, gj) + face(av, gi, jt));
+    TQ& q = aq.at(gi + CF_HALO, gj + CF_HALO);
+    q = (TQ)((double)q + s);
+}
+
+// dL/dQ of the clamp-form source: the sum of the per-box-cell adjoints the
+// reverse advection left where the clamp fired, in a fixed order
+__global__ void __launch_bounds__(kBoxThreads) k_adj_boxsum(const double* buf, int n, double* rbar) {
+    double s = 0.0;
+    for (int k = threadIdx.x; k < n; k += kBoxThreads) s = s + buf[k];
+    __shared__ double ws[kBoxThreads / 32];
+    s = warp_fold(s);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = ws[0];
+        for (int k = 1; k < kBoxThreads / 32; ++k) t = t + ws[k];
+        *rbar += t;
+    }
+}
+
 // host side
 
 template <typename T>
@@ -708,6 +795,8 @@ struct AdjState {
     int* d_err = nullptr;
     double* d_rbar = nullptr;  // dL/d(rate), accumulated on the device
     double* xa = nullptr;      // the adjoint pressure between reverse steps (the warm start)
+    double* qclamp = nullptr;  // clamp-form source: per-box-cell adjoints (inputs_adjoint_gate)
+    size_t qclamp_n = 0;
     // the forward pass left the last segment's states in seg: the backward's
     // first segment needs no recomputation (cleared once seg is reused)
     bool last_seg_valid = false;
@@ -785,12 +874,6 @@ int check_supported(cf_ctx* c) {
     // would depend on a pressure the checkpoints do not hold
     if (c->warm) return fail(c, CF_ERR_UNSUPPORTED, "the adjoint needs cold-started projections (warm start is on)");
     const Phys& p = c->ph;
-    bool src_active = p.bbox[2] > p.bbox[0] && p.bbox[3] > p.bbox[1];
-    if (src_active && p.src_mode == 0 && p.src_q != 0.0)
-        return fail(c, CF_ERR_UNSUPPORTED, "adjoint of the clamp-form quantity source (use the rate form)");
-    if (src_active && (p.src_vel[0] != 0.0 || p.src_vel[1] != 0.0))
-        return fail(c, CF_ERR_UNSUPPORTED, "adjoint of a velocity inflow");
-    if (p.force_density) return fail(c, CF_ERR_UNSUPPORTED, "adjoint of a density-scaled body force");
     if (!(p.quirks & CF_FIX_Q1) && !p.per_y && (p.bc[1] == CF_BC_SOLID || p.bc[3] == CF_BC_SOLID))
         return fail(c, CF_ERR_UNSUPPORTED, "adjoint of the Q1 projection quirk (set CF_FIX_Q1)");
     return CF_OK;
@@ -917,6 +1000,40 @@ int fill_view_ghosts(cf_ctx* c, const StateView& s) {
     return cuda_check(c, e, "fill ghosts");
 }
 
+// Cells of the inflow box when the clamp-form source is on (0 otherwise).
+size_t clamp_cells(const cf_ctx* c) {
+    const Phys& p = c->ph;
+    const int w = p.box[E_CELL][1] - p.box[E_CELL][0], h = p.box[E_CELL][3] - p.box[E_CELL][2];
+    return (p.src_mode == 0 && w > 0 && h > 0) ? (size_t)w * h : 0;
+}
+
+// The inputs' transpose before the advection's: the density-scaled force
+// couples the velocity adjoints into the quantity's, then the rate-form
+// source adds to dL/dQ (the clamp form's share comes from the reverse
+// advection, which knows where the clamp fired).
+template <typename TQ>
+void inputs_transpose(cf_ctx* c, AdjState* A, Grid<TQ> aq) {
+    const Phys& p = c->ph;
+    if (p.force_density && (p.force[0] != 0.0 || p.force[1] != 0.0)) {
+        const dim3 blk(32, 8), g((p.nx + 31) / 32, (p.ny + 7) / 8);
+        k_adj_density<<<g, blk, 0, c->stream>>>(p, aq, A->ag[1], A->ag[2], A->dt, A->mixed ? 1 : 0);
+        c->launches += 1;
+    }
+    const bool src_active = p.bbox[2] > p.bbox[0] && p.bbox[3] > p.bbox[1];
+    if (src_active && p.src_mode == 1) {
+        k_adj_rate<<<1, kBoxThreads, 0, c->stream>>>(p, aq, A->dt, A->d_rbar);
+        c->launches += 1;
+    }
+}
+
+// after the advection's transpose: the clamp-form source's dL/dQ
+void clamp_sum(cf_ctx* c, AdjState* A) {
+    const size_t n = clamp_cells(c);
+    if (!n) return;
+    k_adj_boxsum<<<1, kBoxThreads, 0, c->stream>>>(A->qclamp, (int)n, A->d_rbar);
+    c->launches += 1;
+}
+
 // The transposed projection on the adjoint face arrays (pairs in a mixed
 // context), starting from the previous reverse step's adjoint pressure.
 int adjoint_projection(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_ready) {
@@ -972,11 +1089,7 @@ int adjoint_step_mixed(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_
     dim3 blk(32, 8);
     int rc = adjoint_projection(c, A, so, params_ready);
     if (rc) return rc;
-    bool src_active = p.bbox[2] > p.bbox[0] && p.bbox[3] > p.bbox[1];
-    if (src_active && p.src_mode == 1) {
-        k_adj_rate<<<1, kBoxThreads, 0, c->stream>>>(p, A->aq32, A->dt, A->d_rbar);
-        c->launches += 1;
-    }
+    inputs_transpose(c, A, A->aq32);
     const StateView sv = state_view(c, fwd);
     if ((rc = fill_view_ghosts(c, sv))) return rc;
     AdjAdv32 a;
@@ -997,6 +1110,7 @@ int adjoint_step_mixed(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_
     a.nsx = (wx + AJ_COLS - 1) / AJ_COLS;
     a.nsy = (wy + AJ_ROWS - 1) / AJ_ROWS;
     a.err = A->d_err;
+    a.qclamp = A->qclamp;
     const int blocks = (a.nsx + AJ_WARPS - 1) / AJ_WARPS * a.nsy;
     if (!A->smem_set) {
         for (auto fn : {k_adj_advect32<1>, k_adj_advect32<3>})
@@ -1015,6 +1129,7 @@ int adjoint_step_mixed(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_
     else
         k_adj_advect32<3><<<blocks, AJ_WARPS * 32, AJ_SMEM, c->stream>>>(a);
     c->launches += 1;
+    clamp_sum(c, A);
     if (c->prof) {
         cudaEventRecord(A->ev_adv[1], c->stream);
         float ms = 0.f;
@@ -1055,12 +1170,8 @@ int adjoint_step(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_ready,
     int rc = adjoint_projection(c, A, so, params_ready);
     if (rc) return rc;
     // dL/dQ from the rate source
-    bool src_active = p.bbox[2] > p.bbox[0] && p.bbox[3] > p.bbox[1];
-    if (src_active && p.src_mode == 1) {
-        k_adj_rate<<<1, kBoxThreads, 0, c->stream>>>(p, A->ag[0], A->dt, A->d_rbar);
-        c->launches += 1;
-    }
-    // A^T at the forward state of this step (already loaded)
+    inputs_transpose(c, A, A->ag[0]);
+    // A^T at the forward state of this step
     const StateView sv = state_view(c, fwd);
     if ((rc = fill_view_ghosts(c, sv))) return rc;
     for (int e = 0; e < 3; ++e) A->F[e].n = A->order == 1 ? 2 : 4;
@@ -1082,7 +1193,9 @@ int adjoint_step(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_ready,
         }
     }
     ar.err = A->d_err;
+    ar.qclamp = A->qclamp;
     k_adj_records<<<dim3((p.nx + 1 + 31) / 32, (p.ny + 1 + 7) / 8, 3), blk, 0, c->stream>>>(ar);
+    clamp_sum(c, A);
     for (int gsel = 0; gsel < 3; ++gsel) {
         AdjGather ag{};
         ag.out = A->bg[gsel];
@@ -1252,6 +1365,10 @@ int cf_backward(cf_ctx* ctx, const double* dL_dq_T, const double* dL_du_T, const
     cudaSetDevice(ctx->device);
     int rc = check_supported(ctx);
     if (!rc) rc = A->mixed ? setup_mixed(ctx, A) : setup_records(ctx, A);
+    if (!rc && clamp_cells(ctx) > A->qclamp_n) {
+        rc = dalloc(ctx, A, (void**)&A->qclamp, sizeof(double) * clamp_cells(ctx));
+        A->qclamp_n = clamp_cells(ctx);
+    }
     if (rc) return rc;
     SolveOpts fo{};
     if ((rc = parse_solver_opts(ctx, &A->opts, &fo))) return rc;

@@ -152,12 +152,6 @@ __device__ __forceinline__ bool in_box(const Phys& p, double x, double y) {
     return x >= p.bbox[0] && x < p.bbox[2] && y >= p.bbox[1] && y < p.bbox[3];
 }
 
-// the box test on local indices (ranges the host evaluated with the same
-// FP64 coordinate test, src/InflowSource.hpp:78-88)
-__device__ __forceinline__ bool in_box_idx(const Phys& p, int ent, int li, int lj) {
-    return li >= p.box[ent][0] && li < p.box[ent][1] && lj >= p.box[ent][2] && lj < p.box[ent][3];
-}
-
 __device__ __forceinline__ double inputs_cell_in(const Phys& p, double q, bool inbox, double dt) {
     if (inbox) {
         if (p.src_mode == 0) {

@@ -57,6 +57,12 @@ struct Phys {
     unsigned quirks;
 };
 
+// the inflow box test on local indices (ranges the host evaluated with the
+// FP64 coordinate test, src/InflowSource.hpp:78-88)
+__device__ __forceinline__ bool in_box_idx(const Phys& p, int ent, int li, int lj) {
+    return li >= p.box[ent][0] && li < p.box[ent][1] && lj >= p.box[ent][2] && lj < p.box[ent][3];
+}
+
 // Matrix tables indexed by wall-adjacency bits (1 left, 2 right, 4 bottom, 8 top).
 struct Stencil {
     double diag[16];

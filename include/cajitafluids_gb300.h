@@ -225,7 +225,8 @@ int cf_max_velocity(cf_ctx* ctx, double* umax);
  * ends in s_T.  cf_backward takes dL/dq(T) and optionally dL/du(T), dL/dv(T)
  * (NULL = 0), recomputes each segment from its checkpoint, runs the reverse
  * steps, and writes dL/dq(0), dL/du(0), dL/dv(0) and dL/dQ for the quantity
- * rate of a rate-form source (any output may be NULL); the context is left
+ * source's Q: its rate (rate form) or its level (clamp form) (any output may
+ * be NULL); the context is left
  * in s_T with the pressure at zero.  Host arrays are contiguous owned regions (x fastest).  An FP64
  * context runs the FP64 adjoint; a mixed context checkpoints its own state
  * (FP32 q, velocity pairs), recomputes the mixed forward, and runs the

@@ -13,7 +13,11 @@ Checks:
     the FD step);
   * gradients are bit-for-bit reproducible and do not depend on the
     checkpoint spacing;
-  * unsupported settings return CF_ERR_UNSUPPORTED / CF_ERR_INVALID.
+  * the reference's default inputs (clamp-form source with an inflow
+    velocity, density-scaled buoyancy) against central differences too, with
+    dL/dQ for the clamp level;
+  * unsupported settings (the Q1 quirk's projection, warm starts) return
+    CF_ERR_UNSUPPORTED, a backward without a forward CF_ERR_INVALID.
 A torch.autograd.Function over the same contract is exercised at the end.
 """
 import numpy as np
@@ -116,6 +120,64 @@ def test_gradient_matches_central_differences(periodic, precon):
         lm, _ = loss(q0, u0, v0, rate - hr)
         fd = (lp - lm) / (2 * hr)
         assert abs(fd - g["rate"]) <= 1e-5 * abs(g["rate"]), (fd, g["rate"])
+
+
+def default_physics_ctx(Q=0.8, mixed=False, buoyancy=True):
+    """The reference's default inputs (examples/advection.cpp): a clamp-form
+    quantity source q = max(q, Q) with an inflow velocity (0, 3) in the box,
+    and (config 1) buoyancy scaled by the density."""
+    c = Context(N, N, precision="mixed" if mixed else "fp64")
+    c.set_density(0.1)
+    c.set_quirks(L.CF_FIX_Q1)
+    c.set_source((0.40, 0.10), (0.20, 0.10), (0.0, 3.0), Q, mode=0)
+    if buoyancy:
+        c.set_body_force((0.0, -9.8), density_scaled=True)
+    return c
+
+
+def default_physics_dt(u, v):
+    return 0.4 / N / max(np.abs(u).max(), np.abs(v).max(), 3.0)
+
+
+@pytest.mark.parametrize("precon", PRECONS)
+@pytest.mark.parametrize("buoyancy", [False, True])
+def test_gradient_of_default_physics_matches_central_differences(precon, buoyancy):
+    """Clamp-form source with a velocity inflow, with and without the
+    density-scaled buoyancy: directional derivatives in q, u, v and dL/dQ
+    (the clamp level) against central differences of the FP64 forward."""
+    q0, u0, v0 = initial()
+    dt = default_physics_dt(u0, v0)
+    Q = 0.8
+    c = default_physics_ctx(Q, buoyancy=buoyancy)
+    target = gaussian_blobs(N, 11, count=4, sigma=0.08)
+    rng = np.random.default_rng(7)
+    cu = rng.standard_normal(c.owned_shape("u")) * 0.1
+    cv = rng.standard_normal(c.owned_shape("v")) * 0.1
+
+    def loss(q, u, v, level=Q):
+        c.set_source((0.40, 0.10), (0.20, 0.10), (0.0, 3.0), level, mode=0)
+        qT, uT, vT = run(c, q, u, v, dt, opts=opts_for(precon))
+        return 0.5 * float(np.sum((qT - target) ** 2)) + float(np.sum(cu * uT)) + float(np.sum(cv * vT)), qT
+
+    _, qT = loss(q0, u0, v0)
+    g = c.backward(qT - target, cu, cv)
+    h = 1e-5
+    for k in range(3):
+        dq = rng.standard_normal(q0.shape) * (k in (0, 2))
+        du = rng.standard_normal(u0.shape) * (k in (1, 2))
+        dv = rng.standard_normal(v0.shape) * (k in (1, 2))
+        du[:, 0] = du[:, -1] = 0.0
+        dv[0, :] = dv[-1, :] = 0.0
+        lp, _ = loss(q0 + h * dq, u0 + h * du, v0 + h * dv)
+        lm, _ = loss(q0 - h * dq, u0 - h * du, v0 - h * dv)
+        fd = (lp - lm) / (2 * h)
+        ad = float(np.sum(g["q"] * dq) + np.sum(g["u"] * du) + np.sum(g["v"] * dv))
+        assert abs(fd - ad) <= 1e-5 * abs(ad) + 1e-9, (k, fd, ad)
+    lp, _ = loss(q0, u0, v0, Q + h)
+    lm, _ = loss(q0, u0, v0, Q - h)
+    fd = (lp - lm) / (2 * h)
+    assert g["rate"] != 0.0
+    assert abs(fd - g["rate"]) <= 1e-5 * abs(g["rate"]), (fd, g["rate"])
 
 
 def test_gradient_is_reproducible_and_schedule_independent():

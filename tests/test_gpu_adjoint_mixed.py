@@ -12,6 +12,8 @@ Checks:
   * gradients are bit-for-bit reproducible and independent of the
     checkpoint spacing (the recomputation repeats the mixed forward exactly
     and the reverse advection has no atomics);
+  * the reference's default inputs (clamp-form source with an inflow
+    velocity, density-scaled buoyancy) agree with the FP64 adjoint;
   * a trace that moves a full cell fails the call with CF_ERR_UNSUPPORTED.
 """
 import numpy as np
@@ -116,6 +118,32 @@ def test_mixed_gradient_matches_fp64_adjoint(periodic, precon):
     fd = (loss(q0 + h * dq, u0 + h * du, v0 + h * dv) - loss(q0 - h * dq, u0 - h * du, v0 - h * dv)) / (2 * h)
     ad = float(np.sum(g32["q"] * dq) + np.sum(g32["u"] * du) + np.sum(g32["v"] * dv))
     assert abs(fd - ad) <= 1e-4 * abs(fd), (fd, ad)
+
+
+@pytest.mark.parametrize("buoyancy", [False, True])
+def test_mixed_default_physics_matches_fp64_adjoint(buoyancy):
+    """The reference's default inputs (clamp-form source with an inflow
+    velocity, density-scaled buoyancy) in the mixed adjoint against the FP64
+    adjoint of the same problem."""
+    q0, u0, v0 = initial()
+    dt = 0.4 / N / max(np.abs(u0).max(), np.abs(v0).max(), 3.0)
+    target = gaussian_blobs(N, 11, count=4, sigma=0.08)
+    grads = {}
+    for mixed in (False, True):
+        c = Context(N, N, precision="mixed" if mixed else "fp64")
+        c.set_density(0.1)
+        c.set_quirks(L.CF_FIX_Q1)
+        c.set_source((0.40, 0.10), (0.20, 0.10), (0.0, 3.0), 0.8, mode=0)
+        if buoyancy:
+            c.set_body_force((0.0, -9.8), density_scaled=True)
+        qT, _, _ = run(c, q0, u0, v0, dt, opts=opts_for("PFMG", mixed))
+        grads[mixed] = c.backward(qT - target)
+    g64, g32 = grads[False], grads[True]
+    for f in ("q", "u", "v"):
+        rel = np.linalg.norm(g32[f] - g64[f]) / np.linalg.norm(g64[f])
+        assert rel <= 1e-4, (f, rel)
+    assert g64["rate"] != 0.0
+    assert abs(g32["rate"] - g64["rate"]) <= 1e-4 * abs(g64["rate"]), (g32["rate"], g64["rate"])
 
 
 def test_mixed_gradient_is_reproducible_and_schedule_independent():
