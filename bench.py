@@ -732,7 +732,7 @@ def bench_adjoint4(args, device, dist, peak):
     return {"workload": f"{n}^2 walls, cubic, seeded spectral velocity + scalar, T={T}, checkpoint every {every} "
                         f"(the smallest spacing whose checkpoints fit 150 GB), mixed precision (FP32 bulk, "
                         f"double-float refinement), PCG + {args.precon}, ||div u||_L2 <= {w.abs_tol:g}; adjoint: "
-                        f"FP32 reverse advection, transposed projection to relative 1e-8 (warm-started)",
+                        f"FP32 reverse advection, transposed projection to relative 1e-7 (warm-started)",
             "forward_ms": t_fwd, "forward_steps_per_s": T / (t_fwd / 1e3),
             **main,
             "sqrt_spacing": runs[sq],

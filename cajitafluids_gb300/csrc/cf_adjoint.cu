@@ -383,7 +383,7 @@ __device__ __forceinline__ float aj_safe(float d, bool& bad) {
 // operations), then its transpose with fbar the adjoint of the advected
 // value.  Position derivatives are in index units (the trace moves by
 // d = -c a, c = dt / dx).
-template <int ORDER, int ENT, typename T>
+template <int ORDER, bool GATE, int ENT, typename T>
 __device__ __forceinline__ void aj_target(const AdjAdv32& a, const T& U, const T& V, const T& Q, int li, int lj,
                                           float fbar, float* Pq, float* Pu, float* Pv, bool& bad) {
     const float ox_e = ENT == E_FACEI ? 0.f : 0.5f;
@@ -443,7 +443,7 @@ __device__ __forceinline__ void aj_target(const AdjAdv32& a, const T& U, const T
                 rs = fmaf(wx[k], f, rs);
                 rd = fmaf(dwx[k], f, rd);
             }
-            vs = fmaf(wy[b], rs, vs);
+            if (GATE) vs = fmaf(wy[b], rs, vs);
             gx = fmaf(wy[b], rd, gx);
             gy = fmaf(dwy[b], rs, gy);
         }
@@ -451,7 +451,7 @@ __device__ __forceinline__ void aj_target(const AdjAdv32& a, const T& U, const T
         aj_spread_cub(ox - 1, wx, WX);
         aj_spread_cub(oy - 1, wy, WY);
     }
-    fbar = (float)inputs_adjoint_gate(a.p, ENT, li, lj, val, (double)fbar, a.qclamp);
+    if (GATE) fbar = (float)inputs_adjoint_gate(a.p, ENT, li, lj, val, (double)fbar, a.qclamp);
     if (ORDER == 1)
         aj_lin<0, 0>(PF, fbar, sf);
     else
@@ -541,7 +541,9 @@ struct AjWin {
     __device__ __forceinline__ static float ld(const float* p) { return *p; }
 };
 
-template <int ORDER>
+// GATE: the inflow box is active with a replacing input (clamp-form source
+// or an inflow velocity), so targets compare their advected value
+template <int ORDER, bool GATE>
 __global__ void __launch_bounds__(AJ_WARPS * 32) k_adj_advect32(AdjAdv32 a) {
     extern __shared__ __align__(16) float aw[];  // u, v, q windows
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -596,9 +598,9 @@ __global__ void __launch_bounds__(AJ_WARPS * 32) k_adj_advect32(AdjAdv32 a) {
         for (int k = 0; k < 25; ++k) Pq[k] = Pu[k] = Pv[k] = 0.f;
         const int gj = tr - CF_HALO;
         if (gi >= 0 && gj >= 0) {
-            if (gi < p.nx && gj < p.ny) aj_target<ORDER, E_CELL>(a, U, V, Q, tc, tr, fq, Pq, Pu, Pv, bad);
-            if (gi < oxu && gj < p.ny) aj_target<ORDER, E_FACEI>(a, U, V, Q, tc, tr, fu, Pq, Pu, Pv, bad);
-            if (gi < p.nx && gj < oyv) aj_target<ORDER, E_FACEJ>(a, U, V, Q, tc, tr, fv, Pq, Pu, Pv, bad);
+            if (gi < p.nx && gj < p.ny) aj_target<ORDER, GATE, E_CELL>(a, U, V, Q, tc, tr, fq, Pq, Pu, Pv, bad);
+            if (gi < oxu && gj < p.ny) aj_target<ORDER, GATE, E_FACEI>(a, U, V, Q, tc, tr, fu, Pq, Pu, Pv, bad);
+            if (gi < p.nx && gj < oyv) aj_target<ORDER, GATE, E_FACEJ>(a, U, V, Q, tc, tr, fv, Pq, Pu, Pv, bad);
         }
         fq = nq;
         fu = nu;
@@ -1113,21 +1115,23 @@ int adjoint_step_mixed(cf_ctx* c, AdjState* A, const SolveOpts& so, bool params_
     a.qclamp = A->qclamp;
     const int blocks = (a.nsx + AJ_WARPS - 1) / AJ_WARPS * a.nsy;
     if (!A->smem_set) {
-        for (auto fn : {k_adj_advect32<1>, k_adj_advect32<3>})
+        for (auto fn : {k_adj_advect32<1, false>, k_adj_advect32<3, false>, k_adj_advect32<1, true>,
+                        k_adj_advect32<3, true>})
             if ((rc = cuda_check(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AJ_SMEM),
                                  "adjoint smem")))
                 return rc;
         A->smem_set = true;
     }
+    const bool box = p.bbox[2] > p.bbox[0] && p.bbox[3] > p.bbox[1];
+    const bool gate = box && (p.src_mode == 0 || p.src_vel[0] != 0.0 || p.src_vel[1] != 0.0);
     if (c->prof && !A->ev_adv[0]) {
         for (auto& e : A->ev_adv)
             if ((rc = cuda_check(c, cudaEventCreate(&e), "event create"))) return rc;
     }
     if (c->prof) cudaEventRecord(A->ev_adv[0], c->stream);
-    if (A->order == 1)
-        k_adj_advect32<1><<<blocks, AJ_WARPS * 32, AJ_SMEM, c->stream>>>(a);
-    else
-        k_adj_advect32<3><<<blocks, AJ_WARPS * 32, AJ_SMEM, c->stream>>>(a);
+    auto kern = A->order == 1 ? (gate ? k_adj_advect32<1, true> : k_adj_advect32<1, false>)
+                              : (gate ? k_adj_advect32<3, true> : k_adj_advect32<3, false>);
+    kern<<<blocks, AJ_WARPS * 32, AJ_SMEM, c->stream>>>(a);
     c->launches += 1;
     clamp_sum(c, A);
     if (c->prof) {
@@ -1382,10 +1386,10 @@ int cf_backward(cf_ctx* ctx, const double* dL_dq_T, const double* dL_du_T, const
     so.precon_none = (!strcmp(A->precon.c_str(), "None") || !strcmp(A->precon.c_str(), "none")) ? 1 : 0;
     so.precon_mg = (A->precon == "PFMG" || A->precon == "SMG" || A->precon == "MG") ? 1 : 0;
     // default relative tolerance of the transposed solves: near the FP64
-    // floor; mixed, 1e-8 (the FP32 bulk bounds the gradient's accuracy near
+    // floor; mixed, 1e-7 (the FP32 bulk bounds the gradient's accuracy near
     // 1e-6 relative, and the forward's absolute ||div u|| target is a
-    // relative residual of a few 1e-7 on the spectral workloads)
-    if (!(so.tol > 0.0)) so.tol = A->mixed ? 1e-8 : 1e-12;
+    // relative residual of about 4e-7 on the spectral workloads)
+    if (!(so.tol > 0.0)) so.tol = A->mixed ? 1e-7 : 1e-12;
     // lambda_T
     const double* seeds[3] = {dL_dq_T, dL_du_T, dL_dv_T};
     const int fields[3] = {CF_FIELD_QUANTITY, CF_FIELD_U, CF_FIELD_V};

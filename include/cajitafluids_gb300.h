@@ -232,7 +232,7 @@ int cf_max_velocity(cf_ctx* ctx, double* umax);
  * (FP32 q, velocity pairs), recomputes the mixed forward, and runs the
  * reverse advection in FP32 and the transposed projection with the mixed
  * PCG (FP32 inner iterations, double-float refinement; relative tolerance
- * opts->tol, default 1e-8).  See cf_adjoint.cu for the supported inputs. */
+ * opts->tol, default 1e-7).  See cf_adjoint.cu for the supported inputs. */
 int cf_forward_checkpointed(cf_ctx* ctx, int nsteps, int ckpt_every, double dt, int value_order,
                             const cf_solver_opts* opts, cf_solve_stats* last);
 int cf_backward(cf_ctx* ctx, const double* dL_dq_T, const double* dL_du_T, const double* dL_dv_T, double* dL_dq0,
