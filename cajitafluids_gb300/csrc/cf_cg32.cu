@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     };
     if (tid == 0)
         for (int k = 0; k < kStages && k < ntile; ++k) issue(k);
-    double acc = 0.0;
+    float acc = 0.f;  // FP32 over this block's tiles (no FP64 in the loop)
     for (int k = 0; k < ntile; ++k) {
         const int s = k % kStages;
         const int t = (int)blockIdx.x + k * (int)gridDim.x;
@@ -314,12 +314,12 @@ __global__ void __launch_bounds__(kThreads, 2)
                 put4(a, pnew, i, j, pc, true);
             }
         }
-        acc = acc + (double)part;
+        acc = acc + part;
         fence_proxy_async();
         __syncthreads();
         if (tid == 0 && k + kStages < ntile) issue(k + kStages);
     }
-    double tot = block_sum(acc, red);
+    double tot = block_sum((double)acc, red);
     if (tid == 0) a.part0[blockIdx.x] = tot;
     if (last_block_arrive(&S->ticket[5])) {
         double pq = final_tree(a.part0, gridDim.x);
@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     };
     if (tid == 0)
         for (int k = 0; k < kStages && k < ntile; ++k) issue(k);
-    double arz = 0.0, arr = 0.0;
+    float arz = 0.f, arr = 0.f;  // FP32 over this block's tiles (no FP64 in the loop)
     for (int k = 0; k < ntile; ++k) {
         const int s = k % kStages;
         const int t = (int)blockIdx.x + k * (int)gridDim.x;
@@ -440,13 +440,13 @@ __global__ void __launch_bounds__(kThreads, 2)
                 put4(a, a.r, i, j, rv, true);
             }
         }
-        arz = arz + (double)prz;
-        arr = arr + (double)prr;
+        arz = arz + prz;
+        arr = arr + prr;
         __syncthreads();
         if (tid == 0 && k + kStages < ntile) issue(k + kStages);
     }
-    double trz = block_sum(arz, red);
-    double trr = block_sum(arr, red);
+    double trz = block_sum((double)arz, red);
+    double trr = block_sum((double)arr, red);
     if (tid == 0) {
         a.part0[blockIdx.x] = trz;
         a.part1[blockIdx.x] = trr;

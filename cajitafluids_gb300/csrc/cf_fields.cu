@@ -273,6 +273,8 @@ struct Adv32 {
     int ent0;     // entity of blockIdx.x == 0 (a launch may cover a subset)
     int unstaged; // tests: every tile reads global memory (same bits)
     float2 fdt2[2];  // force[axis] * dt as pairs (zero without a force)
+    int force_on[2]; // force[axis] != 0 (tested on the host: an FP64 compare per face
+                     // would occupy GB300's FP64 pipe)
 };
 
 
@@ -409,7 +411,7 @@ __global__ void __launch_bounds__(256, 8) k_advect32(Adv32 a) {
         float2 w = make_float2(val, 0.f);
         if (a.fuse) {
             if (in_box_idx(p, ent, li, lj) && fabs((double)val) < fabs(p.src_vel[axis])) w = df_split(p.src_vel[axis]);
-            if (p.force[axis] != 0.0) w = df_add(w, a.fdt2[axis]);
+            if (a.force_on[axis]) w = df_add(w, a.fdt2[axis]);
             const int per = axis == 0 ? p.per_x : p.per_y, n = axis == 0 ? p.nx : p.ny, gg = axis == 0 ? gi : gj;
             if (!per) {
                 if (gg <= 0 && p.bc[axis] == 0) w = make_float2(0.f, 0.f);
@@ -598,6 +600,7 @@ cudaError_t launch_advect(cf_ctx* c, double dt, int order, int fuse_inputs, int 
             const double f = p.force[k] * dt;
             const float hi = (float)f;
             a.fdt2[k] = make_float2(hi, (float)(f - (double)hi));
+            a.force_on[k] = p.force[k] != 0.0 ? 1 : 0;
         }
         (void)prep;
         const dim3 tiles(nent, (p.nx + 1 + AT_X - 1) / AT_X, (p.ny + 1 + AT_Y - 1) / AT_Y);

@@ -106,6 +106,15 @@ struct Vec32 {
 // sums are folded by a xor butterfly; the last block to finish folds all
 // unit partials: 256 strided accumulators, a butterfly per warp, and the 8
 // warp sums added in order.
+// FP32 butterfly sum of a warp (fixed order); the FP32 kernels fold their
+// per-lane partials this way and hand the warp total on as FP64, so that no
+// FP64 operation (a slow pipe on GB300) sits in their inner loops
+__device__ __forceinline__ float warp_fold_f(float s) {
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, m);
+    return s;
+}
+
 __device__ __forceinline__ double warp_fold(double s) {
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, m);

@@ -539,8 +539,8 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_div_init_mixed(DivArgs a) {
         });
     }
     // inner r.r equals b.b here (the same squares in the same order)
-    const double dbb = warp_fold((double)abb);
-    const double drz = warp_fold((double)arz);
+    const double dbb = (double)warp_fold_f(abb);
+    const double drz = (double)warp_fold_f(arz);
     if (unit < a.U && lane == 0) {
         a.part0[unit] = dbb;
         a.part1[unit] = drz;
@@ -853,7 +853,7 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
             xp = xpp;
         }
     }
-    double drz = warp_fold((double)arz), drr = warp_fold((double)arr);
+    const double drz = (double)warp_fold_f(arz), drr = (double)warp_fold_f(arr);
     if (unit < a.U && lane == 0) {
         a.part0[unit] = drr;
         a.part1[unit] = drz;
