@@ -676,8 +676,10 @@ __device__ __forceinline__ float2 df_resid_int(const Outer& a, float2 b, float2 
     return df_add_s(b, make_float2(-ax.x, -ax.y));
 }
 
-// Interior unit (every cell and neighbour inside the domain, no wrap, no
-// wall): the same arithmetic without the boundary logic.  The rows arrive
+// Interior unit (no wall next to any of its cells, whole 64-column group):
+// the same arithmetic without the boundary logic.  Along a periodic axis the
+// halo rows and columns are fetched from their wrapped positions, so every
+// full unit of a periodic domain takes this path.  The rows arrive
 // through a per-warp cp.async ring OR_RING - 1 rows ahead (group k: x (and,
 // fused, p) of row j0 - 1 + k, and for the unit's own rows b; the outer
 // columns' neighbours of lanes 0 and 31); each lane reads back only what it
@@ -695,7 +697,11 @@ __device__ __forceinline__ void outer_unit_interior(const Outer& a, const XSrc& 
     const bool upd = FUSED && xs.upd;
     const float m0 = a.minv32[0];
     const bool edge = lane == 0 || lane == 31;
-    const int ec = lane == 0 ? c0 - 1 : c0 + 2;  // outer neighbour column of lanes 0 and 31
+    int ec = lane == 0 ? c0 - 1 : c0 + 2;  // outer neighbour column of lanes 0 and 31 (wrapped)
+    ec = ec < 0 ? ec + a.nx : (ec >= a.nx ? ec - a.nx : ec);
+    // periodic ghost copies of r: columns 0 and nx - 1, rows 0 and ny - 1
+    const bool gx0 = a.per_x && c0 == 0, gx1 = a.per_x && c0 + 2 == a.nx;
+    const bool ghosts = __any_sync(FULLMASK, gx0 || gx1) || (a.per_y && (j0 == 0 || j1 == a.ny));
     const int eo = 256 + (lane == 31 ? 2 : 0);
     const int eop = 328 + (lane == 31 ? 1 : 0);
     const int last = j1;                         // groups cover rows j0 - 1 .. j1
@@ -703,13 +709,14 @@ __device__ __forceinline__ void outer_unit_interior(const Outer& a, const XSrc& 
         const int row = j0 - 1 + k;
         float* sl = ring + (k % OR_RING) * SLOT;
         if (row <= last) {
-            const size_t o = (size_t)row * a.pitch;
+            const int pr = row < 0 ? row + a.ny : (row >= a.ny ? row - a.ny : row);  // wrapped halo row
+            const size_t o = (size_t)pr * a.pitch;
             cpa16(sl + 4 * lane, xs.x + o + c0);
-            if (upd) cpa8(sl + 264 + 2 * lane, xs.p + (ptrdiff_t)row * a.pitch32 + c0);
+            if (upd) cpa8(sl + 264 + 2 * lane, xs.p + (ptrdiff_t)pr * a.pitch32 + c0);
             if (row >= j0 && row < j1) cpa16(sl + 128 + 4 * lane, a.b + o + c0);
             if (edge) {
                 cpa8(sl + eo, xs.x + o + ec);
-                if (upd) cpa4(sl + eop, xs.p + (ptrdiff_t)row * a.pitch32 + ec);
+                if (upd) cpa4(sl + eop, xs.p + (ptrdiff_t)pr * a.pitch32 + ec);
             }
         }
         cpa_commit();
@@ -760,6 +767,19 @@ __device__ __forceinline__ void outer_unit_interior(const Outer& a, const XSrc& 
         const float2 r1 = df_resid_int(a, make_float2(bv.z, bv.w), make_float2(xc.z, xc.w), make_float2(xc.x, xc.y),
                                        right, make_float2(xm.z, xm.w), make_float2(xp.z, xp.w));
         *reinterpret_cast<float2*>(a.r32 + (ptrdiff_t)j * a.pitch32 + c0) = make_float2(r0.x, r1.x);
+        if (ghosts) {  // periodic copies of boundary cells, as put_r32 writes them
+            float* row = a.r32 + (ptrdiff_t)j * a.pitch32;
+            if (gx0) row[a.nx] = r0.x;
+            if (gx1) row[-1] = r1.x;
+            if (a.per_y && j == 0) {
+                a.r32[(ptrdiff_t)a.ny * a.pitch32 + c0] = r0.x;
+                a.r32[(ptrdiff_t)a.ny * a.pitch32 + c0 + 1] = r1.x;
+            }
+            if (a.per_y && j == a.ny - 1) {
+                a.r32[-(ptrdiff_t)a.pitch32 + c0] = r0.x;
+                a.r32[-(ptrdiff_t)a.pitch32 + c0 + 1] = r1.x;
+            }
+        }
         arz = fmaf(r0.x, m0 * r0.x, arz);
         arr = fmaf(r0.x, r0.x, arr);
         arz = fmaf(r1.x, m0 * r1.x, arz);
@@ -804,9 +824,12 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
     float arz = 0.f, arr = 0.f;
     const int g = unit % a.G, band = unit / a.G;
     const int j0u = band * CF_BAND_ROWS, j1u = min(j0u + CF_BAND_ROWS, a.ny);
-    // rows j0u - 1 .. j1u + 1 and columns g * 64 - 1 .. g * 64 + 64 are read
-    const bool interior = unit < a.U && g * CF_UNIT_COLS >= 1 && (g + 1) * CF_UNIT_COLS + 1 <= a.nx &&
-                          j0u >= 1 && j1u + 2 <= a.ny;
+    // rows j0u - 1 .. j1u and columns g * 64 - 1 .. g * 64 + 64 are read:
+    // inside the domain, or wrapped along a periodic axis
+    const bool full_x = (g + 1) * CF_UNIT_COLS <= a.nx;
+    const bool interior = unit < a.U && full_x &&
+                          (a.per_x || (g * CF_UNIT_COLS >= 1 && (g + 1) * CF_UNIT_COLS + 1 <= a.nx)) &&
+                          (a.per_y || (j0u >= 1 && j1u + 2 <= a.ny));
     __shared__ __align__(16) float ring[CF_RED_WARPS * OR_RING * OrSlot<FUSED>::value];
     if (interior) {
         outer_unit_interior<FUSED>(a, xs, xo, ring + (threadIdx.x >> 5) * OR_RING * OrSlot<FUSED>::value, lane,
