@@ -324,26 +324,34 @@ __device__ __forceinline__ void ft_load(const MgLev<T>& L, const MgBc& p, T* xs,
     __syncthreads();
 }
 
-// A tile is interior when its array (tile + halo H) lies in [1, n-1) along
-// both axes: no wrap, no wall, every wall-adjacency bit 0, every transfer
-// weight the interior one.  Those tiles take the index-light paths below.
+// A tile is interior when no wall is within its array (tile + halo H) and
+// the tile is whole: along a non-periodic axis the array lies in [1, n-1),
+// along a periodic one the halo wraps (n >= H, one period at most).  Every
+// wall-adjacency bit is then 0 and every transfer weight the interior one,
+// and those tiles take the index-light paths below, reading their halo
+// through mg_wrap.
 template <int TW, int TH, int H>
-__device__ __forceinline__ bool ft_interior(int nx, int ny, int i0, int j0) {
-    return i0 - H >= 1 && i0 + TW + H <= nx - 1 && j0 - H >= 1 && j0 + TH + H <= ny - 1;
+__device__ __forceinline__ bool ft_interior(int nx, int ny, int i0, int j0, const MgBc& p) {
+    const bool ix = p.per_x ? (i0 + TW <= nx && nx >= H) : (i0 - H >= 1 && i0 + TW + H <= nx - 1);
+    const bool iy = p.per_y ? (j0 + TH <= ny && ny >= H) : (j0 - H >= 1 && j0 + TH + H <= ny - 1);
+    return ix && iy;
 }
+
+// an index within one period of [0, n): wrapped (interior tiles only)
+__device__ __forceinline__ int mg_wrap(int g, int n) { return g < 0 ? g + n : (g >= n ? g - n : g); }
 
 template <typename T, int TW, int TH, int H>
 __device__ __forceinline__ void ft_load_int(const MgLev<T>& L, T* xs, T* bs, int i0, int j0, const T* xsrc) {
     constexpr int W = TW + 2 * H, HT = TH + 2 * H;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const T* b = L.b + (size_t)(j0 - H) * L.pitch + (i0 - H);
-    const T* x = xsrc ? xsrc + (size_t)(j0 - H) * L.pitch + (i0 - H) : nullptr;
-    for (int lj = warp; lj < HT; lj += FT_THREADS / 32)
+    for (int lj = warp; lj < HT; lj += FT_THREADS / 32) {
+        const size_t row = (size_t)mg_wrap(j0 - H + lj, L.ny) * L.pitch;
         for (int li = lane; li < W; li += 32) {
-            const size_t k = (size_t)lj * L.pitch + li;
-            bs[lj * W + li] = b[k];
-            xs[lj * W + li] = x ? x[k] : T(0);
+            const size_t k = row + mg_wrap(i0 - H + li, L.nx);
+            bs[lj * W + li] = L.b[k];
+            xs[lj * W + li] = xsrc ? xsrc[k] : T(0);
         }
+    }
     __syncthreads();
 }
 
@@ -769,7 +777,7 @@ __global__ void __launch_bounds__(FT_THREADS, FtBlocks<T, TW>::value) k_mg_pre(M
     int tx, ty;
     frame_tile(m, blockIdx.x, tx, ty);
     const int i0 = tx * TW, j0 = ty * TH;
-    if (ft_interior<TW, TH, H>(F.nx, F.ny, i0, j0)) {
+    if (ft_interior<TW, TH, H>(F.nx, F.ny, i0, j0, p)) {
         ft_load_int<T, TW, TH, H>(F, xs, bs, i0, j0, nullptr);
         ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 0, 5, true);
         ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 1, 4, false);
@@ -897,23 +905,24 @@ __global__ void __launch_bounds__(FT_THREADS, FtBlocks<T, TW>::value) k_mg_post(
     int tx, ty;
     frame_tile(m, blockIdx.x, tx, ty);
     const int i0 = tx * TW, j0 = ty * TH;
-    if (ft_interior<TW, TH, H>(F.nx, F.ny, i0, j0)) {
-        // coarse block from (i0 - H) / 2 - 1, (j0 - H) / 2 - 1
+    if (ft_interior<TW, TH, H>(F.nx, F.ny, i0, j0, p)) {
+        // coarse block from (i0 - H) / 2 - 1, (j0 - H) / 2 - 1 (wrapped
+        // along periodic axes)
         const int ci0 = (i0 - H) / 2 - 1, cj0 = (j0 - H) / 2 - 1;
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        for (int cj = warp; cj < CH; cj += FT_THREADS / 32)
-            for (int ci = lane; ci < CW; ci += 32) cs[cj * CW + ci] = C.x[(size_t)(cj0 + cj) * C.pitch + ci0 + ci];
+        for (int cj = warp; cj < CH; cj += FT_THREADS / 32) {
+            const size_t crow = (size_t)mg_wrap(cj0 + cj, C.ny) * C.pitch;
+            for (int ci = lane; ci < CW; ci += 32) cs[cj * CW + ci] = C.x[crow + mg_wrap(ci0 + ci, C.nx)];
+        }
         __syncthreads();
         // b, and x (kept in the r array by k_mg_pre) plus the prolongation,
         // one warp per row
-        const size_t base = (size_t)(j0 - H) * F.pitch + (i0 - H);
         for (int lj = warp; lj < HT; lj += FT_THREADS / 32) {
             const int fy = j0 - H + lj;
             const int J = (fy >> 1) - cj0, NJ = J + ((fy & 1) ? 1 : -1);
             const T* c0 = cs + J * CW;
             const T* c1 = cs + NJ * CW;
-            const T* brow = F.b + base + (size_t)lj * F.pitch;
-            const T* xrow = F.r + base + (size_t)lj * F.pitch;
+            const size_t frow = (size_t)mg_wrap(fy, F.ny) * F.pitch;
             for (int li = lane; li < W; li += 32) {
                 const int fx = i0 - H + li;
                 const int I = (fx >> 1) - ci0, NI = I + ((fx & 1) ? 1 : -1);
@@ -923,8 +932,9 @@ __global__ void __launch_bounds__(FT_THREADS, FtBlocks<T, TW>::value) k_mg_post(
                 T row1 = T(0.75) * c1[I];
                 row1 = mg_fma(T(0.25), c1[NI], row1);
                 v = mg_fma(T(0.25), row1, v);
-                bs[lj * W + li] = brow[li];
-                xs[lj * W + li] = xrow[li] + v;
+                const size_t k = frow + mg_wrap(fx, F.nx);
+                bs[lj * W + li] = F.b[k];
+                xs[lj * W + li] = F.r[k] + v;
             }
         }
         __syncthreads();
@@ -934,10 +944,22 @@ __global__ void __launch_bounds__(FT_THREADS, FtBlocks<T, TW>::value) k_mg_post(
         ft_half_int<T, TW, TH, H>(F, xs, bs, i0, j0, 0, 0, false);
         T rz = T(0);
         for (int k = threadIdx.x; k < TW * TH; k += FT_THREADS) {
-            const int li = k % TW, lj = k / TW;
+            const int li = k % TW, lj = k / TW, gi = i0 + li, gj = j0 + lj;
             const int q = (lj + H) * W + li + H;
-            F.x[(size_t)(j0 + lj) * F.pitch + i0 + li] = xs[q];
-            if (E.on && !in_strips(m, i0 + li, j0 + lj)) rz = mg_fma(bs[q], xs[q], rz);
+            T* row = F.x + (size_t)gj * F.pitch;
+            row[gi] = xs[q];
+            if (E.on) {
+                if (!in_strips(m, gi, gj)) rz = mg_fma(bs[q], xs[q], rz);
+                // ghost copies along periodic axes (the finest level's x has a ghost ring)
+                if (p.per_x) {
+                    if (gi == 0) row[F.nx] = xs[q];
+                    if (gi == F.nx - 1) row[-1] = xs[q];
+                }
+                if (p.per_y) {
+                    if (gj == 0) F.x[(ptrdiff_t)F.ny * F.pitch + gi] = xs[q];
+                    if (gj == F.ny - 1) F.x[-(ptrdiff_t)F.pitch + gi] = xs[q];
+                }
+            }
         }
         if (E.on) post_epilogue(E, S, nparts, (double)rz);
         return;
