@@ -822,7 +822,24 @@ __global__ void __launch_bounds__(CF_RED_THREADS) k_outer_resid(Outer a) {
     const int lane = threadIdx.x & 31;
     const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
     float arz = 0.f, arr = 0.f;
-    const int g = unit % a.G, band = unit / a.G;
+    // Units next to a wall along x (column groups 0 and G - 1) take the
+    // general path, several times slower than the interior one: they are
+    // numbered first, two per row band, so that they fill blocks of their own
+    // and no interior warp waits for one at the end-of-block barrier.
+    int g, band;
+    if (!a.per_x && a.G > 2) {
+        const int nb = 2 * (a.U / a.G);
+        if (unit < nb) {
+            band = unit >> 1;
+            g = (unit & 1) ? a.G - 1 : 0;
+        } else {
+            band = (unit - nb) / (a.G - 2);
+            g = 1 + (unit - nb) % (a.G - 2);
+        }
+    } else {
+        g = unit % a.G;
+        band = unit / a.G;
+    }
     const int j0u = band * CF_BAND_ROWS, j1u = min(j0u + CF_BAND_ROWS, a.ny);
     // rows j0u - 1 .. j1u and columns g * 64 - 1 .. g * 64 + 64 are read:
     // inside the domain, or wrapped along a periodic axis
