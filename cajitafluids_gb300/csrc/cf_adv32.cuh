@@ -55,6 +55,34 @@ struct WindowTaps {
     __device__ __forceinline__ static float ld(const float* p) { return *p; }
 };
 
+// Packed FP32 pairs: one f32x2 instruction (sm_100 and later) performs two
+// independent FP32 operations, each rounded exactly as its scalar form, so
+// pairing two rows of a stencil halves their instructions and keeps every bit.
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "sub.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 f2_mul(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "mul.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c) {
+    float2 r;
+    asm("{\n\t.reg .b64 pa, pb, pc, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "mov.b64 pc, {%6, %7};\n\tfma.rn.f32x2 pd, pa, pb, pc;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return r;
+}
+
 template <typename A>
 __device__ __forceinline__ float lin32(const A& g, int bi, int bj, float fx, float fy) {
     float flx = floorf(fx), fly = floorf(fy);
@@ -69,11 +97,11 @@ __device__ __forceinline__ float lin32(const A& g, int bi, int bj, float fx, flo
     const float* r0 = g.at(ix, iy);
     const float* r1 = r0 + g.stride();
     const int e = g.step();
-    float a0 = A::ld(r0), a1 = A::ld(r0 + e);
-    float b0 = A::ld(r1), b1 = A::ld(r1 + e);
-    float s0 = fmaf(tx, a1 - a0, a0);
-    float s1 = fmaf(tx, b1 - b0, b0);
-    return fmaf(ty, s1 - s0, s0);
+    const float2 lo = make_float2(A::ld(r0), A::ld(r1));           // (a0, b0)
+    const float2 hi = make_float2(A::ld(r0 + e), A::ld(r1 + e));   // (a1, b1)
+    // (s0, s1) = (fma(tx, a1 - a0, a0), fma(tx, b1 - b0, b0)), paired
+    const float2 sp = f2_fma(make_float2(tx, tx), f2_sub(hi, lo), lo);
+    return fmaf(ty, sp.y - sp.x, sp.x);
 }
 
 __device__ __forceinline__ void cubic_w32(float t, float* w) {
@@ -107,15 +135,22 @@ __device__ __forceinline__ float cub32(const A& g, int bi, int bj, float fx, flo
     const float* base = g.at(ix - 1, iy - 1);
     const int st = g.stride(), e = g.step();
     const float c = A::ld(base + st + e);
-    float val = 0.f;
+    // rows 0, 1 and rows 2, 3 as packed pairs: rs_b = wx0 (f_b0 - c), then
+    // fma(wx_k, f_bk - c, rs_b) for k = 1 .. 3, each lane as the scalar form
+    const float2 cc = make_float2(c, c);
+    float2 rs01, rs23;
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
-        const float* row = base + b * st;
-        float rs = wx[0] * (A::ld(row) - c);
-#pragma unroll
-        for (int k = 1; k < 4; ++k) rs = fmaf(wx[k], A::ld(row + k * e) - c, rs);
-        val = b == 0 ? wy[0] * rs : fmaf(wy[b], rs, val);
+    for (int k = 0; k < 4; ++k) {
+        const float2 wk = make_float2(wx[k], wx[k]);
+        const float2 d01 = f2_sub(make_float2(A::ld(base + k * e), A::ld(base + st + k * e)), cc);
+        const float2 d23 = f2_sub(make_float2(A::ld(base + 2 * st + k * e), A::ld(base + 3 * st + k * e)), cc);
+        rs01 = k == 0 ? f2_mul(wk, d01) : f2_fma(wk, d01, rs01);
+        rs23 = k == 0 ? f2_mul(wk, d23) : f2_fma(wk, d23, rs23);
     }
+    float val = wy[0] * rs01.x;
+    val = fmaf(wy[1], rs01.y, val);
+    val = fmaf(wy[2], rs23.x, val);
+    val = fmaf(wy[3], rs23.y, val);
     return c + val;
 }
 
