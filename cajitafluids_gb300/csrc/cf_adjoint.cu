@@ -430,22 +430,28 @@ __device__ __forceinline__ void aj_target(const AdjAdv32& a, const T& U, const T
         const float* base = F.at(li + ox - 1, lj + oy - 1);
         const int st = F.stride(), e = F.step();
         const float cc = T::ld(base + st + e);
+        // rows 0, 1 and 2, 3 as packed pairs (each lane as the scalar form)
+        const float2 c2 = make_float2(cc, cc);
+        float2 rs01 = make_float2(0.f, 0.f), rd01 = rs01, rs23 = rs01, rd23 = rs01;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float2 w = make_float2(wx[k], wx[k]), dw = make_float2(dwx[k], dwx[k]);
+            const float2 f01 = f2_sub(make_float2(T::ld(base + k * e), T::ld(base + st + k * e)), c2);
+            const float2 f23 = f2_sub(make_float2(T::ld(base + 2 * st + k * e), T::ld(base + 3 * st + k * e)), c2);
+            rs01 = f2_fma(w, f01, rs01);
+            rd01 = f2_fma(dw, f01, rd01);
+            rs23 = f2_fma(w, f23, rs23);
+            rd23 = f2_fma(dw, f23, rd23);
+        }
+        const float rs[4] = {rs01.x, rs01.y, rs23.x, rs23.y}, rd[4] = {rd01.x, rd01.y, rd23.x, rd23.y};
         gx = 0.f;
         gy = 0.f;
         float vs = 0.f;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-            const float* row = base + b * st;
-            float rs = 0.f, rd = 0.f;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float f = T::ld(row + k * e) - cc;
-                rs = fmaf(wx[k], f, rs);
-                rd = fmaf(dwx[k], f, rd);
-            }
-            if (GATE) vs = fmaf(wy[b], rs, vs);
-            gx = fmaf(wy[b], rd, gx);
-            gy = fmaf(dwy[b], rs, gy);
+            if (GATE) vs = fmaf(wy[b], rs[b], vs);
+            gx = fmaf(wy[b], rd[b], gx);
+            gy = fmaf(dwy[b], rs[b], gy);
         }
         val = cc + vs;
         aj_spread_cub(ox - 1, wx, WX);
