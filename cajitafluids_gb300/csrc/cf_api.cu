@@ -220,6 +220,11 @@ namespace cf {
 int enqueue_step(cf_ctx* ctx, double dt, int value_order, const SolveOpts& so, SolveResult* r, bool* deferred,
                  bool params_ready) {
     const bool fuse = !ctx->ph.force_density;
+    if (!ctx->prof && !ctx->direct && resident_projection()) {
+        // the whole step as one graph (ghost fill, advection, inputs, projection)
+        *deferred = true;
+        return step_resident(ctx, dt, value_order, fuse ? 1 : 0, so, params_ready);
+    }
     int rc = cuda_check(ctx, launch_fill_ghosts(ctx), "fill ghosts");
     if (ctx->prof) cudaEventRecord(ctx->ev[2], ctx->stream);
     if (!rc) rc = cuda_check(ctx, launch_advect(ctx, dt, value_order, fuse ? 1 : 0), "advect");
@@ -359,6 +364,8 @@ int cf_ctx_destroy(cf_ctx* ctx) {
     if (ctx->gmg) cudaGraphExecDestroy(ctx->gmg);
     if (ctx->gmg_pre) cudaGraphExecDestroy(ctx->gmg_pre);
     for (cudaGraphExec_t g : ctx->rgx)
+        if (g) cudaGraphExecDestroy(g);
+    for (cudaGraphExec_t g : ctx->sgx)
         if (g) cudaGraphExecDestroy(g);
     cf::mg_free(ctx);
     for (void* p : ctx->allocs) cudaFree(p);

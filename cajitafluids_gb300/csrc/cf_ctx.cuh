@@ -88,8 +88,17 @@ struct cf_ctx {
     cf::Phys rg_ph[4]{};
     int rg_flags[4] = {-1, -1, -1, -1};
     const double* rg_u[4] = {nullptr, nullptr, nullptr, nullptr};  // the u array each slot projects
-    int rg_head[4] = {0, 0, 0, 0}, rg_trip[4] = {0, 0, 0, 0}, rg_tail[4] = {0, 0, 0, 0};
-    int rg_pending = 0;  // slot of the last resident projection launched
+    // launch counts per graph: projection slots 0-3, whole-step graphs 4, 5
+    int rg_head[6] = {}, rg_trip[6] = {}, rg_tail[6] = {};
+    int rg_pending = 0;  // count slot of the last resident projection launched
+    // whole-step graphs (cf_project.cu step_resident): index = the state
+    // buffer the step starts from; ghost fill, advection and inputs, then the
+    // resident projection of the other buffer; rebuilt when a key changes
+    cudaGraphExec_t sgx[2] = {nullptr, nullptr};
+    double sg_dt[2] = {0.0, 0.0};
+    int sg_order[2] = {0, 0}, sg_fuse[2] = {-1, -1}, sg_flags[2] = {-1, -1};
+    cf::Stencil sg_st[2]{};
+    cf::Phys sg_ph[2]{};
     // FP32 z = M^-1 r of the mixed MG-PCG, ghost ring as the other FP32 vectors
     cf::Vec32 z32{};
     float* z32b = nullptr;
@@ -155,6 +164,11 @@ struct SolveResult {
     double bb, rr, div_l2, div_linf;
 };
 int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res);
+// one whole step (ghost fill, advection, inputs, resident projection) as one
+// graph launch, without a synchronisation (project_collect fills res after
+// the caller has synchronised the stream); the context then holds the new
+// state.  Used when the resident graphs serve (resident_projection()).
+int step_resident(cf_ctx* c, double dt, int order, int fuse, const SolveOpts& o, bool params_ready);
 // project without the final synchronisation when the device-resident graph
 // serves it (*deferred = true; project_collect fills res after the caller has
 // synchronised the stream), else a plain project (*deferred = false)

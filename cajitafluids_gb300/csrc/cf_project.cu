@@ -1464,8 +1464,14 @@ static int capture_graph(cf_ctx* c, cudaGraph_t* g, const std::function<void()>&
 // two pairs of adjoint face arrays); adjoint = 1 builds the transpose of the
 // projection on gu, gv (no wall mask after the gradient subtraction, no
 // warm start, no event for cf_step_host).
+// pre (optional): launches captured into a first child graph the rest
+// depends on (a whole step: ghost fill, advection, inputs, the parameters
+// copy), returning its kernel count; out: where the executable graph goes
+// (null: the projection cache slot).
 static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, bool mg, int slot, Grid<double> gu,
-                          Grid<double> gv, int adjoint) {
+                          Grid<double> gv, int adjoint, const std::function<int()>* pre = nullptr,
+                          cudaGraphExec_t* out = nullptr) {
+    if (!out) out = &c->rgx[slot];
     if (!c->ev_press) {
         int rc0 = cuda_check(c, cudaEventCreateWithFlags(&c->ev_press, cudaEventDisableTiming), "event create");
         if (rc0) return rc0;
@@ -1473,9 +1479,10 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
     const int nb = red_blocks(c);
     const double scale = -st.ms;
     const int warm = adjoint ? c->adj_warm : c->warm;
-    cudaGraph_t g = nullptr, head = nullptr, tail = nullptr;
-    int nhead = 0, ntrip = 0, ntail = 0;
+    cudaGraph_t g = nullptr, head = nullptr, tail = nullptr, preg = nullptr;
+    int nhead = 0, ntrip = 0, ntail = 0, npre = 0;
     int rc = cuda_check(c, cudaGraphCreate(&g, 0), "graph create");
+    if (!rc && pre) rc = capture_graph(c, &preg, [&] { npre = (*pre)(); });
     if (!rc)
         rc = capture_graph(c, &head, [&] {
             DivArgs da = div_args(c, st);
@@ -1500,8 +1507,9 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
                 }
             }
         });
-    cudaGraphNode_t nh = nullptr, nc = nullptr, nt = nullptr;
-    if (!rc) rc = cuda_check(c, cudaGraphAddChildGraphNode(&nh, g, nullptr, 0, head), "graph head");
+    cudaGraphNode_t np = nullptr, nh = nullptr, nc = nullptr, nt = nullptr;
+    if (!rc && preg) rc = cuda_check(c, cudaGraphAddChildGraphNode(&np, g, nullptr, 0, preg), "graph step");
+    if (!rc) rc = cuda_check(c, cudaGraphAddChildGraphNode(&nh, g, np ? &np : nullptr, np ? 1 : 0, head), "graph head");
     cudaGraphConditionalHandle h = 0;
     if (!rc) rc = cuda_check(c, cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault), "handle");
     cudaGraphNodeParams cp{};
@@ -1552,18 +1560,22 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
             cudaMemcpyAsync(c->h_out, c->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
         });
     if (!rc) rc = cuda_check(c, cudaGraphAddChildGraphNode(&nt, g, &nc, 1, tail), "graph tail");
-    if (c->rgx[slot]) {
-        cudaGraphExecDestroy(c->rgx[slot]);
-        c->rgx[slot] = nullptr;
+    if (*out) {
+        cudaGraphExecDestroy(*out);
+        *out = nullptr;
     }
-    if (!rc) rc = cuda_check(c, cudaGraphInstantiate(&c->rgx[slot], g, 0), "graph instantiate");
+    if (!rc) rc = cuda_check(c, cudaGraphInstantiate(out, g, 0), "graph instantiate");
+    if (preg) cudaGraphDestroy(preg);
     if (head) cudaGraphDestroy(head);
     if (tail) cudaGraphDestroy(tail);
     if (g) cudaGraphDestroy(g);
     if (rc) return rc;
-    c->rg_head[slot] = nhead;
-    c->rg_trip[slot] = ntrip;
-    c->rg_tail[slot] = ntail;
+    // launch counts for project_collect (a step graph's ghost fill, advection
+    // and inputs count with its head)
+    const int k = pre ? 4 + slot : slot;
+    c->rg_head[k] = npre + nhead;
+    c->rg_trip[k] = ntrip;
+    c->rg_tail[k] = ntail;
     return CF_OK;
 }
 
@@ -1645,6 +1657,69 @@ static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResul
     if (defer) return CF_OK;
     if ((rc = cuda_check(c, cudaStreamSynchronize(c->stream), "projection"))) return rc;
     project_collect(c, res);
+    return CF_OK;
+}
+
+int step_resident(cf_ctx* c, double dt, int order, int fuse, const SolveOpts& o, bool params_ready) {
+    const bool mixed = c->precision == CF_PREC_MIXED;
+    const bool mg = o.precon_mg != 0;
+    Stencil st{};
+    build_stencil(c, dt, o.precon_none, &st);
+    int rc = mg ? mg_setup(c) : CF_OK;
+    if (rc) return rc;
+    const int s = c->cur, n = 1 - s;
+    c->x_only = (mixed && mg && o.inner_tol >= 0.5) ? 1 : 0;
+    const int flags =
+        (mixed ? 1 : 0) | (mg ? 2 : 0) | (c->warm ? 4 : 0) | (c->x_only ? 8 : 0) | (c->test_unstaged ? 16 : 0);
+    if (!c->sgx[s] || c->sg_dt[s] != dt || c->sg_order[s] != order || c->sg_fuse[s] != fuse ||
+        c->sg_flags[s] != flags || std::memcmp(&c->sg_st[s], &st, sizeof(Stencil)) != 0 ||
+        std::memcmp(&c->sg_ph[s], &c->ph, sizeof(Phys)) != 0) {
+        // the step's own launches, on buffer s, then the parameters copy
+        const std::function<int()> pre = [&]() {
+            const long long l0 = c->launches;
+            cudaError_t e = launch_fill_ghosts(c);
+            if (e == cudaSuccess) e = launch_advect(c, dt, order, fuse, 0, 3, true, false);
+            if (e == cudaSuccess && !fuse) {
+                c->cur = n;
+                e = launch_add_inputs(c, dt);
+                c->cur = s;
+            }
+            cudaMemcpyAsync(c->S, c->hP, sizeof(SolverState), cudaMemcpyHostToDevice, c->stream);
+            const int k = (int)(c->launches - l0);
+            c->launches = l0;  // counted per launch of the graph instead
+            return k;
+        };
+        rc = build_resident(c, st, dt, mixed, mg, n, c->u[n], c->v[n], 0, &pre, &c->sgx[s]);
+        if (rc) return rc;
+        c->sg_dt[s] = dt;
+        c->sg_order[s] = order;
+        c->sg_fuse[s] = fuse;
+        c->sg_flags[s] = flags;
+        c->sg_st[s] = st;
+        c->sg_ph[s] = c->ph;
+    }
+    // a warm start reads the previous solution as FP64 (before the graph's
+    // parameters copy replaces the solver state the conversion reads)
+    if (flags & 4) settle_pressure(c);
+    SolverState* h = c->hP;
+    if (!params_ready) {
+        memset(h, 0, sizeof(SolverState));
+        h->tol2 = o.tol * o.tol;
+        h->abs2 = o.abs_tol * o.abs_tol;
+        h->use_abs = o.abs_tol > 0.0 ? 1 : 0;
+        h->area = c->ph.dx * c->ph.dx;
+        h->max_iter = o.max_iter;
+        h->max_outer = o.max_outer;
+        h->inner_tol2 = o.inner_tol * o.inner_tol;
+        h->status = ST_RUNNING;
+        const int batch = mg ? kResidentBatchMG : kResidentBatch;
+        h->trip_limit = (o.max_iter + (mixed ? o.max_outer : 0)) / batch + 4;
+        h->test_stall = c->test_stall;
+    }
+    if ((rc = cuda_check(c, cudaGraphLaunch(c->sgx[s], c->stream), "step graph launch"))) return rc;
+    c->cur = n;
+    c->p_df = (mixed && !(flags & 4)) ? 1 : 0;
+    c->rg_pending = 4 + n;
     return CF_OK;
 }
 
