@@ -52,3 +52,32 @@ def test_steps_count_unconverged(built):
     assert s["unconverged"] == 0
     s = c.steps(2, dt, 3, opts(tol=1e-9, max_iter=500, precon="PFMG"))
     assert s["unconverged"] == 0 and s["status"] == 0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_step_graphs_follow_changes(built, precision):
+    """cf_steps runs each step as one cached graph (ghost fill, advection,
+    inputs, projection); a change of dt, value order, body force or inflow
+    between calls must rebuild it: the same states as cf_step calls with the
+    same changes."""
+    n = 64
+    pairs = [make_pair(n, n, source=INFLOW, precision=precision, precon_mg=True) for _ in range(2)]
+    st = random_state(pairs[0][0], np.random.default_rng(9), smooth=True)
+    for o, c in pairs:
+        load_state(o, c, st)
+    so = opts(tol=1e-9, max_iter=3000, precon="PFMG")
+    ca, cb = pairs[0][1], pairs[1][1]
+    dt = 0.5 / n / 3.0
+    plan = [(2, dt, 3, None), (2, 0.7 * dt, 3, None), (1, 0.7 * dt, 1, None), (2, 0.7 * dt, 3, (0.0, -9.8)),
+            (2, 0.7 * dt, 3, ((0.40, 0.10), (0.20, 0.10), (0.0, 2.0), 0.5))]
+    for k, d, order, change in plan:
+        for c in (ca, cb):
+            if change is not None and len(change) == 2:
+                c.set_body_force(change, density_scaled=True)
+            elif change is not None:
+                c.set_source(*change)
+        for _ in range(k):
+            ca.step(d, order, so)
+        cb.steps(k, d, order, so)
+        for f in ("q", "u", "v"):
+            assert np.array_equal(ca.download(f), cb.download(f)), (k, d, order, change, f)
