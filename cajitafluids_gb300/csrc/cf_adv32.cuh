@@ -55,34 +55,6 @@ struct WindowTaps {
     __device__ __forceinline__ static float ld(const float* p) { return *p; }
 };
 
-// Packed FP32 pairs: one f32x2 instruction (sm_100 and later) performs two
-// independent FP32 operations, each rounded exactly as its scalar form, so
-// pairing two rows of a stencil halves their instructions and keeps every bit.
-__device__ __forceinline__ float2 f2_sub(float2 a, float2 b) {
-    float2 r;
-    asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
-        "sub.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-__device__ __forceinline__ float2 f2_mul(float2 a, float2 b) {
-    float2 r;
-    asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
-        "mul.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c) {
-    float2 r;
-    asm("{\n\t.reg .b64 pa, pb, pc, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
-        "mov.b64 pc, {%6, %7};\n\tfma.rn.f32x2 pd, pa, pb, pc;\n\tmov.b64 {%0, %1}, pd;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-    return r;
-}
-
 template <typename A>
 __device__ __forceinline__ float lin32(const A& g, int bi, int bj, float fx, float fy) {
     float flx = floorf(fx), fly = floorf(fy);

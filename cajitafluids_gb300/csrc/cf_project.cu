@@ -676,6 +676,49 @@ __device__ __forceinline__ float2 df_resid_int(const Outer& a, float2 b, float2 
     return df_add_s(b, make_float2(-ax.x, -ax.y));
 }
 
+// Two double-float values side by side, (h.x, l.x) and (h.y, l.y): a lane's
+// two cells, so that each error-free step runs as one packed f32x2
+// instruction for both (each half rounded as the scalar form, hence the bits
+// of df_resid_int cell by cell).
+struct DF2 {
+    float2 h, l;
+};
+__device__ __forceinline__ DF2 df2_two_sum(float2 a, float2 b) {
+    const float2 s = f2_add(a, b);
+    const float2 bb = f2_sub(s, a);
+    return DF2{s, f2_add(f2_sub(a, f2_sub(s, bb)), f2_sub(b, bb))};
+}
+__device__ __forceinline__ DF2 df2_quick(float2 a, float2 b) {
+    const float2 s = f2_add(a, b);
+    return DF2{s, f2_sub(b, f2_sub(s, a))};
+}
+__device__ __forceinline__ DF2 df2_add_s(DF2 x, DF2 y) {
+    DF2 s = df2_two_sum(x.h, y.h);
+    s.l = f2_add(s.l, f2_add(x.l, y.l));
+    return df2_quick(s.h, s.l);
+}
+__device__ __forceinline__ DF2 df2_neg(DF2 x) {
+    const float2 m = make_float2(-1.f, -1.f);
+    return DF2{f2_mul(m, x.h), f2_mul(m, x.l)};
+}
+// df_resid_int for a lane's two cells: the residuals' high parts
+__device__ __forceinline__ float2 df2_resid_int(float2 scale, DF2 b, DF2 c, DF2 w, DF2 e, DF2 s, DF2 n) {
+    DF2 nb = df2_add_s(w, e);
+    nb = df2_add_s(nb, s);
+    nb = df2_add_s(nb, n);
+    const float2 four = make_float2(4.f, 4.f);
+    const DF2 t = df2_add_s(DF2{f2_mul(four, c.h), f2_mul(four, c.l)}, df2_neg(nb));
+    // df_mul(scale, t)
+    const float2 sh = make_float2(scale.x, scale.x), sl = make_float2(scale.y, scale.y);
+    const float2 p = f2_mul(sh, t.h);
+    float2 er = f2_fma(sh, t.h, f2_mul(make_float2(-1.f, -1.f), p));
+    er = f2_fma(sh, t.l, er);
+    er = f2_fma(sl, t.h, er);
+    const DF2 ax = df2_quick(p, er);
+    const DF2 r = df2_add_s(b, df2_neg(ax));
+    return r.h;
+}
+
 // Interior unit (no wall next to any of its cells, whole 64-column group):
 // the same arithmetic without the boundary logic.  Along a periodic axis the
 // halo rows and columns are fetched from their wrapped positions, so every
@@ -762,10 +805,15 @@ __device__ __forceinline__ void outer_unit_interior(const Outer& a, const XSrc& 
         float2 right = make_float2(__shfl_down_sync(FULLMASK, xc.x, 1), __shfl_down_sync(FULLMASK, xc.y, 1));
         if (lane == 0) left = ev;
         if (lane == 31) right = ev;
-        const float2 r0 = df_resid_int(a, make_float2(bv.x, bv.y), make_float2(xc.x, xc.y), left,
-                                       make_float2(xc.z, xc.w), make_float2(xm.x, xm.y), make_float2(xp.x, xp.y));
-        const float2 r1 = df_resid_int(a, make_float2(bv.z, bv.w), make_float2(xc.z, xc.w), make_float2(xc.x, xc.y),
-                                       right, make_float2(xm.z, xm.w), make_float2(xp.z, xp.w));
+        // cell c0: W = left, E = the lane's second cell; cell c0 + 1: W = the
+        // first cell, E = right
+        const float2 rr2 = df2_resid_int(a.scale, DF2{make_float2(bv.x, bv.z), make_float2(bv.y, bv.w)},
+                                         DF2{make_float2(xc.x, xc.z), make_float2(xc.y, xc.w)},
+                                         DF2{make_float2(left.x, xc.x), make_float2(left.y, xc.y)},
+                                         DF2{make_float2(xc.z, right.x), make_float2(xc.w, right.y)},
+                                         DF2{make_float2(xm.x, xm.z), make_float2(xm.y, xm.w)},
+                                         DF2{make_float2(xp.x, xp.z), make_float2(xp.y, xp.w)});
+        const float2 r0 = make_float2(rr2.x, 0.f), r1 = make_float2(rr2.y, 0.f);
         *reinterpret_cast<float2*>(a.r32 + (ptrdiff_t)j * a.pitch32 + c0) = make_float2(r0.x, r1.x);
         if (ghosts) {  // periodic copies of boundary cells, as put_r32 writes them
             float* row = a.r32 + (ptrdiff_t)j * a.pitch32;
