@@ -140,6 +140,7 @@ SIGNATURES = {
     "cf_test_fail_alloc": (ctypes.c_int, [ctypes.c_int]),
     "cf_test_stall_wait": (ctypes.c_int, [_vp, ctypes.c_int]),
     "cf_test_advect_unstaged": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "cf_test_apply_general": (ctypes.c_int, [_vp, ctypes.c_int]),
     "cf_set_graphs": (ctypes.c_int, [_vp, ctypes.c_int]),
     "cf_test_conversions": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_float), _dp]),
     "cf_test_strip_geometry": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,

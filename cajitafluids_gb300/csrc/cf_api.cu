@@ -473,6 +473,12 @@ int cf_test_advect_unstaged(cf_ctx* ctx, int on) {
     return CF_OK;
 }
 
+int cf_test_apply_general(cf_ctx* ctx, int on) {
+    if (!ctx) return CF_ERR_INVALID;
+    ctx->test_general_apply = on ? 1 : 0;
+    return CF_OK;
+}
+
 int cf_set_density(cf_ctx* ctx, double density) {
     if (!ctx) return CF_ERR_INVALID;
     if (!(density > 0.0) || !isfinite(density)) return fail(ctx, CF_ERR_INVALID, "density must be positive");

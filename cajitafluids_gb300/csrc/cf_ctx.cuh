@@ -113,6 +113,7 @@ struct cf_ctx {
     // cf_test_advect_unstaged: every FP32 advection tile reads its taps from
     // global memory instead of its shared-memory window (same bits)
     int test_unstaged = 0;
+    int test_general_apply = 0;  // mixed gradient through k_apply_pressure
     // profiling (cf_profile_enable)
     int prof = 0;
     cf_profile pd{};

@@ -1057,46 +1057,139 @@ __device__ __forceinline__ double press_update(const Press& a, const float2* xdf
     return __dadd_rn(w, __dmul_rn(a.ms, d));
 }
 
+// One face: I face (axis 0) or J face (axis 1) of index (gi, gj), with the
+// reference's wall rules (src/VelocityCorrector.hpp:245-262).  (A zero
+// written to u or v is the pair (0, 0) as well.)
+__device__ __forceinline__ void apply_face(const Press& a, const float2* xdf, int axis, int gi, int gj) {
+    const Phys& p = a.p;
+    const bool fix_q1 = (p.quirks & 1u) != 0;
+    if (axis == 0) {
+        double& u = a.u.at(gi + CF_HALO, gj + CF_HALO);
+        // u -= scale * (p(i) - p(i-1)) (src/VelocityCorrector.hpp:245)
+        double w = press_update(a, xdf, u, gi, gj, gi - 1, gj);
+        if (!a.adjoint) {
+            if (!p.per_x) {
+                if (gi <= 0 && p.bc[0] == 0) w = 0.0;
+                if (gi > p.nx - 1 && p.bc[2] == 0) w = 0.0;
+            }
+            if (!fix_q1 && !p.per_y && gj == 0 && gi < p.nx && p.bc[1] == 0) w = 0.0;
+        }
+        u = w;
+    } else {
+        double& v = a.v.at(gi + CF_HALO, gj + CF_HALO);
+        double w = press_update(a, xdf, v, gi, gj, gi, gj - 1);  // :256
+        if (!p.per_y && !a.adjoint) {
+            if (fix_q1) {
+                if (gj <= 0 && p.bc[1] == 0) w = 0.0;
+                if (gj > p.ny - 1 && p.bc[3] == 0) w = 0.0;
+            } else if (gj > p.ny - 1 && p.bc[3] == 0) {
+                a.u.at(gi + CF_HALO, gj + CF_HALO) = 0.0;  // u ghost row ny
+            }
+        }
+        v = w;
+    }
+}
+
+__device__ __forceinline__ const float2* press_pairs(const Press& a) {
+    return a.pairs ? (a.S->xsel ? a.xb : reinterpret_cast<const float2*>(a.x)) : nullptr;
+}
+
 // One thread per (I-face, J-face) of index (gi, gj), both axes in the same
-// block so that a tile's pressure is read from memory once.  (A zero written
-// to u or v is the pair (0, 0) as well.)
+// block so that a tile's pressure is read from memory once.  The FP64
+// gradient, and every face of the mixed one under cf_test_apply_general.
 __global__ void k_apply_pressure(Press a) {
     const Phys& p = a.p;
     const int gi = blockIdx.x * blockDim.x + threadIdx.x;
     const int gj = blockIdx.y * blockDim.y + threadIdx.y;
-    const bool fix_q1 = (p.quirks & 1u) != 0;
-    const float2* xdf = a.pairs ? (a.S->xsel ? a.xb : reinterpret_cast<const float2*>(a.x)) : nullptr;
+    const float2* xdf = press_pairs(a);
 #pragma unroll 1
     for (int axis = 0; axis < 2; ++axis) {
         const int ox = p.nx + ((axis == 0 && !p.per_x) ? 1 : 0);
         const int oy = p.ny + ((axis == 1 && !p.per_y) ? 1 : 0);
         if (gi >= ox || gj >= oy) continue;
-        if (axis == 0) {
-            double& u = a.u.at(gi + CF_HALO, gj + CF_HALO);
-            // u -= scale * (p(i) - p(i-1)) (src/VelocityCorrector.hpp:245)
-            double w = press_update(a, xdf, u, gi, gj, gi - 1, gj);
-            if (!a.adjoint) {
-                if (!p.per_x) {
-                    if (gi <= 0 && p.bc[0] == 0) w = 0.0;
-                    if (gi > p.nx - 1 && p.bc[2] == 0) w = 0.0;
-                }
-                if (!fix_q1 && !p.per_y && gj == 0 && gi < p.nx && p.bc[1] == 0) w = 0.0;
-            }
-            u = w;
-        } else {
-            double& v = a.v.at(gi + CF_HALO, gj + CF_HALO);
-            double w = press_update(a, xdf, v, gi, gj, gi, gj - 1);  // :256
-            if (!p.per_y && !a.adjoint) {
-                if (fix_q1) {
-                    if (gj <= 0 && p.bc[1] == 0) w = 0.0;
-                    if (gj > p.ny - 1 && p.bc[3] == 0) w = 0.0;
-                } else if (gj > p.ny - 1 && p.bc[3] == 0) {
-                    a.u.at(gi + CF_HALO, gj + CF_HALO) = 0.0;  // u ghost row ny
-                }
-            }
-            v = w;
-        }
+        apply_face(a, xdf, axis, gi, gj);
     }
+}
+
+// The mixed gradient on the faces of the owned cells (I faces 0 .. nx - 1, J
+// faces 0 .. ny - 1), one warp per 64-column x 16-row unit as the divergence
+// kernels: lane l updates the I and J faces of columns c0 = 64 g + 2 l and
+// c0 + 1 row by row, each row's solution, u and v pairs as 16-byte vectors
+// (the next row's loaded before this row's stores); p(c0 - 1) comes from the
+// previous lane (lane 0 reads it: its wrap, or 0 beyond a wall) and p(j - 1)
+// from the previous row.  The same operations in the same order as
+// press_update and apply_face, so the same bits as k_apply_pressure; the faces
+// past the last cell of a walled axis are k_apply_edges'.
+__global__ void __launch_bounds__(CF_RED_THREADS) k_apply_pairs(Press a, int G, int U) {
+    const int lane = threadIdx.x & 31;
+    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
+    if (unit >= U) return;  // warp-uniform; no block barrier below
+    const Phys& p = a.p;
+    const int g = unit % G, band = unit / G;
+    const int c0 = g * CF_UNIT_COLS + 2 * lane;
+    const int j0 = band * CF_BAND_ROWS, j1 = min(j0 + CF_BAND_ROWS, p.ny);
+    const float2* xdf = press_pairs(a);
+    const bool live = c0 < p.nx, two = c0 + 1 < p.nx;
+    const bool fix_q1 = (p.quirks & 1u) != 0;
+    const bool walls = !a.adjoint;
+    // I face 0 of a walled x axis; the I faces of row 0 (unfixed Q1 quirk)
+    // and the J faces of row 0 (fixed) of a walled y axis
+    const bool zero_w = walls && !p.per_x && p.bc[0] == 0 && c0 == 0;
+    const bool zero_u0 = walls && !fix_q1 && !p.per_y && p.bc[1] == 0;
+    const bool zero_v0 = walls && fix_q1 && !p.per_y && p.bc[1] == 0;
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto xrow = [&](int j) { return live ? *reinterpret_cast<const float4*>(&xdf[(size_t)j * a.pitch + c0]) : zero4; };
+    auto frow = [&](const Grid<double>& f, int j) {
+        return live ? *reinterpret_cast<const float4*>(&f.at(c0 + CF_HALO, j + CF_HALO)) : zero4;
+    };
+    auto west = [&](int j) { return (lane == 0 && live) ? pval_df(a, xdf, c0 - 1, j) : make_float2(0.f, 0.f); };
+    auto upd = [&](float x0, float x1, float pc0, float pc1, float pn0, float pn1) {
+        const float2 m = df_mul(a.ms2, df_add_s(make_float2(pc0, pc1), make_float2(-pn0, -pn1)));
+        return df_add(make_float2(x0, x1), m);
+    };
+    // p(j0 - 1): the row below, its wrap, or 0 beyond a wall
+    float4 xs = j0 > 0 ? xrow(j0 - 1) : (p.per_y ? xrow(p.ny - 1) : zero4);
+    float4 xn = xrow(j0), un = frow(a.u, j0), vn = frow(a.v, j0);
+    float2 wn = west(j0);
+    for (int j = j0; j < j1; ++j) {
+        const float4 xc = xn, uu = un, vv = vn;
+        float2 xw = make_float2(__shfl_up_sync(FULLMASK, xc.z, 1), __shfl_up_sync(FULLMASK, xc.w, 1));
+        if (lane == 0) xw = wn;
+        if (j + 1 < j1) {
+            xn = xrow(j + 1);
+            un = frow(a.u, j + 1);
+            vn = frow(a.v, j + 1);
+            wn = west(j + 1);
+        }
+        if (!live) continue;
+        float2 u0 = upd(uu.x, uu.y, xc.x, xc.y, xw.x, xw.y);
+        float2 u1 = upd(uu.z, uu.w, xc.z, xc.w, xc.x, xc.y);
+        float2 v0 = upd(vv.x, vv.y, xc.x, xc.y, xs.x, xs.y);
+        float2 v1 = upd(vv.z, vv.w, xc.z, xc.w, xs.z, xs.w);
+        if (zero_w) u0 = make_float2(0.f, 0.f);
+        if (j == 0 && zero_u0) u0 = u1 = make_float2(0.f, 0.f);
+        if (j == 0 && zero_v0) v0 = v1 = make_float2(0.f, 0.f);
+        float2* pu = reinterpret_cast<float2*>(&a.u.at(c0 + CF_HALO, j + CF_HALO));
+        float2* pv = reinterpret_cast<float2*>(&a.v.at(c0 + CF_HALO, j + CF_HALO));
+        if (two) {
+            *reinterpret_cast<float4*>(pu) = make_float4(u0.x, u0.y, u1.x, u1.y);
+            *reinterpret_cast<float4*>(pv) = make_float4(v0.x, v0.y, v1.x, v1.y);
+        } else {
+            pu[0] = u0;
+            pv[0] = v0;
+        }
+        xs = xc;
+    }
+}
+
+// The faces past the last cell of a walled axis (I face nx of rows 0 ..
+// ny - 1, J face ny of columns 0 .. nx - 1): thread t takes one of each.
+__global__ void k_apply_edges(Press a) {
+    const Phys& p = a.p;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const float2* xdf = press_pairs(a);
+    if (!p.per_x && t < p.ny) apply_face(a, xdf, 0, p.nx, t);
+    if (!p.per_y && t < p.nx) apply_face(a, xdf, 1, t, p.ny);
 }
 
 // ||div u||: canonical sum of b^2 and max |b|
@@ -1220,6 +1313,22 @@ static Cg64 cg64_args(cf_ctx* c, const Stencil& st) {
 }
 
 static int red_blocks(const cf_ctx* c) { return (c->n_units + CF_RED_WARPS - 1) / CF_RED_WARPS; }
+
+// The pressure gradient: the mixed one as k_apply_pairs over the owned faces
+// plus k_apply_edges on a walled axis, the FP64 one (and the mixed one under
+// cf_test_apply_general) as k_apply_pressure.  Returns the launches made.
+static int launch_apply(cf_ctx* c, const Press& pa) {
+    if (pa.pairs && !c->test_general_apply) {
+        k_apply_pairs<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(pa, c->G, c->n_units);
+        if (c->ph.per_x && c->ph.per_y) return 1;
+        const int n = std::max(c->ph.nx, c->ph.ny);
+        k_apply_edges<<<(n + 255) / 256, 256, 0, c->stream>>>(pa);
+        return 2;
+    }
+    dim3 blk(32, 8), grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8);
+    k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
+    return 1;
+}
 
 static Outer outer_args(cf_ctx* c, const Stencil& st, int gated) {
     Outer oa{};
@@ -1584,8 +1693,7 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
             // mixed: the gradient reads the double-float solution; a warm
             // start then has it converted to the FP64 pressure it starts from
             Press pa = press_args(c, dt, gu, gv, adjoint);
-            dim3 grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8);
-            k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
+            ntail += launch_apply(c, pa) - 1;
             // u, v are final here: a caller may copy them out beside the norms
             if (!adjoint) cudaEventRecordWithFlags(c->ev_press, c->stream, cudaEventRecordExternal);
             if (mixed && warm) {
@@ -1664,7 +1772,7 @@ static int project_resident(cf_ctx* c, double dt, const SolveOpts& o, SolveResul
     }
     c->x_only = (mixed && mg && o.inner_tol >= 0.5) ? 1 : 0;
     const int flags = (mixed ? 1 : 0) | (mg ? 2 : 0) | ((adjoint ? c->adj_warm : c->warm) ? 4 : 0) | (c->x_only ? 8 : 0) |
-                      (adjoint ? 16 : 0);
+                      (adjoint ? 16 : 0) | (c->test_general_apply ? 32 : 0);
     int rc = CF_OK;
     if (!c->rgx[slot] || c->rg_flags[slot] != flags || c->rg_u[slot] != gu.o ||
         std::memcmp(&c->rg_st[slot], &st, sizeof(Stencil)) != 0 ||
@@ -1718,7 +1826,8 @@ int step_resident(cf_ctx* c, double dt, int order, int fuse, const SolveOpts& o,
     const int s = c->cur, n = 1 - s;
     c->x_only = (mixed && mg && o.inner_tol >= 0.5) ? 1 : 0;
     const int flags =
-        (mixed ? 1 : 0) | (mg ? 2 : 0) | (c->warm ? 4 : 0) | (c->x_only ? 8 : 0) | (c->test_unstaged ? 16 : 0);
+        (mixed ? 1 : 0) | (mg ? 2 : 0) | (c->warm ? 4 : 0) | (c->x_only ? 8 : 0) | (c->test_unstaged ? 16 : 0) |
+        (c->test_general_apply ? 32 : 0);
     if (!c->sgx[s] || c->sg_dt[s] != dt || c->sg_order[s] != order || c->sg_fuse[s] != fuse ||
         c->sg_flags[s] != flags || std::memcmp(&c->sg_st[s], &st, sizeof(Stencil)) != 0 ||
         std::memcmp(&c->sg_ph[s], &c->ph, sizeof(Phys)) != 0) {
@@ -1963,9 +2072,7 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     // gradient subtraction (mixed: from the double-float solution; the FP64
     // pressure is made afterwards for a warm start, or when it is downloaded)
     Press pa = press_args(c, dt, gu, gv, adjoint);
-    dim3 blk(32, 8), grd((c->ph.nx + 1 + 31) / 32, (c->ph.ny + 1 + 7) / 8);
-    k_apply_pressure<<<grd, blk, 0, c->stream>>>(pa);
-    c->launches += 1;
+    c->launches += launch_apply(c, pa);
     c->p_df = mixed ? 1 : 0;
     if (mixed && warm) settle_pressure(c);
     if ((rc = cuda_check(c, cudaGetLastError(), "apply pressure"))) return rc;

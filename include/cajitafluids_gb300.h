@@ -278,6 +278,11 @@ int cf_test_stall_wait(cf_ctx* ctx, int on);
  * could leave its shared-memory window) instead of the staged window.  The
  * results are the same bits either way; 0 switches the hook off. */
 int cf_test_advect_unstaged(cf_ctx* ctx, int on);
+/* Test hook: with on != 0, the mixed-precision pressure gradient updates
+ * every face in the one-thread-per-face kernel the FP64 gradient uses
+ * instead of the unit-per-warp kernel.  The results are the same bits either
+ * way; 0 switches the hook off. */
+int cf_test_apply_general(cf_ctx* ctx, int on);
 
 /* ---- output (replaces the device half of SiloWriter::writeFile) ----
  * SiloWriter interpolates the face velocities to cell centres for its
