@@ -462,47 +462,57 @@ __device__ __forceinline__ float2 df_neg(float2 x) { return make_float2(-x.x, -x
 // on columns c0 = 64 g + 2 l and c0 + 1), row by row: each row loads the
 // lane's two u pairs and two v pairs of row j + 1 as 16-byte vectors (row j's
 // v pairs come from the previous row), the E face of column c0 + 1 from the
-// next lane, and reads directly only what a wrap, the domain's last column
-// or the warp's last lane needs.  Calls f(c, j, div) for every owned cell,
-// div = ((u_E - u_W) + v_N) - v_S of its face pairs in double-float (E across
-// a periodic wrap is column 0, N row 0).
+// next lane, and reads directly only the one pair a wrap, the domain's last
+// column or the warp's last lane needs; every load of row j + 1 is issued
+// before row j's divergences are handed to f.  Calls f(c, j, div) for every
+// owned cell, div = ((u_E - u_W) + v_N) - v_S of its face pairs in
+// double-float (E across a periodic wrap is column 0, N row 0).
 template <typename F>
 __device__ __forceinline__ void div_pairs_unit(const DivArgs& a, int g, int band, int lane, F&& f) {
     const int c0 = g * CF_UNIT_COLS + 2 * lane;
     const int j0 = band * CF_BAND_ROWS, j1 = min(j0 + CF_BAND_ROWS, a.ny);
+    const bool live = c0 < a.nx, two = c0 + 1 < a.nx;
+    // the pair read directly: the E face of column c0 + 1 (the warp's last
+    // lane, the domain's last column: a boundary face, or column 0 across a
+    // periodic wrap), or of column c0 (its wrap to column 0)
+    const bool e2 = live && two && (lane == 31 || c0 + 2 >= a.nx);
+    const bool e1 = live && !two && a.per_x;
+    const int ie = e2 ? ((a.per_x && c0 + 2 == a.nx) ? 0 : c0 + 2) : 0;
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
     // the two pairs at columns c0, c0 + 1 of a row of u or v (in the ghosted
     // arrays: a column past the owned range is a ghost or a boundary face,
     // read but unused)
     auto pair2 = [&](const Grid<double>& g2, int jj) {
-        return *reinterpret_cast<const float4*>(&g2.at(c0 + CF_HALO, jj + CF_HALO));
+        return live ? *reinterpret_cast<const float4*>(&g2.at(c0 + CF_HALO, jj + CF_HALO)) : zero4;
     };
-    const bool live = c0 < a.nx;
-    float4 v0 = live ? pair2(a.v, j0) : make_float4(0.f, 0.f, 0.f, 0.f);
+    auto north = [&](int j) { return (a.per_y && j + 1 == a.ny) ? 0 : j + 1; };
+    auto edge = [&](int j) {
+        return (e1 || e2) ? pair_at(a.u, ie + CF_HALO, j + CF_HALO) : make_float2(0.f, 0.f);
+    };
+    float4 v0 = pair2(a.v, j0);
+    float4 un = pair2(a.u, j0), vn = pair2(a.v, north(j0));
+    float2 en = edge(j0);
     for (int j = j0; j < j1; ++j) {
-        int jn = j + 1;
-        if (a.per_y && jn == a.ny) jn = 0;
-        float4 uu = make_float4(0.f, 0.f, 0.f, 0.f), v1 = uu;
-        if (live) {
-            uu = pair2(a.u, j);
-            v1 = pair2(a.v, jn);
+        const float4 uu = un, v1 = vn;
+        const float2 ex = en;
+        if (j + 1 < j1) {
+            un = pair2(a.u, j + 1);
+            vn = pair2(a.v, north(j + 1));
+            en = edge(j + 1);
         }
-        // u at column c0 + 2 (the E face of column c0 + 1): the next lane's first
-        // pair, or read (the warp's last lane; the domain's last column: the
-        // boundary face, or column 0 across a periodic wrap)
+        // u at column c0 + 2 (the E face of column c0 + 1): the next lane's
+        // first pair, or the pair read directly
         float2 ue2 = make_float2(__shfl_down_sync(FULLMASK, uu.x, 1), __shfl_down_sync(FULLMASK, uu.y, 1));
-        if (live && c0 + 1 < a.nx && (lane == 31 || c0 + 2 >= a.nx)) {
-            const int ie2 = (a.per_x && c0 + 2 == a.nx) ? 0 : c0 + 2;
-            ue2 = pair_at(a.u, ie2 + CF_HALO, j + CF_HALO);
-        }
+        if (e2) ue2 = ex;
         if (live) {
             // column c0: E face c0 + 1 (or column 0 across a periodic wrap)
             float2 ue1 = make_float2(uu.z, uu.w);
-            if (a.per_x && c0 + 1 == a.nx) ue1 = pair_at(a.u, CF_HALO, j + CF_HALO);
+            if (e1) ue1 = ex;
             float2 t = df_add(ue1, df_neg(make_float2(uu.x, uu.y)));
             t = df_add(t, make_float2(v1.x, v1.y));
             t = df_add(t, df_neg(make_float2(v0.x, v0.y)));
             f(c0, j, t);
-            if (c0 + 1 < a.nx) {
+            if (two) {
                 float2 t1 = df_add(ue2, df_neg(make_float2(uu.z, uu.w)));
                 t1 = df_add(t1, make_float2(v1.z, v1.w));
                 t1 = df_add(t1, df_neg(make_float2(v0.z, v0.w)));
