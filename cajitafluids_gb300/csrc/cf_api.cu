@@ -315,6 +315,12 @@ int cf_ctx_create(const cf_grid_desc* d, cf_ctx** out) {
     } else {
         if (!rc) rc = alloc_dev(c, c->b.a, vn);
         if (!rc) rc = alloc_dev(c, c->xb.a, vn);
+        // the old faces on the reduction units' west columns and south rows
+        // (pairs), saved by the divergence for the gradient's fused norms
+        if (!rc)
+            rc = alloc_dev(c, c->bnd,
+                           (size_t)((nx + CF_UNIT_COLS - 1) / CF_UNIT_COLS) * ny +
+                               (size_t)((ny + CF_BAND_ROWS - 1) / CF_BAND_ROWS) * nx);
         // FP32 vectors with a one-cell ghost ring, owned column 0 on 16 bytes
         c->p32 = (int)round_up((size_t)nx + 8, 32);
         size_t n32 = (size_t)c->p32 * (ny + 2);

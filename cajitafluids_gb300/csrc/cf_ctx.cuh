@@ -38,6 +38,7 @@ struct cf_ctx {
     // mixed: the second buffer of the double-float solution (the MG-PCG's
     // fused x update writes the updated x there; SolverState::xsel)
     cf::Vec64 xb{};
+    double* bnd = nullptr;  // mixed: unit-boundary faces of u and v before the gradient
     // the last mixed projection left the pressure as double-float pairs (in
     // the buffer SolverState::xsel names); a download converts it
     int p_df = 0;

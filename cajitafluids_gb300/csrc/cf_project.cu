@@ -361,6 +361,11 @@ struct DivArgs {
     int mixed;        // k_div_norms: squares and magnitudes in FP32
     float mscale32;   // -(1/dx) in FP32
     float2 mscale2;   // -(1/dx) as a double-float pair
+    // k_div_init_mixed (when set): the faces k_apply_pairs_norms cannot read
+    // once the gradient has started, saved as pairs: u on each unit's west
+    // column (ubnd[g * ny + j] = u(64 g, j)) and v on each unit's south row
+    // (vbnd[band * nx + c] = v(c, 16 band))
+    float2 *ubnd, *vbnd;
 };
 
 __device__ __forceinline__ double div_b(const DivArgs& a, int gi, int gj) {
@@ -492,9 +497,14 @@ __device__ __forceinline__ void div_pairs_unit(const DivArgs& a, int g, int band
     float4 v0 = pair2(a.v, j0);
     float4 un = pair2(a.u, j0), vn = pair2(a.v, north(j0));
     float2 en = edge(j0);
+    if (a.vbnd && live) {
+        a.vbnd[(size_t)band * a.nx + c0] = make_float2(v0.x, v0.y);
+        if (two) a.vbnd[(size_t)band * a.nx + c0 + 1] = make_float2(v0.z, v0.w);
+    }
     for (int j = j0; j < j1; ++j) {
         const float4 uu = un, v1 = vn;
         const float2 ex = en;
+        if (a.ubnd && lane == 0 && live) a.ubnd[(size_t)g * a.ny + j] = make_float2(uu.x, uu.y);
         if (j + 1 < j1) {
             un = pair2(a.u, j + 1);
             vn = pair2(a.v, north(j + 1));
@@ -1202,6 +1212,142 @@ __global__ void k_apply_edges(Press a) {
     if (!p.per_y && t < p.nx) apply_face(a, xdf, 1, t, p.ny);
 }
 
+// The mixed gradient of k_apply_pairs fused with the divergence norms of its
+// result (k_div_norms' mixed form), for a grid periodic along both axes (no
+// wall rule, no face past the last cell).  A lane's divergences need two faces
+// that other warps update in place: the I face east of the warp (the next
+// unit's west column, or column 0 across the wrap) and the J faces above the
+// unit (the next band's south row, or row 0).  Their values before the
+// gradient were saved by k_div_init_mixed (d.ubnd, d.vbnd); the lane updates
+// them itself with the owner's operands, so it holds the owner's bits.  The
+// J faces of row j + 1 are updated one row ahead and carried, and each cell's
+// divergence, square and magnitude are taken in k_div_norms' operation order,
+// lane order and folds: the same stored faces and the same norms.
+__global__ void __launch_bounds__(CF_RED_THREADS, 4) k_apply_pairs_norms(Press a, DivArgs d) {
+    const int lane = threadIdx.x & 31;
+    const int unit = blockIdx.x * CF_RED_WARPS + (threadIdx.x >> 5);
+    float fss = 0.f, fmx = 0.f;
+    if (unit < d.U) {  // warp-uniform
+        const int nx = a.p.nx, ny = a.p.ny;
+        const int g = unit % d.G, band = unit / d.G;
+        const int c0 = g * CF_UNIT_COLS + 2 * lane;
+        const int j0 = band * CF_BAND_ROWS, j1 = min(j0 + CF_BAND_ROWS, ny);
+        const int jn = j1 == ny ? 0 : j1;  // the row above the unit
+        const float2* xdf = press_pairs(a);
+        const bool live = c0 < nx, two = c0 + 1 < nx;
+        // the lane whose east face is another warp's: the warp's last lane
+        // (column ie = c0 + 2) or the domain's last column (ie = 0)
+        const bool e2 = live && two && (lane == 31 || c0 + 2 >= nx);
+        const bool e1 = live && !two;
+        const int ie = (e2 && c0 + 2 < nx) ? c0 + 2 : 0;
+        const float2* ub = d.ubnd + (size_t)(ie / CF_UNIT_COLS) * ny;
+        const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        auto xrow = [&](int j) {
+            return live ? *reinterpret_cast<const float4*>(&xdf[(size_t)j * a.pitch + c0]) : zero4;
+        };
+        auto frow = [&](const Grid<double>& f, int j) {
+            return live ? *reinterpret_cast<const float4*>(&f.at(c0 + CF_HALO, j + CF_HALO)) : zero4;
+        };
+        auto west = [&](int j) { return (lane == 0 && live) ? pval_df(a, xdf, c0 - 1, j) : make_float2(0.f, 0.f); };
+        // the saved east face (before the gradient) and p at its column
+        auto halo = [&](int j) {
+            if (!(e1 || e2)) return zero4;
+            const float2 uo = ub[j], xo = xdf[(size_t)j * a.pitch + ie];
+            return make_float4(uo.x, uo.y, xo.x, xo.y);
+        };
+        auto upd = [&](float x0, float x1, float pc0, float pc1, float pn0, float pn1) {
+            const float2 m = df_mul(a.ms2, df_add_s(make_float2(pc0, pc1), make_float2(-pn0, -pn1)));
+            return df_add(make_float2(x0, x1), m);
+        };
+        // the J faces of row j0 (p of the row below: its wrap)
+        const float4 xs = xrow(j0 > 0 ? j0 - 1 : ny - 1);
+        float4 xc = xrow(j0), uu = frow(a.u, j0);
+        const float4 vv = frow(a.v, j0);
+        float2 wc = west(j0);
+        float4 hc = halo(j0);
+        float2 vs0 = upd(vv.x, vv.y, xc.x, xc.y, xs.x, xs.y);
+        float2 vs1 = upd(vv.z, vv.w, xc.z, xc.w, xs.z, xs.w);
+        for (int j = j0; j < j1; ++j) {
+            float4 xn, un = zero4, vn, hn = zero4;
+            float2 wn = make_float2(0.f, 0.f);
+            if (j + 1 < j1) {
+                xn = xrow(j + 1);
+                un = frow(a.u, j + 1);
+                vn = frow(a.v, j + 1);
+                wn = west(j + 1);
+                hn = halo(j + 1);
+            } else {
+                // the row above the unit: p, and the J faces as saved
+                xn = xrow(jn);
+                const float2* vb = d.vbnd + (size_t)(jn / CF_BAND_ROWS) * nx + c0;
+                const float2 b0 = live ? vb[0] : make_float2(0.f, 0.f);
+                const float2 b1 = two ? vb[1] : make_float2(0.f, 0.f);
+                vn = make_float4(b0.x, b0.y, b1.x, b1.y);
+            }
+            float2 xw = make_float2(__shfl_up_sync(FULLMASK, xc.z, 1), __shfl_up_sync(FULLMASK, xc.w, 1));
+            if (lane == 0) xw = wc;
+            const float2 u0 = upd(uu.x, uu.y, xc.x, xc.y, xw.x, xw.y);
+            const float2 u1 = upd(uu.z, uu.w, xc.z, xc.w, xc.x, xc.y);
+            // the J faces of row j + 1
+            const float2 vn0 = upd(vn.x, vn.y, xn.x, xn.y, xc.x, xc.y);
+            const float2 vn1 = upd(vn.z, vn.w, xn.z, xn.w, xc.z, xc.w);
+            // the east faces: the next lane's first I face, or the saved one
+            // updated here (p west of it: the lane's last column)
+            float2 ue2 = make_float2(__shfl_down_sync(FULLMASK, u0.x, 1), __shfl_down_sync(FULLMASK, u0.y, 1));
+            float2 uh = make_float2(0.f, 0.f);
+            if (e1 || e2) uh = upd(hc.x, hc.y, hc.z, hc.w, e2 ? xc.z : xc.x, e2 ? xc.w : xc.y);
+            if (e2) ue2 = uh;
+            if (live) {
+                float2* pu = reinterpret_cast<float2*>(&a.u.at(c0 + CF_HALO, j + CF_HALO));
+                float2* pv = reinterpret_cast<float2*>(&a.v.at(c0 + CF_HALO, j + CF_HALO));
+                if (two) {
+                    *reinterpret_cast<float4*>(pu) = make_float4(u0.x, u0.y, u1.x, u1.y);
+                    *reinterpret_cast<float4*>(pv) = make_float4(vs0.x, vs0.y, vs1.x, vs1.y);
+                } else {
+                    pu[0] = u0;
+                    pv[0] = vs0;
+                }
+                const float2 ue1 = two ? u1 : uh;
+                float2 t = df_add(ue1, df_neg(u0));
+                t = df_add(t, vn0);
+                t = df_add(t, df_neg(vs0));
+                float bf = t.x * d.mscale32;
+                fss = fmaf(bf, bf, fss);
+                fmx = fmaxf(fmx, fabsf(bf));
+                if (two) {
+                    float2 t1 = df_add(ue2, df_neg(u1));
+                    t1 = df_add(t1, vn1);
+                    t1 = df_add(t1, df_neg(vs1));
+                    bf = t1.x * d.mscale32;
+                    fss = fmaf(bf, bf, fss);
+                    fmx = fmaxf(fmx, fabsf(bf));
+                }
+            }
+            xc = xn;
+            uu = un;
+            wc = wn;
+            hc = hn;
+            vs0 = vn0;
+            vs1 = vn1;
+        }
+    }
+    double ass = warp_fold((double)fss);
+    double amx = warp_max((double)fmx);
+    if (unit < d.U && lane == 0) {
+        d.part0[unit] = ass;
+        d.part1[unit] = amx;
+    }
+    if (last_block_arrive(&d.S->ticket[3])) {
+        const double ss = final_tree(d.part0, d.U);
+        const double mx = final_max(d.part1, d.U);
+        if (threadIdx.x == 0) {
+            d.S->ticket[3] = 0;
+            d.out[0] = ss;
+            d.out[1] = mx;
+        }
+    }
+}
+
 // ||div u||: canonical sum of b^2 and max |b|
 __global__ void __launch_bounds__(CF_RED_THREADS) k_div_norms(DivArgs a) {
     SolverState* S = a.S;
@@ -1324,10 +1470,26 @@ static Cg64 cg64_args(cf_ctx* c, const Stencil& st) {
 
 static int red_blocks(const cf_ctx* c) { return (c->n_units + CF_RED_WARPS - 1) / CF_RED_WARPS; }
 
-// The pressure gradient: the mixed one as k_apply_pairs over the owned faces
-// plus k_apply_edges on a walled axis, the FP64 one (and the mixed one under
-// cf_test_apply_general) as k_apply_pressure.  Returns the launches made.
-static int launch_apply(cf_ctx* c, const Press& pa) {
+// The mixed projection of a grid periodic along both axes takes its
+// divergence norms inside the gradient (k_apply_pairs_norms), from faces
+// that k_div_init_mixed saves (the adjoint's projections take no norms).
+static bool fused_norms(const cf_ctx* c, bool mixed, int adjoint) {
+    return mixed && !adjoint && c->ph.per_x && c->ph.per_y && !c->test_general_apply;
+}
+static void save_bounds(const cf_ctx* c, DivArgs* da) {
+    da->ubnd = reinterpret_cast<float2*>(c->bnd);
+    da->vbnd = da->ubnd + (size_t)c->G * c->ph.ny;
+}
+
+// The pressure gradient: with norms (fused_norms), k_apply_pairs_norms; the
+// mixed one as k_apply_pairs over the owned faces plus k_apply_edges on a
+// walled axis; the FP64 one (and the mixed one under cf_test_apply_general)
+// as k_apply_pressure.  Returns the launches made.
+static int launch_apply(cf_ctx* c, const Press& pa, const DivArgs* norms = nullptr) {
+    if (norms) {
+        k_apply_pairs_norms<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(pa, *norms);
+        return 1;
+    }
     if (pa.pairs && !c->test_general_apply) {
         k_apply_pairs<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(pa, c->G, c->n_units);
         if (c->ph.per_x && c->ph.per_y) return 1;
@@ -1656,6 +1818,7 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
             da.u = gu;
             da.v = gv;
             da.warm = warm;
+            if (fused_norms(c, mixed, adjoint)) save_bounds(c, &da);
             if (mixed)
                 k_div_init_mixed<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
             else
@@ -1703,7 +1866,12 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
             // mixed: the gradient reads the double-float solution; a warm
             // start then has it converted to the FP64 pressure it starts from
             Press pa = press_args(c, dt, gu, gv, adjoint);
-            ntail += launch_apply(c, pa) - 1;
+            DivArgs dn = div_args(c, st);
+            dn.u = gu;
+            dn.v = gv;
+            const bool fuse_n = fused_norms(c, mixed, adjoint);
+            if (fuse_n) save_bounds(c, &dn);
+            ntail += launch_apply(c, pa, fuse_n ? &dn : nullptr) - 1;
             // u, v are final here: a caller may copy them out beside the norms
             if (!adjoint) cudaEventRecordWithFlags(c->ev_press, c->stream, cudaEventRecordExternal);
             if (mixed && warm) {
@@ -1713,11 +1881,8 @@ static int build_resident(cf_ctx* c, const Stencil& st, double dt, bool mixed, b
                 ntail += 1;
             }
             // (the adjoint's projections report no divergence norms)
-            if (!adjoint) {
-                DivArgs da = div_args(c, st);
-                da.u = gu;
-                da.v = gv;
-                k_div_norms<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
+            if (!adjoint && !fuse_n) {
+                k_div_norms<<<nb, CF_RED_THREADS, 0, c->stream>>>(dn);
                 ntail += 1;
             }
             k_step_tally<<<1, 1, 0, c->stream>>>(c->S, c->d_tally);
@@ -1941,17 +2106,22 @@ cudaError_t pressure_to_f64(cf_ctx* c, double* out) {
     return cudaGetLastError();
 }
 
-int div_norms(cf_ctx* c, double* l2, double* linf) {
-    Stencil st{};
-    DivArgs a = div_args(c, st);
-    k_div_norms<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(a);
-    c->launches += 1;
+// the norms the last k_div_norms or k_apply_pairs_norms left in d_out
+static int read_norms(cf_ctx* c, double* l2, double* linf) {
     cudaMemcpyAsync(c->h_out, c->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     int rc = cuda_check(c, cudaStreamSynchronize(c->stream), "div norms");
     if (rc) return rc;
     *l2 = sqrt(c->h_out[0]) * c->ph.dx;
     *linf = c->h_out[1];
     return CF_OK;
+}
+
+int div_norms(cf_ctx* c, double* l2, double* linf) {
+    Stencil st{};
+    DivArgs a = div_args(c, st);
+    k_div_norms<<<red_blocks(c), CF_RED_THREADS, 0, c->stream>>>(a);
+    c->launches += 1;
+    return read_norms(c, l2, linf);
 }
 
 int project(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res) {
@@ -2028,7 +2198,9 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
             c->launches += per_batch;
         }
     } else {
-        k_div_init_mixed<<<nb, CF_RED_THREADS, 0, c->stream>>>(da);
+        DivArgs di = da;
+        if (fused_norms(c, mixed, adjoint)) save_bounds(c, &di);
+        k_div_init_mixed<<<nb, CF_RED_THREADS, 0, c->stream>>>(di);
         c->launches += 1;
         if (warm) c->launches += launch_warm_init(c, st, true);
         if (mg) {
@@ -2082,13 +2254,16 @@ int project_grids(cf_ctx* c, double dt, const SolveOpts& o, SolveResult* res, Gr
     // gradient subtraction (mixed: from the double-float solution; the FP64
     // pressure is made afterwards for a warm start, or when it is downloaded)
     Press pa = press_args(c, dt, gu, gv, adjoint);
-    c->launches += launch_apply(c, pa);
+    const bool fuse_n = fused_norms(c, mixed, adjoint);
+    DivArgs dn = da;
+    if (fuse_n) save_bounds(c, &dn);
+    c->launches += launch_apply(c, pa, fuse_n ? &dn : nullptr);
     c->p_df = mixed ? 1 : 0;
     if (mixed && warm) settle_pressure(c);
     if ((rc = cuda_check(c, cudaGetLastError(), "apply pressure"))) return rc;
     if (c->prof) cudaEventRecord(c->ev[5], c->stream);
     if (adjoint) return cuda_check(c, cudaStreamSynchronize(c->stream), "adjoint projection");
-    rc = div_norms(c, &res->div_l2, &res->div_linf);
+    rc = fuse_n ? read_norms(c, &res->div_l2, &res->div_linf) : div_norms(c, &res->div_l2, &res->div_linf);
     if (!rc && c->prof) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]) == cudaSuccess) {

@@ -7,7 +7,9 @@ cf_test_apply_general sends every face through k_apply_pressure, the
 one-thread-per-face kernel of the FP64 gradient.  Both must give the same
 bits: whole mixed steps (graphs and direct launches), odd and small grids,
 every wall rule (solid and free walls, the Q1 quirk fixed and not) and the
-adjoint's transposed projection are compared bit for bit.
+adjoint's transposed projection are compared bit for bit.  On a grid
+periodic along both axes the gradient kernel also takes the divergence norms
+of its result (k_apply_pairs_norms); they must equal k_div_norms' bit for bit.
 """
 import numpy as np
 import pytest
@@ -61,12 +63,17 @@ def test_unit_gradient_equals_per_face_gradient(nx, ny, periodic, bc, quirks, gr
         c = _ctx(nx, ny, periodic, bc, quirks, general, graphs)
         for f in FIELDS:
             c.upload(f, s[f])
+        norms = []
         for _ in range(3):
-            c.step(dt, 3, o)
+            r = c.step(dt, 3, o)
+            norms.append((r["div_l2"], r["div_linf"]))
         out.append({f: c.download(f) for f in FIELDS})
+        out[-1]["norms"] = norms
     for f in FIELDS:
         a, b = out[0][f], out[1][f]
         assert np.array_equal(a, b), (f, np.count_nonzero(a != b))
+    # periodic both ways: the norms come from the gradient kernel itself
+    assert out[0]["norms"] == out[1]["norms"]
 
 
 @pytest.mark.parametrize("periodic", [False, True])
