@@ -401,7 +401,8 @@ def bench_gb300(args, rank, world, dist, device):
                            "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
                            "path": "cf_step_host: q,u,v from pinned host, one step, q,u,v back to pinned host "
                                    "(q's upload overlaps the u,v advection, q's download the projection, "
-                                   "u,v's download the divergence norms)"}
+                                   "u,v's download the step's tail; on this periodic grid the divergence norms are taken "
+                                   "inside the gradient kernel, before u,v go out)"}
             for h in (hq, hu, hv):
                 h.free()
         cm.close()

@@ -885,7 +885,8 @@ int cf_step_host(cf_ctx* ctx, double dt, int value_order, const cf_solver_opts* 
     bool deferred = false;
     rc = project_async(ctx, dt, so, &r, &deferred);
     // the resident projection records ev_press after the gradient subtraction:
-    // u and v go out on the second stream from there, beside the norms
+    // u and v go out on the second stream from there, beside the rest of the
+    // tail (k_div_norms, unless the gradient took the norms itself)
     cudaStream_t out_stream = ctx->stream;
     if (!rc && deferred && (u_out || v_out)) {
         rc = cuda_check(ctx, cudaStreamWaitEvent(ctx->stream2, ctx->ev_press, 0), "event wait");
